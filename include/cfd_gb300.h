@@ -1,0 +1,159 @@
+/*
+ * cfd_gb300.h -- C ABI of the GB300-native jax-cfd time-stepping hot path.
+ *
+ * Plain C types only: device pointers are `float*` (complex64 arrays are
+ * interleaved float pairs, the memory layout of the reference's complex64
+ * rfftn output), streams are `void*` holding a cudaStream_t (NULL = legacy
+ * default stream).  Every entry point returns a cfd_status; on failure
+ * cfd_last_error() returns a message for the calling thread.  Calls only
+ * enqueue work on the stream -- none of them synchronise -- except where a
+ * comment says otherwise.
+ *
+ * Reference interfaces replaced (paths inside the jax-cfd 0.2.1 source tree):
+ *   cfd_fvm_plan_create / cfd_fvm_step
+ *       jax_cfd/base/equations.py:120-151   semi_implicit_navier_stokes(...)
+ *         with forward_euler (time_stepping.py:109-119), the default
+ *         convect = advect_van_leer_using_limiters (advection.py:387-395) or
+ *         advection.convect_linear (advection.py:183-207), diffuse
+ *         (diffusion.py:35-37), forcing built from forcings.py:63-178 and
+ *         pressure_solve = pressure.solve_fast_diag (pressure.py:115-157);
+ *       jax_cfd/base/funcutils.py:82-88     repeated(step_fn, steps)
+ *   cfd_fvm_explicit_terms
+ *       jax_cfd/base/equations.py:77-116    navier_stokes_explicit_terms
+ *   cfd_fvm_projection
+ *       jax_cfd/base/pressure.py:181-198    projection(v, solve_fast_diag)
+ *   cfd_fvm_pressure_solve
+ *       jax_cfd/base/pressure.py:115-157    solve_fast_diag(v)
+ *   cfd_fvm_divergence, cfd_fvm_curl_2d
+ *       jax_cfd/base/finite_differences.py:136-143, 186-193
+ *   cfd_max_speed, cfd_scale_to_max_speed
+ *       jax_cfd/base/initial_conditions.py:67-68, 112-121
+ *   cfd_spec_plan_create / cfd_spec_step
+ *       jax_cfd/spectral/time_stepping.py:117-197
+ *         low_storage_runge_kutta_crank_nicolson / crank_nicolson_rk4 applied
+ *         to spectral/equations.py:129-191 NavierStokes2D
+ *   cfd_spec_set_forcing
+ *       jax_cfd/spectral/equations.py:176-182 (rfft2 of a velocity-independent
+ *         forcing + spectral_curl_2d, spectral/utils.py:199-203)
+ *   cfd_rfft2, cfd_irfft2, cfd_spectral_filter
+ *       jnp.fft.rfftn / irfftn as used by the two steps, and
+ *       jax_cfd/base/filter_utils.py:32-42 filter(...)
+ */
+#ifndef CFD_GB300_H_
+#define CFD_GB300_H_
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum cfd_status {
+  CFD_OK = 0,
+  CFD_ERR_INVALID_ARGUMENT = 1, /* bad shape / size / pointer: ValueError */
+  CFD_ERR_UNSUPPORTED = 2,      /* option outside the hot path: NotImplementedError */
+  CFD_ERR_CUDA = 3,             /* CUDA runtime error: RuntimeError */
+  CFD_ERR_OUT_OF_MEMORY = 4     /* device allocation failed: MemoryError */
+} cfd_status;
+
+/* Advection schemes (the `convect` argument). */
+enum { CFD_CONVECT_VAN_LEER = 0, CFD_CONVECT_LINEAR = 1 };
+
+/* Velocity-independent forcing layouts. */
+enum {
+  CFD_FORCE_NONE = 0,
+  CFD_FORCE_U_OF_Y = 1, /* u-forcing depends on j only: table of ny floats  */
+  CFD_FORCE_V_OF_X = 2, /* v-forcing depends on i only: table of nx floats  */
+  CFD_FORCE_FULL = 3    /* arbitrary fields: force_u, force_v of nx*ny each */
+};
+
+typedef struct cfd_fvm_config {
+  int nx, ny;             /* grid shape; axis 1 contiguous; powers of 2 in [4, 4096] */
+  double hx, hy;          /* grid step along each axis */
+  double density;
+  int has_viscosity;      /* 0 mirrors viscosity=None */
+  double viscosity;
+  double dt;
+  int convect;            /* CFD_CONVECT_* */
+  int has_linear_forcing; /* linear_forcing(grid, coefficient) term present */
+  double linear_coefficient;
+  int const_forcing;      /* CFD_FORCE_* */
+  const float* force_u;   /* HOST pointers, copied at creation (may be NULL) */
+  const float* force_v;
+} cfd_fvm_config;
+
+typedef struct cfd_fvm_plan cfd_fvm_plan;
+
+const char* cfd_last_error(void);
+int cfd_version(void);
+
+int cfd_fvm_plan_create(const cfd_fvm_config* cfg, cfd_fvm_plan** plan);
+int cfd_fvm_plan_destroy(cfd_fvm_plan* plan);
+/* Device bytes held by the plan (workspace + tables). */
+long long cfd_fvm_plan_bytes(const cfd_fvm_plan* plan);
+
+/* `steps` forward-Euler steps; u/v are [nx, ny] float32 on the device at
+ * offsets (1, .5) and (.5, 1).  u_out/v_out may alias u/v. */
+int cfd_fvm_step(cfd_fvm_plan* plan, void* stream, const float* u,
+                 const float* v, float* u_out, float* v_out, int steps);
+/* du/dt from advection + diffusion + forcing (no projection). */
+int cfd_fvm_explicit_terms(cfd_fvm_plan* plan, void* stream, const float* u,
+                           const float* v, float* du, float* dv);
+int cfd_fvm_projection(cfd_fvm_plan* plan, void* stream, const float* u,
+                       const float* v, float* u_out, float* v_out);
+/* Pressure correction q (offset (.5, .5)) with div(v - grad q) = 0. */
+int cfd_fvm_pressure_solve(cfd_fvm_plan* plan, void* stream, const float* u,
+                           const float* v, float* q);
+int cfd_fvm_divergence(cfd_fvm_plan* plan, void* stream, const float* u,
+                       const float* v, float* out);
+int cfd_fvm_curl_2d(cfd_fvm_plan* plan, void* stream, const float* u,
+                    const float* v, float* out);
+
+/* max over cells of sqrt(u^2 + v^2) written as one float to device memory. */
+int cfd_max_speed(void* stream, int n, const float* u, const float* v,
+                  float* out);
+/* u = (maximum_velocity * u) / vmax, same for v (vmax read from device). */
+int cfd_scale_to_max_speed(void* stream, int n, float* u, float* v,
+                           const float* vmax, double maximum_velocity);
+
+typedef struct cfd_spec_config {
+  int nx, ny;         /* powers of 2 in [4, 4096] */
+  double hx, hy;
+  double viscosity;
+  double drag;
+  double dt;
+  int smooth;         /* 1: multiply by the 2/3 brick-wall filter (smooth is
+                         not None, including smooth=False); 0: smooth=None */
+  int num_stages;     /* low-storage RK/CN stages, 1..8 */
+  const double* alphas; /* num_stages + 1 */
+  const double* betas;  /* num_stages */
+  const double* gammas; /* num_stages */
+} cfd_spec_config;
+
+typedef struct cfd_spec_plan cfd_spec_plan;
+
+int cfd_spec_plan_create(const cfd_spec_config* cfg, cfd_spec_plan** plan);
+int cfd_spec_plan_destroy(cfd_spec_plan* plan);
+long long cfd_spec_plan_bytes(const cfd_spec_plan* plan);
+/* Velocity-independent forcing (fx, fy real [nx, ny] on the device, either may
+ * be NULL): stores 2 pi i (kx rfft2(fy) - ky rfft2(fx)).  Synchronises the
+ * stream once to decide whether the table lives only in row kx = 0. */
+int cfd_spec_set_forcing(cfd_spec_plan* plan, void* stream, const float* fx,
+                         const float* fy);
+/* `steps` time steps of the vorticity rfft state [nx, ny/2+1] complex64.
+ * w_out may alias w_in. */
+int cfd_spec_step(cfd_spec_plan* plan, void* stream, const float* w_in,
+                  float* w_out, int steps);
+/* Explicit terms F(w) of NavierStokes2D (advection, filter, forcing). */
+int cfd_spec_explicit_terms(cfd_spec_plan* plan, void* stream,
+                            const float* w, float* out);
+int cfd_rfft2(cfd_spec_plan* plan, void* stream, const float* x, float* xhat);
+/* Destroys nothing: xhat is read-only (a workspace copy is transformed). */
+int cfd_irfft2(cfd_spec_plan* plan, void* stream, const float* xhat, float* x);
+/* out = irfft2(rfft2(x) * table), table real [nx, ny/2+1] on the device. */
+int cfd_spectral_filter(cfd_spec_plan* plan, void* stream, const float* x,
+                        const float* table, float* out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CFD_GB300_H_ */

@@ -1,0 +1,591 @@
+// C ABI: plans own the precomputed tables and the device workspace of one
+// grid; entry points enqueue the kernels of kernels.h on the caller's stream.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/cfd_gb300.h"
+#include "kernels.h"
+#include "common.cuh"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* where) {
+  g_last_error = std::string(where) + ": " + cudaGetErrorString(e);
+  return e == cudaErrorMemoryAllocation ? CFD_ERR_OUT_OF_MEMORY : CFD_ERR_CUDA;
+}
+
+#define CFD_CHECK(expr, where)                  \
+  do {                                          \
+    cudaError_t _e = (expr);                    \
+    if (_e != cudaSuccess) return cuda_fail(_e, where); \
+  } while (0)
+
+bool valid_size(int n) { return n >= 4 && n <= 4096 && is_pow2(n); }
+
+std::vector<float2> twiddles(int n) {
+  std::vector<float2> t(n);
+  for (int k = 0; k < n; ++k) {
+    const double a = -2.0 * M_PI * (double)k / (double)n;
+    t[k] = make_float2((float)std::cos(a), (float)std::sin(a));
+  }
+  return t;
+}
+
+// Eigenvalues of the periodic 1-D Laplacian circulant [-2, 1, 0..0, 1] / h^2
+// (array_utils.py:168-173), i.e. fft of its first column, in double.
+std::vector<float> laplacian_eigenvalues(int n, double h, int count) {
+  std::vector<float> lam(count);
+  for (int k = 0; k < count; ++k) {
+    const double v = (k == 0) ? 0.0
+                              : (2.0 * std::cos(2.0 * M_PI * (double)k / (double)n) - 2.0) /
+                                    (h * h);
+    lam[k] = (float)v;
+  }
+  return lam;
+}
+
+template <typename T>
+cudaError_t upload(T** dev, const T* host, size_t count) {
+  cudaError_t e = cudaMalloc((void**)dev, count * sizeof(T));
+  if (e != cudaSuccess) return e;
+  return cudaMemcpy(*dev, host, count * sizeof(T), cudaMemcpyHostToDevice);
+}
+
+cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+}  // namespace
+
+struct cfd_fvm_plan {
+  cfd::FvmParams p;
+  float* au = nullptr;
+  float* av = nullptr;
+  float* bu = nullptr;
+  float* bv = nullptr;
+  float2* spec = nullptr;  // packed row spectrum / pressure q (nx * ny floats)
+  float* lamx = nullptr;
+  float* lamy = nullptr;
+  float2* twx = nullptr;
+  float2* twy = nullptr;
+  float* fu = nullptr;
+  float* fv = nullptr;
+  long long bytes = 0;
+};
+
+struct cfd_spec_plan {
+  cfd::SpecParams p;
+  int stages = 0;
+  cfd::StageCoef coef[8];
+  float2* t4[4] = {nullptr, nullptr, nullptr, nullptr};
+  float2* ahat = nullptr;
+  float2* h = nullptr;
+  float2* fc = nullptr;     // forcing curl table (full or row 0)
+  float2* work = nullptr;   // scratch spectrum for rfft2 / irfft2 / filter
+  float2* twx = nullptr;
+  float2* twy = nullptr;
+  float* kx = nullptr;
+  float* ky = nullptr;
+  long long bytes = 0;
+};
+
+extern "C" {
+
+const char* cfd_last_error(void) { return g_last_error.c_str(); }
+
+int cfd_version(void) { return 1; }
+
+int cfd_fvm_plan_destroy(cfd_fvm_plan* plan) {
+  if (!plan) return CFD_OK;
+  void* ptrs[] = {plan->au, plan->av, plan->bu, plan->bv, plan->spec, plan->lamx,
+                  plan->lamy, plan->twx, plan->twy, plan->fu, plan->fv};
+  for (void* q : ptrs)
+    if (q) cudaFree(q);
+  delete plan;
+  return CFD_OK;
+}
+
+int cfd_fvm_plan_create(const cfd_fvm_config* cfg, cfd_fvm_plan** out) {
+  if (!cfg || !out) return fail(CFD_ERR_INVALID_ARGUMENT, "null config or output pointer");
+  *out = nullptr;
+  if (!valid_size(cfg->nx) || !valid_size(cfg->ny))
+    return fail(CFD_ERR_UNSUPPORTED,
+                "grid shape must be powers of two in [4, 4096] (real-FFT pressure solve)");
+  if (!(cfg->hx > 0) || !(cfg->hy > 0) || !(cfg->density != 0) || !std::isfinite(cfg->dt))
+    return fail(CFD_ERR_INVALID_ARGUMENT, "invalid step, density or dt");
+  if (cfg->convect != CFD_CONVECT_VAN_LEER && cfg->convect != CFD_CONVECT_LINEAR)
+    return fail(CFD_ERR_UNSUPPORTED, "unsupported convection scheme");
+  if (cfg->const_forcing < CFD_FORCE_NONE || cfg->const_forcing > CFD_FORCE_FULL)
+    return fail(CFD_ERR_UNSUPPORTED, "unsupported forcing layout");
+  if (cfg->const_forcing != CFD_FORCE_NONE && !cfg->force_u && !cfg->force_v)
+    return fail(CFD_ERR_INVALID_ARGUMENT, "forcing layout given without tables");
+
+  cfd_fvm_plan* plan = new cfd_fvm_plan();
+  cfd::FvmParams& p = plan->p;
+  std::memset(&p, 0, sizeof(p));
+  const int nx = cfg->nx, ny = cfg->ny;
+  p.nx = nx;
+  p.ny = ny;
+  p.log2nx = ilog2(nx);
+  p.log2ny = ilog2(ny);
+  // Python floats are rounded once to float32 where the reference's weakly
+  // typed scalars meet float32 arrays.
+  p.hx = (float)cfg->hx;
+  p.hy = (float)cfg->hy;
+  p.cfl_x = (float)(cfg->dt / cfg->hx);
+  p.cfl_y = (float)(cfg->dt / cfg->hy);
+  p.dt = (float)cfg->dt;
+  p.has_visc = cfg->has_viscosity ? 1 : 0;
+  p.nu = cfg->has_viscosity ? (float)(cfg->viscosity / cfg->density) : 0.f;
+  // finite_differences.laplacian: scales = (1 / float32(step))^2 in float32.
+  const float ihx = 1.f / p.hx, ihy = 1.f / p.hy;
+  p.sx = ihx * ihx;
+  p.sy = ihy * ihy;
+  p.ssum = p.sx + p.sy;
+  p.density = (float)cfg->density;
+  p.rho_is_one = cfg->density == 1.0 ? 1 : 0;
+  p.has_lin = cfg->has_linear_forcing ? 1 : 0;
+  p.lin = (float)cfg->linear_coefficient;
+  p.has_forcing = (p.has_lin || cfg->const_forcing != CFD_FORCE_NONE) ? 1 : 0;
+  p.convect = cfg->convect;
+  p.cutoff = 10.f * 1.1920928955078125e-07f;  // 10 * finfo(float32).eps
+  p.pinv_scale = 1.f / ((float)nx * (float)ny);
+
+  const size_t n = (size_t)nx * ny;
+  cudaError_t e;
+  long long bytes = 0;
+#define CFD_ALLOC(ptr, count)                                              \
+  do {                                                                     \
+    e = cudaMalloc((void**)&(ptr), (count) * sizeof(*(ptr)));              \
+    if (e != cudaSuccess) {                                                \
+      cfd_fvm_plan_destroy(plan);                                          \
+      return cuda_fail(e, "cfd_fvm_plan_create: cudaMalloc");              \
+    }                                                                      \
+    bytes += (long long)((count) * sizeof(*(ptr)));                        \
+  } while (0)
+  CFD_ALLOC(plan->au, n);
+  CFD_ALLOC(plan->av, n);
+  CFD_ALLOC(plan->bu, n);
+  CFD_ALLOC(plan->bv, n);
+  CFD_ALLOC(plan->spec, n / 2);
+#undef CFD_ALLOC
+
+  std::vector<float> lamx = laplacian_eigenvalues(nx, cfg->hx, nx);
+  std::vector<float> lamy = laplacian_eigenvalues(ny, cfg->hy, ny / 2 + 1);
+  std::vector<float2> twx = twiddles(nx), twy = twiddles(ny);
+  if ((e = upload(&plan->lamx, lamx.data(), lamx.size())) != cudaSuccess ||
+      (e = upload(&plan->lamy, lamy.data(), lamy.size())) != cudaSuccess ||
+      (e = upload(&plan->twx, twx.data(), twx.size())) != cudaSuccess ||
+      (e = upload(&plan->twy, twy.data(), twy.size())) != cudaSuccess) {
+    cfd_fvm_plan_destroy(plan);
+    return cuda_fail(e, "cfd_fvm_plan_create: tables");
+  }
+  bytes += (long long)(lamx.size() + lamy.size()) * 4 + (long long)(twx.size() + twy.size()) * 8;
+  p.lamx = plan->lamx;
+  p.lamy = plan->lamy;
+  p.tw_x = plan->twx;
+  p.tw_y = plan->twy;
+
+  if (cfg->const_forcing != CFD_FORCE_NONE) {
+    size_t cu = 0, cv = 0;
+    if (cfg->const_forcing == CFD_FORCE_U_OF_Y) cu = ny;
+    if (cfg->const_forcing == CFD_FORCE_V_OF_X) cv = nx;
+    if (cfg->const_forcing == CFD_FORCE_FULL) cu = cv = n;
+    if (cu && cfg->force_u) {
+      if ((e = upload(&plan->fu, cfg->force_u, cu)) != cudaSuccess) {
+        cfd_fvm_plan_destroy(plan);
+        return cuda_fail(e, "cfd_fvm_plan_create: forcing");
+      }
+      bytes += (long long)cu * 4;
+    }
+    if (cv && cfg->force_v) {
+      if ((e = upload(&plan->fv, cfg->force_v, cv)) != cudaSuccess) {
+        cfd_fvm_plan_destroy(plan);
+        return cuda_fail(e, "cfd_fvm_plan_create: forcing");
+      }
+      bytes += (long long)cv * 4;
+    }
+    if (cfg->const_forcing == CFD_FORCE_U_OF_Y) p.fu_y = plan->fu;
+    if (cfg->const_forcing == CFD_FORCE_V_OF_X) p.fv_x = plan->fv;
+    if (cfg->const_forcing == CFD_FORCE_FULL) {
+      p.fu_full = plan->fu;
+      p.fv_full = plan->fv;
+    }
+  }
+  plan->bytes = bytes;
+  *out = plan;
+  return CFD_OK;
+}
+
+long long cfd_fvm_plan_bytes(const cfd_fvm_plan* plan) { return plan ? plan->bytes : 0; }
+
+static int fvm_pressure(cfd_fvm_plan* plan, cudaStream_t s, const float* us,
+                        const float* vs) {
+  CFD_CHECK(cfd::launch_fvm_div_rfft(plan->p, us, vs, plan->spec, s), "div_rfft");
+  CFD_CHECK(cfd::launch_fvm_col_pinv(plan->p, plan->spec, s), "col_pinv");
+  CFD_CHECK(cfd::launch_fvm_irfft(plan->p, plan->spec, s), "irfft");
+  return CFD_OK;
+}
+
+int cfd_fvm_step(cfd_fvm_plan* plan, void* stream, const float* u,
+                 const float* v, float* u_out, float* v_out, int steps) {
+  if (!plan || !u || !v || !u_out || !v_out)
+    return fail(CFD_ERR_INVALID_ARGUMENT, "cfd_fvm_step: null pointer");
+  if (steps < 0) return fail(CFD_ERR_INVALID_ARGUMENT, "cfd_fvm_step: steps < 0");
+  cudaStream_t s = as_stream(stream);
+  const cfd::FvmParams& p = plan->p;
+  const size_t bytes = (size_t)p.nx * p.ny * sizeof(float);
+  if (steps == 0) {
+    if (u_out != u) CFD_CHECK(cudaMemcpyAsync(u_out, u, bytes, cudaMemcpyDeviceToDevice, s), "copy");
+    if (v_out != v) CFD_CHECK(cudaMemcpyAsync(v_out, v, bytes, cudaMemcpyDeviceToDevice, s), "copy");
+    return CFD_OK;
+  }
+  float *au = plan->au, *av = plan->av, *bu = plan->bu, *bv = plan->bv;
+  const float* q = reinterpret_cast<const float*>(plan->spec);
+  CFD_CHECK(cfd::launch_fvm_explicit(p, false, false, u, v, nullptr, au, av, s), "explicit");
+  int rc = fvm_pressure(plan, s, au, av);
+  if (rc) return rc;
+  for (int k = 1; k < steps; ++k) {
+    CFD_CHECK(cfd::launch_fvm_explicit(p, true, false, au, av, q, bu, bv, s), "explicit");
+    rc = fvm_pressure(plan, s, bu, bv);
+    if (rc) return rc;
+    float* t = au; au = bu; bu = t;
+    t = av; av = bv; bv = t;
+  }
+  CFD_CHECK(cfd::launch_fvm_project_out(p, au, av, q, u_out, v_out, s), "project_out");
+  return CFD_OK;
+}
+
+int cfd_fvm_explicit_terms(cfd_fvm_plan* plan, void* stream, const float* u,
+                           const float* v, float* du, float* dv) {
+  if (!plan || !u || !v || !du || !dv)
+    return fail(CFD_ERR_INVALID_ARGUMENT, "cfd_fvm_explicit_terms: null pointer");
+  CFD_CHECK(cfd::launch_fvm_explicit(plan->p, false, true, u, v, nullptr, du, dv,
+                                     as_stream(stream)),
+            "explicit");
+  return CFD_OK;
+}
+
+int cfd_fvm_projection(cfd_fvm_plan* plan, void* stream, const float* u,
+                       const float* v, float* u_out, float* v_out) {
+  if (!plan || !u || !v || !u_out || !v_out)
+    return fail(CFD_ERR_INVALID_ARGUMENT, "cfd_fvm_projection: null pointer");
+  cudaStream_t s = as_stream(stream);
+  int rc = fvm_pressure(plan, s, u, v);
+  if (rc) return rc;
+  CFD_CHECK(cfd::launch_fvm_project_out(plan->p, u, v,
+                                        reinterpret_cast<const float*>(plan->spec),
+                                        u_out, v_out, s),
+            "project_out");
+  return CFD_OK;
+}
+
+int cfd_fvm_pressure_solve(cfd_fvm_plan* plan, void* stream, const float* u,
+                           const float* v, float* q) {
+  if (!plan || !u || !v || !q)
+    return fail(CFD_ERR_INVALID_ARGUMENT, "cfd_fvm_pressure_solve: null pointer");
+  cudaStream_t s = as_stream(stream);
+  int rc = fvm_pressure(plan, s, u, v);
+  if (rc) return rc;
+  CFD_CHECK(cudaMemcpyAsync(q, plan->spec, (size_t)plan->p.nx * plan->p.ny * sizeof(float),
+                            cudaMemcpyDeviceToDevice, s),
+            "copy q");
+  return CFD_OK;
+}
+
+int cfd_fvm_divergence(cfd_fvm_plan* plan, void* stream, const float* u,
+                       const float* v, float* out) {
+  if (!plan || !u || !v || !out)
+    return fail(CFD_ERR_INVALID_ARGUMENT, "cfd_fvm_divergence: null pointer");
+  CFD_CHECK(cfd::launch_divergence(plan->p, u, v, out, as_stream(stream)), "divergence");
+  return CFD_OK;
+}
+
+int cfd_fvm_curl_2d(cfd_fvm_plan* plan, void* stream, const float* u,
+                    const float* v, float* out) {
+  if (!plan || !u || !v || !out)
+    return fail(CFD_ERR_INVALID_ARGUMENT, "cfd_fvm_curl_2d: null pointer");
+  CFD_CHECK(cfd::launch_curl2d(plan->p, u, v, out, as_stream(stream)), "curl_2d");
+  return CFD_OK;
+}
+
+int cfd_max_speed(void* stream, int n, const float* u, const float* v, float* out) {
+  if (n <= 0 || !u || !v || !out)
+    return fail(CFD_ERR_INVALID_ARGUMENT, "cfd_max_speed: bad arguments");
+  CFD_CHECK(cfd::launch_max_speed(n, u, v, reinterpret_cast<unsigned int*>(out),
+                                  as_stream(stream)),
+            "max_speed");
+  return CFD_OK;
+}
+
+}  // extern "C"
+
+namespace {
+__global__ void scale_to_max_kernel(int n, float* u, float* v, const float* vmax,
+                                    float maxv) {
+  const float m = *vmax;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    u[i] = (maxv * u[i]) / m;
+    v[i] = (maxv * v[i]) / m;
+  }
+}
+}  // namespace
+
+extern "C" {
+
+int cfd_scale_to_max_speed(void* stream, int n, float* u, float* v,
+                           const float* vmax, double maximum_velocity) {
+  if (n <= 0 || !u || !v || !vmax)
+    return fail(CFD_ERR_INVALID_ARGUMENT, "cfd_scale_to_max_speed: bad arguments");
+  int blocks = (n + 255) / 256;
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  scale_to_max_kernel<<<blocks, 256, 0, as_stream(stream)>>>(n, u, v, vmax,
+                                                             (float)maximum_velocity);
+  CFD_CHECK(cudaGetLastError(), "scale_to_max_speed");
+  return CFD_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Spectral plan
+// ---------------------------------------------------------------------------
+int cfd_spec_plan_destroy(cfd_spec_plan* plan) {
+  if (!plan) return CFD_OK;
+  void* ptrs[] = {plan->t4[0], plan->t4[1], plan->t4[2], plan->t4[3], plan->ahat,
+                  plan->h, plan->fc, plan->work, plan->twx, plan->twy, plan->kx,
+                  plan->ky};
+  for (void* q : ptrs)
+    if (q) cudaFree(q);
+  delete plan;
+  return CFD_OK;
+}
+
+int cfd_spec_plan_create(const cfd_spec_config* cfg, cfd_spec_plan** out) {
+  if (!cfg || !out) return fail(CFD_ERR_INVALID_ARGUMENT, "null config or output pointer");
+  *out = nullptr;
+  if (!valid_size(cfg->nx) || !valid_size(cfg->ny))
+    return fail(CFD_ERR_UNSUPPORTED, "grid shape must be powers of two in [4, 4096]");
+  if (cfg->num_stages < 1 || cfg->num_stages > 8 || !cfg->alphas || !cfg->betas || !cfg->gammas)
+    return fail(CFD_ERR_INVALID_ARGUMENT, "num_stages must be in [1, 8] with coefficient arrays");
+  if (!(cfg->hx > 0) || !(cfg->hy > 0))
+    return fail(CFD_ERR_INVALID_ARGUMENT, "invalid grid step");
+  cfd_spec_plan* plan = new cfd_spec_plan();
+  cfd::SpecParams& p = plan->p;
+  std::memset(&p, 0, sizeof(p));
+  const int nx = cfg->nx, ny = cfg->ny;
+  p.nx = nx;
+  p.ny = ny;
+  p.L = ny / 2;
+  p.log2nx = ilog2(nx);
+  p.log2ny = ilog2(ny);
+  p.log2L = p.log2ny - 1;
+  p.dn_x = (float)(cfg->hx * nx);
+  p.dn_y = (float)(cfg->hy * ny);
+  p.two_pi = (float)(2.0 * M_PI);
+  p.lap_coef = (float)(-4.0 * M_PI * M_PI);
+  p.nu = (float)cfg->viscosity;
+  p.drag = (float)cfg->drag;
+  p.scale = 1.f / ((float)nx * (float)ny);
+  p.filt_on = cfg->smooth ? 1 : 0;
+  // brick_wall_filter_2d: rows [: int(2/3 n) // 2] and [-int(2/3 n) // 2 :]
+  // (Python floor division of the negated int), cols [: int(2/3 (m//2+1))].
+  {
+    const int a = (int)(2.0 / 3.0 * nx);
+    p.filt_lo = a / 2;
+    const int neg = -a;
+    const int start = (neg >= 0) ? neg / 2 : -((-neg + 1) / 2);  // floor(-a / 2)
+    p.filt_hi = nx + start;
+    p.filt_cols = (int)(2.0 / 3.0 * (ny / 2 + 1));
+  }
+  plan->stages = cfg->num_stages;
+  for (int k = 0; k < cfg->num_stages; ++k) {
+    cfd::StageCoef& c = plan->coef[k];
+    c.beta = (float)cfg->betas[k];
+    c.gdt = (float)(cfg->gammas[k] * cfg->dt);
+    c.mu = (float)(0.5 * cfg->dt * (cfg->alphas[k + 1] - cfg->alphas[k]));
+    c.has_h_in = (k > 0 && cfg->betas[k] != 0.0) ? 1 : 0;
+    c.write_h = (k + 1 < cfg->num_stages) ? 1 : 0;
+    c.prep_next = 1;
+    c.explicit_only = 0;
+  }
+  const size_t ns = (size_t)nx * (p.L + 1);
+  cudaError_t e;
+  long long bytes = 0;
+#define CFD_ALLOC(ptr, count)                                              \
+  do {                                                                     \
+    e = cudaMalloc((void**)&(ptr), (count) * sizeof(*(ptr)));              \
+    if (e != cudaSuccess) {                                                \
+      cfd_spec_plan_destroy(plan);                                         \
+      return cuda_fail(e, "cfd_spec_plan_create: cudaMalloc");             \
+    }                                                                      \
+    bytes += (long long)((count) * sizeof(*(ptr)));                        \
+  } while (0)
+  for (int f = 0; f < 4; ++f) CFD_ALLOC(plan->t4[f], ns);
+  CFD_ALLOC(plan->ahat, ns);
+  CFD_ALLOC(plan->h, ns);
+  CFD_ALLOC(plan->work, ns);
+#undef CFD_ALLOC
+  std::vector<float2> twx = twiddles(nx), twy = twiddles(ny);
+  // fftfreq(n, d) / rfftfreq(n, d): float32 ordinals divided by float32(d*n)
+  // (grids.py:618-658 via jnp.fft.fftfreq).
+  std::vector<float> kxt(nx), kyt(p.L + 1);
+  for (int k = 0; k < nx; ++k) kxt[k] = (float)(k < nx / 2 ? k : k - nx) / p.dn_x;
+  for (int k = 0; k <= p.L; ++k) kyt[k] = (float)k / p.dn_y;
+  if ((e = upload(&plan->twx, twx.data(), twx.size())) != cudaSuccess ||
+      (e = upload(&plan->twy, twy.data(), twy.size())) != cudaSuccess ||
+      (e = upload(&plan->kx, kxt.data(), kxt.size())) != cudaSuccess ||
+      (e = upload(&plan->ky, kyt.data(), kyt.size())) != cudaSuccess) {
+    cfd_spec_plan_destroy(plan);
+    return cuda_fail(e, "cfd_spec_plan_create: tables");
+  }
+  bytes += (long long)(twx.size() + twy.size()) * 8 + (long long)(kxt.size() + kyt.size()) * 4;
+  p.tw_x = plan->twx;
+  p.tw_y = plan->twy;
+  p.kx = plan->kx;
+  p.ky = plan->ky;
+  plan->bytes = bytes;
+  *out = plan;
+  return CFD_OK;
+}
+
+long long cfd_spec_plan_bytes(const cfd_spec_plan* plan) { return plan ? plan->bytes : 0; }
+
+int cfd_rfft2(cfd_spec_plan* plan, void* stream, const float* x, float* xhat) {
+  if (!plan || !x || !xhat) return fail(CFD_ERR_INVALID_ARGUMENT, "cfd_rfft2: null pointer");
+  cudaStream_t s = as_stream(stream);
+  float2* X = reinterpret_cast<float2*>(xhat);
+  CFD_CHECK(cfd::launch_row_rfft(plan->p, x, X, s), "row_rfft");
+  CFD_CHECK(cfd::launch_col_fft(plan->p, X, -1, nullptr, s), "col_fft");
+  return CFD_OK;
+}
+
+int cfd_irfft2(cfd_spec_plan* plan, void* stream, const float* xhat, float* x) {
+  if (!plan || !x || !xhat) return fail(CFD_ERR_INVALID_ARGUMENT, "cfd_irfft2: null pointer");
+  cudaStream_t s = as_stream(stream);
+  const size_t ns = (size_t)plan->p.nx * (plan->p.L + 1);
+  CFD_CHECK(cudaMemcpyAsync(plan->work, xhat, ns * sizeof(float2), cudaMemcpyDeviceToDevice, s),
+            "copy");
+  CFD_CHECK(cfd::launch_col_fft(plan->p, plan->work, 1, nullptr, s), "col_ifft");
+  CFD_CHECK(cfd::launch_row_irfft(plan->p, plan->work, x, plan->p.scale, s), "row_irfft");
+  return CFD_OK;
+}
+
+int cfd_spectral_filter(cfd_spec_plan* plan, void* stream, const float* x,
+                        const float* table, float* out) {
+  if (!plan || !x || !table || !out)
+    return fail(CFD_ERR_INVALID_ARGUMENT, "cfd_spectral_filter: null pointer");
+  cudaStream_t s = as_stream(stream);
+  CFD_CHECK(cfd::launch_row_rfft(plan->p, x, plan->work, s), "row_rfft");
+  CFD_CHECK(cfd::launch_col_fft(plan->p, plan->work, -1, table, s), "col_fft");
+  CFD_CHECK(cfd::launch_col_fft(plan->p, plan->work, 1, nullptr, s), "col_ifft");
+  CFD_CHECK(cfd::launch_row_irfft(plan->p, plan->work, out, plan->p.scale, s), "row_irfft");
+  return CFD_OK;
+}
+
+int cfd_spec_set_forcing(cfd_spec_plan* plan, void* stream, const float* fx,
+                         const float* fy) {
+  if (!plan) return fail(CFD_ERR_INVALID_ARGUMENT, "cfd_spec_set_forcing: null plan");
+  cudaStream_t s = as_stream(stream);
+  cfd::SpecParams& p = plan->p;
+  p.fc_full = nullptr;
+  p.fc_row0 = nullptr;
+  if (plan->fc) {
+    cudaFree(plan->fc);
+    plan->fc = nullptr;
+  }
+  if (!fx && !fy) return CFD_OK;
+  const size_t ns = (size_t)p.nx * (p.L + 1);
+  float2 *fxh = plan->t4[0], *fyh = plan->t4[1];
+  if (fx) {
+    int rc = cfd_rfft2(plan, stream, fx, reinterpret_cast<float*>(fxh));
+    if (rc) return rc;
+  } else {
+    CFD_CHECK(cudaMemsetAsync(fxh, 0, ns * sizeof(float2), s), "memset");
+  }
+  if (fy) {
+    int rc = cfd_rfft2(plan, stream, fy, reinterpret_cast<float*>(fyh));
+    if (rc) return rc;
+  } else {
+    CFD_CHECK(cudaMemsetAsync(fyh, 0, ns * sizeof(float2), s), "memset");
+  }
+  float2* table = nullptr;
+  CFD_CHECK(cudaMalloc((void**)&table, ns * sizeof(float2)), "cfd_spec_set_forcing: cudaMalloc");
+  int rc = CFD_OK;
+  cudaError_t e = cfd::launch_spec_curl_table(p, fxh, fyh, table, s);
+  std::vector<float2> host(ns);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(host.data(), table, ns * sizeof(float2), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) {
+    cudaFree(table);
+    return cuda_fail(e, "cfd_spec_set_forcing");
+  }
+  bool row0_only = true;
+  for (size_t g = (size_t)(p.L + 1); g < ns && row0_only; ++g)
+    if (host[g].x != 0.f || host[g].y != 0.f) row0_only = false;
+  if (row0_only) {
+    // Keep only row kx = 0: the x-transform of an x-independent field.
+    float2* row = nullptr;
+    e = cudaMalloc((void**)&row, (p.L + 1) * sizeof(float2));
+    if (e == cudaSuccess)
+      e = cudaMemcpy(row, host.data(), (p.L + 1) * sizeof(float2), cudaMemcpyHostToDevice);
+    cudaFree(table);
+    if (e != cudaSuccess) return cuda_fail(e, "cfd_spec_set_forcing");
+    plan->fc = row;
+    p.fc_row0 = row;
+  } else {
+    plan->fc = table;
+    p.fc_full = table;
+  }
+  return rc;
+}
+
+int cfd_spec_step(cfd_spec_plan* plan, void* stream, const float* w_in,
+                  float* w_out, int steps) {
+  if (!plan || !w_in || !w_out) return fail(CFD_ERR_INVALID_ARGUMENT, "cfd_spec_step: null pointer");
+  if (steps < 0) return fail(CFD_ERR_INVALID_ARGUMENT, "cfd_spec_step: steps < 0");
+  cudaStream_t s = as_stream(stream);
+  const cfd::SpecParams& p = plan->p;
+  const size_t ns = (size_t)p.nx * (p.L + 1);
+  float2* w = reinterpret_cast<float2*>(w_out);
+  if (w_out != w_in)
+    CFD_CHECK(cudaMemcpyAsync(w_out, w_in, ns * sizeof(float2), cudaMemcpyDeviceToDevice, s),
+              "copy");
+  if (steps == 0) return CFD_OK;
+  CFD_CHECK(cfd::launch_spec_col_prep(p, w, plan->t4, s), "col_prep");
+  for (int st = 0; st < steps; ++st) {
+    for (int k = 0; k < plan->stages; ++k) {
+      CFD_CHECK(cfd::launch_spec_row(p, plan->t4, plan->ahat, s), "row");
+      cfd::StageCoef c = plan->coef[k];
+      c.prep_next = (st + 1 == steps && k + 1 == plan->stages) ? 0 : 1;
+      CFD_CHECK(cfd::launch_spec_col_update(p, c, plan->ahat, w, plan->h, plan->t4, s),
+                "col_update");
+    }
+  }
+  return CFD_OK;
+}
+
+int cfd_spec_explicit_terms(cfd_spec_plan* plan, void* stream, const float* w,
+                            float* out) {
+  if (!plan || !w || !out) return fail(CFD_ERR_INVALID_ARGUMENT, "cfd_spec_explicit_terms: null pointer");
+  cudaStream_t s = as_stream(stream);
+  const cfd::SpecParams& p = plan->p;
+  CFD_CHECK(cfd::launch_spec_col_prep(p, reinterpret_cast<const float2*>(w), plan->t4, s),
+            "col_prep");
+  CFD_CHECK(cfd::launch_spec_row(p, plan->t4, plan->ahat, s), "row");
+  cfd::StageCoef c{};
+  c.explicit_only = 1;
+  CFD_CHECK(cfd::launch_spec_col_update(p, c, plan->ahat, reinterpret_cast<float2*>(out),
+                                        plan->h, plan->t4, s),
+            "col_update");
+  return CFD_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,31 @@
+// Shared helpers for the jax-cfd GB300 kernels (sm_103a).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#define CFD_HD __host__ __device__ __forceinline__
+#define CFD_D __device__ __forceinline__
+
+// Complex numbers are interleaved float2 (the complex64 layout of the
+// reference's rfftn output).
+CFD_D float2 c_add(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+CFD_D float2 c_sub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+CFD_D float2 c_conj(float2 a) { return make_float2(a.x, -a.y); }
+CFD_D float2 c_scale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+CFD_D float2 c_mul(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+// Multiply by SIGN * i (SIGN = -1 gives -i, the forward-transform rotation).
+template <int SIGN>
+CFD_D float2 c_mul_i(float2 a) {
+  return SIGN < 0 ? make_float2(a.y, -a.x) : make_float2(-a.y, a.x);
+}
+
+CFD_HD int ilog2(int x) {
+  int r = 0;
+  while ((1 << r) < x) ++r;
+  return r;
+}
+
+CFD_HD bool is_pow2(int x) { return x > 0 && (x & (x - 1)) == 0; }

@@ -1,0 +1,495 @@
+// Staggered MAC-grid (FVM) kernels: the explicit Van Leer/diffusion/forcing
+// stencil, and the real-FFT fast-diagonalisation pressure projection.
+//
+// One forward-Euler step of semi_implicit_navier_stokes
+// (jax_cfd/base/equations.py:120-151, time_stepping.py:59-119) runs as
+//   explicit   (u, v) [or (u*, v*, q) projected on the fly] -> (u*, v*)
+//   div_rfft   (u*, v*) -> D^ rows            (backward-difference divergence
+//                                              + real FFT along contiguous y)
+//   col_pinv   D^ -> q^ (FFT along x, * pinv(lambda), inverse FFT along x)
+//   irfft      q^ -> q  (inverse real FFT along y, in place)
+// and the projection u = u* - forward_difference(q) is folded into the next
+// step's stencil load, or into project_out at the end of a chunk.
+//
+// The half spectrum of a row of M reals is stored "packed" as M/2 complex
+// numbers: element 0 holds (X[0], X[M/2]), both real.  The x-axis transform
+// of that packed column is untangled with the two-real-signals identity.
+#include "fft.cuh"
+#include "kernels.h"
+
+namespace cfd {
+namespace {
+
+constexpr int kTI = 16;   // stencil tile rows (x)
+constexpr int kTJ = 64;   // stencil tile columns (y, contiguous)
+constexpr int kStencilThreads = 256;
+
+// One face value of apply_tvd_limiter(lax_wendroff, van_leer_limiter) times
+// the face velocity: interpolation.py:96-303 specialised to a forward
+// half-cell interpolation with stencil c[-1], c[0], c[+1], c[+2] along the
+// face normal and face velocity U.
+//   upwind        c_low  = U > 0 ? c0 : c1
+//   lax_wendroff  c_high = U > 0 ? c0 + 0.5(1-C)(c1-c0) : c1 - 0.5(1+C)(c1-c0)
+//   ratio         r = safe_div(U > 0 ? c0-cm : c2-c1, c1-c0)
+//   van Leer      phi = r > 0 ? 2r / (1+r) : 0
+//   face value    c_low - (c_low - c_high) * phi
+// Selecting r before the limiter equals selecting phi after it, because the
+// limiter is applied elementwise.
+CFD_D float tvd_flux(float cm, float c0, float c1, float c2, float U,
+                     float cfl) {
+  const float C = cfl * U;
+  const float d0 = c1 - c0;
+  const bool pos = U > 0.f;
+  const float c_low = pos ? c0 : c1;
+  const float c_high =
+      pos ? c0 + (0.5f * (1.f - C)) * d0 : c1 - (0.5f * (1.f + C)) * d0;
+  const float num = pos ? c0 - cm : c2 - c1;
+  const float den = d0 != 0.f ? d0 : 1.f;
+  const float r = num / den;
+  const float phi = r > 0.f ? (2.f * r) / (1.f + r) : 0.f;
+  const float cf = c_low - (c_low - c_high) * phi;
+  return cf * U;
+}
+
+template <bool PROJECT, bool OUT_K0, int CONVECT>
+__global__ void __launch_bounds__(kStencilThreads)
+    fvm_explicit_kernel(FvmParams p, const float* __restrict__ ua,
+                        const float* __restrict__ va,
+                        const float* __restrict__ q, float* __restrict__ uo,
+                        float* __restrict__ vo) {
+  __shared__ float su[kTI + 4][kTJ + 4];
+  __shared__ float sv[kTI + 4][kTJ + 4];
+  __shared__ float sq[PROJECT ? kTI + 5 : 1][PROJECT ? kTJ + 5 : 1];
+  __shared__ float fx[kTI + 1][kTJ];  // x-face flux of u (offset 1.5, .5)
+  __shared__ float gx[kTI + 1][kTJ];  // x-face flux of v (offset 1, 1)
+  __shared__ float fy[kTI][kTJ + 1];  // y-face flux of u (offset 1, 1)
+  __shared__ float gy[kTI][kTJ + 1];  // y-face flux of v (offset .5, 1.5)
+
+  const int ti = min(kTI, p.nx), tj = min(kTJ, p.ny);
+  const int i0 = blockIdx.y * ti, j0 = blockIdx.x * tj;
+  const int mx = p.nx - 1, my = p.ny - 1;
+  const int tid = threadIdx.x;
+  const size_t ny = (size_t)p.ny;
+
+  if (PROJECT) {
+    // q on rows i0-2 .. i0+ti+2, columns j0-2 .. j0+tj+2.
+    const int bi = ti + 5, bj = tj + 5;
+    for (int idx = tid; idx < bi * bj; idx += kStencilThreads) {
+      const int a = idx / bj, b = idx - a * bj;
+      const int i = (i0 - 2 + a) & mx, j = (j0 - 2 + b) & my;
+      sq[a][b] = __ldg(q + i * ny + j);
+    }
+    __syncthreads();
+  }
+  {
+    // u, v on rows i0-2 .. i0+ti+1, columns j0-2 .. j0+tj+1.  With PROJECT,
+    // u = u* - (q[i+1] - q[i]) / hx and v = v* - (q[j+1] - q[j]) / hy
+    // (pressure.py:193-196, finite_differences.py:117-124).
+    const int bi = ti + 4, bj = tj + 4;
+    for (int idx = tid; idx < bi * bj; idx += kStencilThreads) {
+      const int a = idx / bj, b = idx - a * bj;
+      const int i = (i0 - 2 + a) & mx, j = (j0 - 2 + b) & my;
+      float u = __ldg(ua + i * ny + j);
+      float v = __ldg(va + i * ny + j);
+      if (PROJECT) {
+        u = u - (sq[a + 1][b] - sq[a][b]) / p.hx;
+        v = v - (sq[a][b + 1] - sq[a][b]) / p.hy;
+      }
+      su[a][b] = u;
+      sv[a][b] = v;
+    }
+  }
+  __syncthreads();
+
+  // Faces normal to x: face a sits after cell i = i0 - 1 + a (box row a + 1).
+  for (int idx = tid; idx < (ti + 1) * tj; idx += kStencilThreads) {
+    const int a = idx / tj, b = idx - a * tj;
+    const int c = b + 2;
+    // u's control volume: velocity 0.5 u[i] + 0.5 u[i+1] (interpolation.linear).
+    const float U = 0.5f * su[a + 1][c] + 0.5f * su[a + 2][c];
+    // v's control volume: u interpolated along y to (1, 1).
+    const float Uv = 0.5f * su[a + 1][c] + 0.5f * su[a + 1][c + 1];
+    if (CONVECT == 0) {
+      fx[a][b] = tvd_flux(su[a][c], su[a + 1][c], su[a + 2][c], su[a + 3][c],
+                          U, p.cfl_x);
+      gx[a][b] = tvd_flux(sv[a][c], sv[a + 1][c], sv[a + 2][c], sv[a + 3][c],
+                          Uv, p.cfl_x);
+    } else {
+      fx[a][b] = U * U;
+      gx[a][b] = (0.5f * sv[a + 1][c] + 0.5f * sv[a + 2][c]) * Uv;
+    }
+  }
+  // Faces normal to y: face b sits after cell j = j0 - 1 + b (box col b + 1).
+  for (int idx = tid; idx < ti * (tj + 1); idx += kStencilThreads) {
+    const int a = idx / (tj + 1), b = idx - a * (tj + 1);
+    const int r = a + 2;
+    // u's control volume: v interpolated along x to (1, 1).
+    const float V = 0.5f * sv[r][b + 1] + 0.5f * sv[r + 1][b + 1];
+    // v's control volume: 0.5 v[j] + 0.5 v[j+1].
+    const float Vv = 0.5f * sv[r][b + 1] + 0.5f * sv[r][b + 2];
+    if (CONVECT == 0) {
+      fy[a][b] = tvd_flux(su[r][b], su[r][b + 1], su[r][b + 2], su[r][b + 3],
+                          V, p.cfl_y);
+      gy[a][b] = tvd_flux(sv[r][b], sv[r][b + 1], sv[r][b + 2], sv[r][b + 3],
+                          Vv, p.cfl_y);
+    } else {
+      fy[a][b] = (0.5f * su[r][b + 1] + 0.5f * su[r][b + 2]) * V;
+      gy[a][b] = Vv * Vv;
+    }
+  }
+  __syncthreads();
+
+  // Cell updates (equations.py:102-110, time_stepping.py:89-105).
+  for (int idx = tid; idx < ti * tj; idx += kStencilThreads) {
+    const int a = idx / tj, b = idx - a * tj;
+    const int r = a + 2, c = b + 2;
+    const int i = i0 + a, j = j0 + b;
+    const float u = su[r][c], v = sv[r][c];
+    // -divergence(flux): -((F[i] - F[i-1]) / hx + (F[j] - F[j-1]) / hy)
+    float ku = -((fx[a + 1][b] - fx[a][b]) / p.hx +
+                 (fy[a][b + 1] - fy[a][b]) / p.hy);
+    float kv = -((gx[a + 1][b] - gx[a][b]) / p.hx +
+                 (gy[a][b + 1] - gy[a][b]) / p.hy);
+    if (p.has_visc) {
+      // finite_differences.laplacian: -2c * sum(scales) + pairs * scale
+      const float lu = ((-2.f * u) * p.ssum + (su[r - 1][c] + su[r + 1][c]) * p.sx) +
+                       (su[r][c - 1] + su[r][c + 1]) * p.sy;
+      const float lv = ((-2.f * v) * p.ssum + (sv[r - 1][c] + sv[r + 1][c]) * p.sx) +
+                       (sv[r][c - 1] + sv[r][c + 1]) * p.sy;
+      ku = ku + p.nu * lu;
+      kv = kv + p.nu * lv;
+    }
+    if (p.has_forcing) {
+      // sum_forcings(linear, constant): (0 + lin * u) + const
+      float fu = 0.f, fv = 0.f;
+      bool any_u = false, any_v = false;
+      if (p.has_lin) {
+        fu = p.lin * u;
+        fv = p.lin * v;
+        any_u = any_v = true;
+      }
+      if (p.fu_y) { fu = any_u ? fu + __ldg(p.fu_y + j) : __ldg(p.fu_y + j); any_u = true; }
+      if (p.fv_x) { fv = any_v ? fv + __ldg(p.fv_x + i) : __ldg(p.fv_x + i); any_v = true; }
+      if (p.fu_full) { const float f = __ldg(p.fu_full + i * ny + j); fu = any_u ? fu + f : f; any_u = true; }
+      if (p.fv_full) { const float f = __ldg(p.fv_full + i * ny + j); fv = any_v ? fv + f : f; any_v = true; }
+      if (!p.rho_is_one) {
+        fu = fu / p.density;
+        fv = fv / p.density;
+      }
+      if (any_u) ku = ku + fu;
+      if (any_v) kv = kv + fv;
+    }
+    if (OUT_K0) {
+      uo[i * ny + j] = ku;
+      vo[i * ny + j] = kv;
+    } else {
+      uo[i * ny + j] = u + p.dt * ku;
+      vo[i * ny + j] = v + p.dt * kv;
+    }
+  }
+}
+
+// Backward-difference divergence of (u*, v*) (finite_differences.py:95-143)
+// followed by the packed real FFT of each row along y.
+__global__ void __launch_bounds__(256, 2) fvm_div_rfft_kernel(FvmParams p, int rows,
+                                    const float* __restrict__ us,
+                                    const float* __restrict__ vs,
+                                    float2* __restrict__ spec) {
+  extern __shared__ float2 sbuf[];
+  const int L = p.ny >> 1, log2L = p.log2ny - 1;
+  const int i0 = blockIdx.x * rows;
+  const int mx = p.nx - 1, my = p.ny - 1;
+  const size_t ny = (size_t)p.ny;
+  float* sd = reinterpret_cast<float*>(sbuf);
+  for (int idx = threadIdx.x; idx < rows * p.ny; idx += blockDim.x) {
+    const int r = idx >> p.log2ny, j = idx & my;
+    const int i = i0 + r, im = (i - 1) & mx, jm = (j - 1) & my;
+    const float dx = (__ldg(us + i * ny + j) - __ldg(us + im * ny + j)) / p.hx;
+    const float dy = (__ldg(vs + i * ny + j) - __ldg(vs + i * ny + jm)) / p.hy;
+    sd[idx] = dx + dy;
+  }
+  __syncthreads();
+  fft_inplace<-1>(sbuf, log2L, rows, L, p.tw_y, p.log2ny, threadIdx.x);
+  const int half = L >> 1;
+  for (int idx = threadIdx.x; idx < rows * (half + 1); idx += blockDim.x) {
+    const int r = idx / (half + 1), k = idx - r * (half + 1);
+    float2* out = spec + (size_t)(i0 + r) * L;
+    const float2* z = sbuf + r * L;
+    if (k == 0) {
+      const float2 z0 = z[0];
+      out[0] = make_float2(z0.x + z0.y, z0.x - z0.y);
+    } else {
+      float2 xk, xm;
+      rfft_post_pair(z[k], z[L - k], __ldg(p.tw_y + k), &xk, &xm);
+      out[k] = xk;
+      if (k != L - k) out[L - k] = xm;
+    }
+  }
+}
+
+// Pseudoinverse of the periodic Laplacian in the rfft basis
+// (fast_diagonalization.py:199-266): 1/lambda where |lambda| > cutoff, else 0,
+// with irfftn's 1/(nx*ny) folded in (a power of two, so exact).
+CFD_D float pinv_diag(const FvmParams& p, int kx, int ky) {
+  const float lam = __ldg(p.lamx + kx) + __ldg(p.lamy + ky);
+  return fabsf(lam) > p.cutoff ? p.pinv_scale / lam : 0.f;
+}
+
+__global__ void __launch_bounds__(512, 1) fvm_col_pinv_kernel(FvmParams p, int W, int log2W, int bstride,
+                                    float2* __restrict__ spec) {
+  extern __shared__ float2 sbuf[];
+  const int L = p.ny >> 1, N = p.nx;
+  const int c0 = blockIdx.x * W;
+  const int tid = threadIdx.x;
+  for (int idx = tid; idx < W * N; idx += blockDim.x) {
+    const int w = idx & (W - 1), i = idx >> log2W;
+    sbuf[w * bstride + i] = spec[(size_t)i * L + c0 + w];
+  }
+  __syncthreads();
+  fft_inplace<-1>(sbuf, p.log2nx, W, bstride, p.tw_x, p.log2nx, tid);
+  for (int idx = tid; idx < W * N; idx += blockDim.x) {
+    const int w = idx & (W - 1), kx = idx >> log2W;
+    const int c = c0 + w;
+    if (c == 0) continue;
+    float2* e = sbuf + w * bstride + kx;
+    *e = c_scale(*e, pinv_diag(p, kx, c));
+  }
+  if (c0 == 0) {
+    // Packed column: Z = A + iB with A, B the x-transforms of the DC and
+    // Nyquist columns.  Z' = d0 A + i dN B
+    //                      = (d0 + dN)/2 Z[k] + (d0 - dN)/2 conj Z[-k].
+    for (int k = tid; k <= N / 2; k += blockDim.x) {
+      const int m = (N - k) & (N - 1);
+      const float d0 = pinv_diag(p, k, 0), dn = pinv_diag(p, k, L);
+      const float al = 0.5f * (d0 + dn), be = 0.5f * (d0 - dn);
+      const float2 zk = sbuf[k], zm = sbuf[m];
+      sbuf[k] = c_add(c_scale(zk, al), c_scale(c_conj(zm), be));
+      if (m != k) sbuf[m] = c_add(c_scale(zm, al), c_scale(c_conj(zk), be));
+    }
+  }
+  __syncthreads();
+  fft_inplace<1>(sbuf, p.log2nx, W, bstride, p.tw_x, p.log2nx, tid);
+  for (int idx = tid; idx < W * N; idx += blockDim.x) {
+    const int w = idx & (W - 1), i = idx >> log2W;
+    spec[(size_t)i * L + c0 + w] = sbuf[w * bstride + i];
+  }
+}
+
+// Inverse packed real FFT of each row, in place: q^ rows -> q rows (floats).
+__global__ void __launch_bounds__(256, 2) fvm_irfft_kernel(FvmParams p, int rows, float2* spec) {
+  extern __shared__ float2 sbuf[];
+  const int L = p.ny >> 1, log2L = p.log2ny - 1;
+  const int i0 = blockIdx.x * rows;
+  const int half = L >> 1;
+  for (int idx = threadIdx.x; idx < rows * (half + 1); idx += blockDim.x) {
+    const int r = idx / (half + 1), k = idx - r * (half + 1);
+    const float2* in = spec + (size_t)(i0 + r) * L;
+    float2* z = sbuf + r * L;
+    if (k == 0) {
+      const float2 x0 = in[0];
+      z[0] = make_float2(x0.x + x0.y, x0.x - x0.y);
+    } else {
+      float2 zk, zm;
+      irfft_pre_pair(in[k], in[L - k], __ldg(p.tw_y + k), &zk, &zm);
+      z[k] = zk;
+      if (k != L - k) z[L - k] = zm;
+    }
+  }
+  __syncthreads();
+  fft_inplace<1>(sbuf, log2L, rows, L, p.tw_y, p.log2ny, threadIdx.x);
+  for (int idx = threadIdx.x; idx < rows * L; idx += blockDim.x) {
+    const int r = idx >> log2L, n = idx & (L - 1);
+    spec[(size_t)(i0 + r) * L + n] = sbuf[r * L + n];
+  }
+}
+
+// u = u* - (q[i+1] - q[i]) / hx ; v = v* - (q[j+1] - q[j]) / hy.
+__global__ void fvm_project_out_kernel(FvmParams p, const float* __restrict__ us,
+                                       const float* __restrict__ vs,
+                                       const float* __restrict__ q,
+                                       float* __restrict__ uo,
+                                       float* __restrict__ vo) {
+  const size_t n = (size_t)p.nx * p.ny;
+  const int mx = p.nx - 1, my = p.ny - 1;
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < n;
+       idx += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(idx >> p.log2ny), j = (int)(idx & my);
+    const float q0 = __ldg(q + idx);
+    const float qx = __ldg(q + (size_t)((i + 1) & mx) * p.ny + j);
+    const float qy = __ldg(q + (size_t)i * p.ny + ((j + 1) & my));
+    uo[idx] = __ldg(us + idx) - (qx - q0) / p.hx;
+    vo[idx] = __ldg(vs + idx) - (qy - q0) / p.hy;
+  }
+}
+
+__global__ void divergence_kernel(FvmParams p, const float* __restrict__ u,
+                                  const float* __restrict__ v,
+                                  float* __restrict__ out) {
+  const size_t n = (size_t)p.nx * p.ny;
+  const int mx = p.nx - 1, my = p.ny - 1;
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < n;
+       idx += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(idx >> p.log2ny), j = (int)(idx & my);
+    const float dx = (__ldg(u + idx) - __ldg(u + (size_t)((i - 1) & mx) * p.ny + j)) / p.hx;
+    const float dy = (__ldg(v + idx) - __ldg(v + (size_t)i * p.ny + ((j - 1) & my))) / p.hy;
+    out[idx] = dx + dy;
+  }
+}
+
+// curl_2d (finite_differences.py:186-193): forward_difference(v, x) -
+// forward_difference(u, y), located at offset (1, 1).
+__global__ void curl2d_kernel(FvmParams p, const float* __restrict__ u,
+                              const float* __restrict__ v,
+                              float* __restrict__ out) {
+  const size_t n = (size_t)p.nx * p.ny;
+  const int mx = p.nx - 1, my = p.ny - 1;
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < n;
+       idx += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(idx >> p.log2ny), j = (int)(idx & my);
+    const float dvx = (__ldg(v + (size_t)((i + 1) & mx) * p.ny + j) - __ldg(v + idx)) / p.hx;
+    const float duy = (__ldg(u + (size_t)i * p.ny + ((j + 1) & my)) - __ldg(u + idx)) / p.hy;
+    out[idx] = dvx - duy;
+  }
+}
+
+// max over cells of sqrt(u^2 + v^2); non-negative floats order like their
+// bit patterns, so an unsigned atomicMax on the bits is exact.
+__global__ void max_speed_kernel(int n, const float* __restrict__ u,
+                                 const float* __restrict__ v,
+                                 unsigned int* __restrict__ out) {
+  float m = 0.f;
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n;
+       idx += gridDim.x * blockDim.x) {
+    const float a = __ldg(u + idx), b = __ldg(v + idx);
+    m = fmaxf(m, sqrtf(a * a + b * b));
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, __float_as_uint(m));
+}
+
+int fft_rows_per_block(int log2L, int nrows) {
+  const int P = log2L >= 4 ? 16 : (1 << log2L);
+  int rows = (256 * P) >> log2L;
+  if (rows < 1) rows = 1;
+  if (rows > nrows) rows = nrows;
+  return rows;
+}
+
+int block_threads(int workers) {
+  int t = ((workers + 31) / 32) * 32;
+  return t < 64 ? 64 : t;
+}
+
+template <typename K>
+cudaError_t set_smem(K kernel, size_t bytes) {
+  if (bytes > 48 * 1024)
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)bytes);
+  return cudaSuccess;
+}
+
+}  // namespace
+
+cudaError_t launch_fvm_explicit(const FvmParams& p, bool project, bool out_k0,
+                                const float* ua, const float* va,
+                                const float* q, float* uo, float* vo,
+                                cudaStream_t s) {
+  const int ti = p.nx < kTI ? p.nx : kTI, tj = p.ny < kTJ ? p.ny : kTJ;
+  dim3 grid(p.ny / tj, p.nx / ti);
+#define CFD_EXPLICIT(PR, K0, CV) \
+  fvm_explicit_kernel<PR, K0, CV><<<grid, kStencilThreads, 0, s>>>(p, ua, va, q, uo, vo)
+  if (p.convect == 0) {
+    if (project) {
+      if (out_k0) CFD_EXPLICIT(true, true, 0); else CFD_EXPLICIT(true, false, 0);
+    } else {
+      if (out_k0) CFD_EXPLICIT(false, true, 0); else CFD_EXPLICIT(false, false, 0);
+    }
+  } else {
+    if (project) {
+      if (out_k0) CFD_EXPLICIT(true, true, 1); else CFD_EXPLICIT(true, false, 1);
+    } else {
+      if (out_k0) CFD_EXPLICIT(false, true, 1); else CFD_EXPLICIT(false, false, 1);
+    }
+  }
+#undef CFD_EXPLICIT
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fvm_div_rfft(const FvmParams& p, const float* us,
+                                const float* vs, float2* spec, cudaStream_t s) {
+  const int log2L = p.log2ny - 1;
+  const int rows = fft_rows_per_block(log2L, p.nx);
+  const size_t smem = (size_t)rows * (p.ny / 2) * sizeof(float2);
+  cudaError_t e = set_smem(fvm_div_rfft_kernel, smem);
+  if (e != cudaSuccess) return e;
+  fvm_div_rfft_kernel<<<p.nx / rows, block_threads(fft_workers(log2L, rows)),
+                        smem, s>>>(p, rows, us, vs, spec);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fvm_col_pinv(const FvmParams& p, float2* spec,
+                                cudaStream_t s) {
+  const int L = p.ny / 2;
+  // W columns per block: 32-byte row segments (W = 4) where the 512-thread
+  // cap allows, more columns for short columns.
+  int W = 4096 >> p.log2nx;
+  if (W < 2) W = 2;
+  if (W > L) W = L;
+  const int bstride = p.nx + 4;
+  const size_t smem = (size_t)W * bstride * sizeof(float2);
+  cudaError_t e = set_smem(fvm_col_pinv_kernel, smem);
+  if (e != cudaSuccess) return e;
+  fvm_col_pinv_kernel<<<L / W, block_threads(fft_workers(p.log2nx, W)), smem,
+                        s>>>(p, W, ilog2(W), bstride, spec);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fvm_irfft(const FvmParams& p, float2* spec, cudaStream_t s) {
+  const int log2L = p.log2ny - 1;
+  const int rows = fft_rows_per_block(log2L, p.nx);
+  const size_t smem = (size_t)rows * (p.ny / 2) * sizeof(float2);
+  cudaError_t e = set_smem(fvm_irfft_kernel, smem);
+  if (e != cudaSuccess) return e;
+  fvm_irfft_kernel<<<p.nx / rows, block_threads(fft_workers(log2L, rows)),
+                     smem, s>>>(p, rows, spec);
+  return cudaGetLastError();
+}
+
+static int elementwise_blocks(size_t n) {
+  size_t b = (n + 255) / 256;
+  if (b > 152 * 16) b = 152 * 16;
+  return (int)b;
+}
+
+cudaError_t launch_fvm_project_out(const FvmParams& p, const float* us,
+                                   const float* vs, const float* q, float* uo,
+                                   float* vo, cudaStream_t s) {
+  const size_t n = (size_t)p.nx * p.ny;
+  fvm_project_out_kernel<<<elementwise_blocks(n), 256, 0, s>>>(p, us, vs, q, uo, vo);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_divergence(const FvmParams& p, const float* u,
+                              const float* v, float* out, cudaStream_t s) {
+  const size_t n = (size_t)p.nx * p.ny;
+  divergence_kernel<<<elementwise_blocks(n), 256, 0, s>>>(p, u, v, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_curl2d(const FvmParams& p, const float* u, const float* v,
+                          float* out, cudaStream_t s) {
+  const size_t n = (size_t)p.nx * p.ny;
+  curl2d_kernel<<<elementwise_blocks(n), 256, 0, s>>>(p, u, v, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_max_speed(int n, const float* u, const float* v,
+                             unsigned int* out_bits, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(out_bits, 0, sizeof(unsigned int), s);
+  if (e != cudaSuccess) return e;
+  max_speed_kernel<<<elementwise_blocks((size_t)n), 256, 0, s>>>(n, u, v, out_bits);
+  return cudaGetLastError();
+}
+
+}  // namespace cfd

@@ -1,0 +1,110 @@
+// Internal launch interface between the C ABI (capi.cu) and the kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace cfd {
+
+// Parameters of the staggered-grid (FVM) explicit step, already rounded to
+// float32 the way the reference rounds its weakly typed Python scalars.
+struct FvmParams {
+  int nx, ny;          // grid shape; axis 1 (y, index j) is contiguous
+  int log2nx, log2ny;
+  float hx, hy;        // float32(step)
+  float cfl_x, cfl_y;  // float32(dt / step): Lax-Wendroff Courant factors
+  float dt;            // float32(dt)
+  float nu;            // float32(viscosity / density)
+  float sx, sy, ssum;  // Laplacian scales (1/h)^2 formed in float32
+  float lin;           // linear forcing coefficient
+  float density;
+  int rho_is_one;      // forcing / density is the identity
+  int has_visc;        // viscosity is not None
+  int has_forcing;     // any forcing term
+  int has_lin;         // linear (drag) forcing present
+  int convect;         // 0: Van Leer (TVD Lax-Wendroff), 1: linear
+  const float* fu_y;   // Kolmogorov table for u over j (ny) or null
+  const float* fv_x;   // swapped Kolmogorov table for v over i (nx) or null
+  const float* fu_full;  // general constant forcing fields (nx*ny) or null
+  const float* fv_full;
+  // Pressure solve (fast diagonalisation through the real FFT).
+  const float* lamx;   // eigenvalues of the 1-D Laplacian along x (nx)
+  const float* lamy;   // eigenvalues along y, rfft half (ny/2 + 1)
+  float cutoff;        // 10 * eps(float32)
+  float pinv_scale;    // 1 / (nx * ny), folds irfftn's normalisation
+  const float2* tw_x;  // exp(-2 pi i k / nx), k < nx
+  const float2* tw_y;  // exp(-2 pi i k / ny), k < ny
+};
+
+// Out-of-bounds / configuration errors are reported through return codes.
+cudaError_t launch_fvm_explicit(const FvmParams& p, bool project, bool out_k0,
+                                const float* ua, const float* va,
+                                const float* q, float* uo, float* vo,
+                                cudaStream_t s);
+cudaError_t launch_fvm_div_rfft(const FvmParams& p, const float* us,
+                                const float* vs, float2* spec, cudaStream_t s);
+cudaError_t launch_fvm_col_pinv(const FvmParams& p, float2* spec,
+                                cudaStream_t s);
+cudaError_t launch_fvm_irfft(const FvmParams& p, float2* spec, cudaStream_t s);
+cudaError_t launch_fvm_project_out(const FvmParams& p, const float* us,
+                                   const float* vs, const float* q, float* uo,
+                                   float* vo, cudaStream_t s);
+// Diagnostics on staggered velocity fields.
+cudaError_t launch_divergence(const FvmParams& p, const float* u,
+                              const float* v, float* out, cudaStream_t s);
+cudaError_t launch_curl2d(const FvmParams& p, const float* u, const float* v,
+                          float* out, cudaStream_t s);
+cudaError_t launch_max_speed(int n, const float* u, const float* v,
+                             unsigned int* out_bits, cudaStream_t s);
+
+// Pseudospectral vorticity step.
+struct SpecParams {
+  int nx, ny, L;        // L = ny / 2; rfft half spectrum has L + 1 columns
+  int log2nx, log2ny, log2L;
+  float inv_dn_x;       // unused placeholder for alignment
+  float dn_x, dn_y;     // float32(step * n): fftfreq denominators
+  float two_pi;         // float32(2 pi)
+  float lap_coef;       // float32((2 pi i)^2) = -4 pi^2
+  float nu, drag;       // float32 viscosity and drag
+  float scale;          // 1 / (nx * ny)
+  int filt_on;          // apply the 2/3 brick-wall filter
+  int filt_lo, filt_hi, filt_cols;  // rows [0,lo) U [hi,nx), cols [0,cols)
+  const float2* fc_full;  // forcing curl (nx x (L+1)) or null
+  const float2* fc_row0;  // forcing curl only in row kx = 0 ((L+1)) or null
+  const float2* tw_x;
+  const float2* tw_y;
+  const float* kx;      // fftfreq(nx, hx) in float32 (nx)
+  const float* ky;      // rfftfreq(ny, hy) in float32 (L + 1)
+};
+
+struct StageCoef {
+  float beta;     // float32(beta_k), multiplies the previous h
+  float gdt;      // float32(gamma_k * dt)
+  float mu;       // float32(0.5 * dt * (alpha_{k+1} - alpha_k))
+  int has_h_in;   // beta_k != 0 (the first stage adds a Python 0)
+  int write_h;    // a later stage of this step reads h
+  int prep_next;  // build the next stage's column-transformed fields
+  int explicit_only;  // store F(u) into the state buffer instead of updating
+};
+
+cudaError_t launch_spec_col_prep(const SpecParams& p, const float2* w,
+                                 float2* const t4[4], cudaStream_t s);
+cudaError_t launch_spec_row(const SpecParams& p, const float2* const t4[4],
+                            float2* ahat, cudaStream_t s);
+cudaError_t launch_spec_col_update(const SpecParams& p, const StageCoef& c,
+                                   const float2* ahat, float2* w, float2* h,
+                                   float2* const t4[4], cudaStream_t s);
+// Generic 2-D real transforms on the (nx, ny) grid of a spectral plan.
+cudaError_t launch_row_rfft(const SpecParams& p, const float* x, float2* X,
+                            cudaStream_t s);
+cudaError_t launch_row_irfft(const SpecParams& p, const float2* X, float* x,
+                             float scale, cudaStream_t s);
+// Column FFT over the (L+1) half-spectrum columns; sign -1 forward, +1
+// inverse; an optional real table (nx x (L+1)) multiplies the result.
+cudaError_t launch_col_fft(const SpecParams& p, float2* X, int sign,
+                           const float* mult, cudaStream_t s);
+// curl table: 2 pi i (kx * fy_hat - ky * fx_hat)
+cudaError_t launch_spec_curl_table(const SpecParams& p, const float2* fxh,
+                                   const float2* fyh, float2* out,
+                                   cudaStream_t s);
+
+}  // namespace cfd

@@ -1,0 +1,433 @@
+// Pseudospectral NavierStokes2D kernels (jax_cfd/spectral/equations.py:129-220,
+// spectral/utils.py:128-203, spectral/time_stepping.py:117-197).
+//
+// The state is the rfftn of the vorticity, complex64 [nx, ny/2 + 1]
+// (axis 0 = kx, full FFT; axis 1 = ky, half spectrum).  One low-storage
+// Runge-Kutta / Crank-Nicolson stage is two launches:
+//
+//   col pass  (per ky column)  FFT_x of the advection row spectra,
+//             * 2/3 filter, + forcing curl, h = F + beta h,
+//             u = (u + gamma dt h + mu L u) / (1 - mu L);
+//             then, for the next stage, the four x-inverse transforms of
+//             A = psi^, B = kx psi^, C = kx w^, D = w^ (psi^ = -w^/lap).
+//   row pass  (per x row)      apply the ky factors (vx = i ky A, vy = -i B,
+//             gx = i C, gy = i ky D, all times 2 pi), four inverse real
+//             FFTs, advection = -(gx vx + gy vy), forward real FFT.
+//
+// Multiplying by a function of ky commutes with the x transforms, so the ky
+// factors are applied on the row side.  All transforms are unnormalised; the
+// irfftn 1/(nx*ny) is a power of two applied once to the product.
+#include "fft.cuh"
+#include "kernels.h"
+
+namespace cfd {
+namespace {
+
+// fftfreq / rfftfreq ordinals over float32(step * n) (grids.py:618-658),
+// tabulated on the host in float32 exactly as jnp computes them.
+CFD_D float kx_of(const SpecParams& p, int k) { return __ldg(p.kx + k); }
+CFD_D float ky_of(const SpecParams& p, int k) { return __ldg(p.ky + k); }
+
+// Brick-wall 2/3 filter (spectral/utils.py:128-134).
+CFD_D float filt(const SpecParams& p, int kx, int c) {
+  const bool row = kx < p.filt_lo || kx >= p.filt_hi;
+  return (row && c < p.filt_cols) ? 1.f : 0.f;
+}
+
+// The four column-transformed inputs of the explicit terms for element
+// (kx, c) of the state u.
+CFD_D float2 prep_factor(const SpecParams& p, int f, int kx, int c, float2 u) {
+  const float kxf = kx_of(p, kx), kyf = ky_of(p, c);
+  if (f == 3) return u;
+  const float ax = p.two_pi * kxf;
+  if (f == 2) return make_float2(ax * u.x, ax * u.y);
+  // vorticity_to_velocity: laplace = (2 pi i)^2 (|kx|^2 + |ky|^2), [0,0] = 1;
+  // psi = (-1 / laplace) * w.
+  float lap = p.lap_coef * (kxf * kxf + kyf * kyf);
+  if (kx == 0 && c == 0) lap = 1.f;
+  const float pm = -__frcp_rn(lap);  // -1 / lap, correctly rounded
+  const float2 psi = make_float2(pm * u.x, pm * u.y);
+  if (f == 0) return psi;
+  return make_float2(ax * psi.x, ax * psi.y);
+}
+
+// ky-side factors: vx = i ay A, vy = -i B, gx = i C, gy = i ay D.
+CFD_D float2 row_factor(const SpecParams& p, int f, int k, float2 x) {
+  if (f == 1) return make_float2(x.y, -x.x);
+  if (f == 2) return make_float2(-x.y, x.x);
+  const float ay = p.two_pi * ky_of(p, k);
+  return make_float2(-(ay * x.y), ay * x.x);
+}
+
+struct T4 {
+  float2* t[4];
+};
+
+// Column-transformed inputs of the explicit terms: block (x, f) builds field
+// f of columns [x*W, x*W + W) from the state and writes its inverse
+// x-transform.  One transform per block keeps register use at that of a single
+// FFT.
+__global__ void __launch_bounds__(512, 1)
+    spec_col_prep_kernel(SpecParams p, int W, int log2W, int bstride,
+                         const float2* __restrict__ w, T4 t4) {
+  extern __shared__ float2 sbuf[];
+  const int N = p.nx, ncols = p.L + 1;
+  const int c0 = blockIdx.x * W, f = blockIdx.y;
+  const int tid = threadIdx.x;
+  for (int e = tid; e < W * N; e += blockDim.x) {
+    const int ww = e & (W - 1), kx = e >> log2W, c = c0 + ww;
+    sbuf[ww * bstride + kx] =
+        c < ncols ? prep_factor(p, f, kx, c, w[(size_t)kx * ncols + c])
+                  : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
+  fft_inplace<1>(sbuf, p.log2nx, W, bstride, p.tw_x, p.log2nx, tid);
+  float2* dst = t4.t[f];
+  for (int e = tid; e < W * N; e += blockDim.x) {
+    const int ww = e & (W - 1), i = e >> log2W, c = c0 + ww;
+    if (c < ncols) dst[(size_t)i * ncols + c] = sbuf[ww * bstride + i];
+  }
+}
+
+// x-transform of the advection row spectra, then one low-storage RK/CN stage
+// (or, with explicit_only, just F(u)).
+__global__ void __launch_bounds__(512, 1)
+    spec_col_update_kernel(SpecParams p, StageCoef sc, int W, int log2W,
+                           int bstride, const float2* __restrict__ ahat,
+                           float2* __restrict__ wst, float2* __restrict__ hst) {
+  extern __shared__ float2 sbuf[];
+  const int N = p.nx, ncols = p.L + 1;
+  const int c0 = blockIdx.x * W;
+  const int tid = threadIdx.x;
+  for (int e = tid; e < W * N; e += blockDim.x) {
+    const int w = e & (W - 1), i = e >> log2W, c = c0 + w;
+    sbuf[w * bstride + i] =
+        c < ncols ? ahat[(size_t)i * ncols + c] : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
+  fft_inplace<-1>(sbuf, p.log2nx, W, bstride, p.tw_x, p.log2nx, tid);
+  for (int e = tid; e < W * N; e += blockDim.x) {
+    const int w = e & (W - 1), kx = e >> log2W, c = c0 + w;
+    if (c >= ncols) continue;
+    const size_t g = (size_t)kx * ncols + c;
+    // explicit_terms: rfftn(advection) * filter (+ forcing curl)
+    const float2 a = sbuf[w * bstride + kx];
+    float2 F = a;
+    if (p.filt_on) {
+      const float fl = filt(p, kx, c);
+      F = make_float2(a.x * fl, a.y * fl);
+    }
+    if (p.fc_full) F = c_add(F, __ldg(p.fc_full + g));
+    else if (p.fc_row0 && kx == 0) F = c_add(F, __ldg(p.fc_row0 + c));
+    if (sc.explicit_only) {
+      wst[g] = F;
+      continue;
+    }
+    // h = F(u) + beta_k h
+    float2 h = F;
+    if (sc.has_h_in) {
+      const float2 ho = hst[g];
+      h = c_add(F, make_float2(sc.beta * ho.x, sc.beta * ho.y));
+    }
+    // linear_term = nu * laplace - drag; laplace = (2 pi i)^2 |k|^2
+    const float kxf = kx_of(p, kx), kyf = ky_of(p, c);
+    const float lin = p.nu * (p.lap_coef * (kxf * kxf + kyf * kyf)) - p.drag;
+    const float2 u = wst[g];
+    // u + gamma dt h + mu G(u), G(u) = linear_term * u
+    const float2 x = make_float2((u.x + sc.gdt * h.x) + sc.mu * (lin * u.x),
+                                 (u.y + sc.gdt * h.y) + sc.mu * (lin * u.y));
+    // implicit_solve: 1 / (1 - mu * linear_term) * x
+    const float inv = __frcp_rn(1.f - sc.mu * lin);
+    wst[g] = make_float2(inv * x.x, inv * x.y);
+    if (sc.write_h) hst[g] = h;
+  }
+}
+
+__global__ void __launch_bounds__(256, 2) spec_row_kernel(SpecParams p, int rows,
+                                const float2* __restrict__ t0,
+                                const float2* __restrict__ t1,
+                                const float2* __restrict__ t2,
+                                const float2* __restrict__ t3,
+                                float2* __restrict__ ahat) {
+  extern __shared__ float2 sbuf[];
+  const int L = p.L, log2L = p.log2L, ncols = L + 1;
+  const int half = L >> 1;
+  const int i0 = blockIdx.x * rows;
+  const float2* tf[4] = {t0, t1, t2, t3};
+  // Inverse real transforms along y: build the half-length complex inputs.
+  for (int idx = threadIdx.x; idx < rows * 4 * (half + 1); idx += blockDim.x) {
+    const int rf = idx / (half + 1), k = idx - rf * (half + 1);
+    const int r = rf >> 2, f = rf & 3;
+    const float2* in = tf[f] + (size_t)(i0 + r) * ncols;
+    float2* z = sbuf + rf * L;
+    if (k == 0) {
+      const float2 x0 = row_factor(p, f, 0, in[0]);
+      const float2 xl = row_factor(p, f, L, in[L]);
+      z[0] = make_float2(x0.x + xl.x, x0.x - xl.x);
+    } else {
+      const float2 xk = row_factor(p, f, k, in[k]);
+      const float2 xm = row_factor(p, f, L - k, in[L - k]);
+      float2 zk, zm;
+      irfft_pre_pair(xk, xm, __ldg(p.tw_y + k), &zk, &zm);
+      z[k] = zk;
+      if (k != L - k) z[L - k] = zm;
+    }
+  }
+  __syncthreads();
+  fft_inplace<1>(sbuf, log2L, rows * 4, L, p.tw_y, p.log2ny, threadIdx.x);
+  // advection = -(gx * vx + gy * vy), each field scaled by 1/(nx*ny).
+  const float s2 = p.scale * p.scale;
+  for (int idx = threadIdx.x; idx < rows * L; idx += blockDim.x) {
+    const int r = idx >> log2L, n = idx & (L - 1);
+    float2* z = sbuf + (r * 4) * L + n;
+    const float2 vx = z[0], vy = z[L], gx = z[2 * L], gy = z[3 * L];
+    z[0] = make_float2(-(gx.x * vx.x + gy.x * vy.x) * s2,
+                       -(gx.y * vx.y + gy.y * vy.y) * s2);
+  }
+  __syncthreads();
+  fft_inplace<-1>(sbuf, log2L, rows, 4 * L, p.tw_y, p.log2ny, threadIdx.x);
+  for (int idx = threadIdx.x; idx < rows * (half + 1); idx += blockDim.x) {
+    const int r = idx / (half + 1), k = idx - r * (half + 1);
+    const float2* z = sbuf + (r * 4) * L;
+    float2* out = ahat + (size_t)(i0 + r) * ncols;
+    if (k == 0) {
+      const float2 z0 = z[0];
+      out[0] = make_float2(z0.x + z0.y, 0.f);
+      out[L] = make_float2(z0.x - z0.y, 0.f);
+    } else {
+      float2 xk, xm;
+      rfft_post_pair(z[k], z[L - k], __ldg(p.tw_y + k), &xk, &xm);
+      out[k] = xk;
+      if (k != L - k) out[L - k] = xm;
+    }
+  }
+}
+
+// Real rows -> unpacked half spectra (rfft along y).
+__global__ void __launch_bounds__(256, 2) row_rfft_kernel(SpecParams p, int rows, const float* __restrict__ x,
+                                float2* __restrict__ X) {
+  extern __shared__ float2 sbuf[];
+  const int L = p.L, log2L = p.log2L, ncols = L + 1, half = L >> 1;
+  const int i0 = blockIdx.x * rows;
+  float* sd = reinterpret_cast<float*>(sbuf);
+  for (int idx = threadIdx.x; idx < rows * p.ny; idx += blockDim.x)
+    sd[idx] = __ldg(x + (size_t)i0 * p.ny + idx);
+  __syncthreads();
+  fft_inplace<-1>(sbuf, log2L, rows, L, p.tw_y, p.log2ny, threadIdx.x);
+  for (int idx = threadIdx.x; idx < rows * (half + 1); idx += blockDim.x) {
+    const int r = idx / (half + 1), k = idx - r * (half + 1);
+    const float2* z = sbuf + r * L;
+    float2* out = X + (size_t)(i0 + r) * ncols;
+    if (k == 0) {
+      const float2 z0 = z[0];
+      out[0] = make_float2(z0.x + z0.y, 0.f);
+      out[L] = make_float2(z0.x - z0.y, 0.f);
+    } else {
+      float2 xk, xm;
+      rfft_post_pair(z[k], z[L - k], __ldg(p.tw_y + k), &xk, &xm);
+      out[k] = xk;
+      if (k != L - k) out[L - k] = xm;
+    }
+  }
+}
+
+// Unpacked half spectra -> real rows (irfft along y), times `scale`.
+__global__ void __launch_bounds__(256, 2) row_irfft_kernel(SpecParams p, int rows, const float2* __restrict__ X,
+                                 float* __restrict__ x, float scale) {
+  extern __shared__ float2 sbuf[];
+  const int L = p.L, log2L = p.log2L, ncols = L + 1, half = L >> 1;
+  const int i0 = blockIdx.x * rows;
+  for (int idx = threadIdx.x; idx < rows * (half + 1); idx += blockDim.x) {
+    const int r = idx / (half + 1), k = idx - r * (half + 1);
+    const float2* in = X + (size_t)(i0 + r) * ncols;
+    float2* z = sbuf + r * L;
+    if (k == 0) {
+      const float2 x0 = in[0], xl = in[L];
+      z[0] = make_float2(x0.x + xl.x, x0.x - xl.x);
+    } else {
+      float2 zk, zm;
+      irfft_pre_pair(in[k], in[L - k], __ldg(p.tw_y + k), &zk, &zm);
+      z[k] = zk;
+      if (k != L - k) z[L - k] = zm;
+    }
+  }
+  __syncthreads();
+  fft_inplace<1>(sbuf, log2L, rows, L, p.tw_y, p.log2ny, threadIdx.x);
+  const float* sd = reinterpret_cast<const float*>(sbuf);
+  for (int idx = threadIdx.x; idx < rows * p.ny; idx += blockDim.x)
+    x[(size_t)i0 * p.ny + idx] = sd[idx] * scale;
+}
+
+template <int SIGN>
+__global__ void __launch_bounds__(512, 1) col_fft_kernel(SpecParams p, int W, int log2W, int bstride,
+                               float2* __restrict__ X,
+                               const float* __restrict__ mult) {
+  extern __shared__ float2 sbuf[];
+  const int N = p.nx, ncols = p.L + 1;
+  const int c0 = blockIdx.x * W;
+  for (int e = threadIdx.x; e < W * N; e += blockDim.x) {
+    const int w = e & (W - 1), i = e >> log2W, c = c0 + w;
+    sbuf[w * bstride + i] = c < ncols ? X[(size_t)i * ncols + c] : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
+  fft_inplace<SIGN>(sbuf, p.log2nx, W, bstride, p.tw_x, p.log2nx, threadIdx.x);
+  for (int e = threadIdx.x; e < W * N; e += blockDim.x) {
+    const int w = e & (W - 1), i = e >> log2W, c = c0 + w;
+    if (c < ncols) {
+      float2 v = sbuf[w * bstride + i];
+      if (mult) v = c_scale(v, __ldg(mult + (size_t)i * ncols + c));
+      X[(size_t)i * ncols + c] = v;
+    }
+  }
+}
+
+// spectral_curl_2d (spectral/utils.py:199-203): 2 pi i (vhat kx - uhat ky).
+__global__ void curl_table_kernel(SpecParams p, const float2* __restrict__ fxh,
+                                  const float2* __restrict__ fyh,
+                                  float2* __restrict__ out) {
+  const int ncols = p.L + 1;
+  const size_t n = (size_t)p.nx * ncols;
+  for (size_t g = blockIdx.x * (size_t)blockDim.x + threadIdx.x; g < n;
+       g += (size_t)gridDim.x * blockDim.x) {
+    const int kx = (int)(g / ncols), c = (int)(g - (size_t)kx * ncols);
+    const float kxf = kx_of(p, kx), kyf = ky_of(p, c);
+    const float2 a = fyh[g], b = fxh[g];
+    const float2 d = make_float2(a.x * kxf - b.x * kyf, a.y * kxf - b.y * kyf);
+    out[g] = make_float2(-(p.two_pi * d.y), p.two_pi * d.x);
+  }
+}
+
+struct ColCfg {
+  int W, log2W, bstride, blocks, threads;
+  size_t smem;
+};
+
+ColCfg col_cfg(const SpecParams& p) {
+  ColCfg c;
+  int W = 4096 >> p.log2nx;
+  if (W < 2) W = 2;
+  const int ncols = p.L + 1;
+  // W never needs to exceed the next power of two above ncols.
+  int cap = 1;
+  while (cap < ncols) cap <<= 1;
+  if (W > cap) W = cap;
+  c.W = W;
+  c.log2W = ilog2(W);
+  c.bstride = p.nx + 4;
+  c.blocks = (ncols + W - 1) / W;
+  const int workers = fft_workers(p.log2nx, W);
+  int t = ((workers + 31) / 32) * 32;
+  c.threads = t < 64 ? 64 : t;
+  c.smem = (size_t)W * c.bstride * sizeof(float2);
+  return c;
+}
+
+int rows_per_block(int log2L, int batch_per_row, int nrows) {
+  const int P = log2L >= 4 ? 16 : (1 << log2L);
+  int rows = (256 * P) / (batch_per_row << log2L);
+  if (rows < 1) rows = 1;
+  if (rows > nrows) rows = nrows;
+  return rows;
+}
+
+int threads_for(int workers) {
+  int t = ((workers + 31) / 32) * 32;
+  return t < 64 ? 64 : t;
+}
+
+template <typename K>
+cudaError_t set_smem(K kernel, size_t bytes) {
+  if (bytes > 48 * 1024)
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)bytes);
+  return cudaSuccess;
+}
+
+}  // namespace
+
+cudaError_t launch_spec_col_prep(const SpecParams& p, const float2* w,
+                                 float2* const t4[4], cudaStream_t s) {
+  const ColCfg c = col_cfg(p);
+  cudaError_t e = set_smem(spec_col_prep_kernel, c.smem);
+  if (e != cudaSuccess) return e;
+  T4 t{{t4[0], t4[1], t4[2], t4[3]}};
+  spec_col_prep_kernel<<<dim3(c.blocks, 4), c.threads, c.smem, s>>>(
+      p, c.W, c.log2W, c.bstride, w, t);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_spec_col_update(const SpecParams& p, const StageCoef& sc,
+                                   const float2* ahat, float2* w, float2* h,
+                                   float2* const t4[4], cudaStream_t s) {
+  const ColCfg c = col_cfg(p);
+  cudaError_t e = set_smem(spec_col_update_kernel, c.smem);
+  if (e != cudaSuccess) return e;
+  spec_col_update_kernel<<<c.blocks, c.threads, c.smem, s>>>(
+      p, sc, c.W, c.log2W, c.bstride, ahat, w, h);
+  e = cudaGetLastError();
+  if (e != cudaSuccess || !sc.prep_next || sc.explicit_only) return e;
+  return launch_spec_col_prep(p, w, t4, s);
+}
+
+cudaError_t launch_spec_row(const SpecParams& p, const float2* const t4[4],
+                            float2* ahat, cudaStream_t s) {
+  const int rows = rows_per_block(p.log2L, 4, p.nx);
+  const size_t smem = (size_t)rows * 4 * p.L * sizeof(float2);
+  cudaError_t e = set_smem(spec_row_kernel, smem);
+  if (e != cudaSuccess) return e;
+  spec_row_kernel<<<p.nx / rows, threads_for(fft_workers(p.log2L, rows * 4)),
+                    smem, s>>>(p, rows, t4[0], t4[1], t4[2], t4[3], ahat);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_row_rfft(const SpecParams& p, const float* x, float2* X,
+                            cudaStream_t s) {
+  const int rows = rows_per_block(p.log2L, 1, p.nx);
+  const size_t smem = (size_t)rows * p.L * sizeof(float2);
+  cudaError_t e = set_smem(row_rfft_kernel, smem);
+  if (e != cudaSuccess) return e;
+  row_rfft_kernel<<<p.nx / rows, threads_for(fft_workers(p.log2L, rows)), smem,
+                    s>>>(p, rows, x, X);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_row_irfft(const SpecParams& p, const float2* X, float* x,
+                             float scale, cudaStream_t s) {
+  const int rows = rows_per_block(p.log2L, 1, p.nx);
+  const size_t smem = (size_t)rows * p.L * sizeof(float2);
+  cudaError_t e = set_smem(row_irfft_kernel, smem);
+  if (e != cudaSuccess) return e;
+  row_irfft_kernel<<<p.nx / rows, threads_for(fft_workers(p.log2L, rows)), smem,
+                     s>>>(p, rows, X, x, scale);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_col_fft(const SpecParams& p, float2* X, int sign,
+                           const float* mult, cudaStream_t s) {
+  const ColCfg c = col_cfg(p);
+  cudaError_t e;
+  if (sign < 0) {
+    e = set_smem(col_fft_kernel<-1>, c.smem);
+    if (e != cudaSuccess) return e;
+    col_fft_kernel<-1><<<c.blocks, c.threads, c.smem, s>>>(p, c.W, c.log2W,
+                                                           c.bstride, X, mult);
+  } else {
+    e = set_smem(col_fft_kernel<1>, c.smem);
+    if (e != cudaSuccess) return e;
+    col_fft_kernel<1><<<c.blocks, c.threads, c.smem, s>>>(p, c.W, c.log2W,
+                                                          c.bstride, X, mult);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_spec_curl_table(const SpecParams& p, const float2* fxh,
+                                   const float2* fyh, float2* out,
+                                   cudaStream_t s) {
+  const size_t n = (size_t)p.nx * (p.L + 1);
+  size_t b = (n + 255) / 256;
+  if (b > 152 * 16) b = 152 * 16;
+  curl_table_kernel<<<(int)b, 256, 0, s>>>(p, fxh, fyh, out);
+  return cudaGetLastError();
+}
+
+}  // namespace cfd

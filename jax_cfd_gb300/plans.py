@@ -1,0 +1,282 @@
+"""Owning wrappers around the native FVM and spectral plans.
+
+A plan holds one grid's precomputed tables (Laplacian eigenvalues, FFT
+twiddles, wavenumbers, forcing) and its device workspace.  Entry points take
+torch CUDA tensors and enqueue on the current torch stream; nothing here
+synchronises except ``SpecPlan.set_forcing`` (documented in the C header).
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import Optional, Sequence
+
+import numpy as np
+import torch
+
+from jax_cfd_gb300 import _native as nat
+
+
+def current_stream_ptr(device: Optional[torch.device] = None) -> int:
+  return torch.cuda.current_stream(device).cuda_stream
+
+
+def ptr(t: torch.Tensor) -> int:
+  return t.data_ptr()
+
+
+def require_field(t: torch.Tensor, shape, dtype=torch.float32, name='array'):
+  """Validates a device field the kernels read or write."""
+  if not isinstance(t, torch.Tensor):
+    raise TypeError(f'{name} must be a torch.Tensor, got {type(t)}')
+  if not t.is_cuda:
+    raise ValueError(f'{name} must be a CUDA tensor (the native kernels run on the GPU)')
+  if t.dtype != dtype:
+    raise ValueError(f'{name}.dtype={t.dtype} does not match dtype={dtype}')
+  if tuple(t.shape) != tuple(shape):
+    raise ValueError(f'{name}.shape={tuple(t.shape)} does not match shape={tuple(shape)}')
+  if not t.is_contiguous():
+    raise ValueError(f'{name} must be contiguous')
+  return t
+
+
+class FvmPlan:
+  """Native plan for the staggered-grid step and pressure projection."""
+
+  def __init__(self, shape: Sequence[int], step: Sequence[float], *,
+               density: float = 1.0, viscosity: Optional[float] = None,
+               dt: float = 0.0, convect: int = nat.CONVECT_VAN_LEER,
+               linear_coefficient: Optional[float] = None,
+               const_forcing: int = nat.FORCE_NONE,
+               force_u: Optional[np.ndarray] = None,
+               force_v: Optional[np.ndarray] = None,
+               device: Optional[torch.device] = None):
+    if len(shape) != 2:
+      raise NotImplementedError('only 2-D grids are on the GB300 hot path')
+    self.shape = (int(shape[0]), int(shape[1]))
+    self.device = torch.device(device) if device is not None else torch.device(
+        'cuda', torch.cuda.current_device())
+    cfg = nat.FvmConfig()
+    cfg.nx, cfg.ny = self.shape
+    cfg.hx, cfg.hy = float(step[0]), float(step[1])
+    cfg.density = float(density)
+    cfg.has_viscosity = 0 if viscosity is None else 1
+    cfg.viscosity = 0.0 if viscosity is None else float(viscosity)
+    cfg.dt = float(dt)
+    cfg.convect = int(convect)
+    cfg.has_linear_forcing = 0 if linear_coefficient is None else 1
+    cfg.linear_coefficient = 0.0 if linear_coefficient is None else float(linear_coefficient)
+    cfg.const_forcing = int(const_forcing)
+    self._keep = []
+    for name, arr in (('force_u', force_u), ('force_v', force_v)):
+      if arr is not None:
+        a = np.ascontiguousarray(arr, dtype=np.float32)
+        self._keep.append(a)
+        setattr(cfg, name, a.ctypes.data_as(ctypes.POINTER(ctypes.c_float)))
+    handle = ctypes.c_void_p()
+    with torch.cuda.device(self.device):
+      nat.check(nat.load().cfd_fvm_plan_create(ctypes.byref(cfg), ctypes.byref(handle)),
+                'cfd_fvm_plan_create')
+    self._h = handle
+    self._lib = nat.load()
+
+  def __del__(self):
+    h = getattr(self, '_h', None)
+    if h is not None and h.value:
+      try:
+        self._lib.cfd_fvm_plan_destroy(h)
+      except Exception:  # pylint: disable=broad-except
+        pass
+      self._h = None
+
+  @property
+  def handle(self):
+    return self._h
+
+  @property
+  def nbytes(self) -> int:
+    return int(self._lib.cfd_fvm_plan_bytes(self._h))
+
+  def _fields(self, *ts):
+    for t in ts:
+      require_field(t, self.shape)
+    return [ptr(t) for t in ts]
+
+  def step(self, u, v, steps: int, u_out=None, v_out=None):
+    if steps < 0:
+      raise ValueError('steps must be non-negative')
+    u_out = torch.empty_like(u) if u_out is None else u_out
+    v_out = torch.empty_like(v) if v_out is None else v_out
+    a = self._fields(u, v, u_out, v_out)
+    nat.check(self._lib.cfd_fvm_step(self._h, current_stream_ptr(u.device), *a, int(steps)),
+              'cfd_fvm_step')
+    return u_out, v_out
+
+  def explicit_terms(self, u, v):
+    du, dv = torch.empty_like(u), torch.empty_like(v)
+    a = self._fields(u, v, du, dv)
+    nat.check(self._lib.cfd_fvm_explicit_terms(self._h, current_stream_ptr(u.device), *a),
+              'cfd_fvm_explicit_terms')
+    return du, dv
+
+  def projection(self, u, v):
+    uo, vo = torch.empty_like(u), torch.empty_like(v)
+    a = self._fields(u, v, uo, vo)
+    nat.check(self._lib.cfd_fvm_projection(self._h, current_stream_ptr(u.device), *a),
+              'cfd_fvm_projection')
+    return uo, vo
+
+  def pressure_solve(self, u, v):
+    q = torch.empty_like(u)
+    a = self._fields(u, v, q)
+    nat.check(self._lib.cfd_fvm_pressure_solve(self._h, current_stream_ptr(u.device), *a),
+              'cfd_fvm_pressure_solve')
+    return q
+
+  def divergence(self, u, v):
+    out = torch.empty_like(u)
+    a = self._fields(u, v, out)
+    nat.check(self._lib.cfd_fvm_divergence(self._h, current_stream_ptr(u.device), *a),
+              'cfd_fvm_divergence')
+    return out
+
+  def curl_2d(self, u, v):
+    out = torch.empty_like(u)
+    a = self._fields(u, v, out)
+    nat.check(self._lib.cfd_fvm_curl_2d(self._h, current_stream_ptr(u.device), *a),
+              'cfd_fvm_curl_2d')
+    return out
+
+
+def max_speed(u: torch.Tensor, v: torch.Tensor) -> torch.Tensor:
+  """Device scalar max over cells of sqrt(u^2 + v^2)."""
+  require_field(u, u.shape, name='u')
+  require_field(v, u.shape, name='v')
+  out = torch.empty((), dtype=torch.float32, device=u.device)
+  nat.check(nat.load().cfd_max_speed(current_stream_ptr(u.device), u.numel(), ptr(u), ptr(v),
+                                     ptr(out)), 'cfd_max_speed')
+  return out
+
+
+def scale_to_max_speed(u, v, vmax: torch.Tensor, maximum_velocity: float):
+  """In place: u = (maximum_velocity * u) / vmax (same for v)."""
+  nat.check(nat.load().cfd_scale_to_max_speed(
+      current_stream_ptr(u.device), u.numel(), ptr(u), ptr(v), ptr(vmax),
+      float(maximum_velocity)), 'cfd_scale_to_max_speed')
+
+
+class SpecPlan:
+  """Native plan for the pseudospectral step and the 2-D real transforms."""
+
+  def __init__(self, shape: Sequence[int], step: Sequence[float], *,
+               viscosity: float = 0.0, drag: float = 0.0, dt: float = 0.0,
+               smooth: bool = True, alphas=(0., 1.), betas=(0.,), gammas=(1.,),
+               device: Optional[torch.device] = None):
+    if len(shape) != 2:
+      raise NotImplementedError('only 2-D grids are on the GB300 hot path')
+    self.shape = (int(shape[0]), int(shape[1]))
+    self.half_shape = (self.shape[0], self.shape[1] // 2 + 1)
+    self.device = torch.device(device) if device is not None else torch.device(
+        'cuda', torch.cuda.current_device())
+    self._coef = [np.ascontiguousarray(c, dtype=np.float64) for c in (alphas, betas, gammas)]
+    cfg = nat.SpecConfig()
+    cfg.nx, cfg.ny = self.shape
+    cfg.hx, cfg.hy = float(step[0]), float(step[1])
+    cfg.viscosity = float(viscosity)
+    cfg.drag = float(drag)
+    cfg.dt = float(dt)
+    cfg.smooth = 1 if smooth else 0
+    cfg.num_stages = len(self._coef[1])
+    cfg.alphas, cfg.betas, cfg.gammas = (
+        c.ctypes.data_as(ctypes.POINTER(ctypes.c_double)) for c in self._coef)
+    handle = ctypes.c_void_p()
+    with torch.cuda.device(self.device):
+      nat.check(nat.load().cfd_spec_plan_create(ctypes.byref(cfg), ctypes.byref(handle)),
+                'cfd_spec_plan_create')
+    self._h = handle
+    self._lib = nat.load()
+
+  def __del__(self):
+    h = getattr(self, '_h', None)
+    if h is not None and h.value:
+      try:
+        self._lib.cfd_spec_plan_destroy(h)
+      except Exception:  # pylint: disable=broad-except
+        pass
+      self._h = None
+
+  @property
+  def nbytes(self) -> int:
+    return int(self._lib.cfd_spec_plan_bytes(self._h))
+
+  def _real(self, t, name='x'):
+    return require_field(t, self.shape, name=name)
+
+  def _half(self, t, name='xhat'):
+    return require_field(t, self.half_shape, dtype=torch.complex64, name=name)
+
+  def set_forcing(self, fx: Optional[torch.Tensor], fy: Optional[torch.Tensor]):
+    a = []
+    for t, name in ((fx, 'fx'), (fy, 'fy')):
+      if t is None:
+        a.append(None)
+      else:
+        a.append(ptr(self._real(t, name)))
+    dev = (fx if fx is not None else fy).device if (fx is not None or fy is not None) else self.device
+    nat.check(self._lib.cfd_spec_set_forcing(self._h, current_stream_ptr(dev), *a),
+              'cfd_spec_set_forcing')
+
+  def step(self, w_hat: torch.Tensor, steps: int, out: Optional[torch.Tensor] = None):
+    if steps < 0:
+      raise ValueError('steps must be non-negative')
+    self._half(w_hat, 'vorticity_hat')
+    out = torch.empty_like(w_hat) if out is None else self._half(out, 'out')
+    nat.check(self._lib.cfd_spec_step(self._h, current_stream_ptr(w_hat.device), ptr(w_hat),
+                                      ptr(out), int(steps)), 'cfd_spec_step')
+    return out
+
+  def explicit_terms(self, w_hat: torch.Tensor) -> torch.Tensor:
+    self._half(w_hat, 'vorticity_hat')
+    out = torch.empty_like(w_hat)
+    nat.check(self._lib.cfd_spec_explicit_terms(self._h, current_stream_ptr(w_hat.device),
+                                                ptr(w_hat), ptr(out)),
+              'cfd_spec_explicit_terms')
+    return out
+
+  def rfft2(self, x: torch.Tensor) -> torch.Tensor:
+    self._real(x)
+    out = torch.empty(self.half_shape, dtype=torch.complex64, device=x.device)
+    nat.check(self._lib.cfd_rfft2(self._h, current_stream_ptr(x.device), ptr(x), ptr(out)),
+              'cfd_rfft2')
+    return out
+
+  def irfft2(self, xhat: torch.Tensor) -> torch.Tensor:
+    self._half(xhat)
+    out = torch.empty(self.shape, dtype=torch.float32, device=xhat.device)
+    nat.check(self._lib.cfd_irfft2(self._h, current_stream_ptr(xhat.device), ptr(xhat),
+                                   ptr(out)), 'cfd_irfft2')
+    return out
+
+  def spectral_filter(self, x: torch.Tensor, table: torch.Tensor) -> torch.Tensor:
+    self._real(x)
+    require_field(table, self.half_shape, name='table')
+    out = torch.empty_like(x)
+    nat.check(self._lib.cfd_spectral_filter(self._h, current_stream_ptr(x.device), ptr(x),
+                                            ptr(table), ptr(out)), 'cfd_spectral_filter')
+    return out
+
+
+_PLAN_CACHE = {}
+
+
+def cached(kind, key, factory):
+  """Per-process cache of plans keyed by (kind, device, parameters)."""
+  k = (kind, key)
+  plan = _PLAN_CACHE.get(k)
+  if plan is None:
+    plan = factory()
+    _PLAN_CACHE[k] = plan
+  return plan
+
+
+def clear_cache():
+  _PLAN_CACHE.clear()
