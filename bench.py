@@ -1,0 +1,399 @@
+"""Benchmark of the jax-cfd hot path on GB300 (one JSON line on stdout).
+
+Workload (the configuration the headline metric is quoted on): the
+staggered-grid semi_implicit_navier_stokes step (Van Leer advection, explicit
+diffusion, Kolmogorov sin(4y) + linear drag -0.1 forcing, solve_fast_diag
+projection, forward Euler) on a 2048 x 2048 periodic [0, 2pi]^2 float32 grid,
+nu = 1e-3, rho = 1, dt = stable_time_step(2, 0.5) = 7.6699e-4, from a seeded
+filtered random velocity field with max speed 2 (synthetic: no dataset exists
+for this path).  One bench "step" is one ``funcutils.repeated(step, chunk)``
+call, i.e. `chunk` (default 200) FVM time steps; the default 10 timed steps
+are the 2000 steps of the 2048^2 scale-up configuration.
+
+Timing: CUDA events around each chunk on the launching stream, the L2 flushed
+(a 256 MiB write) between chunks, a barrier + synchronize on both sides of the
+timed loop, max over ranks.  `value` = grid cells x time steps / second with
+the state resident in HBM; `e2e` is the same metric through the public API
+with the velocity copied from pinned host memory before, and back after,
+every chunk.  `roofline` uses per-kernel CUDA-event durations from a second
+pass over the same workload and the HBM bandwidth in MEASURED_PEAKS.json.
+
+`--impl reference` times the reference algorithm on the host CPU (the NumPy
+restatement of jax-cfd's step; JAX cannot be installed here) on a bounded
+sample of the same workload.
+
+Multi-GPU: replicas only (each rank advances its own trajectory; no
+collective on the data path); value sums the ranks' cell-steps.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+  sys.path.insert(0, ROOT)
+
+N = 2048
+VISCOSITY = 1e-3
+MAX_VELOCITY = 2.0
+CFL = 0.5
+DOMAIN = ((0, 2 * np.pi), (0, 2 * np.pi))
+# Algorithmic HBM bytes per cell and FVM step (float32): explicit stencil reads
+# u*, v*, q and writes u*, v* (20); divergence + row rFFT reads u*, v*, writes
+# the packed spectrum (12); column pass reads/writes the spectrum (8); row
+# irFFT reads/writes it (8).
+FVM_BYTES_PER_CELL = {'explicit': 20, 'div_rfft': 12, 'col_pinv': 8, 'irfft': 8,
+                      'project_out': 20}
+FVM_STEP_BYTES_PER_CELL = 48
+# Spectral stage (per cell of the N x N grid): row pass reads 4 complex
+# half-spectrum fields (16) and writes one (4); column update reads the
+# advection spectrum, state and h (12) and writes state and h (8); column prep
+# reads the state (4) and writes 4 fields (16).
+SPEC_BYTES_PER_CELL = {'row': 20, 'col_update': 20, 'col_prep': 20}
+SPEC_STEP_BYTES_PER_CELL = 300
+
+
+def _peaks():
+  path = os.path.join(ROOT, 'MEASURED_PEAKS.json')
+  try:
+    with open(path) as f:
+      d = json.load(f)
+    return float(d['hbm_gbs']), 'measured'
+  except Exception:  # pylint: disable=broad-except
+    return 6800.0, 'fallback'
+
+
+def _traffic_table():
+  path = os.path.join(ROOT, 'profiles', 'dram_traffic.json')
+  try:
+    with open(path) as f:
+      return json.load(f)
+  except Exception:  # pylint: disable=broad-except
+    return {}
+
+
+class ClockSampler:
+  """Samples nvidia-smi clocks and throttle reasons while running."""
+  QUERY = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
+           'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
+           'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
+
+  def __init__(self, index: int):
+    self.index = index
+    self.proc = None
+    self.lines = []
+    self._t = None
+
+  def __enter__(self):
+    try:
+      self.proc = subprocess.Popen(
+          ['nvidia-smi', '-i', str(self.index), f'--query-gpu={self.QUERY}',
+           '--format=csv,noheader,nounits', '-lms', '200'],
+          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+      self._t = threading.Thread(target=self._read, daemon=True)
+      self._t.start()
+    except Exception:  # pylint: disable=broad-except
+      self.proc = None
+    return self
+
+  def _read(self):
+    for line in self.proc.stdout:
+      self.lines.append(line.strip())
+
+  def __exit__(self, *exc):
+    if self.proc is not None:
+      self.proc.terminate()
+      try:
+        self.proc.wait(timeout=5)
+      except Exception:  # pylint: disable=broad-except
+        self.proc.kill()
+      if self._t is not None:
+        self._t.join(timeout=2)
+
+  def summary(self):
+    sm, smax, reasons = [], [], set()
+    names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+    for line in self.lines:
+      parts = [p.strip() for p in line.split(',')]
+      if len(parts) < 9:
+        continue
+      try:
+        sm.append(float(parts[1]))
+        smax.append(float(parts[2]))
+      except ValueError:
+        continue
+      for name, val in zip(names, parts[5:9]):
+        if val.lower().startswith('active'):
+          reasons.add(name)
+    if not sm:
+      return {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': ['unsampled'], 'samples': 0}
+    return {'sm_mhz': statistics.median(sm), 'sm_max_mhz': max(smax),
+            'reasons': sorted(reasons), 'samples': len(sm)}
+
+
+def _dist():
+  world = int(os.environ.get('WORLD_SIZE', '1'))
+  rank = int(os.environ.get('RANK', '0'))
+  local = int(os.environ.get('LOCAL_RANK', '0'))
+  return world, rank, local
+
+
+def _json_line(obj):
+  print(json.dumps(obj), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# Reference arm: the jax-cfd algorithm on the host CPU.
+# ---------------------------------------------------------------------------
+def _cpu_sample(steps: int, warmup: int, n: int = N):
+  """Times the NumPy restatement of the reference step on a bounded sample
+  (`steps` FVM steps at n x n); returns (cell-steps/s, seconds, threads)."""
+  from oracle import fvm as ofvm  # pylint: disable=import-outside-toplevel
+  og = ofvm.Grid.make((n, n), domain=DOMAIN)
+  rng = np.random.default_rng(0)
+  v = tuple((0.5 * rng.standard_normal((n, n))).astype(np.float32) for _ in range(2))
+  dt = ofvm.stable_time_step(MAX_VELOCITY, CFL, VISCOSITY, og)
+  step = ofvm.semi_implicit_navier_stokes(
+      1.0, VISCOSITY, dt, og, forcing=ofvm.simple_turbulence_forcing(og, 1, 4, -0.1))
+  for _ in range(warmup):
+    v = step(v)
+  t0 = time.perf_counter()
+  for _ in range(steps):
+    v = step(v)
+  dt_s = time.perf_counter() - t0
+  return n * n * steps / dt_s, dt_s, 1
+
+
+def run_reference(args):
+  world, rank, _ = _dist()
+  if rank != 0:
+    return
+  k = max(1, args.steps)
+  w = max(0, min(args.warmup, 3))
+  # Each reference "step" is one FVM time step of the 2048^2 workload (a
+  # bounded sample: the full 2000-step run would take about an hour on CPU).
+  value, secs, threads = _cpu_sample(k, w)
+  sample = f'{k} FVM steps at {N}x{N} after {w} warm-up steps ({secs:.1f} s)'
+  _json_line({
+      'metric': 'FVM cell-steps/s at 2048^2', 'value': value, 'unit': 'cell-steps/s',
+      'impl': 'reference', 'n_gpus': world, 'steps': k, 'warmup': w,
+      'ms_per_step': 1000.0 * secs / k, 'higher_is_better': True, 'scaling': 'weak',
+      'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic',
+      'config': {'workload': f'semi_implicit_navier_stokes {N}x{N} Van Leer + Kolmogorov, '
+                             'NumPy restatement of the reference on the host CPU',
+                 'grid': [N, N], 'parallelism': 'host'},
+      'cpu_baseline': {'value': value, 'unit': 'cell-steps/s', 'cores': threads,
+                       'kind': 'port', 'sample': sample},
+      'e2e': {'value': value, 'unit': 'cell-steps/s', 'h2d_bytes_per_step': 0,
+              'd2h_bytes_per_step': 0},
+  })
+
+
+# ---------------------------------------------------------------------------
+# GB300 arm.
+# ---------------------------------------------------------------------------
+def run_gb300(args):
+  import torch  # pylint: disable=import-outside-toplevel
+  import jax_cfd_gb300.base as cfd  # pylint: disable=import-outside-toplevel
+  from jax_cfd_gb300.spectral import equations as seq  # pylint: disable=import-outside-toplevel
+  from jax_cfd_gb300.spectral import time_stepping as sts  # pylint: disable=import-outside-toplevel
+
+  world, rank, local = _dist()
+  torch.cuda.set_device(local)
+  dev = torch.device('cuda', local)
+  dist = None
+  if world > 1:
+    import torch.distributed as dist  # pylint: disable=import-outside-toplevel
+    dist.init_process_group('nccl', device_id=dev)
+
+  def barrier():
+    if dist is not None:
+      dist.barrier()
+
+  n, chunk = args.size, args.chunk
+  grid = cfd.grids.Grid((n, n), domain=DOMAIN)
+  v0 = cfd.initial_conditions.filtered_velocity_field(rank, grid, MAX_VELOCITY, 4, device=dev)
+  dt = cfd.equations.stable_time_step(MAX_VELOCITY, CFL, VISCOSITY, grid)
+  forcing = cfd.forcings.simple_turbulence_forcing(grid, 1, 4, -0.1)
+  step = cfd.equations.semi_implicit_navier_stokes(1.0, VISCOSITY, dt, grid, forcing=forcing)
+  run = cfd.funcutils.repeated(step, chunk)
+  flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+  stream = torch.cuda.current_stream(dev)
+
+  v = v0
+  for _ in range(args.warmup):
+    v = run(v)
+  torch.cuda.synchronize(dev)
+
+  starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+  ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+  sampler = ClockSampler(local)
+  barrier()
+  torch.cuda.synchronize(dev)
+  with sampler:
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+      flush.zero_()
+      starts[k].record(stream)
+      v = run(v)
+      ends[k].record(stream)
+    torch.cuda.synchronize(dev)
+    wall = time.perf_counter() - t0
+  barrier()
+  chunk_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+  total_s = sum(chunk_ms) / 1000.0
+  if dist is not None:
+    t = torch.tensor([total_s], device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    total_s = float(t)
+  cells = n * n
+  value = world * cells * chunk * args.steps / total_s
+  finite = bool(torch.isfinite(v[0].data).all() and torch.isfinite(v[1].data).all())
+
+  # Per-kernel durations (second pass, same workload and state).
+  plan = step.plan(dev)
+  kernel_ms = plan.profile(v[0].data, v[1].data, chunk)
+  kernel_time = {k: kernel_ms[k] * (chunk if k != 'project_out' else 1) for k in kernel_ms}
+  dominant = max(kernel_time, key=kernel_time.get)
+  peak, peak_kind = _peaks()
+  achieved = FVM_BYTES_PER_CELL[dominant] * cells / (kernel_ms[dominant] / 1000.0) / 1e9
+  traffic = _traffic_table().get(f'fvm_{dominant}_{n}')
+  step_achieved = FVM_STEP_BYTES_PER_CELL * value / world / 1e9
+
+  # End to end through the public API with host buffers.
+  host_u = torch.empty((n, n), dtype=torch.float32, pin_memory=True)
+  host_v = torch.empty((n, n), dtype=torch.float32, pin_memory=True)
+  host_u.copy_(v0[0].data)
+  host_v.copy_(v0[1].data)
+  out_u = torch.empty_like(host_u, pin_memory=True)
+  out_v = torch.empty_like(host_v, pin_memory=True)
+  bc = cfd.boundaries.periodic_boundary_conditions(2)
+  e2e_steps = max(1, min(args.steps, 5))
+  e_start = [torch.cuda.Event(enable_timing=True) for _ in range(e2e_steps)]
+  e_end = [torch.cuda.Event(enable_timing=True) for _ in range(e2e_steps)]
+  torch.cuda.synchronize(dev)
+  for k in range(e2e_steps):
+    flush.zero_()
+    e_start[k].record(stream)
+    du = host_u.to(dev, non_blocking=True)
+    dv = host_v.to(dev, non_blocking=True)
+    state = (cfd.grids.GridVariable(cfd.grids.GridArray(du, grid.cell_faces[0], grid), bc),
+             cfd.grids.GridVariable(cfd.grids.GridArray(dv, grid.cell_faces[1], grid), bc))
+    res = run(state)
+    out_u.copy_(res[0].data, non_blocking=True)
+    out_v.copy_(res[1].data, non_blocking=True)
+    e_end[k].record(stream)
+  torch.cuda.synchronize(dev)
+  e2e_s = sum(s.elapsed_time(e) for s, e in zip(e_start, e_end)) / 1000.0
+  e2e_value = world * cells * chunk * e2e_steps / e2e_s
+
+  # Secondary: the pseudospectral step at the same size (CN-RK4, dt = 1e-3).
+  spectral = None
+  if not args.skip_spectral:
+    from jax_cfd_gb300.spectral import utils as su  # pylint: disable=import-outside-toplevel
+    w = su.rfft2(cfd.finite_differences.curl_2d(v0).data, grid)
+    eq = seq.ForcedNavierStokes2D(VISCOSITY, grid, smooth=True)
+    sstep = sts.crank_nicolson_rk4(eq, 1e-3)
+    srun = cfd.funcutils.repeated(sstep, args.spectral_chunk)
+    w = srun(w)
+    torch.cuda.synchronize(dev)
+    s0 = torch.cuda.Event(enable_timing=True)
+    s1 = torch.cuda.Event(enable_timing=True)
+    s_ms = 0.0
+    for _ in range(3):
+      flush.zero_()
+      s0.record(stream)
+      w = srun(w)
+      s1.record(stream)
+      torch.cuda.synchronize(dev)
+      s_ms += s0.elapsed_time(s1)
+    s_value = cells * args.spectral_chunk * 3 / (s_ms / 1000.0)
+    sk = sstep.plan(dev).profile(w, 2)
+    s_dom = max(('row', 'col_update', 'col_prep'), key=lambda k: sk[k])
+    s_ach = SPEC_BYTES_PER_CELL[s_dom] * cells / (sk[s_dom] / 1000.0) / 1e9
+    spectral = {
+        'workload': f'NavierStokes2D {n}x{n} crank_nicolson_rk4 dt=1e-3, Kolmogorov k=4, drag 0.1',
+        'value': s_value, 'unit': 'cell-steps/s',
+        'ms_per_time_step': s_ms / (3 * args.spectral_chunk),
+        'step_roofline': {'bytes_per_cell_step': SPEC_STEP_BYTES_PER_CELL,
+                          'achieved': SPEC_STEP_BYTES_PER_CELL * s_value / 1e9,
+                          'peak': peak, 'unit': 'GB/s',
+                          'frac': SPEC_STEP_BYTES_PER_CELL * s_value / 1e9 / peak},
+        'kernel_ms': sk,
+        'roofline': {'kernel': s_dom, 'bound': 'hbm', 'achieved': s_ach, 'peak': peak,
+                     'unit': 'GB/s', 'frac': s_ach / peak},
+        'finite': bool(torch.isfinite(torch.view_as_real(w)).all()),
+    }
+
+  cpu = None
+  if rank == 0 and not args.skip_cpu:
+    cv, csecs, cthreads = _cpu_sample(args.cpu_steps, 1)
+    cpu = {'value': cv, 'unit': 'cell-steps/s', 'cores': cthreads, 'kind': 'port',
+           'sample': f'{args.cpu_steps} FVM steps at {N}x{N} of the NumPy restatement '
+                     f'after 1 warm-up step ({csecs:.1f} s)'}
+
+  if rank != 0:
+    return
+  launches = args.steps * (4 * chunk + 1)
+  _json_line({
+      'metric': 'FVM cell-steps/s at 2048^2', 'value': value, 'unit': 'cell-steps/s',
+      'n_gpus': world, 'steps': args.steps, 'warmup': args.warmup,
+      'ms_per_step': 1000.0 * total_s / args.steps, 'higher_is_better': True,
+      'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic',
+      'config': {'workload': f'semi_implicit_navier_stokes {n}x{n} float32, Van Leer, '
+                             f'nu=1e-3, Kolmogorov k=4 + drag 0.1, forward Euler, '
+                             f'{chunk} time steps per bench step',
+                 'grid': [n, n], 'time_steps_per_step': chunk, 'dt': dt,
+                 'l2': 'flushed (256 MiB write) between bench steps',
+                 'parallelism': 'replicas' if world > 1 else 'single'},
+      'roofline': {'kernel': dominant, 'bound': 'hbm', 'achieved': achieved, 'peak': peak,
+                   'unit': 'GB/s', 'frac': achieved / peak, 'traffic': traffic,
+                   'peak_source': peak_kind,
+                   'bytes_per_cell': FVM_BYTES_PER_CELL[dominant]},
+      'step_roofline': {'bytes_per_cell_step': FVM_STEP_BYTES_PER_CELL,
+                        'achieved': step_achieved, 'peak': peak, 'unit': 'GB/s',
+                        'frac': step_achieved / peak},
+      'kernel_ms': kernel_ms,
+      'cpu_baseline': cpu,
+      'e2e': {'value': e2e_value, 'unit': 'cell-steps/s',
+              'h2d_bytes_per_step': 2 * cells * 4, 'd2h_bytes_per_step': 2 * cells * 4},
+      'gpu_launches': launches,
+      'clocks': sampler.summary(),
+      'wall_s': wall,
+      'finite': finite,
+      'spectral': spectral,
+  })
+
+
+def main():
+  ap = argparse.ArgumentParser(description=__doc__.split('\n')[0])
+  ap.add_argument('--gpus', type=int, default=1)
+  ap.add_argument('--steps', type=int, default=10)
+  ap.add_argument('--warmup', type=int, default=3)
+  ap.add_argument('--impl', choices=['gb300', 'reference'], default='gb300')
+  ap.add_argument('--size', type=int, default=N)
+  ap.add_argument('--chunk', type=int, default=200)
+  ap.add_argument('--spectral-chunk', type=int, default=20)
+  ap.add_argument('--cpu-steps', type=int, default=5)
+  ap.add_argument('--skip-cpu', action='store_true')
+  ap.add_argument('--skip-spectral', action='store_true')
+  args = ap.parse_args()
+  if args.warmup < 3:
+    ap.error('at least 3 warm-up steps are required')
+  if args.impl == 'reference':
+    run_reference(args)
+  else:
+    run_gb300(args)
+
+
+if __name__ == '__main__':
+  main()

@@ -94,6 +94,13 @@ long long cfd_fvm_plan_bytes(const cfd_fvm_plan* plan);
  * offsets (1, .5) and (.5, 1).  u_out/v_out may alias u/v. */
 int cfd_fvm_step(cfd_fvm_plan* plan, void* stream, const float* u,
                  const float* v, float* u_out, float* v_out, int steps);
+/* cfd_fvm_step with a CUDA event pair around every launch; synchronises the
+ * stream at the end and writes the mean duration in ms of each kernel kind to
+ * ms_out[5] = {explicit stencil, divergence + row rFFT, column pinv,
+ * row irFFT, final projection}.  For measurement (bench.py roofline). */
+int cfd_fvm_profile(cfd_fvm_plan* plan, void* stream, const float* u,
+                    const float* v, float* u_out, float* v_out, int steps,
+                    float* ms_out);
 /* du/dt from advection + diffusion + forcing (no projection). */
 int cfd_fvm_explicit_terms(cfd_fvm_plan* plan, void* stream, const float* u,
                            const float* v, float* du, float* dv);
@@ -142,6 +149,10 @@ int cfd_spec_set_forcing(cfd_spec_plan* plan, void* stream, const float* fx,
  * w_out may alias w_in. */
 int cfd_spec_step(cfd_spec_plan* plan, void* stream, const float* w_in,
                   float* w_out, int steps);
+/* cfd_spec_step with event pairs; ms_out[3] = {row pass, column update,
+ * column prep} mean durations in ms.  Synchronises the stream. */
+int cfd_spec_profile(cfd_spec_plan* plan, void* stream, const float* w_in,
+                     float* w_out, int steps, float* ms_out);
 /* Explicit terms F(w) of NavierStokes2D (advection, filter, forcing). */
 int cfd_spec_explicit_terms(cfd_spec_plan* plan, void* stream,
                             const float* w, float* out);

@@ -67,6 +67,7 @@ _SIGNATURES = {
     'cfd_fvm_plan_destroy': (ctypes.c_int, [_vp]),
     'cfd_fvm_plan_bytes': (ctypes.c_longlong, [_vp]),
     'cfd_fvm_step': (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_int]),
+    'cfd_fvm_profile': (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_int, _vp]),
     'cfd_fvm_explicit_terms': (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp]),
     'cfd_fvm_projection': (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp]),
     'cfd_fvm_pressure_solve': (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp]),
@@ -79,6 +80,7 @@ _SIGNATURES = {
     'cfd_spec_plan_bytes': (ctypes.c_longlong, [_vp]),
     'cfd_spec_set_forcing': (ctypes.c_int, [_vp, _vp, _vp, _vp]),
     'cfd_spec_step': (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_int]),
+    'cfd_spec_profile': (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_int, _vp]),
     'cfd_spec_explicit_terms': (ctypes.c_int, [_vp, _vp, _vp, _vp]),
     'cfd_rfft2': (ctypes.c_int, [_vp, _vp, _vp, _vp]),
     'cfd_irfft2': (ctypes.c_int, [_vp, _vp, _vp, _vp]),

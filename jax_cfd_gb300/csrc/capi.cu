@@ -140,6 +140,8 @@ int cfd_fvm_plan_create(const cfd_fvm_config* cfg, cfd_fvm_plan** out) {
   // typed scalars meet float32 arrays.
   p.hx = (float)cfg->hx;
   p.hy = (float)cfg->hy;
+  p.inv_hx = 1.f / p.hx;
+  p.inv_hy = 1.f / p.hy;
   p.cfl_x = (float)(cfg->dt / cfg->hx);
   p.cfl_y = (float)(cfg->dt / cfg->hy);
   p.dt = (float)cfg->dt;
@@ -261,6 +263,94 @@ int cfd_fvm_step(cfd_fvm_plan* plan, void* stream, const float* u,
     t = av; av = bv; bv = t;
   }
   CFD_CHECK(cfd::launch_fvm_project_out(p, au, av, q, u_out, v_out, s), "project_out");
+  return CFD_OK;
+}
+
+// Same launches as cfd_fvm_step, with an event pair recorded around every
+// launch on `stream`; synchronises once at the end and writes the mean
+// duration (ms) of each kernel kind to ms_out[CFD_FVM_PROFILE_KINDS].
+int cfd_fvm_profile(cfd_fvm_plan* plan, void* stream, const float* u,
+                    const float* v, float* u_out, float* v_out, int steps,
+                    float* ms_out) {
+  if (!plan || !u || !v || !u_out || !v_out || !ms_out || steps < 1)
+    return fail(CFD_ERR_INVALID_ARGUMENT, "cfd_fvm_profile: bad arguments");
+  cudaStream_t s = as_stream(stream);
+  const cfd::FvmParams& p = plan->p;
+  const int launches = 4 * steps + 1;
+  std::vector<cudaEvent_t> ev(2 * launches);
+  std::vector<int> kind(launches);
+  for (auto& e : ev) CFD_CHECK(cudaEventCreate(&e), "cudaEventCreate");
+  int li = 0;
+  auto timed = [&](int k, cudaError_t (*fn)(void*), void* ctx) -> cudaError_t {
+    cudaError_t e = cudaEventRecord(ev[2 * li], s);
+    if (e == cudaSuccess) e = fn(ctx);
+    if (e == cudaSuccess) e = cudaEventRecord(ev[2 * li + 1], s);
+    kind[li++] = k;
+    return e;
+  };
+  struct Ctx {
+    const cfd::FvmParams* p;
+    const float *a, *b, *q;
+    float *c, *d;
+    float2* spec;
+    bool project;
+    cudaStream_t s;
+  } ctx{&p, u, v, nullptr, plan->au, plan->av, plan->spec, false, s};
+  auto explicit_fn = [](void* c) -> cudaError_t {
+    Ctx* x = (Ctx*)c;
+    return cfd::launch_fvm_explicit(*x->p, x->project, false, x->a, x->b, x->q, x->c, x->d, x->s);
+  };
+  auto div_fn = [](void* c) -> cudaError_t {
+    Ctx* x = (Ctx*)c;
+    return cfd::launch_fvm_div_rfft(*x->p, x->c, x->d, x->spec, x->s);
+  };
+  auto col_fn = [](void* c) -> cudaError_t {
+    Ctx* x = (Ctx*)c;
+    return cfd::launch_fvm_col_pinv(*x->p, x->spec, x->s);
+  };
+  auto irfft_fn = [](void* c) -> cudaError_t {
+    Ctx* x = (Ctx*)c;
+    return cfd::launch_fvm_irfft(*x->p, x->spec, x->s);
+  };
+  auto out_fn = [](void* c) -> cudaError_t {
+    Ctx* x = (Ctx*)c;
+    return cfd::launch_fvm_project_out(*x->p, x->a, x->b, x->q, x->c, x->d, x->s);
+  };
+  cudaError_t e = cudaSuccess;
+  float *au = plan->au, *av = plan->av, *bu = plan->bu, *bv = plan->bv;
+  const float* q = reinterpret_cast<const float*>(plan->spec);
+  for (int k = 0; k < steps && e == cudaSuccess; ++k) {
+    ctx.project = k > 0;
+    ctx.a = k > 0 ? au : u;
+    ctx.b = k > 0 ? av : v;
+    ctx.q = q;
+    ctx.c = k > 0 ? bu : au;
+    ctx.d = k > 0 ? bv : av;
+    e = timed(0, explicit_fn, &ctx);
+    if (e == cudaSuccess) e = timed(1, div_fn, &ctx);
+    if (e == cudaSuccess) e = timed(2, col_fn, &ctx);
+    if (e == cudaSuccess) e = timed(3, irfft_fn, &ctx);
+    if (k > 0) {
+      float* t = au; au = bu; bu = t;
+      t = av; av = bv; bv = t;
+    }
+  }
+  if (e == cudaSuccess) {
+    ctx.a = au; ctx.b = av; ctx.q = q; ctx.c = u_out; ctx.d = v_out;
+    e = timed(4, out_fn, &ctx);
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  double sum[5] = {0, 0, 0, 0, 0};
+  int cnt[5] = {0, 0, 0, 0, 0};
+  for (int i = 0; i < li && e == cudaSuccess; ++i) {
+    float ms = 0.f;
+    e = cudaEventElapsedTime(&ms, ev[2 * i], ev[2 * i + 1]);
+    sum[kind[i]] += ms;
+    cnt[kind[i]] += 1;
+  }
+  for (auto& x : ev) cudaEventDestroy(x);
+  if (e != cudaSuccess) return cuda_fail(e, "cfd_fvm_profile");
+  for (int k = 0; k < 5; ++k) ms_out[k] = cnt[k] ? (float)(sum[k] / cnt[k]) : 0.f;
   return CFD_OK;
 }
 
@@ -569,6 +659,68 @@ int cfd_spec_step(cfd_spec_plan* plan, void* stream, const float* w_in,
                 "col_update");
     }
   }
+  return CFD_OK;
+}
+
+// cfd_spec_step with an event pair around every launch; mean ms per kernel
+// kind written to ms_out[3] = {row pass, column update, column prep}.
+int cfd_spec_profile(cfd_spec_plan* plan, void* stream, const float* w_in,
+                     float* w_out, int steps, float* ms_out) {
+  if (!plan || !w_in || !w_out || !ms_out || steps < 1)
+    return fail(CFD_ERR_INVALID_ARGUMENT, "cfd_spec_profile: bad arguments");
+  cudaStream_t s = as_stream(stream);
+  const cfd::SpecParams& p = plan->p;
+  const size_t ns = (size_t)p.nx * (p.L + 1);
+  float2* w = reinterpret_cast<float2*>(w_out);
+  if (w_out != w_in)
+    CFD_CHECK(cudaMemcpyAsync(w_out, w_in, ns * sizeof(float2), cudaMemcpyDeviceToDevice, s),
+              "copy");
+  const int launches = 1 + steps * plan->stages * 3;
+  std::vector<cudaEvent_t> ev(2 * launches);
+  std::vector<int> kind;
+  for (auto& e : ev) CFD_CHECK(cudaEventCreate(&e), "cudaEventCreate");
+  int li = 0;
+  cudaError_t e = cudaSuccess;
+  auto rec = [&](int k, bool start) {
+    if (e == cudaSuccess) e = cudaEventRecord(ev[2 * li + (start ? 0 : 1)], s);
+    if (!start) {
+      kind.push_back(k);
+      ++li;
+    }
+  };
+  rec(2, true);
+  if (e == cudaSuccess) e = cfd::launch_spec_col_prep(p, w, plan->t4, s);
+  rec(2, false);
+  for (int st = 0; st < steps && e == cudaSuccess; ++st) {
+    for (int k = 0; k < plan->stages && e == cudaSuccess; ++k) {
+      rec(0, true);
+      if (e == cudaSuccess) e = cfd::launch_spec_row(p, plan->t4, plan->ahat, s);
+      rec(0, false);
+      cfd::StageCoef c = plan->coef[k];
+      const bool prep = !(st + 1 == steps && k + 1 == plan->stages);
+      c.prep_next = 0;
+      rec(1, true);
+      if (e == cudaSuccess) e = cfd::launch_spec_col_update(p, c, plan->ahat, w, plan->h, plan->t4, s);
+      rec(1, false);
+      if (prep) {
+        rec(2, true);
+        if (e == cudaSuccess) e = cfd::launch_spec_col_prep(p, w, plan->t4, s);
+        rec(2, false);
+      }
+    }
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  double sum[3] = {0, 0, 0};
+  int cnt[3] = {0, 0, 0};
+  for (int i = 0; i < li && e == cudaSuccess; ++i) {
+    float ms = 0.f;
+    e = cudaEventElapsedTime(&ms, ev[2 * i], ev[2 * i + 1]);
+    sum[kind[i]] += ms;
+    cnt[kind[i]] += 1;
+  }
+  for (auto& x : ev) cudaEventDestroy(x);
+  if (e != cudaSuccess) return cuda_fail(e, "cfd_spec_profile");
+  for (int k = 0; k < 3; ++k) ms_out[k] = cnt[k] ? (float)(sum[k] / cnt[k]) : 0.f;
   return CFD_OK;
 }
 

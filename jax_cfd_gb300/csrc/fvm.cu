@@ -30,11 +30,15 @@ constexpr int kStencilThreads = 256;
 // face normal and face velocity U.
 //   upwind        c_low  = U > 0 ? c0 : c1
 //   lax_wendroff  c_high = U > 0 ? c0 + 0.5(1-C)(c1-c0) : c1 - 0.5(1+C)(c1-c0)
-//   ratio         r = safe_div(U > 0 ? c0-cm : c2-c1, c1-c0)
+//   ratio         r = safe_div(num, den), num = U > 0 ? c0-cm : c2-c1,
+//                 den = c1-c0 (1 where c1 == c0)
 //   van Leer      phi = r > 0 ? 2r / (1+r) : 0
 //   face value    c_low - (c_low - c_high) * phi
-// Selecting r before the limiter equals selecting phi after it, because the
-// limiter is applied elementwise.
+// Selecting r before the limiter equals selecting phi after it (the limiter
+// is elementwise).  With r = num/den, 2r/(1+r) = 2 num / (den + num) and
+// r > 0 exactly when num and den are non-zero with equal signs, so the
+// limiter costs one division instead of two; the result differs from the
+// two-division form only in the last bits.
 CFD_D float tvd_flux(float cm, float c0, float c1, float c2, float U,
                      float cfl) {
   const float C = cfl * U;
@@ -45,8 +49,8 @@ CFD_D float tvd_flux(float cm, float c0, float c1, float c2, float U,
       pos ? c0 + (0.5f * (1.f - C)) * d0 : c1 - (0.5f * (1.f + C)) * d0;
   const float num = pos ? c0 - cm : c2 - c1;
   const float den = d0 != 0.f ? d0 : 1.f;
-  const float r = num / den;
-  const float phi = r > 0.f ? (2.f * r) / (1.f + r) : 0.f;
+  const bool rpos = (num > 0.f && den > 0.f) || (num < 0.f && den < 0.f);
+  const float phi = rpos ? __fdividef(2.f * num, den + num) : 0.f;
   const float cf = c_low - (c_low - c_high) * phi;
   return cf * U;
 }
@@ -92,8 +96,8 @@ __global__ void __launch_bounds__(kStencilThreads)
       float u = __ldg(ua + i * ny + j);
       float v = __ldg(va + i * ny + j);
       if (PROJECT) {
-        u = u - (sq[a + 1][b] - sq[a][b]) / p.hx;
-        v = v - (sq[a][b + 1] - sq[a][b]) / p.hy;
+        u = u - (sq[a + 1][b] - sq[a][b]) * p.inv_hx;
+        v = v - (sq[a][b + 1] - sq[a][b]) * p.inv_hy;
       }
       su[a][b] = u;
       sv[a][b] = v;
@@ -146,10 +150,10 @@ __global__ void __launch_bounds__(kStencilThreads)
     const int i = i0 + a, j = j0 + b;
     const float u = su[r][c], v = sv[r][c];
     // -divergence(flux): -((F[i] - F[i-1]) / hx + (F[j] - F[j-1]) / hy)
-    float ku = -((fx[a + 1][b] - fx[a][b]) / p.hx +
-                 (fy[a][b + 1] - fy[a][b]) / p.hy);
-    float kv = -((gx[a + 1][b] - gx[a][b]) / p.hx +
-                 (gy[a][b + 1] - gy[a][b]) / p.hy);
+    float ku = -((fx[a + 1][b] - fx[a][b]) * p.inv_hx +
+                 (fy[a][b + 1] - fy[a][b]) * p.inv_hy);
+    float kv = -((gx[a + 1][b] - gx[a][b]) * p.inv_hx +
+                 (gy[a][b + 1] - gy[a][b]) * p.inv_hy);
     if (p.has_visc) {
       // finite_differences.laplacian: -2c * sum(scales) + pairs * scale
       const float lu = ((-2.f * u) * p.ssum + (su[r - 1][c] + su[r + 1][c]) * p.sx) +
@@ -161,6 +165,156 @@ __global__ void __launch_bounds__(kStencilThreads)
     }
     if (p.has_forcing) {
       // sum_forcings(linear, constant): (0 + lin * u) + const
+      float fu = 0.f, fv = 0.f;
+      bool any_u = false, any_v = false;
+      if (p.has_lin) {
+        fu = p.lin * u;
+        fv = p.lin * v;
+        any_u = any_v = true;
+      }
+      if (p.fu_y) { fu = any_u ? fu + __ldg(p.fu_y + j) : __ldg(p.fu_y + j); any_u = true; }
+      if (p.fv_x) { fv = any_v ? fv + __ldg(p.fv_x + i) : __ldg(p.fv_x + i); any_v = true; }
+      if (p.fu_full) { const float f = __ldg(p.fu_full + i * ny + j); fu = any_u ? fu + f : f; any_u = true; }
+      if (p.fv_full) { const float f = __ldg(p.fv_full + i * ny + j); fv = any_v ? fv + f : f; any_v = true; }
+      if (!p.rho_is_one) {
+        fu = fu / p.density;
+        fv = fv / p.density;
+      }
+      if (any_u) ku = ku + fu;
+      if (any_v) kv = kv + fv;
+    }
+    if (OUT_K0) {
+      uo[i * ny + j] = ku;
+      vo[i * ny + j] = kv;
+    } else {
+      uo[i * ny + j] = u + p.dt * ku;
+      vo[i * ny + j] = v + p.dt * kv;
+    }
+  }
+}
+
+// The same step for grids whose shape is a multiple of the 16 x 64 tile, with
+// compile-time tile geometry: the halo box (rows i0-2 .. i0+17, columns
+// j0-4 .. j0+67) is loaded with aligned float4 reads (a 4-column group never
+// straddles the periodic seam because ny is a multiple of 4), face fluxes are
+// computed once per face into shared memory, and each thread then updates 4
+// cells of one column.
+constexpr int kBoxW = kTJ + 8;  // 72 columns: j0-4 .. j0+67
+template <bool PROJECT, bool OUT_K0, int CONVECT>
+__global__ void __launch_bounds__(kStencilThreads)
+    fvm_explicit_tiled_kernel(FvmParams p, const float* __restrict__ ua,
+                              const float* __restrict__ va,
+                              const float* __restrict__ q,
+                              float* __restrict__ uo, float* __restrict__ vo) {
+  __shared__ __align__(16) float su[kTI + 4][kBoxW];
+  __shared__ __align__(16) float sv[kTI + 4][kBoxW];
+  __shared__ __align__(16) float sq[PROJECT ? kTI + 5 : 1][PROJECT ? kBoxW : 4];
+  __shared__ float fx[kTI + 1][kTJ];
+  __shared__ float gx[kTI + 1][kTJ];
+  __shared__ float fy[kTI][kTJ + 1];
+  __shared__ float gy[kTI][kTJ + 1];
+
+  const int i0 = blockIdx.y * kTI, j0 = blockIdx.x * kTJ;
+  const int mx = p.nx - 1, my = p.ny - 1;
+  const int tid = threadIdx.x;
+  const size_t ny = (size_t)p.ny;
+  constexpr int kV4 = kBoxW / 4;  // float4 groups per box row
+
+  if (PROJECT) {
+    for (int idx = tid; idx < (kTI + 5) * kV4; idx += kStencilThreads) {
+      const int a = idx / kV4, k = idx - a * kV4;
+      const int i = (i0 - 2 + a) & mx, j = (j0 - 4 + 4 * k) & my;
+      *reinterpret_cast<float4*>(&sq[a][4 * k]) =
+          __ldg(reinterpret_cast<const float4*>(q + i * ny + j));
+    }
+    __syncthreads();
+  }
+  for (int idx = tid; idx < (kTI + 4) * kV4; idx += kStencilThreads) {
+    const int a = idx / kV4, k = idx - a * kV4;
+    const int i = (i0 - 2 + a) & mx, j = (j0 - 4 + 4 * k) & my;
+    float4 u = __ldg(reinterpret_cast<const float4*>(ua + i * ny + j));
+    float4 v = __ldg(reinterpret_cast<const float4*>(va + i * ny + j));
+    if (PROJECT) {
+      // u = u* - (q[i+1] - q[i]) / hx ; v = v* - (q[j+1] - q[j]) / hy
+      const int c = 4 * k;
+      const float q0 = sq[a][c], q1 = sq[a][c + 1], q2 = sq[a][c + 2], q3 = sq[a][c + 3];
+      const float q4 = sq[a][c + 4 < kBoxW ? c + 4 : c + 3];
+      u.x = u.x - (sq[a + 1][c] - q0) * p.inv_hx;
+      u.y = u.y - (sq[a + 1][c + 1] - q1) * p.inv_hx;
+      u.z = u.z - (sq[a + 1][c + 2] - q2) * p.inv_hx;
+      u.w = u.w - (sq[a + 1][c + 3] - q3) * p.inv_hx;
+      v.x = v.x - (q1 - q0) * p.inv_hy;
+      v.y = v.y - (q2 - q1) * p.inv_hy;
+      v.z = v.z - (q3 - q2) * p.inv_hy;
+      v.w = v.w - (q4 - q3) * p.inv_hy;  // last group unused (box column 71)
+    }
+    *reinterpret_cast<float4*>(&su[a][4 * k]) = u;
+    *reinterpret_cast<float4*>(&sv[a][4 * k]) = v;
+  }
+  __syncthreads();
+
+  const int b = tid & (kTJ - 1);
+  const int w = tid >> 6;  // 0..3
+  // x-normal faces: face a follows cell i0 - 1 + a (box row a + 1), a < 17.
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    const int a = w + 4 * k;
+    if (a <= kTI) {
+      const int c = b + 4;
+      const float U = 0.5f * su[a + 1][c] + 0.5f * su[a + 2][c];
+      const float Uv = 0.5f * su[a + 1][c] + 0.5f * su[a + 1][c + 1];
+      if (CONVECT == 0) {
+        fx[a][b] = tvd_flux(su[a][c], su[a + 1][c], su[a + 2][c], su[a + 3][c], U, p.cfl_x);
+        gx[a][b] = tvd_flux(sv[a][c], sv[a + 1][c], sv[a + 2][c], sv[a + 3][c], Uv, p.cfl_x);
+      } else {
+        fx[a][b] = U * U;
+        gx[a][b] = (0.5f * sv[a + 1][c] + 0.5f * sv[a + 2][c]) * Uv;
+      }
+    }
+  }
+  // y-normal faces: face f follows cell j0 - 1 + f (box column f + 3), f < 65;
+  // columns f = 0..63 by all threads, f = 64 by the first 16 threads.
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    int a, f;
+    if (k < 4) {
+      a = w + 4 * k;
+      f = b;
+    } else {
+      if (tid >= kTI) break;
+      a = tid;
+      f = kTJ;
+    }
+    const int r = a + 2, c = f + 3;
+    const float V = 0.5f * sv[r][c] + 0.5f * sv[r + 1][c];
+    const float Vv = 0.5f * sv[r][c] + 0.5f * sv[r][c + 1];
+    if (CONVECT == 0) {
+      fy[a][f] = tvd_flux(su[r][c - 1], su[r][c], su[r][c + 1], su[r][c + 2], V, p.cfl_y);
+      gy[a][f] = tvd_flux(sv[r][c - 1], sv[r][c], sv[r][c + 1], sv[r][c + 2], Vv, p.cfl_y);
+    } else {
+      fy[a][f] = (0.5f * su[r][c] + 0.5f * su[r][c + 1]) * V;
+      gy[a][f] = Vv * Vv;
+    }
+  }
+  __syncthreads();
+
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int a = w + 4 * k;
+    const int r = a + 2, c = b + 4;
+    const int i = i0 + a, j = j0 + b;
+    const float u = su[r][c], v = sv[r][c];
+    float ku = -((fx[a + 1][b] - fx[a][b]) * p.inv_hx + (fy[a][b + 1] - fy[a][b]) * p.inv_hy);
+    float kv = -((gx[a + 1][b] - gx[a][b]) * p.inv_hx + (gy[a][b + 1] - gy[a][b]) * p.inv_hy);
+    if (p.has_visc) {
+      const float lu = ((-2.f * u) * p.ssum + (su[r - 1][c] + su[r + 1][c]) * p.sx) +
+                       (su[r][c - 1] + su[r][c + 1]) * p.sy;
+      const float lv = ((-2.f * v) * p.ssum + (sv[r - 1][c] + sv[r + 1][c]) * p.sx) +
+                       (sv[r][c - 1] + sv[r][c + 1]) * p.sy;
+      ku = ku + p.nu * lu;
+      kv = kv + p.nu * lv;
+    }
+    if (p.has_forcing) {
       float fu = 0.f, fv = 0.f;
       bool any_u = false, any_v = false;
       if (p.has_lin) {
@@ -204,8 +358,8 @@ __global__ void __launch_bounds__(256, 2) fvm_div_rfft_kernel(FvmParams p, int r
   for (int idx = threadIdx.x; idx < rows * p.ny; idx += blockDim.x) {
     const int r = idx >> p.log2ny, j = idx & my;
     const int i = i0 + r, im = (i - 1) & mx, jm = (j - 1) & my;
-    const float dx = (__ldg(us + i * ny + j) - __ldg(us + im * ny + j)) / p.hx;
-    const float dy = (__ldg(vs + i * ny + j) - __ldg(vs + i * ny + jm)) / p.hy;
+    const float dx = (__ldg(us + i * ny + j) - __ldg(us + im * ny + j)) * p.inv_hx;
+    const float dy = (__ldg(vs + i * ny + j) - __ldg(vs + i * ny + jm)) * p.inv_hy;
     sd[idx] = dx + dy;
   }
   __syncthreads();
@@ -317,8 +471,8 @@ __global__ void fvm_project_out_kernel(FvmParams p, const float* __restrict__ us
     const float q0 = __ldg(q + idx);
     const float qx = __ldg(q + (size_t)((i + 1) & mx) * p.ny + j);
     const float qy = __ldg(q + (size_t)i * p.ny + ((j + 1) & my));
-    uo[idx] = __ldg(us + idx) - (qx - q0) / p.hx;
-    vo[idx] = __ldg(vs + idx) - (qy - q0) / p.hy;
+    uo[idx] = __ldg(us + idx) - (qx - q0) * p.inv_hx;
+    vo[idx] = __ldg(vs + idx) - (qy - q0) * p.inv_hy;
   }
 }
 
@@ -395,10 +549,17 @@ cudaError_t launch_fvm_explicit(const FvmParams& p, bool project, bool out_k0,
                                 const float* ua, const float* va,
                                 const float* q, float* uo, float* vo,
                                 cudaStream_t s) {
-  const int ti = p.nx < kTI ? p.nx : kTI, tj = p.ny < kTJ ? p.ny : kTJ;
+  const bool tiled = p.nx % kTI == 0 && p.ny % kTJ == 0;
+  const int ti = tiled ? kTI : (p.nx < kTI ? p.nx : kTI);
+  const int tj = tiled ? kTJ : (p.ny < kTJ ? p.ny : kTJ);
   dim3 grid(p.ny / tj, p.nx / ti);
-#define CFD_EXPLICIT(PR, K0, CV) \
-  fvm_explicit_kernel<PR, K0, CV><<<grid, kStencilThreads, 0, s>>>(p, ua, va, q, uo, vo)
+#define CFD_EXPLICIT(PR, K0, CV)                                                         \
+  do {                                                                                   \
+    if (tiled)                                                                           \
+      fvm_explicit_tiled_kernel<PR, K0, CV><<<grid, kStencilThreads, 0, s>>>(p, ua, va, q, uo, vo); \
+    else                                                                                 \
+      fvm_explicit_kernel<PR, K0, CV><<<grid, kStencilThreads, 0, s>>>(p, ua, va, q, uo, vo);       \
+  } while (0)
   if (p.convect == 0) {
     if (project) {
       if (out_k0) CFD_EXPLICIT(true, true, 0); else CFD_EXPLICIT(true, false, 0);

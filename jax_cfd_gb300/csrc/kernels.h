@@ -11,6 +11,7 @@ struct FvmParams {
   int nx, ny;          // grid shape; axis 1 (y, index j) is contiguous
   int log2nx, log2ny;
   float hx, hy;        // float32(step)
+  float inv_hx, inv_hy;  // float32(1 / float32(step)): x / h is taken as x * (1/h)
   float cfl_x, cfl_y;  // float32(dt / step): Lax-Wendroff Courant factors
   float dt;            // float32(dt)
   float nu;            // float32(viscosity / density)

@@ -111,6 +111,18 @@ class FvmPlan:
               'cfd_fvm_step')
     return u_out, v_out
 
+  PROFILE_KINDS = ('explicit', 'div_rfft', 'col_pinv', 'irfft', 'project_out')
+
+  def profile(self, u, v, steps: int):
+    """Mean per-launch duration (ms) of each kernel kind over `steps` steps,
+    from CUDA events recorded around every launch on the current stream."""
+    uo, vo = torch.empty_like(u), torch.empty_like(v)
+    ms = (ctypes.c_float * 5)()
+    a = self._fields(u, v, uo, vo)
+    nat.check(self._lib.cfd_fvm_profile(self._h, current_stream_ptr(u.device), *a, int(steps),
+                                        ctypes.cast(ms, ctypes.c_void_p)), 'cfd_fvm_profile')
+    return dict(zip(self.PROFILE_KINDS, (float(x) for x in ms)))
+
   def explicit_terms(self, u, v):
     du, dv = torch.empty_like(u), torch.empty_like(v)
     a = self._fields(u, v, du, dv)
@@ -233,6 +245,18 @@ class SpecPlan:
     nat.check(self._lib.cfd_spec_step(self._h, current_stream_ptr(w_hat.device), ptr(w_hat),
                                       ptr(out), int(steps)), 'cfd_spec_step')
     return out
+
+  PROFILE_KINDS = ('row', 'col_update', 'col_prep')
+
+  def profile(self, w_hat: torch.Tensor, steps: int):
+    """Mean per-launch duration (ms) of each spectral kernel kind."""
+    self._half(w_hat, 'vorticity_hat')
+    out = torch.empty_like(w_hat)
+    ms = (ctypes.c_float * 3)()
+    nat.check(self._lib.cfd_spec_profile(self._h, current_stream_ptr(w_hat.device), ptr(w_hat),
+                                         ptr(out), int(steps), ctypes.cast(ms, ctypes.c_void_p)),
+              'cfd_spec_profile')
+    return dict(zip(self.PROFILE_KINDS, (float(x) for x in ms)))
 
   def explicit_terms(self, w_hat: torch.Tensor) -> torch.Tensor:
     self._half(w_hat, 'vorticity_hat')
