@@ -114,6 +114,22 @@ int cfd_fvm_divergence(cfd_fvm_plan* plan, void* stream, const float* u,
 int cfd_fvm_curl_2d(cfd_fvm_plan* plan, void* stream, const float* u,
                     const float* v, float* out);
 
+/* Pressure projection that allocates nothing -- no counterpart in the
+ * reference.  For callers that cannot call cudaMalloc (while capturing into a
+ * graph memory pool they do not own, under allocators that forbid allocation
+ * after start-up, or as a plugin handed only pre-allocated buffers): same
+ * result as cfd_fvm_projection, without a plan.  Its scratch (row spectrum,
+ * twiddles, Laplacian eigenvalues) is a fixed __device__ array that every GPU
+ * loading the library keeps until exit.  Limit: nx * ny <= 262144 (512 x 512),
+ * sides powers of two in [4, 4096]; larger grids return
+ * CFD_ERR_INVALID_ARGUMENT.  The first call on a device looks up the array's
+ * device address (cudaGetSymbolAddress), so make that first call before any
+ * stream capture.  All calls share the array: calls that overlap on the GPU
+ * race and must be ordered by the caller.  u_out/v_out may alias u/v. */
+int cfd_fvm_projection_noalloc(void* stream, int nx, int ny, double hx,
+                               double hy, const float* u, const float* v,
+                               float* u_out, float* v_out);
+
 /* max over cells of sqrt(u^2 + v^2) written as one float to device memory. */
 int cfd_max_speed(void* stream, int n, const float* u, const float* v,
                   float* out);

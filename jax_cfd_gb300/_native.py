@@ -73,6 +73,8 @@ _SIGNATURES = {
     'cfd_fvm_pressure_solve': (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp]),
     'cfd_fvm_divergence': (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp]),
     'cfd_fvm_curl_2d': (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp]),
+    'cfd_fvm_projection_noalloc': (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                                   ctypes.c_double, _vp, _vp, _vp, _vp]),
     'cfd_max_speed': (ctypes.c_int, [_vp, ctypes.c_int, _vp, _vp, _vp]),
     'cfd_scale_to_max_speed': (ctypes.c_int, [_vp, ctypes.c_int, _vp, _vp, _vp, ctypes.c_double]),
     'cfd_spec_plan_create': (ctypes.c_int, [ctypes.POINTER(SpecConfig), ctypes.POINTER(_vp)]),

@@ -65,6 +65,10 @@ cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
 }  // namespace
 
+namespace cfd {
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+}  // namespace cfd
+
 struct cfd_fvm_plan {
   cfd::FvmParams p;
   float* au = nullptr;

@@ -3,7 +3,12 @@
 
 #include <cuda_runtime.h>
 
+#include <string>
+
 namespace cfd {
+
+// Records the message cfd_last_error() returns on this thread.
+void set_last_error(const std::string& msg);
 
 // Parameters of the staggered-grid (FVM) explicit step, already rounded to
 // float32 the way the reference rounds its weakly typed Python scalars.

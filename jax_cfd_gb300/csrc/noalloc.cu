@@ -1,0 +1,155 @@
+// Pressure projection that allocates nothing on the device.
+//
+// Some callers cannot call cudaMalloc: code that runs while a CUDA graph is
+// being captured into a pool they do not own, allocators that forbid
+// allocation after start-up (real-time or embedded hosts that reserve all
+// device memory up front), and plugin hosts that hand the library only
+// pre-allocated input and output buffers.  For them,
+// cfd_fvm_projection_noalloc does the same work as cfd_fvm_projection (the
+// real-FFT solve_fast_diag pressure projection) without a plan: its scratch
+// -- the packed row spectrum / pressure field and the twiddle and Laplacian
+// eigenvalue tables -- lives in one file-scope __device__ array of fixed size,
+// which every GPU that loads this library holds until the process exits.
+//
+// Limit: nx * ny <= kNoallocMaxCells (512 * 512 cells), each side a power of
+// two in [4, 4096].  The array is shared by every call on a device and keeps
+// the previous call's contents; every byte a call reads is written earlier in
+// the same call (tables first, then the spectrum), so nothing needs clearing.
+// Calls whose work overlaps on the GPU (different streams, or different host
+// threads on one device) race on the array; callers must order them.
+#include <cmath>
+#include <mutex>
+#include <string>
+
+#include "../../include/cfd_gb300.h"
+#include "common.cuh"
+#include "kernels.h"
+
+namespace {
+
+constexpr int kNoallocMaxCells = 512 * 512;
+constexpr int kNoallocMaxSide = 4096;
+// Layout (in floats): spectrum [nx*ny] | tw_x [2*nx] | tw_y [2*ny] |
+// lam_x [nx] | lam_y [ny/2 + 1], each region rounded up to 64 floats.
+constexpr int kNoallocFloats =
+    kNoallocMaxCells + 2 * kNoallocMaxSide + 2 * kNoallocMaxSide + kNoallocMaxSide +
+    (kNoallocMaxSide / 2 + 1) + 5 * 64;
+
+__device__ __align__(256) float g_noalloc_scratch[kNoallocFloats];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mu;
+float* g_noalloc_ptr[kMaxDevices] = {};
+
+int round64(int n) { return (n + 63) & ~63; }
+
+// Twiddles exp(-2 pi i k / n) and Laplacian eigenvalues
+// (2 cos(2 pi k / n) - 2) / h^2 (array_utils.py:168-173, the fft of the
+// circulant's first column), in double precision, rounded once to float.
+__global__ void noalloc_tables_kernel(int nx, int ny, double hx, double hy,
+                                      float2* tw_x, float2* tw_y, float* lam_x,
+                                      float* lam_y) {
+  const int total = nx + ny + nx + (ny / 2 + 1);
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total;
+       t += gridDim.x * blockDim.x) {
+    if (t < nx) {
+      double s, c;
+      sincospi(-2.0 * t / nx, &s, &c);
+      tw_x[t] = make_float2((float)c, (float)s);
+    } else if (t < nx + ny) {
+      const int k = t - nx;
+      double s, c;
+      sincospi(-2.0 * k / ny, &s, &c);
+      tw_y[k] = make_float2((float)c, (float)s);
+    } else if (t < 2 * nx + ny) {
+      const int k = t - nx - ny;
+      lam_x[k] = k == 0 ? 0.f : (float)((2.0 * cospi(2.0 * k / nx) - 2.0) / (hx * hx));
+    } else {
+      const int k = t - 2 * nx - ny;
+      lam_y[k] = k == 0 ? 0.f : (float)((2.0 * cospi(2.0 * k / ny) - 2.0) / (hy * hy));
+    }
+  }
+}
+
+int noalloc_fail(int code, const std::string& msg) {
+  cfd::set_last_error(msg);
+  return code;
+}
+
+// Device address of the scratch array for the current device.  The first call
+// on each device looks it up with cudaGetSymbolAddress (host code may not use
+// the array's name as a device pointer).
+int noalloc_scratch(float** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return noalloc_fail(CFD_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+  if (dev < 0 || dev >= kMaxDevices) return noalloc_fail(CFD_ERR_UNSUPPORTED, "device ordinal out of range");
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p)
+      return noalloc_fail(CFD_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+    g_noalloc_ptr[dev] = static_cast<float*>(p);
+  }
+  *out = g_noalloc_ptr[dev];
+  return CFD_OK;
+}
+
+}  // namespace
+
+extern "C" int cfd_fvm_projection_noalloc(void* stream, int nx, int ny, double hx,
+                                          double hy, const float* u, const float* v,
+                                          float* u_out, float* v_out) {
+  if (!u || !v || !u_out || !v_out)
+    return noalloc_fail(CFD_ERR_INVALID_ARGUMENT, "cfd_fvm_projection_noalloc: null pointer");
+  if (!is_pow2(nx) || !is_pow2(ny) || nx < 4 || ny < 4 || nx > kNoallocMaxSide ||
+      ny > kNoallocMaxSide)
+    return noalloc_fail(CFD_ERR_INVALID_ARGUMENT,
+                        "cfd_fvm_projection_noalloc: nx and ny must be powers of two in [4, 4096]");
+  if ((long long)nx * ny > kNoallocMaxCells)
+    return noalloc_fail(CFD_ERR_INVALID_ARGUMENT,
+                        "cfd_fvm_projection_noalloc: nx * ny exceeds the static scratch limit of "
+                        "262144 cells (512 x 512); use cfd_fvm_projection with a plan");
+  if (!(hx > 0) || !(hy > 0))
+    return noalloc_fail(CFD_ERR_INVALID_ARGUMENT, "cfd_fvm_projection_noalloc: invalid grid step");
+  float* base = nullptr;
+  int rc = noalloc_scratch(&base);
+  if (rc != CFD_OK) return rc;
+
+  float* spec = base;
+  float2* tw_x = reinterpret_cast<float2*>(spec + round64(nx * ny));
+  float2* tw_y = reinterpret_cast<float2*>(reinterpret_cast<float*>(tw_x) + round64(2 * nx));
+  float* lam_x = reinterpret_cast<float*>(tw_y) + round64(2 * ny);
+  float* lam_y = lam_x + round64(nx);
+
+  cfd::FvmParams p{};
+  p.nx = nx;
+  p.ny = ny;
+  p.log2nx = ilog2(nx);
+  p.log2ny = ilog2(ny);
+  p.hx = (float)hx;
+  p.hy = (float)hy;
+  p.inv_hx = 1.f / p.hx;
+  p.inv_hy = 1.f / p.hy;
+  p.cutoff = 10.f * 1.1920928955078125e-07f;
+  p.pinv_scale = 1.f / ((float)nx * (float)ny);
+  p.lamx = lam_x;
+  p.lamy = lam_y;
+  p.tw_x = tw_x;
+  p.tw_y = tw_y;
+
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  const int total = 2 * nx + ny + ny / 2 + 1;
+  noalloc_tables_kernel<<<(total + 255) / 256, 256, 0, s>>>(nx, ny, hx, hy, tw_x, tw_y,
+                                                            lam_x, lam_y);
+  cudaError_t e = cudaGetLastError();
+  float2* sp = reinterpret_cast<float2*>(spec);
+  if (e == cudaSuccess) e = cfd::launch_fvm_div_rfft(p, u, v, sp, s);
+  if (e == cudaSuccess) e = cfd::launch_fvm_col_pinv(p, sp, s);
+  if (e == cudaSuccess) e = cfd::launch_fvm_irfft(p, sp, s);
+  if (e == cudaSuccess) e = cfd::launch_fvm_project_out(p, u, v, spec, u_out, v_out, s);
+  if (e != cudaSuccess)
+    return noalloc_fail(CFD_ERR_CUDA, std::string("cfd_fvm_projection_noalloc: ") + cudaGetErrorString(e));
+  return CFD_OK;
+}
