@@ -151,6 +151,22 @@ def _json_line(obj):
   print(json.dumps(obj), flush=True)
 
 
+def max_over_ranks(x: float) -> float:
+  """Max of a per-rank float over the process group (identity without one).
+
+  Ranks are independent replicas, so this is the only cross-rank operation:
+  the slowest rank's timed region defines the job's time."""
+  import torch  # pylint: disable=import-outside-toplevel
+  import torch.distributed as dist  # pylint: disable=import-outside-toplevel
+  if not (dist.is_available() and dist.is_initialized()):
+    return float(x)
+  dev = (torch.device('cuda', torch.cuda.current_device())
+         if dist.get_backend() == 'nccl' else torch.device('cpu'))
+  t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+  dist.all_reduce(t, op=dist.ReduceOp.MAX)
+  return float(t.item())
+
+
 # ---------------------------------------------------------------------------
 # Reference arm: the jax-cfd algorithm on the host CPU.
 # ---------------------------------------------------------------------------
@@ -250,11 +266,7 @@ def run_gb300(args):
     wall = time.perf_counter() - t0
   barrier()
   chunk_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-  total_s = sum(chunk_ms) / 1000.0
-  if dist is not None:
-    t = torch.tensor([total_s], device=dev)
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    total_s = float(t)
+  total_s = max_over_ranks(sum(chunk_ms) / 1000.0)
   cells = n * n
   value = world * cells * chunk * args.steps / total_s
   finite = bool(torch.isfinite(v[0].data).all() and torch.isfinite(v[1].data).all())

@@ -389,6 +389,16 @@ def pinv_diagonal(grid: Grid, dtype=np.float32) -> np.ndarray:
   return diag.astype(cdtype)
 
 
+def fast_diag_pinv(rhs, grid: Grid, diag=None):
+  """Pseudoinverse of the periodic Laplacian applied to ``rhs`` through the
+  rfft diagonalisation (fast_diagonalization.py:199-225, 228-266)."""
+  if diag is None:
+    diag = pinv_diagonal(grid, rhs.dtype)
+  axes = tuple(range(rhs.ndim))
+  out = np.fft.irfftn(diag * np.fft.rfftn(rhs), s=rhs.shape, axes=axes)
+  return out.astype(rhs.dtype)
+
+
 def solve_fast_diag(v, grid: Grid, diag=None):
   """pressure.py:115-157 with the periodic 'rfft' implementation."""
   rhs = divergence(v, grid.step)

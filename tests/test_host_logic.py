@@ -1,0 +1,155 @@
+"""Host-side logic of the drop-in API and the C ABI (CPU only, no GPU work).
+
+* the native library loads and exports every entry point the public header
+  declares (no compute calls: there is no GPU here);
+* argument pattern-matching of semi_implicit_navier_stokes onto the fused
+  kernels, with the reference's exception types for unsupported options;
+* forcing descriptors, grid geometry and driver semantics.
+"""
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+import torch
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def _header_functions():
+  text = (ROOT / 'include' / 'cfd_gb300.h').read_text()
+  text = re.sub(r'/\*.*?\*/', '', text, flags=re.S)
+  return sorted(set(re.findall(r'\b(cfd_[a-z0-9_]+)\s*\(', text)))
+
+
+@pytest.fixture(scope='module')
+def lib():
+  from jax_cfd_gb300 import _native, build_native
+  build_native.build()
+  return _native.load()
+
+
+def test_library_exports_every_declared_symbol(lib):
+  declared = _header_functions()
+  assert 'cfd_fvm_step' in declared and 'cfd_spec_step' in declared
+  for name in declared:
+    assert hasattr(lib, name), name
+
+
+def test_binding_declares_exactly_the_header(lib):
+  from jax_cfd_gb300 import _native
+  assert sorted(_native.exported_symbols()) == _header_functions()
+
+
+def test_status_codes_map_to_reference_exceptions(lib):
+  from jax_cfd_gb300 import _native
+  _native.check(_native.CFD_OK)
+  for code, exc in ((_native.CFD_ERR_INVALID_ARGUMENT, ValueError),
+                    (_native.CFD_ERR_UNSUPPORTED, NotImplementedError),
+                    (_native.CFD_ERR_OUT_OF_MEMORY, MemoryError),
+                    (_native.CFD_ERR_CUDA, RuntimeError)):
+    with pytest.raises(exc):
+      _native.check(code)
+
+
+def test_plan_rejects_non_power_of_two_before_touching_the_gpu(lib):
+  import ctypes
+  from jax_cfd_gb300 import _native
+  cfg = _native.FvmConfig()
+  cfg.nx, cfg.ny, cfg.hx, cfg.hy, cfg.density, cfg.dt = 100, 100, 0.1, 0.1, 1.0, 1e-3
+  handle = ctypes.c_void_p()
+  rc = lib.cfd_fvm_plan_create(ctypes.byref(cfg), ctypes.byref(handle))
+  assert rc == _native.CFD_ERR_UNSUPPORTED
+  assert 'powers of two' in _native.last_error()
+
+
+def _grid(n=64):
+  import jax_cfd_gb300.base as cfd
+  return cfd.grids.Grid((n, n), domain=((0, 2 * np.pi), (0, 2 * np.pi)))
+
+
+def test_grid_geometry_matches_reference_conventions():
+  from oracle import fvm
+  g = _grid()
+  og = fvm.Grid.make((64, 64), domain=((0, 2 * np.pi), (0, 2 * np.pi)))
+  assert g.step == og.step
+  assert g.cell_faces == ((1.0, 0.5), (0.5, 1.0))
+  for a, b in zip(g.mesh_numpy(g.cell_faces[0]), og.mesh(og.cell_faces[0])):
+    np.testing.assert_array_equal(a, b)
+  for a, b in zip(g.rfft_axes_numpy(), (fvm.fftfreq(64, g.step[0]), fvm.rfftfreq(64, g.step[1]))):
+    np.testing.assert_array_equal(a, b)
+
+
+def test_kolmogorov_descriptor_matches_oracle_field():
+  import jax_cfd_gb300.base as cfd
+  from jax_cfd_gb300 import _native
+  from oracle import fvm
+  g = _grid()
+  og = fvm.Grid.make((64, 64), domain=((0, 2 * np.pi), (0, 2 * np.pi)))
+  f = cfd.forcings.simple_turbulence_forcing(g, 1, 4, -0.1)
+  assert f.linear == -0.1 and f.const_kind == _native.FORCE_U_OF_Y
+  want_u = fvm.kolmogorov_forcing(og, 1, 4)(None)[0]
+  np.testing.assert_array_equal(np.broadcast_to(f.const_u[None, :], (64, 64)), want_u)
+  spec = cfd.forcings.kolmogorov_forcing(g, k=4, offsets=((0, 0), (0, 0)))
+  fu, fv = spec.constant_fields()
+  np.testing.assert_array_equal(fu, fvm.kolmogorov_forcing(og, k=4, offsets=((0, 0), (0, 0)))(None)[0])
+  assert fv is None
+
+
+def test_unsupported_options_raise_not_implemented():
+  import jax_cfd_gb300.base as cfd
+  g = _grid()
+  with pytest.raises(NotImplementedError):
+    cfd.equations.semi_implicit_navier_stokes(1.0, 1e-3, 1e-3, g, convect=lambda v: v)
+  with pytest.raises(NotImplementedError):
+    cfd.equations.semi_implicit_navier_stokes(1.0, 1e-3, 1e-3, g,
+                                              pressure_solve=cfd.pressure.solve_cg)
+  with pytest.raises(NotImplementedError):
+    cfd.equations.semi_implicit_navier_stokes(1.0, 1e-3, 1e-3, g,
+                                              time_stepper=cfd.time_stepping.classic_rk4)
+  with pytest.raises(NotImplementedError):
+    cfd.equations.semi_implicit_navier_stokes(1.0, 1e-3, 1e-3, g, diffuse=lambda c, nu: c)
+  three = cfd.forcings.sum_forcings(cfd.forcings.linear_forcing(g, 1.0),
+                                    cfd.forcings.linear_forcing(g, 2.0),
+                                    cfd.forcings.kolmogorov_forcing(g))
+  with pytest.raises(NotImplementedError):
+    cfd.equations.semi_implicit_navier_stokes(1.0, 1e-3, 1e-3, g, forcing=three)
+
+
+def test_step_function_is_built_without_gpu_work():
+  import jax_cfd_gb300.base as cfd
+  g = _grid()
+  step = cfd.equations.semi_implicit_navier_stokes(
+      1.0, 1e-3, 1e-3, g, forcing=cfd.forcings.simple_turbulence_forcing(g, 1, 4, -0.1))
+  assert isinstance(step, cfd.equations.FvmStep)
+  assert cfd.funcutils.repeated(step, 3).gb300_steps == 3
+
+
+def test_stable_time_step_raises_like_reference():
+  import jax_cfd_gb300.base as cfd
+  g = _grid(2048)
+  assert abs(cfd.equations.stable_time_step(2.0, 0.5, 1e-3, g) - 7.66990e-4) < 1e-9
+  with pytest.raises(ValueError):
+    cfd.equations.stable_time_step(2.0, 0.5, 1.0, g)
+
+
+def test_repeated_and_trajectory_host_semantics():
+  import jax_cfd_gb300.base as cfd
+  f = lambda x: x + 1
+  assert cfd.funcutils.repeated(f, 5)(torch.zeros(2)).tolist() == [5.0, 5.0]
+  final, frames = cfd.funcutils.trajectory(f, 3)(torch.zeros(2))
+  assert final.tolist() == [3.0, 3.0]
+  assert frames[:, 0].tolist() == [1.0, 2.0, 3.0]
+  _, frames = cfd.funcutils.trajectory(f, 3, start_with_input=True)(torch.zeros(2))
+  assert frames[:, 0].tolist() == [0.0, 1.0, 2.0]
+
+
+def test_brick_wall_filter_mirror():
+  from jax_cfd_gb300.base import grids
+  from jax_cfd_gb300.spectral import utils as su
+  from oracle import fvm
+  from oracle import spectral as ospec
+  for n in (64, 128):
+    g = grids.Grid((n, n))
+    got = su.brick_wall_filter_2d(g, device='cpu').numpy()
+    np.testing.assert_array_equal(got, ospec.brick_wall_filter_2d(fvm.Grid.make((n, n))))
