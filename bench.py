@@ -245,9 +245,16 @@ def run_gb300(args):
   flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
   stream = torch.cuda.current_stream(dev)
 
+  # Every bench step advances the same seeded initial condition by `chunk`
+  # steps.  (A single 2000-step trajectory of this configuration leaves the
+  # explicit scheme's stability region: the forcing accelerates the flow past
+  # the speed dt was chosen for, and the reference algorithm overflows near
+  # t = 0.9 at 2048^2 -- the oracle and this path blow up at the same step.)
+  plan = step.plan(dev)
+  shape = plan.autotune(v0[0].data, v0[1].data, 20)
   v = v0
   for _ in range(args.warmup):
-    v = run(v)
+    v = run(v0)
   torch.cuda.synchronize(dev)
 
   starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
@@ -260,7 +267,7 @@ def run_gb300(args):
     for k in range(args.steps):
       flush.zero_()
       starts[k].record(stream)
-      v = run(v)
+      v = run(v0)
       ends[k].record(stream)
     torch.cuda.synchronize(dev)
     wall = time.perf_counter() - t0
@@ -272,8 +279,7 @@ def run_gb300(args):
   finite = bool(torch.isfinite(v[0].data).all() and torch.isfinite(v[1].data).all())
 
   # Per-kernel durations (second pass, same workload and state).
-  plan = step.plan(dev)
-  kernel_ms = plan.profile(v[0].data, v[1].data, chunk)
+  kernel_ms = plan.profile(v0[0].data, v0[1].data, chunk)
   kernel_time = {k: kernel_ms[k] * (chunk if k != 'project_out' else 1) for k in kernel_ms}
   dominant = max(kernel_time, key=kernel_time.get)
   peak, peak_kind = _peaks()
@@ -312,11 +318,12 @@ def run_gb300(args):
   spectral = None
   if not args.skip_spectral:
     from jax_cfd_gb300.spectral import utils as su  # pylint: disable=import-outside-toplevel
-    w = su.rfft2(cfd.finite_differences.curl_2d(v0).data, grid)
+    w0 = su.rfft2(cfd.finite_differences.curl_2d(v0).data, grid)
     eq = seq.ForcedNavierStokes2D(VISCOSITY, grid, smooth=True)
     sstep = sts.crank_nicolson_rk4(eq, 1e-3)
     srun = cfd.funcutils.repeated(sstep, args.spectral_chunk)
-    w = srun(w)
+    for _ in range(3):
+      w = srun(w0)
     torch.cuda.synchronize(dev)
     s0 = torch.cuda.Event(enable_timing=True)
     s1 = torch.cuda.Event(enable_timing=True)
@@ -324,12 +331,12 @@ def run_gb300(args):
     for _ in range(3):
       flush.zero_()
       s0.record(stream)
-      w = srun(w)
+      w = srun(w0)
       s1.record(stream)
       torch.cuda.synchronize(dev)
       s_ms += s0.elapsed_time(s1)
     s_value = cells * args.spectral_chunk * 3 / (s_ms / 1000.0)
-    sk = sstep.plan(dev).profile(w, 2)
+    sk = sstep.plan(dev).profile(w0, 2)
     s_dom = max(('row', 'col_update', 'col_prep'), key=lambda k: sk[k])
     s_ach = SPEC_BYTES_PER_CELL[s_dom] * cells / (sk[s_dom] / 1000.0) / 1e9
     spectral = {
@@ -366,6 +373,7 @@ def run_gb300(args):
                              f'{chunk} time steps per bench step',
                  'grid': [n, n], 'time_steps_per_step': chunk, 'dt': dt,
                  'l2': 'flushed (256 MiB write) between bench steps',
+                 'transform_shape': ['wide', 'narrow'][shape],
                  'parallelism': 'replicas' if world > 1 else 'single'},
       'roofline': {'kernel': dominant, 'bound': 'hbm', 'achieved': achieved, 'peak': peak,
                    'unit': 'GB/s', 'frac': achieved / peak, 'traffic': traffic,

@@ -101,6 +101,13 @@ int cfd_fvm_step(cfd_fvm_plan* plan, void* stream, const float* u,
 int cfd_fvm_profile(cfd_fvm_plan* plan, void* stream, const float* u,
                     const float* v, float* u_out, float* v_out, int steps,
                     float* ms_out);
+/* Autotuner: times `steps` steps for each candidate launch shape of the
+ * transform kernels (u, v read-only; results go to the scratch arrays),
+ * keeps the fastest in the plan and writes its index to *chosen (may be
+ * NULL).  Synchronises the stream. */
+int cfd_fvm_plan_autotune(cfd_fvm_plan* plan, void* stream, const float* u,
+                          const float* v, float* u_scratch, float* v_scratch,
+                          int steps, int* chosen);
 /* du/dt from advection + diffusion + forcing (no projection). */
 int cfd_fvm_explicit_terms(cfd_fvm_plan* plan, void* stream, const float* u,
                            const float* v, float* du, float* dv);

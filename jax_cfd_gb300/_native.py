@@ -67,6 +67,7 @@ _SIGNATURES = {
     'cfd_fvm_plan_destroy': (ctypes.c_int, [_vp]),
     'cfd_fvm_plan_bytes': (ctypes.c_longlong, [_vp]),
     'cfd_fvm_step': (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_int]),
+    'cfd_fvm_plan_autotune': (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_int, _vp]),
     'cfd_fvm_profile': (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_int, _vp]),
     'cfd_fvm_explicit_terms': (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp]),
     'cfd_fvm_projection': (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp]),

@@ -8,7 +8,7 @@
 
 #include "../../include/cfd_gb300.h"
 #include "kernels.h"
-#include "common.cuh"
+#include "fft.cuh"
 
 namespace {
 
@@ -37,6 +37,27 @@ std::vector<float2> twiddles(int n) {
   for (int k = 0; k < n; ++k) {
     const double a = -2.0 * M_PI * (double)k / (double)n;
     t[k] = make_float2((float)std::cos(a), (float)std::sin(a));
+  }
+  return t;
+}
+
+// Concatenated pass twiddle tables of a length-2^log2L FFT (layout in
+// fft.cuh): entry [r-1][k] of the pass with span Ns and radix R is
+// exp(-2 pi i r k / (Ns R)), computed in double and rounded once.
+std::vector<float2> pass_twiddles(int log2L) {
+  std::vector<float2> t(cfd::fft_pass_table_size(log2L) > 0 ? cfd::fft_pass_table_size(log2L) : 1);
+  int off = 0, ns = 1;
+  for (int q = 0; q < cfd::fft_num_passes(log2L); ++q) {
+    const int R = cfd::fft_pass_radix(log2L, q);
+    if (ns > 1) {
+      for (int r = 1; r < R; ++r)
+        for (int k = 0; k < ns; ++k) {
+          const double a = -2.0 * M_PI * (double)r * (double)k / ((double)ns * R);
+          t[off + (r - 1) * ns + k] = make_float2((float)std::cos(a), (float)std::sin(a));
+        }
+      off += (R - 1) * ns;
+    }
+    ns *= R;
   }
   return t;
 }
@@ -78,8 +99,9 @@ struct cfd_fvm_plan {
   float2* spec = nullptr;  // packed row spectrum / pressure q (nx * ny floats)
   float* lamx = nullptr;
   float* lamy = nullptr;
-  float2* twx = nullptr;
   float2* twy = nullptr;
+  float2* twpx = nullptr;
+  float2* twpy = nullptr;
   float* fu = nullptr;
   float* fv = nullptr;
   long long bytes = 0;
@@ -94,8 +116,9 @@ struct cfd_spec_plan {
   float2* h = nullptr;
   float2* fc = nullptr;     // forcing curl table (full or row 0)
   float2* work = nullptr;   // scratch spectrum for rfft2 / irfft2 / filter
-  float2* twx = nullptr;
   float2* twy = nullptr;
+  float2* twpx = nullptr;
+  float2* twpy = nullptr;
   float* kx = nullptr;
   float* ky = nullptr;
   long long bytes = 0;
@@ -110,7 +133,7 @@ int cfd_version(void) { return 1; }
 int cfd_fvm_plan_destroy(cfd_fvm_plan* plan) {
   if (!plan) return CFD_OK;
   void* ptrs[] = {plan->au, plan->av, plan->bu, plan->bv, plan->spec, plan->lamx,
-                  plan->lamy, plan->twx, plan->twy, plan->fu, plan->fv};
+                  plan->lamy, plan->twy, plan->twpx, plan->twpy, plan->fu, plan->fv};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   delete plan;
@@ -164,6 +187,9 @@ int cfd_fvm_plan_create(const cfd_fvm_config* cfg, cfd_fvm_plan** out) {
   p.convect = cfg->convect;
   p.cutoff = 10.f * 1.1920928955078125e-07f;  // 10 * finfo(float32).eps
   p.pinv_scale = 1.f / ((float)nx * (float)ny);
+  // Narrow transform blocks keep large grids resident in one wave; the
+  // autotuner can revise the choice on the device.
+  p.fft_shape = (nx >= 1024 && ny >= 1024) ? 1 : 0;
 
   const size_t n = (size_t)nx * ny;
   cudaError_t e;
@@ -186,19 +212,23 @@ int cfd_fvm_plan_create(const cfd_fvm_config* cfg, cfd_fvm_plan** out) {
 
   std::vector<float> lamx = laplacian_eigenvalues(nx, cfg->hx, nx);
   std::vector<float> lamy = laplacian_eigenvalues(ny, cfg->hy, ny / 2 + 1);
-  std::vector<float2> twx = twiddles(nx), twy = twiddles(ny);
+  std::vector<float2> twy = twiddles(ny);
+  std::vector<float2> twpx = pass_twiddles(p.log2nx), twpy = pass_twiddles(p.log2ny - 1);
   if ((e = upload(&plan->lamx, lamx.data(), lamx.size())) != cudaSuccess ||
       (e = upload(&plan->lamy, lamy.data(), lamy.size())) != cudaSuccess ||
-      (e = upload(&plan->twx, twx.data(), twx.size())) != cudaSuccess ||
-      (e = upload(&plan->twy, twy.data(), twy.size())) != cudaSuccess) {
+      (e = upload(&plan->twy, twy.data(), twy.size())) != cudaSuccess ||
+      (e = upload(&plan->twpx, twpx.data(), twpx.size())) != cudaSuccess ||
+      (e = upload(&plan->twpy, twpy.data(), twpy.size())) != cudaSuccess) {
     cfd_fvm_plan_destroy(plan);
     return cuda_fail(e, "cfd_fvm_plan_create: tables");
   }
-  bytes += (long long)(lamx.size() + lamy.size()) * 4 + (long long)(twx.size() + twy.size()) * 8;
+  bytes += (long long)(lamx.size() + lamy.size()) * 4 +
+           (long long)(twy.size() + twpx.size() + twpy.size()) * 8;
   p.lamx = plan->lamx;
   p.lamy = plan->lamy;
-  p.tw_x = plan->twx;
   p.tw_y = plan->twy;
+  p.twp_x = plan->twpx;
+  p.twp_y = plan->twpy;
 
   if (cfg->const_forcing != CFD_FORCE_NONE) {
     size_t cu = 0, cv = 0;
@@ -358,6 +388,48 @@ int cfd_fvm_profile(cfd_fvm_plan* plan, void* stream, const float* u,
   return CFD_OK;
 }
 
+// Autotuner over the transform block shapes (FvmParams::fft_shape): runs
+// `steps` steps per candidate after one warm-up step, times them with CUDA
+// events on `stream` (synchronising), and keeps the fastest in the plan.
+int cfd_fvm_plan_autotune(cfd_fvm_plan* plan, void* stream, const float* u,
+                          const float* v, float* u_scratch, float* v_scratch,
+                          int steps, int* chosen) {
+  if (!plan || !u || !v || !u_scratch || !v_scratch || steps < 1)
+    return fail(CFD_ERR_INVALID_ARGUMENT, "cfd_fvm_plan_autotune: bad arguments");
+  cudaStream_t s = as_stream(stream);
+  cudaEvent_t e0, e1;
+  CFD_CHECK(cudaEventCreate(&e0), "cudaEventCreate");
+  CFD_CHECK(cudaEventCreate(&e1), "cudaEventCreate");
+  float best_ms = 0.f;
+  int best = plan->p.fft_shape;
+  int rc = CFD_OK;
+  for (int shape = 0; shape < 2 && rc == CFD_OK; ++shape) {
+    plan->p.fft_shape = shape;
+    rc = cfd_fvm_step(plan, stream, u, v, u_scratch, v_scratch, 1);
+    if (rc) break;
+    cudaError_t e = cudaEventRecord(e0, s);
+    if (e == cudaSuccess) rc = cfd_fvm_step(plan, stream, u, v, u_scratch, v_scratch, steps);
+    if (rc) break;
+    if (e == cudaSuccess) e = cudaEventRecord(e1, s);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    float ms = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+    if (e != cudaSuccess) {
+      rc = cuda_fail(e, "cfd_fvm_plan_autotune");
+      break;
+    }
+    if (shape == 0 || ms < best_ms) {
+      best_ms = ms;
+      best = shape;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  plan->p.fft_shape = best;
+  if (chosen) *chosen = best;
+  return rc;
+}
+
 int cfd_fvm_explicit_terms(cfd_fvm_plan* plan, void* stream, const float* u,
                            const float* v, float* du, float* dv) {
   if (!plan || !u || !v || !du || !dv)
@@ -453,8 +525,8 @@ int cfd_scale_to_max_speed(void* stream, int n, float* u, float* v,
 int cfd_spec_plan_destroy(cfd_spec_plan* plan) {
   if (!plan) return CFD_OK;
   void* ptrs[] = {plan->t4[0], plan->t4[1], plan->t4[2], plan->t4[3], plan->ahat,
-                  plan->h, plan->fc, plan->work, plan->twx, plan->twy, plan->kx,
-                  plan->ky};
+                  plan->h, plan->fc, plan->work, plan->twy, plan->twpx, plan->twpy,
+                  plan->kx, plan->ky};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   delete plan;
@@ -526,22 +598,26 @@ int cfd_spec_plan_create(const cfd_spec_config* cfg, cfd_spec_plan** out) {
   CFD_ALLOC(plan->h, ns);
   CFD_ALLOC(plan->work, ns);
 #undef CFD_ALLOC
-  std::vector<float2> twx = twiddles(nx), twy = twiddles(ny);
+  std::vector<float2> twy = twiddles(ny);
+  std::vector<float2> twpx = pass_twiddles(p.log2nx), twpy = pass_twiddles(p.log2L);
   // fftfreq(n, d) / rfftfreq(n, d): float32 ordinals divided by float32(d*n)
   // (grids.py:618-658 via jnp.fft.fftfreq).
   std::vector<float> kxt(nx), kyt(p.L + 1);
   for (int k = 0; k < nx; ++k) kxt[k] = (float)(k < nx / 2 ? k : k - nx) / p.dn_x;
   for (int k = 0; k <= p.L; ++k) kyt[k] = (float)k / p.dn_y;
-  if ((e = upload(&plan->twx, twx.data(), twx.size())) != cudaSuccess ||
-      (e = upload(&plan->twy, twy.data(), twy.size())) != cudaSuccess ||
+  if ((e = upload(&plan->twy, twy.data(), twy.size())) != cudaSuccess ||
+      (e = upload(&plan->twpx, twpx.data(), twpx.size())) != cudaSuccess ||
+      (e = upload(&plan->twpy, twpy.data(), twpy.size())) != cudaSuccess ||
       (e = upload(&plan->kx, kxt.data(), kxt.size())) != cudaSuccess ||
       (e = upload(&plan->ky, kyt.data(), kyt.size())) != cudaSuccess) {
     cfd_spec_plan_destroy(plan);
     return cuda_fail(e, "cfd_spec_plan_create: tables");
   }
-  bytes += (long long)(twx.size() + twy.size()) * 8 + (long long)(kxt.size() + kyt.size()) * 4;
-  p.tw_x = plan->twx;
+  bytes += (long long)(twy.size() + twpx.size() + twpy.size()) * 8 +
+           (long long)(kxt.size() + kyt.size()) * 4;
   p.tw_y = plan->twy;
+  p.twp_x = plan->twpx;
+  p.twp_y = plan->twpy;
   p.kx = plan->kx;
   p.ky = plan->ky;
   plan->bytes = bytes;

@@ -10,10 +10,10 @@
 // batch*L/P threads of work; all reads of a pass land in registers before a
 // barrier and all writes happen after it, which is what makes in-place legal.
 //
-// Twiddles come from a table tw[k] = exp(-2*pi*i*k/T) (T = 2^log2T >= L)
-// computed on the host in double precision and rounded once to float.  The
-// inverse transform (SIGN = +1) conjugates them and is unnormalised, like the
-// backward pass of numpy/jnp before their 1/n factor.
+// Twiddles come from per-pass tables (fft_pass_table_offset) computed on the
+// host in double precision and rounded once to float.  The inverse transform
+// (SIGN = +1) conjugates them and is unnormalised, like the backward pass of
+// numpy/jnp before their 1/n factor.
 #pragma once
 
 #include "common.cuh"
@@ -108,18 +108,54 @@ template <> struct Log2c<4> { static constexpr int v = 2; };
 template <> struct Log2c<8> { static constexpr int v = 3; };
 template <> struct Log2c<16> { static constexpr int v = 4; };
 
+// Shared-memory index of complex element n: one padding slot after every 16
+// elements, which spreads the stride-16 writes of the first radix-16 pass over
+// all banks.  Every FFT buffer access goes through pidx(); a sequence of L
+// elements occupies padded_len(L) slots.
+CFD_HD int pidx(int n) { return n + (n >> 4); }
+CFD_HD int padded_len(int L) { return L + (L >> 4); }
+
+// Pass twiddle tables.  An FFT of length 2^log2L runs radix-16 passes at spans
+// Ns = 1, 16, 256, ... and then one pass of the remaining radix R (2, 4 or 8);
+// a pass with Ns > 1 reads w^(r*k), w = exp(-2 pi i / (Ns*R)), for r = 1..R-1
+// and k = 0..Ns-1 from a table laid out [r-1][k] (k contiguous, so the lanes
+// of a warp, which hold consecutive k, read consecutive addresses).  The
+// tables of all passes are concatenated in pass order.
+CFD_HD int fft_pass_radix(int log2L, int pass) {
+  const int n16 = log2L >> 2;
+  if (log2L < 4) return 1 << log2L;
+  return pass < n16 ? 16 : (1 << (log2L & 3));
+}
+CFD_HD int fft_num_passes(int log2L) {
+  if (log2L < 4) return 1;
+  return (log2L >> 2) + ((log2L & 3) ? 1 : 0);
+}
+// Offset (in complex entries) of pass `pass`'s table.
+CFD_HD int fft_pass_table_offset(int log2L, int pass) {
+  int off = 0, ns = 1;
+  for (int q = 0; q < pass; ++q) {
+    const int R = fft_pass_radix(log2L, q);
+    if (ns > 1) off += (R - 1) * ns;
+    ns *= R;
+  }
+  return off;
+}
+CFD_HD int fft_pass_table_size(int log2L) {
+  return fft_pass_table_offset(log2L, fft_num_passes(log2L));
+}
+
 // One in-place Stockham pass.  `t` is the worker index in [0, nthr); threads of
-// the block with t >= nthr only take part in the barriers.
+// the block with t >= nthr only take part in the barriers.  `twp` is this
+// pass's twiddle table (unused when Ns == 1).
 template <int R, int NB, int SIGN>
 CFD_D void stockham_pass(float2* buf, int log2L, int log2Ns, int bstride,
-                         const float2* __restrict__ tw, int log2T, int t,
-                         int nthr) {
+                         const float2* __restrict__ twp, int t, int nthr) {
   constexpr int lr = Log2c<R>::v;
   const int log2LR = log2L - lr;
   const int LR = 1 << log2LR;
   const int Ns = 1 << log2Ns;
   float2 v[NB][R];
-  int kk[NB], out[NB];
+  int kk[NB], out[NB], bb[NB];
   const bool active = t < nthr;
   if (active) {
 #pragma unroll
@@ -127,31 +163,31 @@ CFD_D void stockham_pass(float2* buf, int log2L, int log2Ns, int bstride,
       const int it = t + q * nthr;
       const int b = it >> log2LR;
       const int j = it & (LR - 1);
-      const float2* s = buf + b * bstride + j;
+      const float2* s = buf + b * bstride;
 #pragma unroll
-      for (int r = 0; r < R; ++r) v[q][r] = s[r << log2LR];
+      for (int r = 0; r < R; ++r) v[q][r] = s[pidx(j + (r << log2LR))];
       const int k = j & (Ns - 1);
       kk[q] = k;
-      out[q] = b * bstride + ((j - k) << lr) + k;
+      bb[q] = b * bstride;
+      out[q] = ((j - k) << lr) + k;
     }
   }
   __syncthreads();
   if (active) {
-    const int sh = log2T - log2Ns - lr;  // table stride T / (Ns * R)
 #pragma unroll
     for (int q = 0; q < NB; ++q) {
       if (Ns > 1) {
 #pragma unroll
         for (int r = 1; r < R; ++r) {
-          float2 w = __ldg(tw + ((r * kk[q]) << sh));
+          float2 w = __ldg(twp + (r - 1) * Ns + kk[q]);
           if (SIGN > 0) w.y = -w.y;
           v[q][r] = c_mul(v[q][r], w);
         }
       }
       Dft<R, SIGN>::run(v[q]);
-      float2* d = buf + out[q];
+      float2* d = buf + bb[q];
 #pragma unroll
-      for (int r = 0; r < R; ++r) d[r << log2Ns] = v[q][r];
+      for (int r = 0; r < R; ++r) d[pidx(out[q] + (r << log2Ns))] = v[q][r];
     }
   }
   __syncthreads();
@@ -163,36 +199,40 @@ CFD_HD int fft_workers(int log2L, int batch) {
   return (batch << log2L) / P;
 }
 
-// In-place batched FFT of `batch` sequences; must be called by every thread of
-// the block (it contains barriers).  t = worker index (usually threadIdx.x).
-// Radix-16 passes first, then one pass of the remaining radix; sequences
-// shorter than 16 take a single pass.  (Keeping the pass sequence in this
-// shape, with the radix-16 loop not unrolled, holds register use near that of
-// a single pass.)
+// In-place batched FFT of `batch` sequences (sequence b at buf + b*bstride,
+// element n at pidx(n)); must be called by every thread of the block (it
+// contains barriers).  t = worker index (usually threadIdx.x); `twp` is the
+// concatenated pass twiddle table for this length.  Radix-16 passes first,
+// then one pass of the remaining radix; sequences shorter than 16 take a
+// single pass.  (Keeping the pass sequence in this shape, with the radix-16
+// loop not unrolled, holds register use near that of a single pass.)
 template <int SIGN>
 CFD_D void fft_inplace(float2* buf, int log2L, int batch, int bstride,
-                       const float2* __restrict__ tw, int log2T, int t) {
+                       const float2* __restrict__ twp, int t) {
   const int nthr = fft_workers(log2L, batch);
   if (log2L < 4) {
     if (log2L == 3)
-      stockham_pass<8, 1, SIGN>(buf, log2L, 0, bstride, tw, log2T, t, nthr);
+      stockham_pass<8, 1, SIGN>(buf, log2L, 0, bstride, twp, t, nthr);
     else if (log2L == 2)
-      stockham_pass<4, 1, SIGN>(buf, log2L, 0, bstride, tw, log2T, t, nthr);
+      stockham_pass<4, 1, SIGN>(buf, log2L, 0, bstride, twp, t, nthr);
     else if (log2L == 1)
-      stockham_pass<2, 1, SIGN>(buf, log2L, 0, bstride, tw, log2T, t, nthr);
+      stockham_pass<2, 1, SIGN>(buf, log2L, 0, bstride, twp, t, nthr);
     return;
   }
   const int n16 = log2L >> 2, rem = log2L & 3;
+  const float2* tp = twp;
 #pragma unroll 1
-  for (int q = 0; q < n16; ++q)
-    stockham_pass<16, 1, SIGN>(buf, log2L, 4 * q, bstride, tw, log2T, t, nthr);
+  for (int q = 0; q < n16; ++q) {
+    stockham_pass<16, 1, SIGN>(buf, log2L, 4 * q, bstride, tp, t, nthr);
+    if (q > 0) tp += 15 << (4 * q);
+  }
   const int ns = 4 * n16;
   if (rem == 3)
-    stockham_pass<8, 2, SIGN>(buf, log2L, ns, bstride, tw, log2T, t, nthr);
+    stockham_pass<8, 2, SIGN>(buf, log2L, ns, bstride, tp, t, nthr);
   else if (rem == 2)
-    stockham_pass<4, 4, SIGN>(buf, log2L, ns, bstride, tw, log2T, t, nthr);
+    stockham_pass<4, 4, SIGN>(buf, log2L, ns, bstride, tp, t, nthr);
   else if (rem == 1)
-    stockham_pass<2, 8, SIGN>(buf, log2L, ns, bstride, tw, log2T, t, nthr);
+    stockham_pass<2, 8, SIGN>(buf, log2L, ns, bstride, tp, t, nthr);
 }
 
 // --- Real <-> half-complex helpers (length M = 2L real, via an L-point FFT) ---

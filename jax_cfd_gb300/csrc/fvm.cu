@@ -344,39 +344,61 @@ __global__ void __launch_bounds__(kStencilThreads)
 }
 
 // Backward-difference divergence of (u*, v*) (finite_differences.py:95-143)
-// followed by the packed real FFT of each row along y.
-__global__ void __launch_bounds__(256, 2) fvm_div_rfft_kernel(FvmParams p, int rows,
-                                    const float* __restrict__ us,
-                                    const float* __restrict__ vs,
-                                    float2* __restrict__ spec) {
+// followed by the packed real FFT of each row along y.  Shared memory holds
+// `rows` padded sequences of L = ny/2 complex values (pidx layout).
+// MAXT/MINB: launch bounds of the block shape the launcher picked (wide
+// 256-thread blocks, or narrow blocks capped at 72 registers so that a whole
+// 2048^2 grid is resident in one wave).
+template <int MAXT, int MINB>
+__global__ void __launch_bounds__(MAXT, MINB)
+    fvm_div_rfft_kernel(FvmParams p, int rows, const float* __restrict__ us,
+                        const float* __restrict__ vs, float2* __restrict__ spec) {
   extern __shared__ float2 sbuf[];
-  const int L = p.ny >> 1, log2L = p.log2ny - 1;
+  const int L = p.ny >> 1, log2L = p.log2ny - 1, PL = padded_len(L);
   const int i0 = blockIdx.x * rows;
   const int mx = p.nx - 1, my = p.ny - 1;
   const size_t ny = (size_t)p.ny;
-  float* sd = reinterpret_cast<float*>(sbuf);
-  for (int idx = threadIdx.x; idx < rows * p.ny; idx += blockDim.x) {
-    const int r = idx >> p.log2ny, j = idx & my;
-    const int i = i0 + r, im = (i - 1) & mx, jm = (j - 1) & my;
-    const float dx = (__ldg(us + i * ny + j) - __ldg(us + im * ny + j)) * p.inv_hx;
-    const float dy = (__ldg(vs + i * ny + j) - __ldg(vs + i * ny + jm)) * p.inv_hy;
-    sd[idx] = dx + dy;
+  const int log2g = p.log2ny - 2;  // float4 groups per row
+  const int groups = rows << log2g;
+#pragma unroll 4
+  for (int g = threadIdx.x; g < groups; g += blockDim.x) {
+    const int r = g >> log2g, jj = (g & ((1 << log2g) - 1)) << 2;
+    const int i = i0 + r, im = (i - 1) & mx;
+    const float4 a = __ldg(reinterpret_cast<const float4*>(us + i * ny + jj));
+    const float4 b = __ldg(reinterpret_cast<const float4*>(us + im * ny + jj));
+    const float4 c = __ldg(reinterpret_cast<const float4*>(vs + i * ny + jj));
+    const float cm = __ldg(vs + i * ny + ((jj - 1) & my));
+    // D = (u - u[i-1]) / hx + (v - v[j-1]) / hy
+    const float d0 = (a.x - b.x) * p.inv_hx + (c.x - cm) * p.inv_hy;
+    const float d1 = (a.y - b.y) * p.inv_hx + (c.y - c.x) * p.inv_hy;
+    const float d2 = (a.z - b.z) * p.inv_hx + (c.z - c.y) * p.inv_hy;
+    const float d3 = (a.w - b.w) * p.inv_hx + (c.w - c.z) * p.inv_hy;
+    const int n = jj >> 1;
+    float2* z = sbuf + r * PL;
+    z[pidx(n)] = make_float2(d0, d1);
+    z[pidx(n + 1)] = make_float2(d2, d3);
   }
   __syncthreads();
-  fft_inplace<-1>(sbuf, log2L, rows, L, p.tw_y, p.log2ny, threadIdx.x);
-  const int half = L >> 1;
-  for (int idx = threadIdx.x; idx < rows * (half + 1); idx += blockDim.x) {
-    const int r = idx / (half + 1), k = idx - r * (half + 1);
+  fft_inplace<-1>(sbuf, log2L, rows, PL, p.twp_y, threadIdx.x);
+  // Untangle: pairs (k, L-k) for k in [1, L/2); the k = 0 slot also handles
+  // the DC/Nyquist pair and the middle element k = L/2.
+  const int half = L >> 1, log2h = log2L - 1;
+  for (int idx = threadIdx.x; idx < (rows << log2h); idx += blockDim.x) {
+    const int r = idx >> log2h, k = idx & (half - 1);
     float2* out = spec + (size_t)(i0 + r) * L;
-    const float2* z = sbuf + r * L;
+    const float2* z = sbuf + r * PL;
     if (k == 0) {
       const float2 z0 = z[0];
       out[0] = make_float2(z0.x + z0.y, z0.x - z0.y);
+      float2 xk, xm;
+      const float2 zh = z[pidx(half)];
+      rfft_post_pair(zh, zh, __ldg(p.tw_y + half), &xk, &xm);
+      out[half] = xk;
     } else {
       float2 xk, xm;
-      rfft_post_pair(z[k], z[L - k], __ldg(p.tw_y + k), &xk, &xm);
+      rfft_post_pair(z[pidx(k)], z[pidx(L - k)], __ldg(p.tw_y + k), &xk, &xm);
       out[k] = xk;
-      if (k != L - k) out[L - k] = xm;
+      out[L - k] = xm;
     }
   }
 }
@@ -389,23 +411,26 @@ CFD_D float pinv_diag(const FvmParams& p, int kx, int ky) {
   return fabsf(lam) > p.cutoff ? p.pinv_scale / lam : 0.f;
 }
 
-__global__ void __launch_bounds__(512, 1) fvm_col_pinv_kernel(FvmParams p, int W, int log2W, int bstride,
-                                    float2* __restrict__ spec) {
+template <int MAXT, int MINB>
+__global__ void __launch_bounds__(MAXT, MINB)
+    fvm_col_pinv_kernel(FvmParams p, int W, int log2W, int bstride,
+                        float2* __restrict__ spec) {
   extern __shared__ float2 sbuf[];
   const int L = p.ny >> 1, N = p.nx;
   const int c0 = blockIdx.x * W;
   const int tid = threadIdx.x;
+#pragma unroll 4
   for (int idx = tid; idx < W * N; idx += blockDim.x) {
     const int w = idx & (W - 1), i = idx >> log2W;
-    sbuf[w * bstride + i] = spec[(size_t)i * L + c0 + w];
+    sbuf[w * bstride + pidx(i)] = spec[(size_t)i * L + c0 + w];
   }
   __syncthreads();
-  fft_inplace<-1>(sbuf, p.log2nx, W, bstride, p.tw_x, p.log2nx, tid);
+  fft_inplace<-1>(sbuf, p.log2nx, W, bstride, p.twp_x, tid);
   for (int idx = tid; idx < W * N; idx += blockDim.x) {
     const int w = idx & (W - 1), kx = idx >> log2W;
     const int c = c0 + w;
     if (c == 0) continue;
-    float2* e = sbuf + w * bstride + kx;
+    float2* e = sbuf + w * bstride + pidx(kx);
     *e = c_scale(*e, pinv_diag(p, kx, c));
   }
   if (c0 == 0) {
@@ -416,44 +441,54 @@ __global__ void __launch_bounds__(512, 1) fvm_col_pinv_kernel(FvmParams p, int W
       const int m = (N - k) & (N - 1);
       const float d0 = pinv_diag(p, k, 0), dn = pinv_diag(p, k, L);
       const float al = 0.5f * (d0 + dn), be = 0.5f * (d0 - dn);
-      const float2 zk = sbuf[k], zm = sbuf[m];
-      sbuf[k] = c_add(c_scale(zk, al), c_scale(c_conj(zm), be));
-      if (m != k) sbuf[m] = c_add(c_scale(zm, al), c_scale(c_conj(zk), be));
+      const float2 zk = sbuf[pidx(k)], zm = sbuf[pidx(m)];
+      sbuf[pidx(k)] = c_add(c_scale(zk, al), c_scale(c_conj(zm), be));
+      if (m != k) sbuf[pidx(m)] = c_add(c_scale(zm, al), c_scale(c_conj(zk), be));
     }
   }
   __syncthreads();
-  fft_inplace<1>(sbuf, p.log2nx, W, bstride, p.tw_x, p.log2nx, tid);
+  fft_inplace<1>(sbuf, p.log2nx, W, bstride, p.twp_x, tid);
+#pragma unroll 4
   for (int idx = tid; idx < W * N; idx += blockDim.x) {
     const int w = idx & (W - 1), i = idx >> log2W;
-    spec[(size_t)i * L + c0 + w] = sbuf[w * bstride + i];
+    spec[(size_t)i * L + c0 + w] = sbuf[w * bstride + pidx(i)];
   }
 }
 
 // Inverse packed real FFT of each row, in place: q^ rows -> q rows (floats).
-__global__ void __launch_bounds__(256, 2) fvm_irfft_kernel(FvmParams p, int rows, float2* spec) {
+template <int MAXT, int MINB>
+__global__ void __launch_bounds__(MAXT, MINB)
+    fvm_irfft_kernel(FvmParams p, int rows, float2* spec) {
   extern __shared__ float2 sbuf[];
-  const int L = p.ny >> 1, log2L = p.log2ny - 1;
+  const int L = p.ny >> 1, log2L = p.log2ny - 1, PL = padded_len(L);
   const int i0 = blockIdx.x * rows;
-  const int half = L >> 1;
-  for (int idx = threadIdx.x; idx < rows * (half + 1); idx += blockDim.x) {
-    const int r = idx / (half + 1), k = idx - r * (half + 1);
+  const int half = L >> 1, log2h = log2L - 1;
+  for (int idx = threadIdx.x; idx < (rows << log2h); idx += blockDim.x) {
+    const int r = idx >> log2h, k = idx & (half - 1);
     const float2* in = spec + (size_t)(i0 + r) * L;
-    float2* z = sbuf + r * L;
+    float2* z = sbuf + r * PL;
     if (k == 0) {
       const float2 x0 = in[0];
       z[0] = make_float2(x0.x + x0.y, x0.x - x0.y);
+      const float2 xh = in[half];
+      float2 zk, zm;
+      irfft_pre_pair(xh, xh, __ldg(p.tw_y + half), &zk, &zm);
+      z[pidx(half)] = zk;
     } else {
       float2 zk, zm;
       irfft_pre_pair(in[k], in[L - k], __ldg(p.tw_y + k), &zk, &zm);
-      z[k] = zk;
-      if (k != L - k) z[L - k] = zm;
+      z[pidx(k)] = zk;
+      z[pidx(L - k)] = zm;
     }
   }
   __syncthreads();
-  fft_inplace<1>(sbuf, log2L, rows, L, p.tw_y, p.log2ny, threadIdx.x);
-  for (int idx = threadIdx.x; idx < rows * L; idx += blockDim.x) {
-    const int r = idx >> log2L, n = idx & (L - 1);
-    spec[(size_t)(i0 + r) * L + n] = sbuf[r * L + n];
+  fft_inplace<1>(sbuf, log2L, rows, PL, p.twp_y, threadIdx.x);
+  // q[2n], q[2n+1] = z[n]; two complex values per float4 store.
+  const int log2p = log2L - 1;  // pairs per row
+  for (int idx = threadIdx.x; idx < (rows << log2p); idx += blockDim.x) {
+    const int r = idx >> log2p, n = (idx & ((1 << log2p) - 1)) << 1;
+    const float2 a = sbuf[r * PL + pidx(n)], b = sbuf[r * PL + pidx(n + 1)];
+    reinterpret_cast<float4*>(spec + (size_t)(i0 + r) * L)[n >> 1] = make_float4(a.x, a.y, b.x, b.y);
   }
 }
 
@@ -522,9 +557,9 @@ __global__ void max_speed_kernel(int n, const float* __restrict__ u,
   if ((threadIdx.x & 31) == 0) atomicMax(out, __float_as_uint(m));
 }
 
-int fft_rows_per_block(int log2L, int nrows) {
+int fft_rows_per_block(int log2L, int nrows, int target_threads = 256) {
   const int P = log2L >= 4 ? 16 : (1 << log2L);
-  int rows = (256 * P) >> log2L;
+  int rows = (target_threads * P) >> log2L;
   if (rows < 1) rows = 1;
   if (rows > nrows) rows = nrows;
   return rows;
@@ -577,44 +612,69 @@ cudaError_t launch_fvm_explicit(const FvmParams& p, bool project, bool out_k0,
   return cudaGetLastError();
 }
 
+// Block shapes of the transform kernels (FvmParams::fft_shape): 0 = wide
+// (256-thread blocks, up to 85 registers), 1 = narrow (64-thread row blocks
+// and 128-thread column blocks capped at 72 registers).
+template <int MAXT, int MINB>
+static cudaError_t div_rfft_impl(const FvmParams& p, int target, const float* us,
+                                 const float* vs, float2* spec, cudaStream_t s) {
+  const int log2L = p.log2ny - 1;
+  const int rows = fft_rows_per_block(log2L, p.nx, target);
+  const size_t smem = (size_t)rows * padded_len(p.ny / 2) * sizeof(float2);
+  cudaError_t e = set_smem(fvm_div_rfft_kernel<MAXT, MINB>, smem);
+  if (e != cudaSuccess) return e;
+  fvm_div_rfft_kernel<MAXT, MINB><<<p.nx / rows, block_threads(fft_workers(log2L, rows)),
+                                    smem, s>>>(p, rows, us, vs, spec);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_fvm_div_rfft(const FvmParams& p, const float* us,
                                 const float* vs, float2* spec, cudaStream_t s) {
-  const int log2L = p.log2ny - 1;
-  const int rows = fft_rows_per_block(log2L, p.nx);
-  const size_t smem = (size_t)rows * (p.ny / 2) * sizeof(float2);
-  cudaError_t e = set_smem(fvm_div_rfft_kernel, smem);
+  return p.fft_shape == 1 ? div_rfft_impl<64, 14>(p, 64, us, vs, spec, s)
+                          : div_rfft_impl<256, 3>(p, 256, us, vs, spec, s);
+}
+
+template <int MAXT, int MINB>
+static cudaError_t col_pinv_impl(const FvmParams& p, int target, float2* spec,
+                                 cudaStream_t s) {
+  const int L = p.ny / 2;
+  // W columns per block so that the block has `target` threads (W * nx =
+  // 16 * target points); one column at least.
+  int W = (16 * target) >> p.log2nx;
+  if (W < 1) W = 1;
+  if (W > L) W = L;
+  // +8 slots: consecutive columns start 16 banks apart.
+  const int bstride = padded_len(p.nx) + 8;
+  const size_t smem = (size_t)W * bstride * sizeof(float2);
+  cudaError_t e = set_smem(fvm_col_pinv_kernel<MAXT, MINB>, smem);
   if (e != cudaSuccess) return e;
-  fvm_div_rfft_kernel<<<p.nx / rows, block_threads(fft_workers(log2L, rows)),
-                        smem, s>>>(p, rows, us, vs, spec);
+  fvm_col_pinv_kernel<MAXT, MINB><<<L / W, block_threads(fft_workers(p.log2nx, W)), smem,
+                                    s>>>(p, W, ilog2(W), bstride, spec);
   return cudaGetLastError();
 }
 
 cudaError_t launch_fvm_col_pinv(const FvmParams& p, float2* spec,
                                 cudaStream_t s) {
-  const int L = p.ny / 2;
-  // W columns per block: 32-byte row segments (W = 4) where the 512-thread
-  // cap allows, more columns for short columns.
-  int W = 4096 >> p.log2nx;
-  if (W < 2) W = 2;
-  if (W > L) W = L;
-  const int bstride = p.nx + 4;
-  const size_t smem = (size_t)W * bstride * sizeof(float2);
-  cudaError_t e = set_smem(fvm_col_pinv_kernel, smem);
+  return p.fft_shape == 1 ? col_pinv_impl<128, 7>(p, 128, spec, s)
+                          : col_pinv_impl<256, 3>(p, 256, spec, s);
+}
+
+template <int MAXT, int MINB>
+static cudaError_t irfft_impl(const FvmParams& p, int target, float2* spec,
+                              cudaStream_t s) {
+  const int log2L = p.log2ny - 1;
+  const int rows = fft_rows_per_block(log2L, p.nx, target);
+  const size_t smem = (size_t)rows * padded_len(p.ny / 2) * sizeof(float2);
+  cudaError_t e = set_smem(fvm_irfft_kernel<MAXT, MINB>, smem);
   if (e != cudaSuccess) return e;
-  fvm_col_pinv_kernel<<<L / W, block_threads(fft_workers(p.log2nx, W)), smem,
-                        s>>>(p, W, ilog2(W), bstride, spec);
+  fvm_irfft_kernel<MAXT, MINB><<<p.nx / rows, block_threads(fft_workers(log2L, rows)),
+                                 smem, s>>>(p, rows, spec);
   return cudaGetLastError();
 }
 
 cudaError_t launch_fvm_irfft(const FvmParams& p, float2* spec, cudaStream_t s) {
-  const int log2L = p.log2ny - 1;
-  const int rows = fft_rows_per_block(log2L, p.nx);
-  const size_t smem = (size_t)rows * (p.ny / 2) * sizeof(float2);
-  cudaError_t e = set_smem(fvm_irfft_kernel, smem);
-  if (e != cudaSuccess) return e;
-  fvm_irfft_kernel<<<p.nx / rows, block_threads(fft_workers(log2L, rows)),
-                     smem, s>>>(p, rows, spec);
-  return cudaGetLastError();
+  return p.fft_shape == 1 ? irfft_impl<64, 14>(p, 64, spec, s)
+                          : irfft_impl<256, 3>(p, 256, spec, s);
 }
 
 static int elementwise_blocks(size_t n) {

@@ -37,8 +37,10 @@ struct FvmParams {
   const float* lamy;   // eigenvalues along y, rfft half (ny/2 + 1)
   float cutoff;        // 10 * eps(float32)
   float pinv_scale;    // 1 / (nx * ny), folds irfftn's normalisation
-  const float2* tw_x;  // exp(-2 pi i k / nx), k < nx
-  const float2* tw_y;  // exp(-2 pi i k / ny), k < ny
+  const float2* tw_y;  // exp(-2 pi i k / ny), k <= ny/4: real-FFT untangling
+  const float2* twp_x;  // pass twiddle tables of the length-nx column FFT
+  const float2* twp_y;  // pass twiddle tables of the length-ny/2 row FFT
+  int fft_shape;       // transform block shape: 0 wide, 1 narrow (see fvm.cu)
 };
 
 // Out-of-bounds / configuration errors are reported through return codes.
@@ -76,8 +78,9 @@ struct SpecParams {
   int filt_lo, filt_hi, filt_cols;  // rows [0,lo) U [hi,nx), cols [0,cols)
   const float2* fc_full;  // forcing curl (nx x (L+1)) or null
   const float2* fc_row0;  // forcing curl only in row kx = 0 ((L+1)) or null
-  const float2* tw_x;
-  const float2* tw_y;
+  const float2* tw_y;   // exp(-2 pi i k / ny): real-FFT untangling
+  const float2* twp_x;  // pass twiddle tables of the length-nx column FFT
+  const float2* twp_y;  // pass twiddle tables of the length-ny/2 row FFT
   const float* kx;      // fftfreq(nx, hx) in float32 (nx)
   const float* ky;      // rfftfreq(ny, hy) in float32 (L + 1)
 };

@@ -22,18 +22,19 @@
 #include <string>
 
 #include "../../include/cfd_gb300.h"
-#include "common.cuh"
+#include "fft.cuh"
 #include "kernels.h"
 
 namespace {
 
 constexpr int kNoallocMaxCells = 512 * 512;
 constexpr int kNoallocMaxSide = 4096;
-// Layout (in floats): spectrum [nx*ny] | tw_x [2*nx] | tw_y [2*ny] |
-// lam_x [nx] | lam_y [ny/2 + 1], each region rounded up to 64 floats.
+// Layout (in floats): spectrum [nx*ny] | tw_y [2*ny] | pass tables of the
+// column FFT [2*nx] and of the row FFT [2*(ny/2)] | lam_x [nx] |
+// lam_y [ny/2 + 1], each region rounded up to 64 floats.
 constexpr int kNoallocFloats =
     kNoallocMaxCells + 2 * kNoallocMaxSide + 2 * kNoallocMaxSide + kNoallocMaxSide +
-    (kNoallocMaxSide / 2 + 1) + 5 * 64;
+    kNoallocMaxSide + (kNoallocMaxSide / 2 + 1) + 6 * 64;
 
 __device__ __align__(256) float g_noalloc_scratch[kNoallocFloats];
 
@@ -43,29 +44,58 @@ float* g_noalloc_ptr[kMaxDevices] = {};
 
 int round64(int n) { return (n + 63) & ~63; }
 
-// Twiddles exp(-2 pi i k / n) and Laplacian eigenvalues
-// (2 cos(2 pi k / n) - 2) / h^2 (array_utils.py:168-173, the fft of the
-// circulant's first column), in double precision, rounded once to float.
+// Angle numerator/denominator of entry `idx` of the concatenated pass tables
+// of a length-2^log2L FFT (layout in fft.cuh): the entry is
+// exp(-2 pi i num / den).
+__device__ void pass_entry(int log2L, int idx, int* num, int* den) {
+  int ns = 1;
+  for (int q = 0; q < cfd::fft_num_passes(log2L); ++q) {
+    const int R = cfd::fft_pass_radix(log2L, q);
+    if (ns > 1) {
+      const int size = (R - 1) * ns;
+      if (idx < size) {
+        *num = (idx / ns + 1) * (idx % ns);
+        *den = ns * R;
+        return;
+      }
+      idx -= size;
+    }
+    ns *= R;
+  }
+  *num = 0;
+  *den = 1;
+}
+
+// Twiddles and Laplacian eigenvalues (2 cos(2 pi k / n) - 2) / h^2
+// (array_utils.py:168-173, the fft of the circulant's first column), in double
+// precision with sincospi/cospi, rounded once to float.
 __global__ void noalloc_tables_kernel(int nx, int ny, double hx, double hy,
-                                      float2* tw_x, float2* tw_y, float* lam_x,
-                                      float* lam_y) {
-  const int total = nx + ny + nx + (ny / 2 + 1);
+                                      float2* tw_y, float2* twp_x, float2* twp_y,
+                                      float* lam_x, float* lam_y) {
+  const int log2nx = ilog2(nx), log2L = ilog2(ny) - 1;
+  const int sx = cfd::fft_pass_table_size(log2nx), sy = cfd::fft_pass_table_size(log2L);
+  const int total = ny + sx + sy + nx + (ny / 2 + 1);
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total;
        t += gridDim.x * blockDim.x) {
-    if (t < nx) {
-      double s, c;
-      sincospi(-2.0 * t / nx, &s, &c);
-      tw_x[t] = make_float2((float)c, (float)s);
-    } else if (t < nx + ny) {
-      const int k = t - nx;
-      double s, c;
-      sincospi(-2.0 * k / ny, &s, &c);
-      tw_y[k] = make_float2((float)c, (float)s);
-    } else if (t < 2 * nx + ny) {
-      const int k = t - nx - ny;
+    double s, c;
+    if (t < ny) {
+      sincospi(-2.0 * t / ny, &s, &c);
+      tw_y[t] = make_float2((float)c, (float)s);
+    } else if (t < ny + sx) {
+      int num, den;
+      pass_entry(log2nx, t - ny, &num, &den);
+      sincospi(-2.0 * num / den, &s, &c);
+      twp_x[t - ny] = make_float2((float)c, (float)s);
+    } else if (t < ny + sx + sy) {
+      int num, den;
+      pass_entry(log2L, t - ny - sx, &num, &den);
+      sincospi(-2.0 * num / den, &s, &c);
+      twp_y[t - ny - sx] = make_float2((float)c, (float)s);
+    } else if (t < ny + sx + sy + nx) {
+      const int k = t - ny - sx - sy;
       lam_x[k] = k == 0 ? 0.f : (float)((2.0 * cospi(2.0 * k / nx) - 2.0) / (hx * hx));
     } else {
-      const int k = t - 2 * nx - ny;
+      const int k = t - ny - sx - sy - nx;
       lam_y[k] = k == 0 ? 0.f : (float)((2.0 * cospi(2.0 * k / ny) - 2.0) / (hy * hy));
     }
   }
@@ -118,9 +148,10 @@ extern "C" int cfd_fvm_projection_noalloc(void* stream, int nx, int ny, double h
   if (rc != CFD_OK) return rc;
 
   float* spec = base;
-  float2* tw_x = reinterpret_cast<float2*>(spec + round64(nx * ny));
-  float2* tw_y = reinterpret_cast<float2*>(reinterpret_cast<float*>(tw_x) + round64(2 * nx));
-  float* lam_x = reinterpret_cast<float*>(tw_y) + round64(2 * ny);
+  float2* tw_y = reinterpret_cast<float2*>(spec + round64(nx * ny));
+  float2* twp_x = reinterpret_cast<float2*>(reinterpret_cast<float*>(tw_y) + round64(2 * ny));
+  float2* twp_y = reinterpret_cast<float2*>(reinterpret_cast<float*>(twp_x) + round64(2 * nx));
+  float* lam_x = reinterpret_cast<float*>(twp_y) + round64(ny);
   float* lam_y = lam_x + round64(nx);
 
   cfd::FvmParams p{};
@@ -136,13 +167,14 @@ extern "C" int cfd_fvm_projection_noalloc(void* stream, int nx, int ny, double h
   p.pinv_scale = 1.f / ((float)nx * (float)ny);
   p.lamx = lam_x;
   p.lamy = lam_y;
-  p.tw_x = tw_x;
   p.tw_y = tw_y;
+  p.twp_x = twp_x;
+  p.twp_y = twp_y;
 
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
-  const int total = 2 * nx + ny + ny / 2 + 1;
-  noalloc_tables_kernel<<<(total + 255) / 256, 256, 0, s>>>(nx, ny, hx, hy, tw_x, tw_y,
-                                                            lam_x, lam_y);
+  const int total = ny + 2 * nx + ny + ny / 2 + 1;  // upper bound of the table entries
+  noalloc_tables_kernel<<<(total + 255) / 256, 256, 0, s>>>(nx, ny, hx, hy, tw_y, twp_x,
+                                                            twp_y, lam_x, lam_y);
   cudaError_t e = cudaGetLastError();
   float2* sp = reinterpret_cast<float2*>(spec);
   if (e == cudaSuccess) e = cfd::launch_fvm_div_rfft(p, u, v, sp, s);

@@ -67,31 +67,33 @@ struct T4 {
 // f of columns [x*W, x*W + W) from the state and writes its inverse
 // x-transform.  One transform per block keeps register use at that of a single
 // FFT.
-__global__ void __launch_bounds__(512, 1)
+__global__ void __launch_bounds__(256, 3)
     spec_col_prep_kernel(SpecParams p, int W, int log2W, int bstride,
                          const float2* __restrict__ w, T4 t4) {
   extern __shared__ float2 sbuf[];
   const int N = p.nx, ncols = p.L + 1;
   const int c0 = blockIdx.x * W, f = blockIdx.y;
   const int tid = threadIdx.x;
+#pragma unroll 4
   for (int e = tid; e < W * N; e += blockDim.x) {
     const int ww = e & (W - 1), kx = e >> log2W, c = c0 + ww;
-    sbuf[ww * bstride + kx] =
+    sbuf[ww * bstride + pidx(kx)] =
         c < ncols ? prep_factor(p, f, kx, c, w[(size_t)kx * ncols + c])
                   : make_float2(0.f, 0.f);
   }
   __syncthreads();
-  fft_inplace<1>(sbuf, p.log2nx, W, bstride, p.tw_x, p.log2nx, tid);
+  fft_inplace<1>(sbuf, p.log2nx, W, bstride, p.twp_x, tid);
   float2* dst = t4.t[f];
+#pragma unroll 4
   for (int e = tid; e < W * N; e += blockDim.x) {
     const int ww = e & (W - 1), i = e >> log2W, c = c0 + ww;
-    if (c < ncols) dst[(size_t)i * ncols + c] = sbuf[ww * bstride + i];
+    if (c < ncols) dst[(size_t)i * ncols + c] = sbuf[ww * bstride + pidx(i)];
   }
 }
 
 // x-transform of the advection row spectra, then one low-storage RK/CN stage
 // (or, with explicit_only, just F(u)).
-__global__ void __launch_bounds__(512, 1)
+__global__ void __launch_bounds__(256, 3)
     spec_col_update_kernel(SpecParams p, StageCoef sc, int W, int log2W,
                            int bstride, const float2* __restrict__ ahat,
                            float2* __restrict__ wst, float2* __restrict__ hst) {
@@ -99,19 +101,20 @@ __global__ void __launch_bounds__(512, 1)
   const int N = p.nx, ncols = p.L + 1;
   const int c0 = blockIdx.x * W;
   const int tid = threadIdx.x;
+#pragma unroll 4
   for (int e = tid; e < W * N; e += blockDim.x) {
     const int w = e & (W - 1), i = e >> log2W, c = c0 + w;
-    sbuf[w * bstride + i] =
+    sbuf[w * bstride + pidx(i)] =
         c < ncols ? ahat[(size_t)i * ncols + c] : make_float2(0.f, 0.f);
   }
   __syncthreads();
-  fft_inplace<-1>(sbuf, p.log2nx, W, bstride, p.tw_x, p.log2nx, tid);
+  fft_inplace<-1>(sbuf, p.log2nx, W, bstride, p.twp_x, tid);
   for (int e = tid; e < W * N; e += blockDim.x) {
     const int w = e & (W - 1), kx = e >> log2W, c = c0 + w;
     if (c >= ncols) continue;
     const size_t g = (size_t)kx * ncols + c;
     // explicit_terms: rfftn(advection) * filter (+ forcing curl)
-    const float2 a = sbuf[w * bstride + kx];
+    const float2 a = sbuf[w * bstride + pidx(kx)];
     float2 F = a;
     if (p.filt_on) {
       const float fl = filt(p, kx, c);
@@ -143,123 +146,148 @@ __global__ void __launch_bounds__(512, 1)
   }
 }
 
-__global__ void __launch_bounds__(256, 2) spec_row_kernel(SpecParams p, int rows,
-                                const float2* __restrict__ t0,
-                                const float2* __restrict__ t1,
-                                const float2* __restrict__ t2,
-                                const float2* __restrict__ t3,
-                                float2* __restrict__ ahat) {
+__global__ void __launch_bounds__(256, 3)
+    spec_row_kernel(SpecParams p, int rows, const float2* __restrict__ t0,
+                    const float2* __restrict__ t1, const float2* __restrict__ t2,
+                    const float2* __restrict__ t3, float2* __restrict__ ahat) {
   extern __shared__ float2 sbuf[];
-  const int L = p.L, log2L = p.log2L, ncols = L + 1;
-  const int half = L >> 1;
+  const int L = p.L, log2L = p.log2L, ncols = L + 1, PL = padded_len(L);
+  const int half = L >> 1, log2h = log2L - 1;
   const int i0 = blockIdx.x * rows;
   const float2* tf[4] = {t0, t1, t2, t3};
   // Inverse real transforms along y: build the half-length complex inputs.
-  for (int idx = threadIdx.x; idx < rows * 4 * (half + 1); idx += blockDim.x) {
-    const int rf = idx / (half + 1), k = idx - rf * (half + 1);
+  // Pairs (k, L-k) for k in [1, L/2); the k = 0 slot also does DC/Nyquist and
+  // the middle element.
+  for (int idx = threadIdx.x; idx < ((rows * 4) << log2h); idx += blockDim.x) {
+    const int rf = idx >> log2h, k = idx & (half - 1);
     const int r = rf >> 2, f = rf & 3;
     const float2* in = tf[f] + (size_t)(i0 + r) * ncols;
-    float2* z = sbuf + rf * L;
+    float2* z = sbuf + rf * PL;
     if (k == 0) {
       const float2 x0 = row_factor(p, f, 0, in[0]);
       const float2 xl = row_factor(p, f, L, in[L]);
       z[0] = make_float2(x0.x + xl.x, x0.x - xl.x);
+      const float2 xh = row_factor(p, f, half, in[half]);
+      float2 zk, zm;
+      irfft_pre_pair(xh, xh, __ldg(p.tw_y + half), &zk, &zm);
+      z[pidx(half)] = zk;
     } else {
       const float2 xk = row_factor(p, f, k, in[k]);
       const float2 xm = row_factor(p, f, L - k, in[L - k]);
       float2 zk, zm;
       irfft_pre_pair(xk, xm, __ldg(p.tw_y + k), &zk, &zm);
-      z[k] = zk;
-      if (k != L - k) z[L - k] = zm;
+      z[pidx(k)] = zk;
+      z[pidx(L - k)] = zm;
     }
   }
   __syncthreads();
-  fft_inplace<1>(sbuf, log2L, rows * 4, L, p.tw_y, p.log2ny, threadIdx.x);
+  fft_inplace<1>(sbuf, log2L, rows * 4, PL, p.twp_y, threadIdx.x);
   // advection = -(gx * vx + gy * vy), each field scaled by 1/(nx*ny).
   const float s2 = p.scale * p.scale;
-  for (int idx = threadIdx.x; idx < rows * L; idx += blockDim.x) {
+  for (int idx = threadIdx.x; idx < (rows << log2L); idx += blockDim.x) {
     const int r = idx >> log2L, n = idx & (L - 1);
-    float2* z = sbuf + (r * 4) * L + n;
-    const float2 vx = z[0], vy = z[L], gx = z[2 * L], gy = z[3 * L];
+    float2* z = sbuf + (r * 4) * PL + pidx(n);
+    const float2 vx = z[0], vy = z[PL], gx = z[2 * PL], gy = z[3 * PL];
     z[0] = make_float2(-(gx.x * vx.x + gy.x * vy.x) * s2,
                        -(gx.y * vx.y + gy.y * vy.y) * s2);
   }
   __syncthreads();
-  fft_inplace<-1>(sbuf, log2L, rows, 4 * L, p.tw_y, p.log2ny, threadIdx.x);
-  for (int idx = threadIdx.x; idx < rows * (half + 1); idx += blockDim.x) {
-    const int r = idx / (half + 1), k = idx - r * (half + 1);
-    const float2* z = sbuf + (r * 4) * L;
+  fft_inplace<-1>(sbuf, log2L, rows, 4 * PL, p.twp_y, threadIdx.x);
+  for (int idx = threadIdx.x; idx < (rows << log2h); idx += blockDim.x) {
+    const int r = idx >> log2h, k = idx & (half - 1);
+    const float2* z = sbuf + (r * 4) * PL;
     float2* out = ahat + (size_t)(i0 + r) * ncols;
     if (k == 0) {
       const float2 z0 = z[0];
       out[0] = make_float2(z0.x + z0.y, 0.f);
       out[L] = make_float2(z0.x - z0.y, 0.f);
+      const float2 zh = z[pidx(half)];
+      float2 xk, xm;
+      rfft_post_pair(zh, zh, __ldg(p.tw_y + half), &xk, &xm);
+      out[half] = xk;
     } else {
       float2 xk, xm;
-      rfft_post_pair(z[k], z[L - k], __ldg(p.tw_y + k), &xk, &xm);
+      rfft_post_pair(z[pidx(k)], z[pidx(L - k)], __ldg(p.tw_y + k), &xk, &xm);
       out[k] = xk;
-      if (k != L - k) out[L - k] = xm;
+      out[L - k] = xm;
     }
   }
 }
 
 // Real rows -> unpacked half spectra (rfft along y).
-__global__ void __launch_bounds__(256, 2) row_rfft_kernel(SpecParams p, int rows, const float* __restrict__ x,
-                                float2* __restrict__ X) {
+__global__ void __launch_bounds__(256, 3)
+    row_rfft_kernel(SpecParams p, int rows, const float* __restrict__ x,
+                    float2* __restrict__ X) {
   extern __shared__ float2 sbuf[];
-  const int L = p.L, log2L = p.log2L, ncols = L + 1, half = L >> 1;
+  const int L = p.L, log2L = p.log2L, ncols = L + 1, PL = padded_len(L);
+  const int half = L >> 1, log2h = log2L - 1;
   const int i0 = blockIdx.x * rows;
-  float* sd = reinterpret_cast<float*>(sbuf);
-  for (int idx = threadIdx.x; idx < rows * p.ny; idx += blockDim.x)
-    sd[idx] = __ldg(x + (size_t)i0 * p.ny + idx);
+  for (int idx = threadIdx.x; idx < (rows << log2L); idx += blockDim.x) {
+    const int r = idx >> log2L, n = idx & (L - 1);
+    sbuf[r * PL + pidx(n)] =
+        __ldg(reinterpret_cast<const float2*>(x + (size_t)(i0 + r) * p.ny) + n);
+  }
   __syncthreads();
-  fft_inplace<-1>(sbuf, log2L, rows, L, p.tw_y, p.log2ny, threadIdx.x);
-  for (int idx = threadIdx.x; idx < rows * (half + 1); idx += blockDim.x) {
-    const int r = idx / (half + 1), k = idx - r * (half + 1);
-    const float2* z = sbuf + r * L;
+  fft_inplace<-1>(sbuf, log2L, rows, PL, p.twp_y, threadIdx.x);
+  for (int idx = threadIdx.x; idx < (rows << log2h); idx += blockDim.x) {
+    const int r = idx >> log2h, k = idx & (half - 1);
+    const float2* z = sbuf + r * PL;
     float2* out = X + (size_t)(i0 + r) * ncols;
     if (k == 0) {
       const float2 z0 = z[0];
       out[0] = make_float2(z0.x + z0.y, 0.f);
       out[L] = make_float2(z0.x - z0.y, 0.f);
+      const float2 zh = z[pidx(half)];
+      float2 xk, xm;
+      rfft_post_pair(zh, zh, __ldg(p.tw_y + half), &xk, &xm);
+      out[half] = xk;
     } else {
       float2 xk, xm;
-      rfft_post_pair(z[k], z[L - k], __ldg(p.tw_y + k), &xk, &xm);
+      rfft_post_pair(z[pidx(k)], z[pidx(L - k)], __ldg(p.tw_y + k), &xk, &xm);
       out[k] = xk;
-      if (k != L - k) out[L - k] = xm;
+      out[L - k] = xm;
     }
   }
 }
 
 // Unpacked half spectra -> real rows (irfft along y), times `scale`.
-__global__ void __launch_bounds__(256, 2) row_irfft_kernel(SpecParams p, int rows, const float2* __restrict__ X,
-                                 float* __restrict__ x, float scale) {
+__global__ void __launch_bounds__(256, 3)
+    row_irfft_kernel(SpecParams p, int rows, const float2* __restrict__ X,
+                     float* __restrict__ x, float scale) {
   extern __shared__ float2 sbuf[];
-  const int L = p.L, log2L = p.log2L, ncols = L + 1, half = L >> 1;
+  const int L = p.L, log2L = p.log2L, ncols = L + 1, PL = padded_len(L);
+  const int half = L >> 1, log2h = log2L - 1;
   const int i0 = blockIdx.x * rows;
-  for (int idx = threadIdx.x; idx < rows * (half + 1); idx += blockDim.x) {
-    const int r = idx / (half + 1), k = idx - r * (half + 1);
+  for (int idx = threadIdx.x; idx < (rows << log2h); idx += blockDim.x) {
+    const int r = idx >> log2h, k = idx & (half - 1);
     const float2* in = X + (size_t)(i0 + r) * ncols;
-    float2* z = sbuf + r * L;
+    float2* z = sbuf + r * PL;
     if (k == 0) {
       const float2 x0 = in[0], xl = in[L];
       z[0] = make_float2(x0.x + xl.x, x0.x - xl.x);
+      const float2 xh = in[half];
+      float2 zk, zm;
+      irfft_pre_pair(xh, xh, __ldg(p.tw_y + half), &zk, &zm);
+      z[pidx(half)] = zk;
     } else {
       float2 zk, zm;
       irfft_pre_pair(in[k], in[L - k], __ldg(p.tw_y + k), &zk, &zm);
-      z[k] = zk;
-      if (k != L - k) z[L - k] = zm;
+      z[pidx(k)] = zk;
+      z[pidx(L - k)] = zm;
     }
   }
   __syncthreads();
-  fft_inplace<1>(sbuf, log2L, rows, L, p.tw_y, p.log2ny, threadIdx.x);
-  const float* sd = reinterpret_cast<const float*>(sbuf);
-  for (int idx = threadIdx.x; idx < rows * p.ny; idx += blockDim.x)
-    x[(size_t)i0 * p.ny + idx] = sd[idx] * scale;
+  fft_inplace<1>(sbuf, log2L, rows, PL, p.twp_y, threadIdx.x);
+  for (int idx = threadIdx.x; idx < (rows << log2L); idx += blockDim.x) {
+    const int r = idx >> log2L, n = idx & (L - 1);
+    const float2 z = sbuf[r * PL + pidx(n)];
+    reinterpret_cast<float2*>(x + (size_t)(i0 + r) * p.ny)[n] =
+        make_float2(z.x * scale, z.y * scale);
+  }
 }
 
 template <int SIGN>
-__global__ void __launch_bounds__(512, 1) col_fft_kernel(SpecParams p, int W, int log2W, int bstride,
+__global__ void __launch_bounds__(256, 3) col_fft_kernel(SpecParams p, int W, int log2W, int bstride,
                                float2* __restrict__ X,
                                const float* __restrict__ mult) {
   extern __shared__ float2 sbuf[];
@@ -267,14 +295,14 @@ __global__ void __launch_bounds__(512, 1) col_fft_kernel(SpecParams p, int W, in
   const int c0 = blockIdx.x * W;
   for (int e = threadIdx.x; e < W * N; e += blockDim.x) {
     const int w = e & (W - 1), i = e >> log2W, c = c0 + w;
-    sbuf[w * bstride + i] = c < ncols ? X[(size_t)i * ncols + c] : make_float2(0.f, 0.f);
+    sbuf[w * bstride + pidx(i)] = c < ncols ? X[(size_t)i * ncols + c] : make_float2(0.f, 0.f);
   }
   __syncthreads();
-  fft_inplace<SIGN>(sbuf, p.log2nx, W, bstride, p.tw_x, p.log2nx, threadIdx.x);
+  fft_inplace<SIGN>(sbuf, p.log2nx, W, bstride, p.twp_x, threadIdx.x);
   for (int e = threadIdx.x; e < W * N; e += blockDim.x) {
     const int w = e & (W - 1), i = e >> log2W, c = c0 + w;
     if (c < ncols) {
-      float2 v = sbuf[w * bstride + i];
+      float2 v = sbuf[w * bstride + pidx(i)];
       if (mult) v = c_scale(v, __ldg(mult + (size_t)i * ncols + c));
       X[(size_t)i * ncols + c] = v;
     }
@@ -304,8 +332,8 @@ struct ColCfg {
 
 ColCfg col_cfg(const SpecParams& p) {
   ColCfg c;
-  int W = 4096 >> p.log2nx;
-  if (W < 2) W = 2;
+  int W = 4096 >> p.log2nx;  // 256-thread blocks
+  if (W < 1) W = 1;
   const int ncols = p.L + 1;
   // W never needs to exceed the next power of two above ncols.
   int cap = 1;
@@ -313,7 +341,7 @@ ColCfg col_cfg(const SpecParams& p) {
   if (W > cap) W = cap;
   c.W = W;
   c.log2W = ilog2(W);
-  c.bstride = p.nx + 4;
+  c.bstride = padded_len(p.nx) + 8;  // consecutive columns 16 banks apart
   c.blocks = (ncols + W - 1) / W;
   const int workers = fft_workers(p.log2nx, W);
   int t = ((workers + 31) / 32) * 32;
@@ -372,7 +400,7 @@ cudaError_t launch_spec_col_update(const SpecParams& p, const StageCoef& sc,
 cudaError_t launch_spec_row(const SpecParams& p, const float2* const t4[4],
                             float2* ahat, cudaStream_t s) {
   const int rows = rows_per_block(p.log2L, 4, p.nx);
-  const size_t smem = (size_t)rows * 4 * p.L * sizeof(float2);
+  const size_t smem = (size_t)rows * 4 * padded_len(p.L) * sizeof(float2);
   cudaError_t e = set_smem(spec_row_kernel, smem);
   if (e != cudaSuccess) return e;
   spec_row_kernel<<<p.nx / rows, threads_for(fft_workers(p.log2L, rows * 4)),
@@ -383,7 +411,7 @@ cudaError_t launch_spec_row(const SpecParams& p, const float2* const t4[4],
 cudaError_t launch_row_rfft(const SpecParams& p, const float* x, float2* X,
                             cudaStream_t s) {
   const int rows = rows_per_block(p.log2L, 1, p.nx);
-  const size_t smem = (size_t)rows * p.L * sizeof(float2);
+  const size_t smem = (size_t)rows * padded_len(p.L) * sizeof(float2);
   cudaError_t e = set_smem(row_rfft_kernel, smem);
   if (e != cudaSuccess) return e;
   row_rfft_kernel<<<p.nx / rows, threads_for(fft_workers(p.log2L, rows)), smem,
@@ -394,7 +422,7 @@ cudaError_t launch_row_rfft(const SpecParams& p, const float* x, float2* X,
 cudaError_t launch_row_irfft(const SpecParams& p, const float2* X, float* x,
                              float scale, cudaStream_t s) {
   const int rows = rows_per_block(p.log2L, 1, p.nx);
-  const size_t smem = (size_t)rows * p.L * sizeof(float2);
+  const size_t smem = (size_t)rows * padded_len(p.L) * sizeof(float2);
   cudaError_t e = set_smem(row_irfft_kernel, smem);
   if (e != cudaSuccess) return e;
   row_irfft_kernel<<<p.nx / rows, threads_for(fft_workers(p.log2L, rows)), smem,

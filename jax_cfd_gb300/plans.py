@@ -111,6 +111,17 @@ class FvmPlan:
               'cfd_fvm_step')
     return u_out, v_out
 
+  def autotune(self, u, v, steps: int = 20) -> int:
+    """Times each transform launch shape on (u, v) and keeps the fastest;
+    returns the chosen shape index.  Synchronises the stream."""
+    us, vs = torch.empty_like(u), torch.empty_like(v)
+    chosen = ctypes.c_int(-1)
+    a = self._fields(u, v, us, vs)
+    nat.check(self._lib.cfd_fvm_plan_autotune(self._h, current_stream_ptr(u.device), *a,
+                                              int(steps), ctypes.byref(chosen)),
+              'cfd_fvm_plan_autotune')
+    return int(chosen.value)
+
   PROFILE_KINDS = ('explicit', 'div_rfft', 'col_pinv', 'irfft', 'project_out')
 
   def profile(self, u, v, steps: int):

@@ -176,3 +176,23 @@ def test_initial_conditions_match_oracle(cuda_device):
   assert np.abs(ofvm.divergence(got, og.step)).max() <= 5e-4
   speed = np.sqrt(got[0] ** 2 + got[1] ** 2).max()
   assert abs(speed - 2.0) <= 1e-5 * 2.0
+
+
+@pytest.mark.parametrize('shape', [(64, 64), (1024, 1024)])
+def test_autotune_keeps_results_bitwise(cuda_device, shape):
+  """The transform launch shapes compute identical bits; the autotuner only
+  changes speed."""
+  import jax_cfd_gb300.base as cfd
+  from oracle import fvm as ofvm
+  og, v0 = _setup(shape, seed=4)
+  grid = cfd.grids.Grid(shape, domain=((0, TWO_PI), (0, TWO_PI)))
+  dt = ofvm.stable_time_step(2.0, 0.5, 1e-3, og)
+  step = cfd.equations.semi_implicit_navier_stokes(
+      1.0, 1e-3, dt, grid, forcing=cfd.forcings.simple_turbulence_forcing(grid, 1, 4, -0.1))
+  v = _to_gpu(v0, grid, cuda_device)
+  before = cfd.funcutils.repeated(step, 3)(v)
+  plan = step.plan(cuda_device)
+  assert plan.autotune(v[0].data, v[1].data, 2) in (0, 1)
+  after = cfd.funcutils.repeated(step, 3)(v)
+  for x, y in zip(before, after):
+    assert torch.equal(x.data, y.data)
