@@ -27,31 +27,30 @@ constexpr int kStencilThreads = 256;
 // One face value of apply_tvd_limiter(lax_wendroff, van_leer_limiter) times
 // the face velocity: interpolation.py:96-303 specialised to a forward
 // half-cell interpolation with stencil c[-1], c[0], c[+1], c[+2] along the
-// face normal and face velocity U.
+// face normal and face velocity U.  The reference computes
 //   upwind        c_low  = U > 0 ? c0 : c1
 //   lax_wendroff  c_high = U > 0 ? c0 + 0.5(1-C)(c1-c0) : c1 - 0.5(1+C)(c1-c0)
-//   ratio         r = safe_div(num, den), num = U > 0 ? c0-cm : c2-c1,
-//                 den = c1-c0 (1 where c1 == c0)
+//   ratio         r = safe_div(U > 0 ? c0-cm : c2-c1, c1-c0)
 //   van Leer      phi = r > 0 ? 2r / (1+r) : 0
 //   face value    c_low - (c_low - c_high) * phi
-// Selecting r before the limiter equals selecting phi after it (the limiter
-// is elementwise).  With r = num/den, 2r/(1+r) = 2 num / (den + num) and
-// r > 0 exactly when num and den are non-zero with equal signs, so the
-// limiter costs one division instead of two; the result differs from the
-// two-division form only in the last bits.
+// In upwind-mirrored variables (a, b, c) = U > 0 ? (cm, c0, c1) : (c2, c1, c0)
+// this is c_low = b, c_high = b + 0.5(1 - |C|)(c - b) and r = (b - a)/(c - b):
+// both branches round exactly as above (the mirrored forms differ from them
+// only by exact negations).  2r/(1+r) = 2 num / (den + num) with num = b - a,
+// den = c - b, and r > 0 exactly when num * den > 0 (up to underflow of the
+// product), so the limiter costs one approximate division.  Where c - b == 0
+// the reference divides by 1 instead; there c_high - c_low is exactly 0, so
+// phi does not change the face value.
 CFD_D float tvd_flux(float cm, float c0, float c1, float c2, float U,
                      float cfl) {
-  const float C = cfl * U;
-  const float d0 = c1 - c0;
   const bool pos = U > 0.f;
-  const float c_low = pos ? c0 : c1;
-  const float c_high =
-      pos ? c0 + (0.5f * (1.f - C)) * d0 : c1 - (0.5f * (1.f + C)) * d0;
-  const float num = pos ? c0 - cm : c2 - c1;
-  const float den = d0 != 0.f ? d0 : 1.f;
-  const bool rpos = (num > 0.f && den > 0.f) || (num < 0.f && den < 0.f);
-  const float phi = rpos ? __fdividef(2.f * num, den + num) : 0.f;
-  const float cf = c_low - (c_low - c_high) * phi;
+  const float a = pos ? cm : c2, b = pos ? c0 : c1, c = pos ? c1 : c0;
+  const float C = cfl * U;
+  const float diff = c - b;
+  const float c_high = b + (0.5f * (1.f - fabsf(C))) * diff;
+  const float num = b - a;
+  const float phi = num * diff > 0.f ? __fdividef(num + num, diff + num) : 0.f;
+  const float cf = b + (c_high - b) * phi;
   return cf * U;
 }
 
@@ -193,12 +192,50 @@ __global__ void __launch_bounds__(kStencilThreads)
   }
 }
 
-// The same step for grids whose shape is a multiple of the 16 x 64 tile, with
+// Paired float32 arithmetic (sm_100+ f32x2 instructions): the u- and
+// v-components of a face or cell run the same operation sequence, so they are
+// packed as (u, v) pairs.  Each paired op rounds exactly like its scalar form.
+CFD_D float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+CFD_D float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+CFD_D float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+CFD_D float2 sub2(float2 a, float2 b) {
+  unsigned long long r;
+  const unsigned long long x = *reinterpret_cast<unsigned long long*>(&a);
+  const unsigned long long y = *reinterpret_cast<unsigned long long*>(&b);
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(x), "l"(y));
+  return *reinterpret_cast<float2*>(&r);
+}
+CFD_D float2 splat2(float a) { return make_float2(a, a); }
+CFD_D float2 sel2(bool px, bool py, float2 a, float2 b) {
+  return make_float2(px ? a.x : b.x, py ? a.y : b.y);
+}
+
+// Van Leer face values of two faces at once (tvd_flux in paired arithmetic).
+CFD_D float2 tvd_flux2(float2 cm, float2 c0, float2 c1, float2 c2, float2 U,
+                       float cfl) {
+  const bool px = U.x > 0.f, py = U.y > 0.f;
+  const float2 a = sel2(px, py, cm, c2), b = sel2(px, py, c0, c1),
+               c = sel2(px, py, c1, c0);
+  const float2 C = mul2(splat2(cfl), U);
+  const float2 diff = sub2(c, b);
+  const float2 t = mul2(splat2(0.5f), make_float2(1.f - fabsf(C.x), 1.f - fabsf(C.y)));
+  const float2 c_high = fma2(t, diff, b);
+  const float2 num = sub2(b, a);
+  const float2 prod = mul2(num, diff);
+  const float2 n2 = add2(num, num), dn = add2(diff, num);
+  const float2 phi = make_float2(prod.x > 0.f ? __fdividef(n2.x, dn.x) : 0.f,
+                                 prod.y > 0.f ? __fdividef(n2.y, dn.y) : 0.f);
+  const float2 cf = fma2(sub2(c_high, b), phi, b);
+  return mul2(cf, U);
+}
+
+// The step for grids whose shape is a multiple of the 16 x 64 tile, with
 // compile-time tile geometry: the halo box (rows i0-2 .. i0+17, columns
 // j0-4 .. j0+67) is loaded with aligned float4 reads (a 4-column group never
-// straddles the periodic seam because ny is a multiple of 4), face fluxes are
-// computed once per face into shared memory, and each thread then updates 4
-// cells of one column.
+// straddles the periodic seam because ny is a multiple of 4) and stored
+// interleaved as (u, v) pairs; face fluxes are computed once per face, for the
+// u- and v-control volumes together, into paired shared arrays; each thread
+// then updates 4 cells of one column.
 constexpr int kBoxW = kTJ + 8;  // 72 columns: j0-4 .. j0+67
 template <bool PROJECT, bool OUT_K0, int CONVECT>
 __global__ void __launch_bounds__(kStencilThreads)
@@ -206,13 +243,10 @@ __global__ void __launch_bounds__(kStencilThreads)
                               const float* __restrict__ va,
                               const float* __restrict__ q,
                               float* __restrict__ uo, float* __restrict__ vo) {
-  __shared__ __align__(16) float su[kTI + 4][kBoxW];
-  __shared__ __align__(16) float sv[kTI + 4][kBoxW];
+  __shared__ __align__(16) float2 sw[kTI + 4][kBoxW];  // (u, v)
   __shared__ __align__(16) float sq[PROJECT ? kTI + 5 : 1][PROJECT ? kBoxW : 4];
-  __shared__ float fx[kTI + 1][kTJ];
-  __shared__ float gx[kTI + 1][kTJ];
-  __shared__ float fy[kTI][kTJ + 1];
-  __shared__ float gy[kTI][kTJ + 1];
+  __shared__ float2 fxg[kTI + 1][kTJ];  // x-normal faces: (F, G)
+  __shared__ float2 fyg[kTI][kTJ + 1];  // y-normal faces: (F, G)
 
   const int i0 = blockIdx.y * kTI, j0 = blockIdx.x * kTJ;
   const int mx = p.nx - 1, my = p.ny - 1;
@@ -248,32 +282,38 @@ __global__ void __launch_bounds__(kStencilThreads)
       v.z = v.z - (q3 - q2) * p.inv_hy;
       v.w = v.w - (q4 - q3) * p.inv_hy;  // last group unused (box column 71)
     }
-    *reinterpret_cast<float4*>(&su[a][4 * k]) = u;
-    *reinterpret_cast<float4*>(&sv[a][4 * k]) = v;
+    float4* dst = reinterpret_cast<float4*>(&sw[a][4 * k]);
+    dst[0] = make_float4(u.x, v.x, u.y, v.y);
+    dst[1] = make_float4(u.z, v.z, u.w, v.w);
   }
   __syncthreads();
 
   const int b = tid & (kTJ - 1);
   const int w = tid >> 6;  // 0..3
   // x-normal faces: face a follows cell i0 - 1 + a (box row a + 1), a < 17.
+  // u's control volume: face velocity 0.5 u[i] + 0.5 u[i+1];
+  // v's control volume: u interpolated along y, 0.5 u[j] + 0.5 u[j+1].
 #pragma unroll
   for (int k = 0; k < 5; ++k) {
     const int a = w + 4 * k;
     if (a <= kTI) {
       const int c = b + 4;
-      const float U = 0.5f * su[a + 1][c] + 0.5f * su[a + 2][c];
-      const float Uv = 0.5f * su[a + 1][c] + 0.5f * su[a + 1][c + 1];
+      const float2 cm = sw[a][c], c0 = sw[a + 1][c], c1 = sw[a + 2][c], c2 = sw[a + 3][c];
+      const float uy1 = sw[a + 1][c + 1].x;
+      const float2 U = mul2(splat2(0.5f), add2(splat2(c0.x), make_float2(c1.x, uy1)));
       if (CONVECT == 0) {
-        fx[a][b] = tvd_flux(su[a][c], su[a + 1][c], su[a + 2][c], su[a + 3][c], U, p.cfl_x);
-        gx[a][b] = tvd_flux(sv[a][c], sv[a + 1][c], sv[a + 2][c], sv[a + 3][c], Uv, p.cfl_x);
+        fxg[a][b] = tvd_flux2(cm, c0, c1, c2, U, p.cfl_x);
       } else {
-        fx[a][b] = U * U;
-        gx[a][b] = (0.5f * sv[a + 1][c] + 0.5f * sv[a + 2][c]) * Uv;
+        // flux = c_face * U with c_face = linear interpolation of (u, v)
+        const float2 cface = mul2(splat2(0.5f), add2(c0, c1));
+        fxg[a][b] = mul2(make_float2(U.x, cface.y), make_float2(U.x, U.y));
       }
     }
   }
   // y-normal faces: face f follows cell j0 - 1 + f (box column f + 3), f < 65;
   // columns f = 0..63 by all threads, f = 64 by the first 16 threads.
+  // u's control volume: v interpolated along x, 0.5 v[i] + 0.5 v[i+1];
+  // v's control volume: 0.5 v[j] + 0.5 v[j+1].
 #pragma unroll
   for (int k = 0; k < 5; ++k) {
     int a, f;
@@ -286,40 +326,45 @@ __global__ void __launch_bounds__(kStencilThreads)
       f = kTJ;
     }
     const int r = a + 2, c = f + 3;
-    const float V = 0.5f * sv[r][c] + 0.5f * sv[r + 1][c];
-    const float Vv = 0.5f * sv[r][c] + 0.5f * sv[r][c + 1];
+    const float2 cm = sw[r][c - 1], c0 = sw[r][c], c1 = sw[r][c + 1], c2 = sw[r][c + 2];
+    const float vx1 = sw[r + 1][c].y;
+    const float2 V = mul2(splat2(0.5f), add2(splat2(c0.y), make_float2(vx1, c1.y)));
     if (CONVECT == 0) {
-      fy[a][f] = tvd_flux(su[r][c - 1], su[r][c], su[r][c + 1], su[r][c + 2], V, p.cfl_y);
-      gy[a][f] = tvd_flux(sv[r][c - 1], sv[r][c], sv[r][c + 1], sv[r][c + 2], Vv, p.cfl_y);
+      fyg[a][f] = tvd_flux2(cm, c0, c1, c2, V, p.cfl_y);
     } else {
-      fy[a][f] = (0.5f * su[r][c] + 0.5f * su[r][c + 1]) * V;
-      gy[a][f] = Vv * Vv;
+      const float2 cface = mul2(splat2(0.5f), add2(c0, c1));
+      fyg[a][f] = mul2(make_float2(cface.x, V.y), make_float2(V.x, V.y));
     }
   }
   __syncthreads();
 
+  const float2 ihx = splat2(p.inv_hx), ihy = splat2(p.inv_hy);
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
     const int a = w + 4 * k;
     const int r = a + 2, c = b + 4;
     const int i = i0 + a, j = j0 + b;
-    const float u = su[r][c], v = sv[r][c];
-    float ku = -((fx[a + 1][b] - fx[a][b]) * p.inv_hx + (fy[a][b + 1] - fy[a][b]) * p.inv_hy);
-    float kv = -((gx[a + 1][b] - gx[a][b]) * p.inv_hx + (gy[a][b + 1] - gy[a][b]) * p.inv_hy);
+    const float2 uv = sw[r][c];
+    // -divergence(flux): -((F[i] - F[i-1]) / hx + (F[j] - F[j-1]) / hy)
+    const float2 dx = mul2(sub2(fxg[a + 1][b], fxg[a][b]), ihx);
+    float2 kk = fma2(sub2(fyg[a][b + 1], fyg[a][b]), ihy, dx);
+    kk = make_float2(-kk.x, -kk.y);
     if (p.has_visc) {
-      const float lu = ((-2.f * u) * p.ssum + (su[r - 1][c] + su[r + 1][c]) * p.sx) +
-                       (su[r][c - 1] + su[r][c + 1]) * p.sy;
-      const float lv = ((-2.f * v) * p.ssum + (sv[r - 1][c] + sv[r + 1][c]) * p.sx) +
-                       (sv[r][c - 1] + sv[r][c + 1]) * p.sy;
-      ku = ku + p.nu * lu;
-      kv = kv + p.nu * lv;
+      // finite_differences.laplacian: -2c * sum(scales) + pairs * scale
+      const float2 lx = add2(sw[r - 1][c], sw[r + 1][c]);
+      const float2 ly = add2(sw[r][c - 1], sw[r][c + 1]);
+      const float2 m2 = mul2(splat2(-2.f), uv);
+      float2 lap = fma2(lx, splat2(p.sx), mul2(m2, splat2(p.ssum)));
+      lap = fma2(ly, splat2(p.sy), lap);
+      kk = fma2(splat2(p.nu), lap, kk);
     }
     if (p.has_forcing) {
+      // sum_forcings(linear, constant): (0 + lin * u) + const
       float fu = 0.f, fv = 0.f;
       bool any_u = false, any_v = false;
       if (p.has_lin) {
-        fu = p.lin * u;
-        fv = p.lin * v;
+        fu = p.lin * uv.x;
+        fv = p.lin * uv.y;
         any_u = any_v = true;
       }
       if (p.fu_y) { fu = any_u ? fu + __ldg(p.fu_y + j) : __ldg(p.fu_y + j); any_u = true; }
@@ -330,15 +375,16 @@ __global__ void __launch_bounds__(kStencilThreads)
         fu = fu / p.density;
         fv = fv / p.density;
       }
-      if (any_u) ku = ku + fu;
-      if (any_v) kv = kv + fv;
+      if (any_u) kk.x = kk.x + fu;
+      if (any_v) kk.y = kk.y + fv;
     }
     if (OUT_K0) {
-      uo[i * ny + j] = ku;
-      vo[i * ny + j] = kv;
+      uo[i * ny + j] = kk.x;
+      vo[i * ny + j] = kk.y;
     } else {
-      uo[i * ny + j] = u + p.dt * ku;
-      vo[i * ny + j] = v + p.dt * kv;
+      const float2 nxt = fma2(splat2(p.dt), kk, uv);
+      uo[i * ny + j] = nxt.x;
+      vo[i * ny + j] = nxt.y;
     }
   }
 }
