@@ -101,10 +101,11 @@ int cfd_fvm_step(cfd_fvm_plan* plan, void* stream, const float* u,
 int cfd_fvm_profile(cfd_fvm_plan* plan, void* stream, const float* u,
                     const float* v, float* u_out, float* v_out, int steps,
                     float* ms_out);
-/* Autotuner: times `steps` steps for each candidate launch shape of the
- * transform kernels (u, v read-only; results go to the scratch arrays),
- * keeps the fastest in the plan and writes its index to *chosen (may be
- * NULL).  Synchronises the stream. */
+/* Autotuner: times `steps` steps for each candidate launch configuration of
+ * the transform kernels (row block shape x column-pass scheme; u, v
+ * read-only, results go to the scratch arrays), keeps the fastest in the plan
+ * and writes its index (shape + 2 * column scheme) to *chosen (may be NULL).
+ * Synchronises the stream. */
 int cfd_fvm_plan_autotune(cfd_fvm_plan* plan, void* stream, const float* u,
                           const float* v, float* u_scratch, float* v_scratch,
                           int steps, int* chosen);

@@ -401,10 +401,15 @@ int cfd_fvm_plan_autotune(cfd_fvm_plan* plan, void* stream, const float* u,
   CFD_CHECK(cudaEventCreate(&e0), "cudaEventCreate");
   CFD_CHECK(cudaEventCreate(&e1), "cudaEventCreate");
   float best_ms = 0.f;
-  int best = plan->p.fft_shape;
+  int best = -1;
   int rc = CFD_OK;
-  for (int shape = 0; shape < 2 && rc == CFD_OK; ++shape) {
+  // Candidates: transform block shape (wide, narrow) x column pass (per-block
+  // columns, clusters of 4, clusters of 8); index = shape + 2 * col_mode.
+  for (int cand = 0; cand < 6 && rc == CFD_OK; ++cand) {
+    const int shape = cand & 1, col = cand >> 1;
     plan->p.fft_shape = shape;
+    plan->p.col_mode = col;
+    if (col > 0 && !cfd::col_cluster_ok(plan->p, col == 1 ? 4 : 8)) continue;
     rc = cfd_fvm_step(plan, stream, u, v, u_scratch, v_scratch, 1);
     if (rc) break;
     cudaError_t e = cudaEventRecord(e0, s);
@@ -418,14 +423,16 @@ int cfd_fvm_plan_autotune(cfd_fvm_plan* plan, void* stream, const float* u,
       rc = cuda_fail(e, "cfd_fvm_plan_autotune");
       break;
     }
-    if (shape == 0 || ms < best_ms) {
+    if (best < 0 || ms < best_ms) {
       best_ms = ms;
-      best = shape;
+      best = cand;
     }
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  plan->p.fft_shape = best;
+  if (best < 0) best = 0;
+  plan->p.fft_shape = best & 1;
+  plan->p.col_mode = best >> 1;
   if (chosen) *chosen = best;
   return rc;
 }

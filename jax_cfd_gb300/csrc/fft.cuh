@@ -144,6 +144,43 @@ CFD_HD int fft_pass_table_size(int log2L) {
   return fft_pass_table_offset(log2L, fft_num_passes(log2L));
 }
 
+// Multiplies v[r] by w^(r k) (conjugated for the inverse), r = 1..R-1.  Only
+// w^k and, for R >= 8, w^(4k) are read from the pass table; the other powers
+// are products of at most three table values (a few ulp), which replaces R-1
+// dependent table loads per butterfly with complex multiplications.
+template <int R, int SIGN>
+CFD_D void apply_twiddles(float2* v, const float2* __restrict__ twp, int Ns,
+                          int k) {
+  float2 w1 = __ldg(twp + k);
+  if (SIGN > 0) w1.y = -w1.y;
+  if (R == 2) {
+    v[1] = c_mul(v[1], w1);
+    return;
+  }
+  const float2 w2 = c_mul(w1, w1);
+  const float2 w3 = c_mul(w2, w1);
+  v[1] = c_mul(v[1], w1);
+  v[2] = c_mul(v[2], w2);
+  v[3] = c_mul(v[3], w3);
+  if (R == 4) return;
+  float2 w4 = __ldg(twp + 3 * Ns + k);
+  if (SIGN > 0) w4.y = -w4.y;
+  float2 wb[4];
+  wb[0] = make_float2(1.f, 0.f);
+  wb[1] = w4;
+  if (R == 16) {
+    wb[2] = c_mul(w4, w4);
+    wb[3] = c_mul(wb[2], w4);
+  }
+  const float2 wa[4] = {make_float2(1.f, 0.f), w1, w2, w3};
+#pragma unroll
+  for (int b = 1; b < R / 4; ++b) {
+    v[4 * b] = c_mul(v[4 * b], wb[b]);
+#pragma unroll
+    for (int a = 1; a < 4; ++a) v[4 * b + a] = c_mul(v[4 * b + a], c_mul(wa[a], wb[b]));
+  }
+}
+
 // One in-place Stockham pass.  `t` is the worker index in [0, nthr); threads of
 // the block with t >= nthr only take part in the barriers.  `twp` is this
 // pass's twiddle table (unused when Ns == 1).
@@ -176,14 +213,7 @@ CFD_D void stockham_pass(float2* buf, int log2L, int log2Ns, int bstride,
   if (active) {
 #pragma unroll
     for (int q = 0; q < NB; ++q) {
-      if (Ns > 1) {
-#pragma unroll
-        for (int r = 1; r < R; ++r) {
-          float2 w = __ldg(twp + (r - 1) * Ns + kk[q]);
-          if (SIGN > 0) w.y = -w.y;
-          v[q][r] = c_mul(v[q][r], w);
-        }
-      }
+      if (Ns > 1) apply_twiddles<R, SIGN>(v[q], twp, Ns, kk[q]);
       Dft<R, SIGN>::run(v[q]);
       float2* d = buf + bb[q];
 #pragma unroll

@@ -14,8 +14,12 @@
 // The half spectrum of a row of M reals is stored "packed" as M/2 complex
 // numbers: element 0 holds (X[0], X[M/2]), both real.  The x-axis transform
 // of that packed column is untangled with the two-real-signals identity.
+#include <cooperative_groups.h>
+
 #include "fft.cuh"
 #include "kernels.h"
+
+namespace cg = cooperative_groups;
 
 namespace cfd {
 namespace {
@@ -501,6 +505,70 @@ __global__ void __launch_bounds__(MAXT, MINB)
   }
 }
 
+// The column pass with one column per block and CL adjacent columns per
+// thread-block cluster.  Global memory is read and written in CL-column row
+// segments (32 or 64 bytes: whole sectors) through distributed shared memory:
+// block `rank` of the cluster moves rows [rank*nx/CL, (rank+1)*nx/CL) of all
+// CL columns between global memory and the owning blocks' shared memory, and
+// each block transforms its own column.
+template <int CL>
+__global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(128, 7)
+    fvm_col_pinv_cluster_kernel(FvmParams p, float2* __restrict__ spec) {
+  extern __shared__ float2 sbuf[];
+  cg::cluster_group cluster = cg::this_cluster();
+  const int rank = (int)cluster.block_rank();
+  const int L = p.ny >> 1, N = p.nx;
+  const int c0 = blockIdx.x - rank;  // first column of this cluster
+  const int c = c0 + rank;
+  const int tid = threadIdx.x;
+  const int rows_per = N / CL, r0 = rank * rows_per;
+  float2* dsm[CL];
+#pragma unroll
+  for (int r = 0; r < CL; ++r) dsm[r] = cluster.map_shared_rank(sbuf, r);
+#pragma unroll 2
+  for (int row = r0 + tid; row < r0 + rows_per; row += blockDim.x) {
+    const float4* src = reinterpret_cast<const float4*>(spec + (size_t)row * L + c0);
+    float4 v[CL / 2];
+#pragma unroll
+    for (int h = 0; h < CL / 2; ++h) v[h] = src[h];
+#pragma unroll
+    for (int h = 0; h < CL / 2; ++h) {
+      dsm[2 * h][pidx(row)] = make_float2(v[h].x, v[h].y);
+      dsm[2 * h + 1][pidx(row)] = make_float2(v[h].z, v[h].w);
+    }
+  }
+  cluster.sync();
+  fft_inplace<-1>(sbuf, p.log2nx, 1, padded_len(N), p.twp_x, tid);
+  if (c != 0) {
+    for (int kx = tid; kx < N; kx += blockDim.x)
+      sbuf[pidx(kx)] = c_scale(sbuf[pidx(kx)], pinv_diag(p, kx, c));
+  } else {
+    // Packed DC/Nyquist column (see fvm_col_pinv_kernel).
+    for (int k = tid; k <= N / 2; k += blockDim.x) {
+      const int m = (N - k) & (N - 1);
+      const float d0 = pinv_diag(p, k, 0), dn = pinv_diag(p, k, L);
+      const float al = 0.5f * (d0 + dn), be = 0.5f * (d0 - dn);
+      const float2 zk = sbuf[pidx(k)], zm = sbuf[pidx(m)];
+      sbuf[pidx(k)] = c_add(c_scale(zk, al), c_scale(c_conj(zm), be));
+      if (m != k) sbuf[pidx(m)] = c_add(c_scale(zm, al), c_scale(c_conj(zk), be));
+    }
+  }
+  __syncthreads();
+  fft_inplace<1>(sbuf, p.log2nx, 1, padded_len(N), p.twp_x, tid);
+  cluster.sync();
+#pragma unroll 2
+  for (int row = r0 + tid; row < r0 + rows_per; row += blockDim.x) {
+    float4* dst = reinterpret_cast<float4*>(spec + (size_t)row * L + c0);
+#pragma unroll
+    for (int h = 0; h < CL / 2; ++h) {
+      const float2 a = dsm[2 * h][pidx(row)], b = dsm[2 * h + 1][pidx(row)];
+      dst[h] = make_float4(a.x, a.y, b.x, b.y);
+    }
+  }
+  // No block may leave while a peer still reads its shared memory.
+  cluster.sync();
+}
+
 // Inverse packed real FFT of each row, in place: q^ rows -> q rows (floats).
 template <int MAXT, int MINB>
 __global__ void __launch_bounds__(MAXT, MINB)
@@ -699,8 +767,26 @@ static cudaError_t col_pinv_impl(const FvmParams& p, int target, float2* spec,
   return cudaGetLastError();
 }
 
+template <int CL>
+static cudaError_t col_pinv_cluster_impl(const FvmParams& p, float2* spec, cudaStream_t s) {
+  const int L = p.ny / 2;
+  const size_t smem = (size_t)padded_len(p.nx) * sizeof(float2);
+  cudaError_t e = set_smem(fvm_col_pinv_cluster_kernel<CL>, smem);
+  if (e != cudaSuccess) return e;
+  fvm_col_pinv_cluster_kernel<CL><<<L, block_threads(fft_workers(p.log2nx, 1)), smem, s>>>(p, spec);
+  return cudaGetLastError();
+}
+
+bool col_cluster_ok(const FvmParams& p, int cl) {
+  // One column per block with nx/16 <= 128 workers; nx/CL rows per block.
+  return p.nx >= 256 && p.nx <= 2048 && (p.ny / 2) % cl == 0;
+}
+
+// col_mode 1/2: clusters of 4/8 single-column blocks.
 cudaError_t launch_fvm_col_pinv(const FvmParams& p, float2* spec,
                                 cudaStream_t s) {
+  if (p.col_mode == 2 && col_cluster_ok(p, 8)) return col_pinv_cluster_impl<8>(p, spec, s);
+  if (p.col_mode >= 1 && col_cluster_ok(p, 4)) return col_pinv_cluster_impl<4>(p, spec, s);
   return p.fft_shape == 1 ? col_pinv_impl<128, 7>(p, 128, spec, s)
                           : col_pinv_impl<256, 3>(p, 256, spec, s);
 }

@@ -112,8 +112,9 @@ class FvmPlan:
     return u_out, v_out
 
   def autotune(self, u, v, steps: int = 20) -> int:
-    """Times each transform launch shape on (u, v) and keeps the fastest;
-    returns the chosen shape index.  Synchronises the stream."""
+    """Times each transform launch configuration on (u, v) and keeps the
+    fastest; returns its index (row block shape + 2 * column-pass scheme).
+    Synchronises the stream."""
     us, vs = torch.empty_like(u), torch.empty_like(v)
     chosen = ctypes.c_int(-1)
     a = self._fields(u, v, us, vs)

@@ -178,7 +178,7 @@ def test_initial_conditions_match_oracle(cuda_device):
   assert abs(speed - 2.0) <= 1e-5 * 2.0
 
 
-@pytest.mark.parametrize('shape', [(64, 64), (1024, 1024)])
+@pytest.mark.parametrize('shape', [(64, 64), (1024, 1024), (2048, 256)])
 def test_autotune_keeps_results_bitwise(cuda_device, shape):
   """The transform launch shapes compute identical bits; the autotuner only
   changes speed."""
@@ -192,7 +192,7 @@ def test_autotune_keeps_results_bitwise(cuda_device, shape):
   v = _to_gpu(v0, grid, cuda_device)
   before = cfd.funcutils.repeated(step, 3)(v)
   plan = step.plan(cuda_device)
-  assert plan.autotune(v[0].data, v[1].data, 2) in (0, 1)
+  assert plan.autotune(v[0].data, v[1].data, 2) in range(6)
   after = cfd.funcutils.repeated(step, 3)(v)
   for x, y in zip(before, after):
     assert torch.equal(x.data, y.data)
