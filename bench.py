@@ -217,6 +217,118 @@ def run_reference(args):
 # ---------------------------------------------------------------------------
 # GB300 arm.
 # ---------------------------------------------------------------------------
+def ensemble_draws(count: int, seed: int = 2024):
+  """Members of the ragged FVM ensemble: grid N uniform in {64..1024},
+  viscosity log-uniform in [1e-4, 1e-2], forcing wavenumber in {2, 4, 8}, max
+  initial speed uniform in [1, 4], initial-condition seed 1000 + i.  dt is
+  stable_time_step(vmax, 0.5, nu) where the reference accepts it, else the
+  diffusive limit h^2 / (4 nu) (the reference raises for those draws)."""
+  rng = np.random.default_rng(seed)
+  out = []
+  for i in range(count):
+    n = int(rng.choice([64, 128, 256, 512, 1024]))
+    nu = float(10 ** rng.uniform(-4, -2))
+    k = int(rng.choice([2, 4, 8]))
+    vmax = float(rng.uniform(1, 4))
+    h = 2 * np.pi / n
+    dt = min(CFL * h / vmax, h * h / (4 * nu))
+    out.append(dict(n=n, nu=nu, k=k, vmax=vmax, dt=dt, seed=1000 + i))
+  return out
+
+
+def run_ensemble(dev, args, flush):
+  """Ragged ensemble (batched launches per grid shape, one CUDA graph per
+  chunk) against the plain per-trajectory loop (one funcutils.repeated call per
+  trajectory, same GPU, same states).  Returns the JSON sub-object."""
+  import torch  # pylint: disable=import-outside-toplevel
+  import jax_cfd_gb300.base as cfd  # pylint: disable=import-outside-toplevel
+  from jax_cfd_gb300 import batching, plans  # pylint: disable=import-outside-toplevel
+  draws = ensemble_draws(args.ensemble_members)
+  steps = args.ensemble_steps
+  members, states = [], []
+  for d in draws:
+    grid = cfd.grids.Grid((d['n'], d['n']), domain=DOMAIN)
+    members.append(batching.kolmogorov_member((d['n'], d['n']), d['nu'], d['dt'], d['k']))
+    v0 = cfd.initial_conditions.filtered_velocity_field(d['seed'], grid, d['vmax'], 4,
+                                                        device=dev)
+    states.append((v0[0].data.clone(), v0[1].data.clone()))
+  stream = torch.cuda.current_stream(dev)
+  cells = sum(d['n'] ** 2 for d in draws)
+
+  ens = batching.FvmEnsemble(members, device=dev)
+  for i, (u, v) in enumerate(states):
+    ens.set_state(i, u, v)
+  ens.autotune(10)
+
+  def load_all():
+    for i, (u, v) in enumerate(states):
+      ens.set_state(i, u, v)
+
+  ens.step(steps, graph=True)  # capture + warm-up
+  ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+  ens_ms = []
+  for _ in range(2):
+    load_all()
+    flush.zero_()
+    ev[0].record(stream)
+    ens.step(steps, graph=True)
+    ev[1].record(stream)
+    torch.cuda.synchronize(dev)
+    ens_ms.append(ev[0].elapsed_time(ev[1]))
+  finite = sum(bool(torch.isfinite(ens.state(i)[0]).all()) for i in range(len(draws)))
+
+  # Plain loop: each trajectory through its own plan, one after another.
+  plain_plans = []
+  for m, (u, v) in zip(members, states):
+    kw = dict(m)
+    shape, step = kw.pop('shape'), kw.pop('step')
+    pl = plans.FvmPlan(shape, step, device=dev, **kw)
+    pl.autotune(u, v, 5)
+    plain_plans.append(pl)
+  outs = [(torch.empty_like(u), torch.empty_like(v)) for u, v in states]
+
+  def plain():
+    for pl, (u, v), (uo, vo) in zip(plain_plans, states, outs):
+      pl.step(u, v, steps, uo, vo)
+
+  plain()
+  torch.cuda.synchronize(dev)
+  plain_ms = []
+  for _ in range(2):
+    flush.zero_()
+    ev[2].record(stream)
+    plain()
+    ev[3].record(stream)
+    torch.cuda.synchronize(dev)
+    plain_ms.append(ev[2].elapsed_time(ev[3]))
+  def bits(t):
+    return t.view(torch.int32)
+  same = all(torch.equal(bits(ens.state(i)[0]), bits(outs[i][0])) and
+             torch.equal(bits(ens.state(i)[1]), bits(outs[i][1])) for i in range(len(draws)))
+  e_s, p_s = min(ens_ms) / 1000.0, min(plain_ms) / 1000.0
+  sizes = {}
+  for d in draws:
+    sizes[d['n']] = sizes.get(d['n'], 0) + 1
+  return {
+      'workload': f'ragged FVM ensemble: {len(draws)} trajectories x {steps} steps, N in '
+                  '{64..1024} uniform, nu log-uniform [1e-4, 1e-2], k in {2,4,8}, '
+                  'vmax in [1, 4], own stable dt',
+      'members_per_size': {str(k): v for k, v in sorted(sizes.items())},
+      'value': len(draws) * steps / e_s, 'unit': 'trajectory-steps/s',
+      'cell_steps_per_s': cells * steps / e_s,
+      'ms': e_s * 1000.0,
+      'plain_loop': {'value': len(draws) * steps / p_s, 'unit': 'trajectory-steps/s',
+                     'cell_steps_per_s': cells * steps / p_s, 'ms': p_s * 1000.0,
+                     'launches': len(draws) * (4 * steps + 1)},
+      'speedup_vs_plain': p_s / e_s,
+      'batches': ens.num_batches,
+      'graph_launches_per_chunk': 1,
+      'kernel_launches': ens.num_batches * (4 * steps + 1),
+      'bitwise_equal_to_plain': bool(same),
+      'finite_members': int(finite),
+  }
+
+
 def run_gb300(args):
   import torch  # pylint: disable=import-outside-toplevel
   import jax_cfd_gb300.base as cfd  # pylint: disable=import-outside-toplevel
@@ -353,6 +465,10 @@ def run_gb300(args):
         'finite': bool(torch.isfinite(torch.view_as_real(w)).all()),
     }
 
+  ensemble = None
+  if not args.skip_ensemble:
+    ensemble = run_ensemble(dev, args, flush)
+
   cpu = None
   if rank == 0 and not args.skip_cpu:
     cv, csecs, cthreads = _cpu_sample(args.cpu_steps, 1)
@@ -393,6 +509,7 @@ def run_gb300(args):
       'wall_s': wall,
       'finite': finite,
       'spectral': spectral,
+      'ensemble': ensemble,
   })
 
 
@@ -408,6 +525,9 @@ def main():
   ap.add_argument('--cpu-steps', type=int, default=5)
   ap.add_argument('--skip-cpu', action='store_true')
   ap.add_argument('--skip-spectral', action='store_true')
+  ap.add_argument('--skip-ensemble', action='store_true')
+  ap.add_argument('--ensemble-members', type=int, default=96)
+  ap.add_argument('--ensemble-steps', type=int, default=1000)
   args = ap.parse_args()
   if args.warmup < 3:
     ap.error('at least 3 warm-up steps are required')

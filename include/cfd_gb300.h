@@ -138,6 +138,56 @@ int cfd_fvm_projection_noalloc(void* stream, int nx, int ny, double hx,
                                double hy, const float* u, const float* v,
                                float* u_out, float* v_out);
 
+/* ---- Batched FVM trajectories ----
+ * Replaces the reference's one-trajectory-at-a-time use of
+ * semi_implicit_navier_stokes + funcutils.repeated (equations.py:120-151,
+ * funcutils.py:82-88) for many independent trajectories; the reference itself
+ * has no batched entry point (callers vmap or loop in Python).
+ *
+ * A batch holds `count` slots of ONE grid shape, step and convection scheme
+ * (taken from `shape`).  Each slot has its own viscosity, density, dt and
+ * forcing (set with cfd_fvm_batch_set_slot; forcing tables over one axis
+ * only), its own state (u, v) owned by the batch (cfd_fvm_batch_state returns
+ * the device pointers) and its own step count for the next chunk
+ * (cfd_fvm_batch_set_steps; 0 = idle).  cfd_fvm_batch_run advances every slot
+ * by min(its steps, chunk) steps in place with one launch per kernel kind per
+ * step for the whole batch; with use_graph != 0 the chunk is captured once per
+ * chunk length as a CUDA graph and replayed.  Slot parameters and steps may
+ * change between runs (they live in a device table uploaded on the run's
+ * stream).  A slot's result does not depend on the other slots. */
+typedef struct cfd_fvm_batch cfd_fvm_batch;
+int cfd_fvm_batch_create(const cfd_fvm_config* shape, int count, cfd_fvm_batch** batch);
+int cfd_fvm_batch_destroy(cfd_fvm_batch* batch);
+int cfd_fvm_batch_size(const cfd_fvm_batch* batch);
+long long cfd_fvm_batch_bytes(const cfd_fvm_batch* batch);
+int cfd_fvm_batch_state(cfd_fvm_batch* batch, int slot, float** u, float** v);
+/* Enqueues the forcing-table upload on `stream` (host tables may be reused
+ * once the call returns). */
+int cfd_fvm_batch_set_slot(cfd_fvm_batch* batch, void* stream, int slot,
+                           const cfd_fvm_config* cfg);
+int cfd_fvm_batch_set_steps(cfd_fvm_batch* batch, int slot, int steps);
+int cfd_fvm_batch_run(cfd_fvm_batch* batch, void* stream, int chunk, int use_graph);
+/* Times the transform launch configurations on a `steps`-step chunk of the
+ * current slots, restores their states and keeps the fastest (index as in
+ * cfd_fvm_plan_autotune).  Synchronises. */
+int cfd_fvm_batch_autotune(cfd_fvm_batch* batch, void* stream, int steps, int* chosen);
+
+/* A ragged ensemble: members of any grid shapes, grouped into one batch per
+ * (shape, step, convection).  cfd_fvm_ensemble_step advances every member by
+ * `steps`; the batches run on forked streams (overlapping on the device), and
+ * with use_graph != 0 the whole chunk is one CUDA graph launch. */
+typedef struct cfd_fvm_ensemble cfd_fvm_ensemble;
+int cfd_fvm_ensemble_create(const cfd_fvm_config* cfgs, int count,
+                            cfd_fvm_ensemble** ens);
+int cfd_fvm_ensemble_destroy(cfd_fvm_ensemble* ens);
+int cfd_fvm_ensemble_size(const cfd_fvm_ensemble* ens);
+int cfd_fvm_ensemble_batches(const cfd_fvm_ensemble* ens);
+int cfd_fvm_ensemble_state(cfd_fvm_ensemble* ens, int index, float** u,
+                           float** v);
+int cfd_fvm_ensemble_autotune(cfd_fvm_ensemble* ens, void* stream, int steps);
+int cfd_fvm_ensemble_step(cfd_fvm_ensemble* ens, void* stream, int steps,
+                          int use_graph);
+
 /* max over cells of sqrt(u^2 + v^2) written as one float to device memory. */
 int cfd_max_speed(void* stream, int n, const float* u, const float* v,
                   float* out);

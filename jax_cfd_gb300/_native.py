@@ -76,6 +76,26 @@ _SIGNATURES = {
     'cfd_fvm_curl_2d': (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp]),
     'cfd_fvm_projection_noalloc': (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                                    ctypes.c_double, _vp, _vp, _vp, _vp]),
+    'cfd_fvm_batch_create': (ctypes.c_int, [ctypes.POINTER(FvmConfig), ctypes.c_int,
+                                             ctypes.POINTER(_vp)]),
+    'cfd_fvm_batch_destroy': (ctypes.c_int, [_vp]),
+    'cfd_fvm_batch_size': (ctypes.c_int, [_vp]),
+    'cfd_fvm_batch_bytes': (ctypes.c_longlong, [_vp]),
+    'cfd_fvm_batch_state': (ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(_vp),
+                                            ctypes.POINTER(_vp)]),
+    'cfd_fvm_batch_set_slot': (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.POINTER(FvmConfig)]),
+    'cfd_fvm_batch_set_steps': (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int]),
+    'cfd_fvm_batch_run': (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_int]),
+    'cfd_fvm_batch_autotune': (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
+    'cfd_fvm_ensemble_create': (ctypes.c_int, [ctypes.POINTER(FvmConfig), ctypes.c_int,
+                                                ctypes.POINTER(_vp)]),
+    'cfd_fvm_ensemble_destroy': (ctypes.c_int, [_vp]),
+    'cfd_fvm_ensemble_size': (ctypes.c_int, [_vp]),
+    'cfd_fvm_ensemble_batches': (ctypes.c_int, [_vp]),
+    'cfd_fvm_ensemble_state': (ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(_vp),
+                                               ctypes.POINTER(_vp)]),
+    'cfd_fvm_ensemble_autotune': (ctypes.c_int, [_vp, _vp, ctypes.c_int]),
+    'cfd_fvm_ensemble_step': (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_int]),
     'cfd_max_speed': (ctypes.c_int, [_vp, ctypes.c_int, _vp, _vp, _vp]),
     'cfd_scale_to_max_speed': (ctypes.c_int, [_vp, ctypes.c_int, _vp, _vp, _vp, ctypes.c_double]),
     'cfd_spec_plan_create': (ctypes.c_int, [ctypes.POINTER(SpecConfig), ctypes.POINTER(_vp)]),

@@ -20,7 +20,9 @@ LIB = PKG / 'libcfd_gb300.so'
 INCLUDE = PKG.parent / 'include'
 
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
-NVCC_FLAGS = ['-O3', '-lineinfo', '-std=c++17', '-Xcompiler', '-fPIC',
+# -fmad=false: no implicit multiply-add contraction; kernels spell out each
+# fma they want, so results do not depend on how a body is inlined.
+NVCC_FLAGS = ['-O3', '-lineinfo', '-std=c++17', '-fmad=false', '-Xcompiler', '-fPIC',
               '--expt-relaxed-constexpr', '-I', str(INCLUDE)]
 
 

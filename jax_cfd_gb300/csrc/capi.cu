@@ -1,5 +1,6 @@
 // C ABI: plans own the precomputed tables and the device workspace of one
 // grid; entry points enqueue the kernels of kernels.h on the caller's stream.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -84,6 +85,34 @@ cudaError_t upload(T** dev, const T* host, size_t count) {
 
 cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
+// Captures `enqueue` (run on a private capture stream) into an executable graph.
+template <typename F>
+int capture_graph(F enqueue, cudaGraph_t* graph, cudaGraphExec_t* exec) {
+  cudaStream_t cap;
+  CFD_CHECK(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking), "cudaStreamCreate");
+  cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeRelaxed);
+  int rc = e == cudaSuccess ? enqueue(cap) : CFD_OK;
+  cudaGraph_t g = nullptr;
+  cudaError_t e2 = e == cudaSuccess ? cudaStreamEndCapture(cap, &g) : cudaSuccess;
+  cudaStreamDestroy(cap);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaStreamBeginCapture");
+  if (rc) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  if (e2 != cudaSuccess) return cuda_fail(e2, "cudaStreamEndCapture");
+  cudaGraphExec_t x = nullptr;
+  e = cudaGraphInstantiate(&x, g, 0);
+  if (e != cudaSuccess) {
+    cudaGraphDestroy(g);
+    return cuda_fail(e, "cudaGraphInstantiate");
+  }
+  *graph = g;
+  *exec = x;
+  return CFD_OK;
+}
+
+
 }  // namespace
 
 namespace cfd {
@@ -105,6 +134,46 @@ struct cfd_fvm_plan {
   float* fu = nullptr;
   float* fv = nullptr;
   long long bytes = 0;
+};
+
+// A batch of same-shape FVM trajectories ("slots"): one device table of
+// cfd::FvmMember entries read by the batched kernels, one slab of per-slot
+// buffers, and the grid tables shared by every slot.
+struct cfd_fvm_batch {
+  cfd::FvmParams shape;  // grid, convection and launch choices of the batch
+  double hx = 0, hy = 0;
+  int count = 0;
+  size_t n = 0;
+  float* slab = nullptr;   // per slot: u, v, au, av, bu, bv, spec (7 n floats)
+  float* force = nullptr;  // per slot: u-forcing over y (ny) then v-forcing over x (nx)
+  float* lamx = nullptr;
+  float* lamy = nullptr;
+  float2* twy = nullptr;
+  float2* twpx = nullptr;
+  float2* twpy = nullptr;
+  std::vector<cfd::FvmMember> host;
+  std::vector<int> want;   // requested steps per slot
+  cfd::FvmMember* dev = nullptr;
+  int uploaded_chunk = -1;  // chunk length the device table was clamped to
+  bool dirty = true;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int graph_chunk = -1;
+  long long bytes = 0;
+};
+
+// Several batches (one per grid shape) stepped together: a chunk forks one
+// stream per batch so the batches' kernels overlap, and can be captured as
+// one CUDA graph.
+struct cfd_fvm_ensemble {
+  std::vector<cfd_fvm_batch*> batches;
+  std::vector<std::pair<int, int>> where;  // member -> (batch, slot)
+  std::vector<cudaStream_t> streams;
+  std::vector<cudaEvent_t> joins;
+  cudaEvent_t fork = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int graph_steps = -1;
 };
 
 struct cfd_spec_plan {
@@ -140,9 +209,9 @@ int cfd_fvm_plan_destroy(cfd_fvm_plan* plan) {
   return CFD_OK;
 }
 
-int cfd_fvm_plan_create(const cfd_fvm_config* cfg, cfd_fvm_plan** out) {
-  if (!cfg || !out) return fail(CFD_ERR_INVALID_ARGUMENT, "null config or output pointer");
-  *out = nullptr;
+// Scalar step parameters of one configuration (no device tables); shared by
+// plans and batch slots.
+static int fvm_params_from_config(const cfd_fvm_config* cfg, cfd::FvmParams* out) {
   if (!valid_size(cfg->nx) || !valid_size(cfg->ny))
     return fail(CFD_ERR_UNSUPPORTED,
                 "grid shape must be powers of two in [4, 4096] (real-FFT pressure solve)");
@@ -154,9 +223,7 @@ int cfd_fvm_plan_create(const cfd_fvm_config* cfg, cfd_fvm_plan** out) {
     return fail(CFD_ERR_UNSUPPORTED, "unsupported forcing layout");
   if (cfg->const_forcing != CFD_FORCE_NONE && !cfg->force_u && !cfg->force_v)
     return fail(CFD_ERR_INVALID_ARGUMENT, "forcing layout given without tables");
-
-  cfd_fvm_plan* plan = new cfd_fvm_plan();
-  cfd::FvmParams& p = plan->p;
+  cfd::FvmParams& p = *out;
   std::memset(&p, 0, sizeof(p));
   const int nx = cfg->nx, ny = cfg->ny;
   p.nx = nx;
@@ -190,6 +257,19 @@ int cfd_fvm_plan_create(const cfd_fvm_config* cfg, cfd_fvm_plan** out) {
   // Narrow transform blocks keep large grids resident in one wave; the
   // autotuner can revise the choice on the device.
   p.fft_shape = (nx >= 1024 && ny >= 1024) ? 1 : 0;
+  return CFD_OK;
+}
+
+int cfd_fvm_plan_create(const cfd_fvm_config* cfg, cfd_fvm_plan** out) {
+  if (!cfg || !out) return fail(CFD_ERR_INVALID_ARGUMENT, "null config or output pointer");
+  *out = nullptr;
+  cfd::FvmParams params;
+  int rc = fvm_params_from_config(cfg, &params);
+  if (rc) return rc;
+  cfd_fvm_plan* plan = new cfd_fvm_plan();
+  cfd::FvmParams& p = plan->p;
+  p = params;
+  const int nx = cfg->nx, ny = cfg->ny;
 
   const size_t n = (size_t)nx * ny;
   cudaError_t e;
@@ -435,6 +515,400 @@ int cfd_fvm_plan_autotune(cfd_fvm_plan* plan, void* stream, const float* u,
   plan->p.col_mode = best >> 1;
   if (chosen) *chosen = best;
   return rc;
+}
+
+// ---- Same-shape batches -------------------------------------------------
+
+static void batch_drop_graph(cfd_fvm_batch* b) {
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  b->exec = nullptr;
+  b->graph = nullptr;
+  b->graph_chunk = -1;
+}
+
+int cfd_fvm_batch_destroy(cfd_fvm_batch* b) {
+  if (!b) return CFD_OK;
+  batch_drop_graph(b);
+  void* ptrs[] = {b->slab, b->force, b->lamx, b->lamy, b->twy, b->twpx, b->twpy, b->dev};
+  for (void* q : ptrs)
+    if (q) cudaFree(q);
+  delete b;
+  return CFD_OK;
+}
+
+int cfd_fvm_batch_create(const cfd_fvm_config* shape, int count, cfd_fvm_batch** out) {
+  if (!shape || !out || count < 1 || count > 65535)
+    return fail(CFD_ERR_INVALID_ARGUMENT, "cfd_fvm_batch_create: bad arguments");
+  *out = nullptr;
+  cfd::FvmParams p;
+  int rc = fvm_params_from_config(shape, &p);
+  if (rc) return rc;
+  if (!cfd::fvm_batch_shape_ok(p))
+    return fail(CFD_ERR_UNSUPPORTED, "batched steps need nx % 16 == 0 and ny % 64 == 0");
+  cfd_fvm_batch* b = new cfd_fvm_batch();
+  b->shape = p;
+  b->hx = shape->hx;
+  b->hy = shape->hy;
+  b->count = count;
+  const int nx = p.nx, ny = p.ny;
+  const size_t n = (size_t)nx * ny;
+  b->n = n;
+  cudaError_t e = cudaMalloc((void**)&b->slab, (size_t)count * 7 * n * sizeof(float));
+  if (e == cudaSuccess) e = cudaMemset(b->slab, 0, (size_t)count * 7 * n * sizeof(float));
+  if (e == cudaSuccess)
+    e = cudaMalloc((void**)&b->force, (size_t)count * (nx + ny) * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&b->dev, (size_t)count * sizeof(cfd::FvmMember));
+  std::vector<float> lamx = laplacian_eigenvalues(nx, shape->hx, nx);
+  std::vector<float> lamy = laplacian_eigenvalues(ny, shape->hy, ny / 2 + 1);
+  std::vector<float2> twy = twiddles(ny);
+  std::vector<float2> twpx = pass_twiddles(p.log2nx), twpy = pass_twiddles(p.log2ny - 1);
+  if (e == cudaSuccess) e = upload(&b->lamx, lamx.data(), lamx.size());
+  if (e == cudaSuccess) e = upload(&b->lamy, lamy.data(), lamy.size());
+  if (e == cudaSuccess) e = upload(&b->twy, twy.data(), twy.size());
+  if (e == cudaSuccess) e = upload(&b->twpx, twpx.data(), twpx.size());
+  if (e == cudaSuccess) e = upload(&b->twpy, twpy.data(), twpy.size());
+  if (e != cudaSuccess) {
+    cfd_fvm_batch_destroy(b);
+    return cuda_fail(e, "cfd_fvm_batch_create");
+  }
+  b->bytes = (long long)count * (7 * (long long)n + nx + ny) * 4 +
+             (long long)count * sizeof(cfd::FvmMember);
+  b->host.assign(count, cfd::FvmMember());
+  b->want.assign(count, 0);
+  for (int i = 0; i < count; ++i) {
+    cfd::FvmMember& m = b->host[i];
+    std::memset(&m, 0, sizeof(m));
+    m.p = p;
+    m.p.lamx = b->lamx;
+    m.p.lamy = b->lamy;
+    m.p.tw_y = b->twy;
+    m.p.twp_x = b->twpx;
+    m.p.twp_y = b->twpy;
+    float* base = b->slab + (size_t)i * 7 * n;
+    for (int set = 0; set < 3; ++set) {
+      m.f[set][0] = base + (2 * set) * n;
+      m.f[set][1] = base + (2 * set + 1) * n;
+    }
+    m.spec = reinterpret_cast<float2*>(base + 6 * n);
+    m.steps = 0;
+  }
+  *out = b;
+  return CFD_OK;
+}
+
+int cfd_fvm_batch_size(const cfd_fvm_batch* b) { return b ? b->count : 0; }
+
+long long cfd_fvm_batch_bytes(const cfd_fvm_batch* b) { return b ? b->bytes : 0; }
+
+int cfd_fvm_batch_state(cfd_fvm_batch* b, int slot, float** u, float** v) {
+  if (!b || !u || !v || slot < 0 || slot >= b->count)
+    return fail(CFD_ERR_INVALID_ARGUMENT, "cfd_fvm_batch_state: bad arguments");
+  *u = b->host[slot].f[0][0];
+  *v = b->host[slot].f[0][1];
+  return CFD_OK;
+}
+
+int cfd_fvm_batch_set_slot(cfd_fvm_batch* b, void* stream, int slot, const cfd_fvm_config* cfg) {
+  if (!b || !cfg || slot < 0 || slot >= b->count)
+    return fail(CFD_ERR_INVALID_ARGUMENT, "cfd_fvm_batch_set_slot: bad arguments");
+  if (cfg->nx != b->shape.nx || cfg->ny != b->shape.ny || cfg->hx != b->hx ||
+      cfg->hy != b->hy || cfg->convect != b->shape.convect)
+    return fail(CFD_ERR_INVALID_ARGUMENT,
+                "cfd_fvm_batch_set_slot: grid, step and convection must match the batch");
+  if (cfg->const_forcing == CFD_FORCE_FULL)
+    return fail(CFD_ERR_UNSUPPORTED, "batched steps take forcing tables over one axis only");
+  cfd::FvmParams p;
+  int rc = fvm_params_from_config(cfg, &p);
+  if (rc) return rc;
+  cfd::FvmMember& m = b->host[slot];
+  const int nx = b->shape.nx, ny = b->shape.ny;
+  float* fu = b->force + (size_t)slot * (nx + ny);
+  float* fv = fu + ny;
+  cudaStream_t s = as_stream(stream);
+  if (cfg->const_forcing == CFD_FORCE_U_OF_Y && cfg->force_u)
+    CFD_CHECK(cudaMemcpyAsync(fu, cfg->force_u, ny * sizeof(float), cudaMemcpyHostToDevice, s),
+              "cfd_fvm_batch_set_slot: forcing");
+  if (cfg->const_forcing == CFD_FORCE_V_OF_X && cfg->force_v)
+    CFD_CHECK(cudaMemcpyAsync(fv, cfg->force_v, nx * sizeof(float), cudaMemcpyHostToDevice, s),
+              "cfd_fvm_batch_set_slot: forcing");
+  p.lamx = b->lamx;
+  p.lamy = b->lamy;
+  p.tw_y = b->twy;
+  p.twp_x = b->twpx;
+  p.twp_y = b->twpy;
+  p.fu_y = (cfg->const_forcing == CFD_FORCE_U_OF_Y && cfg->force_u) ? fu : nullptr;
+  p.fv_x = (cfg->const_forcing == CFD_FORCE_V_OF_X && cfg->force_v) ? fv : nullptr;
+  p.fft_shape = b->shape.fft_shape;
+  p.col_mode = b->shape.col_mode;
+  m.p = p;
+  b->dirty = true;
+  return CFD_OK;
+}
+
+int cfd_fvm_batch_set_steps(cfd_fvm_batch* b, int slot, int steps) {
+  if (!b || slot < 0 || slot >= b->count || steps < 0)
+    return fail(CFD_ERR_INVALID_ARGUMENT, "cfd_fvm_batch_set_steps: bad arguments");
+  if (b->want[slot] != steps) b->dirty = true;
+  b->want[slot] = steps;
+  return CFD_OK;
+}
+
+// Uploads the slot table with every slot's steps clamped to `chunk`.
+static int batch_upload(cfd_fvm_batch* b, cudaStream_t s, int chunk) {
+  if (!b->dirty && b->uploaded_chunk == chunk) return CFD_OK;
+  for (int i = 0; i < b->count; ++i) {
+    b->host[i].steps = std::min(b->want[i], chunk);
+    b->host[i].p.fft_shape = b->shape.fft_shape;
+    b->host[i].p.col_mode = b->shape.col_mode;
+  }
+  CFD_CHECK(cudaMemcpyAsync(b->dev, b->host.data(), b->host.size() * sizeof(cfd::FvmMember),
+                            cudaMemcpyHostToDevice, s),
+            "cfd_fvm_batch: slot table");
+  b->dirty = false;
+  b->uploaded_chunk = chunk;
+  return CFD_OK;
+}
+
+static int batch_enqueue(cfd_fvm_batch* b, cudaStream_t s, int chunk) {
+  for (int k = 0; k < chunk; ++k)
+    CFD_CHECK(cfd::launch_fvm_batch_step(b->shape, b->dev, b->count, k, s), "batch step");
+  CFD_CHECK(cfd::launch_fvm_batch_project_out(b->shape, b->dev, b->count, s), "batch project_out");
+  return CFD_OK;
+}
+
+int cfd_fvm_batch_run(cfd_fvm_batch* b, void* stream, int chunk, int use_graph) {
+  if (!b || chunk < 0) return fail(CFD_ERR_INVALID_ARGUMENT, "cfd_fvm_batch_run: bad arguments");
+  if (chunk == 0) return CFD_OK;
+  cudaStream_t s = as_stream(stream);
+  int rc = batch_upload(b, s, chunk);
+  if (rc) return rc;
+  if (!use_graph) return batch_enqueue(b, s, chunk);
+  if (!b->exec || b->graph_chunk != chunk) {
+    batch_drop_graph(b);
+    rc = capture_graph([&](cudaStream_t c) { return batch_enqueue(b, c, chunk); }, &b->graph,
+                       &b->exec);
+    if (rc) return rc;
+    b->graph_chunk = chunk;
+  }
+  CFD_CHECK(cudaGraphLaunch(b->exec, s), "cudaGraphLaunch");
+  return CFD_OK;
+}
+
+// Times every transform launch configuration on a `steps`-step chunk of all
+// slots (with their current parameters and steps = `steps`), restores the
+// slot states afterwards and keeps the fastest configuration.  Synchronises.
+int cfd_fvm_batch_autotune(cfd_fvm_batch* b, void* stream, int steps, int* chosen) {
+  if (!b || steps < 1) return fail(CFD_ERR_INVALID_ARGUMENT, "cfd_fvm_batch_autotune: bad arguments");
+  cudaStream_t s = as_stream(stream);
+  const size_t n = b->n;
+  float* backup = nullptr;
+  CFD_CHECK(cudaMalloc((void**)&backup, (size_t)b->count * 2 * n * sizeof(float)),
+            "cfd_fvm_batch_autotune");
+  std::vector<int> want = b->want;
+  auto save = [&](bool restore) -> cudaError_t {
+    for (int i = 0; i < b->count; ++i) {
+      float* st = b->host[i].f[0][0];  // u then v, contiguous in the slab
+      float* bk = backup + (size_t)i * 2 * n;
+      cudaError_t e = restore ? cudaMemcpyAsync(st, bk, 2 * n * sizeof(float),
+                                                cudaMemcpyDeviceToDevice, s)
+                              : cudaMemcpyAsync(bk, st, 2 * n * sizeof(float),
+                                                cudaMemcpyDeviceToDevice, s);
+      if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+  };
+  cudaEvent_t e0, e1;
+  cudaError_t e = save(false);
+  if (e == cudaSuccess) e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  if (e != cudaSuccess) {
+    cudaFree(backup);
+    return cuda_fail(e, "cfd_fvm_batch_autotune");
+  }
+  for (int i = 0; i < b->count; ++i) b->want[i] = steps;
+  b->dirty = true;
+  int rc = CFD_OK, best = -1;
+  float best_ms = 0.f;
+  for (int cand = 0; cand < 6 && rc == CFD_OK; ++cand) {
+    b->shape.fft_shape = cand & 1;
+    b->shape.col_mode = cand >> 1;
+    if (b->shape.col_mode > 0 && !cfd::col_cluster_ok(b->shape, b->shape.col_mode == 1 ? 4 : 8))
+      continue;
+    b->dirty = true;
+    rc = cfd_fvm_batch_run(b, stream, 1, 0);  // warm-up (and per-kernel smem setup)
+    if (rc) break;
+    e = cudaEventRecord(e0, s);
+    if (e == cudaSuccess) rc = cfd_fvm_batch_run(b, stream, steps, 0);
+    if (rc) break;
+    if (e == cudaSuccess) e = cudaEventRecord(e1, s);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    float ms = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+    if (e == cudaSuccess) e = save(true);
+    if (e != cudaSuccess) {
+      rc = cuda_fail(e, "cfd_fvm_batch_autotune");
+      break;
+    }
+    if (best < 0 || ms < best_ms) {
+      best_ms = ms;
+      best = cand;
+    }
+  }
+  if (rc == CFD_OK) {
+    e = save(true);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) rc = cuda_fail(e, "cfd_fvm_batch_autotune");
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(backup);
+  if (best < 0) best = 0;
+  b->shape.fft_shape = best & 1;
+  b->shape.col_mode = best >> 1;
+  b->want = want;
+  b->dirty = true;
+  batch_drop_graph(b);
+  if (chosen) *chosen = best;
+  return rc;
+}
+
+// ---- Ensembles of batches ------------------------------------------------
+
+static void ensemble_drop_graph(cfd_fvm_ensemble* ens) {
+  if (ens->exec) cudaGraphExecDestroy(ens->exec);
+  if (ens->graph) cudaGraphDestroy(ens->graph);
+  ens->exec = nullptr;
+  ens->graph = nullptr;
+  ens->graph_steps = -1;
+}
+
+int cfd_fvm_ensemble_destroy(cfd_fvm_ensemble* ens) {
+  if (!ens) return CFD_OK;
+  ensemble_drop_graph(ens);
+  for (auto e : ens->joins) if (e) cudaEventDestroy(e);
+  if (ens->fork) cudaEventDestroy(ens->fork);
+  for (auto st : ens->streams) if (st) cudaStreamDestroy(st);
+  for (auto b : ens->batches) cfd_fvm_batch_destroy(b);
+  delete ens;
+  return CFD_OK;
+}
+
+int cfd_fvm_ensemble_create(const cfd_fvm_config* cfgs, int count, cfd_fvm_ensemble** out) {
+  if (!cfgs || !out || count < 1)
+    return fail(CFD_ERR_INVALID_ARGUMENT, "cfd_fvm_ensemble_create: bad arguments");
+  *out = nullptr;
+  // Members with the same grid, step and convection scheme share a batch.
+  std::vector<int> bucket(count, -1);
+  std::vector<int> reps, sizes;
+  for (int i = 0; i < count; ++i) {
+    const cfd_fvm_config& c = cfgs[i];
+    for (size_t r = 0; r < reps.size(); ++r) {
+      const cfd_fvm_config& d = cfgs[reps[r]];
+      if (c.nx == d.nx && c.ny == d.ny && c.hx == d.hx && c.hy == d.hy &&
+          c.convect == d.convect) {
+        bucket[i] = (int)r;
+        break;
+      }
+    }
+    if (bucket[i] < 0) {
+      bucket[i] = (int)reps.size();
+      reps.push_back(i);
+      sizes.push_back(0);
+    }
+    ++sizes[bucket[i]];
+  }
+  cfd_fvm_ensemble* ens = new cfd_fvm_ensemble();
+  ens->where.assign(count, {0, 0});
+  int rc = CFD_OK;
+  for (size_t r = 0; r < reps.size() && rc == CFD_OK; ++r) {
+    cfd_fvm_batch* b = nullptr;
+    rc = cfd_fvm_batch_create(&cfgs[reps[r]], sizes[r], &b);
+    if (rc == CFD_OK) ens->batches.push_back(b);
+  }
+  std::vector<int> fill(reps.size(), 0);
+  for (int i = 0; i < count && rc == CFD_OK; ++i) {
+    const int r = bucket[i];
+    const int slot = fill[r]++;
+    ens->where[i] = {r, slot};
+    rc = cfd_fvm_batch_set_slot(ens->batches[r], nullptr, slot, &cfgs[i]);
+  }
+  cudaError_t e = cudaSuccess;
+  if (rc == CFD_OK) e = cudaStreamSynchronize(nullptr);
+  if (rc == CFD_OK && e == cudaSuccess) e = cudaEventCreateWithFlags(&ens->fork, cudaEventDisableTiming);
+  for (size_t r = 0; r < ens->batches.size() && rc == CFD_OK && e == cudaSuccess; ++r) {
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev = nullptr;
+    e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+    ens->streams.push_back(st);
+    ens->joins.push_back(ev);
+  }
+  if (rc == CFD_OK && e != cudaSuccess) rc = cuda_fail(e, "cfd_fvm_ensemble_create");
+  if (rc) {
+    cfd_fvm_ensemble_destroy(ens);
+    return rc;
+  }
+  *out = ens;
+  return CFD_OK;
+}
+
+int cfd_fvm_ensemble_size(const cfd_fvm_ensemble* ens) {
+  return ens ? (int)ens->where.size() : 0;
+}
+
+int cfd_fvm_ensemble_batches(const cfd_fvm_ensemble* ens) {
+  return ens ? (int)ens->batches.size() : 0;
+}
+
+int cfd_fvm_ensemble_state(cfd_fvm_ensemble* ens, int index, float** u, float** v) {
+  if (!ens || index < 0 || index >= (int)ens->where.size())
+    return fail(CFD_ERR_INVALID_ARGUMENT, "cfd_fvm_ensemble_state: bad arguments");
+  const auto w = ens->where[index];
+  return cfd_fvm_batch_state(ens->batches[w.first], w.second, u, v);
+}
+
+int cfd_fvm_ensemble_autotune(cfd_fvm_ensemble* ens, void* stream, int steps) {
+  if (!ens) return fail(CFD_ERR_INVALID_ARGUMENT, "cfd_fvm_ensemble_autotune: null");
+  for (auto* b : ens->batches) {
+    int rc = cfd_fvm_batch_autotune(b, stream, steps, nullptr);
+    if (rc) return rc;
+  }
+  ensemble_drop_graph(ens);
+  return CFD_OK;
+}
+
+static int ensemble_enqueue(cfd_fvm_ensemble* ens, cudaStream_t s, int steps) {
+  CFD_CHECK(cudaEventRecord(ens->fork, s), "cudaEventRecord");
+  for (size_t r = 0; r < ens->batches.size(); ++r) {
+    CFD_CHECK(cudaStreamWaitEvent(ens->streams[r], ens->fork, 0), "cudaStreamWaitEvent");
+    int rc = batch_enqueue(ens->batches[r], ens->streams[r], steps);
+    if (rc) return rc;
+    CFD_CHECK(cudaEventRecord(ens->joins[r], ens->streams[r]), "cudaEventRecord");
+    CFD_CHECK(cudaStreamWaitEvent(s, ens->joins[r], 0), "cudaStreamWaitEvent");
+  }
+  return CFD_OK;
+}
+
+int cfd_fvm_ensemble_step(cfd_fvm_ensemble* ens, void* stream, int steps, int use_graph) {
+  if (!ens || steps < 0) return fail(CFD_ERR_INVALID_ARGUMENT, "cfd_fvm_ensemble_step: bad arguments");
+  if (steps == 0) return CFD_OK;
+  cudaStream_t s = as_stream(stream);
+  for (auto* b : ens->batches) {
+    for (int i = 0; i < b->count; ++i) cfd_fvm_batch_set_steps(b, i, steps);
+    int rc = batch_upload(b, s, steps);
+    if (rc) return rc;
+  }
+  if (!use_graph) return ensemble_enqueue(ens, s, steps);
+  if (!ens->exec || ens->graph_steps != steps) {
+    ensemble_drop_graph(ens);
+    int rc = capture_graph([&](cudaStream_t c) { return ensemble_enqueue(ens, c, steps); },
+                           &ens->graph, &ens->exec);
+    if (rc) return rc;
+    ens->graph_steps = steps;
+  }
+  CFD_CHECK(cudaGraphLaunch(ens->exec, s), "cudaGraphLaunch");
+  return CFD_OK;
 }
 
 int cfd_fvm_explicit_terms(cfd_fvm_plan* plan, void* stream, const float* u,

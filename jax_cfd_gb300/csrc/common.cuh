@@ -13,8 +13,13 @@ CFD_D float2 c_add(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y
 CFD_D float2 c_sub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
 CFD_D float2 c_conj(float2 a) { return make_float2(a.x, -a.y); }
 CFD_D float2 c_scale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+// The library is compiled with -fmad=false, so every multiply-add that should
+// fuse is written as an explicit fma: the rounding of each expression is then
+// fixed by the source, not by the inlining context it is compiled in (the
+// batched and single-trajectory kernels share their bodies and must agree bit
+// for bit).
 CFD_D float2 c_mul(float2 a, float2 b) {
-  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+  return make_float2(__fmaf_rn(a.x, b.x, -(a.y * b.y)), __fmaf_rn(a.x, b.y, a.y * b.x));
 }
 // Multiply by SIGN * i (SIGN = -1 gives -i, the forward-transform rotation).
 template <int SIGN>

@@ -24,7 +24,7 @@ namespace cfd {
 template <int SIGN>
 CFD_D float2 twmul(float2 a, float c, float s) {
   const float ss = SIGN < 0 ? -s : s;
-  return make_float2(a.x * c - a.y * ss, a.x * ss + a.y * c);
+  return make_float2(__fmaf_rn(a.x, c, -(a.y * ss)), __fmaf_rn(a.x, ss, a.y * c));
 }
 
 constexpr float kC1_16 = 0.92387953251128675613f;  // cos(pi/8)
@@ -144,33 +144,38 @@ CFD_HD int fft_pass_table_size(int log2L) {
   return fft_pass_table_offset(log2L, fft_num_passes(log2L));
 }
 
-// Multiplies v[r] by w^(r k) (conjugated for the inverse), r = 1..R-1.  Only
-// w^k and, for R >= 8, w^(4k) are read from the pass table; the other powers
-// are products of at most three table values (a few ulp), which replaces R-1
-// dependent table loads per butterfly with complex multiplications.
+// Multiplies v[r] by w^(r k) (conjugated for the inverse), r = 1..R-1.  The
+// powers r = 1, 2, 3 and 4, 8, 12 come straight from the pass table (each
+// rounded once from double); the others are one product of two table values,
+// r = 4b + a -> w^(4b k) * w^(a k), so no twiddle is more than one complex
+// rounding away from the correctly rounded value.
+template <int R, int SIGN>
+CFD_D float2 load_tw(const float2* __restrict__ twp, int Ns, int r, int k) {
+  float2 w = __ldg(twp + (r - 1) * Ns + k);
+  if (SIGN > 0) w.y = -w.y;
+  return w;
+}
+
 template <int R, int SIGN>
 CFD_D void apply_twiddles(float2* v, const float2* __restrict__ twp, int Ns,
                           int k) {
-  float2 w1 = __ldg(twp + k);
-  if (SIGN > 0) w1.y = -w1.y;
+  const float2 w1 = load_tw<R, SIGN>(twp, Ns, 1, k);
   if (R == 2) {
     v[1] = c_mul(v[1], w1);
     return;
   }
-  const float2 w2 = c_mul(w1, w1);
-  const float2 w3 = c_mul(w2, w1);
+  const float2 w2 = load_tw<R, SIGN>(twp, Ns, 2, k);
+  const float2 w3 = load_tw<R, SIGN>(twp, Ns, 3, k);
   v[1] = c_mul(v[1], w1);
   v[2] = c_mul(v[2], w2);
   v[3] = c_mul(v[3], w3);
   if (R == 4) return;
-  float2 w4 = __ldg(twp + 3 * Ns + k);
-  if (SIGN > 0) w4.y = -w4.y;
   float2 wb[4];
   wb[0] = make_float2(1.f, 0.f);
-  wb[1] = w4;
+  wb[1] = load_tw<R, SIGN>(twp, Ns, 4, k);
   if (R == 16) {
-    wb[2] = c_mul(w4, w4);
-    wb[3] = c_mul(wb[2], w4);
+    wb[2] = load_tw<R, SIGN>(twp, Ns, 8, k);
+    wb[3] = load_tw<R, SIGN>(twp, Ns, 12, k);
   }
   const float2 wa[4] = {make_float2(1.f, 0.f), w1, w2, w3};
 #pragma unroll

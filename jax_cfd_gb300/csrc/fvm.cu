@@ -242,17 +242,16 @@ CFD_D float2 tvd_flux2(float2 cm, float2 c0, float2 c1, float2 c2, float2 U,
 // then updates 4 cells of one column.
 constexpr int kBoxW = kTJ + 8;  // 72 columns: j0-4 .. j0+67
 template <bool PROJECT, bool OUT_K0, int CONVECT>
-__global__ void __launch_bounds__(kStencilThreads)
-    fvm_explicit_tiled_kernel(FvmParams p, const float* __restrict__ ua,
-                              const float* __restrict__ va,
-                              const float* __restrict__ q,
-                              float* __restrict__ uo, float* __restrict__ vo) {
+CFD_D void explicit_tile(const FvmParams& p, int bx, int by,
+                         const float* __restrict__ ua, const float* __restrict__ va,
+                         const float* __restrict__ q, float* __restrict__ uo,
+                         float* __restrict__ vo) {
   __shared__ __align__(16) float2 sw[kTI + 4][kBoxW];  // (u, v)
   __shared__ __align__(16) float sq[PROJECT ? kTI + 5 : 1][PROJECT ? kBoxW : 4];
   __shared__ float2 fxg[kTI + 1][kTJ];  // x-normal faces: (F, G)
   __shared__ float2 fyg[kTI][kTJ + 1];  // y-normal faces: (F, G)
 
-  const int i0 = blockIdx.y * kTI, j0 = blockIdx.x * kTJ;
+  const int i0 = by * kTI, j0 = bx * kTJ;
   const int mx = p.nx - 1, my = p.ny - 1;
   const int tid = threadIdx.x;
   const size_t ny = (size_t)p.ny;
@@ -393,19 +392,27 @@ __global__ void __launch_bounds__(kStencilThreads)
   }
 }
 
+template <bool PROJECT, bool OUT_K0, int CONVECT>
+__global__ void __launch_bounds__(kStencilThreads)
+    fvm_explicit_tiled_kernel(FvmParams p, const float* __restrict__ ua,
+                              const float* __restrict__ va,
+                              const float* __restrict__ q,
+                              float* __restrict__ uo, float* __restrict__ vo) {
+  explicit_tile<PROJECT, OUT_K0, CONVECT>(p, blockIdx.x, blockIdx.y, ua, va, q, uo, vo);
+}
+
 // Backward-difference divergence of (u*, v*) (finite_differences.py:95-143)
 // followed by the packed real FFT of each row along y.  Shared memory holds
 // `rows` padded sequences of L = ny/2 complex values (pidx layout).
 // MAXT/MINB: launch bounds of the block shape the launcher picked (wide
 // 256-thread blocks, or narrow blocks capped at 72 registers so that a whole
 // 2048^2 grid is resident in one wave).
-template <int MAXT, int MINB>
-__global__ void __launch_bounds__(MAXT, MINB)
-    fvm_div_rfft_kernel(FvmParams p, int rows, const float* __restrict__ us,
-                        const float* __restrict__ vs, float2* __restrict__ spec) {
+CFD_D void div_rfft_rows(const FvmParams& p, int blk, int rows,
+                         const float* __restrict__ us, const float* __restrict__ vs,
+                         float2* __restrict__ spec) {
   extern __shared__ float2 sbuf[];
   const int L = p.ny >> 1, log2L = p.log2ny - 1, PL = padded_len(L);
-  const int i0 = blockIdx.x * rows;
+  const int i0 = blk * rows;
   const int mx = p.nx - 1, my = p.ny - 1;
   const size_t ny = (size_t)p.ny;
   const int log2g = p.log2ny - 2;  // float4 groups per row
@@ -453,6 +460,13 @@ __global__ void __launch_bounds__(MAXT, MINB)
   }
 }
 
+template <int MAXT, int MINB>
+__global__ void __launch_bounds__(MAXT, MINB)
+    fvm_div_rfft_kernel(FvmParams p, int rows, const float* __restrict__ us,
+                        const float* __restrict__ vs, float2* __restrict__ spec) {
+  div_rfft_rows(p, blockIdx.x, rows, us, vs, spec);
+}
+
 // Pseudoinverse of the periodic Laplacian in the rfft basis
 // (fast_diagonalization.py:199-266): 1/lambda where |lambda| > cutoff, else 0,
 // with irfftn's 1/(nx*ny) folded in (a power of two, so exact).
@@ -461,13 +475,11 @@ CFD_D float pinv_diag(const FvmParams& p, int kx, int ky) {
   return fabsf(lam) > p.cutoff ? p.pinv_scale / lam : 0.f;
 }
 
-template <int MAXT, int MINB>
-__global__ void __launch_bounds__(MAXT, MINB)
-    fvm_col_pinv_kernel(FvmParams p, int W, int log2W, int bstride,
-                        float2* __restrict__ spec) {
+CFD_D void col_pinv_cols(const FvmParams& p, int blk, int W, int log2W, int bstride,
+                          float2* __restrict__ spec) {
   extern __shared__ float2 sbuf[];
   const int L = p.ny >> 1, N = p.nx;
-  const int c0 = blockIdx.x * W;
+  const int c0 = blk * W;
   const int tid = threadIdx.x;
 #pragma unroll 4
   for (int idx = tid; idx < W * N; idx += blockDim.x) {
@@ -505,6 +517,13 @@ __global__ void __launch_bounds__(MAXT, MINB)
   }
 }
 
+template <int MAXT, int MINB>
+__global__ void __launch_bounds__(MAXT, MINB)
+    fvm_col_pinv_kernel(FvmParams p, int W, int log2W, int bstride,
+                        float2* __restrict__ spec) {
+  col_pinv_cols(p, blockIdx.x, W, log2W, bstride, spec);
+}
+
 // The column pass with one column per block and CL adjacent columns per
 // thread-block cluster.  Global memory is read and written in CL-column row
 // segments (32 or 64 bytes: whole sectors) through distributed shared memory:
@@ -512,8 +531,7 @@ __global__ void __launch_bounds__(MAXT, MINB)
 // CL columns between global memory and the owning blocks' shared memory, and
 // each block transforms its own column.
 template <int CL>
-__global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(128, 7)
-    fvm_col_pinv_cluster_kernel(FvmParams p, float2* __restrict__ spec) {
+CFD_D void col_pinv_cluster_cols(const FvmParams& p, float2* __restrict__ spec) {
   extern __shared__ float2 sbuf[];
   cg::cluster_group cluster = cg::this_cluster();
   const int rank = (int)cluster.block_rank();
@@ -525,6 +543,9 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(128, 7)
   float2* dsm[CL];
 #pragma unroll
   for (int r = 0; r < CL; ++r) dsm[r] = cluster.map_shared_rank(sbuf, r);
+  // Every block of the cluster must be running before any block touches a
+  // peer's shared memory.
+  cluster.sync();
 #pragma unroll 2
   for (int row = r0 + tid; row < r0 + rows_per; row += blockDim.x) {
     const float4* src = reinterpret_cast<const float4*>(spec + (size_t)row * L + c0);
@@ -569,13 +590,17 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(128, 7)
   cluster.sync();
 }
 
+template <int CL>
+__global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(128, 7)
+    fvm_col_pinv_cluster_kernel(FvmParams p, float2* __restrict__ spec) {
+  col_pinv_cluster_cols<CL>(p, spec);
+}
+
 // Inverse packed real FFT of each row, in place: q^ rows -> q rows (floats).
-template <int MAXT, int MINB>
-__global__ void __launch_bounds__(MAXT, MINB)
-    fvm_irfft_kernel(FvmParams p, int rows, float2* spec) {
+CFD_D void irfft_rows(const FvmParams& p, int blk, int rows, float2* spec) {
   extern __shared__ float2 sbuf[];
   const int L = p.ny >> 1, log2L = p.log2ny - 1, PL = padded_len(L);
-  const int i0 = blockIdx.x * rows;
+  const int i0 = blk * rows;
   const int half = L >> 1, log2h = log2L - 1;
   for (int idx = threadIdx.x; idx < (rows << log2h); idx += blockDim.x) {
     const int r = idx >> log2h, k = idx & (half - 1);
@@ -606,16 +631,21 @@ __global__ void __launch_bounds__(MAXT, MINB)
   }
 }
 
+template <int MAXT, int MINB>
+__global__ void __launch_bounds__(MAXT, MINB)
+    fvm_irfft_kernel(FvmParams p, int rows, float2* spec) {
+  irfft_rows(p, blockIdx.x, rows, spec);
+}
+
 // u = u* - (q[i+1] - q[i]) / hx ; v = v* - (q[j+1] - q[j]) / hy.
-__global__ void fvm_project_out_kernel(FvmParams p, const float* __restrict__ us,
-                                       const float* __restrict__ vs,
-                                       const float* __restrict__ q,
-                                       float* __restrict__ uo,
-                                       float* __restrict__ vo) {
+CFD_D void project_out_cells(const FvmParams& p, int blk, int nblk,
+                              const float* __restrict__ us, const float* __restrict__ vs,
+                              const float* __restrict__ q, float* __restrict__ uo,
+                              float* __restrict__ vo) {
   const size_t n = (size_t)p.nx * p.ny;
   const int mx = p.nx - 1, my = p.ny - 1;
-  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < n;
-       idx += (size_t)gridDim.x * blockDim.x) {
+  for (size_t idx = blk * (size_t)blockDim.x + threadIdx.x; idx < n;
+       idx += (size_t)nblk * blockDim.x) {
     const int i = (int)(idx >> p.log2ny), j = (int)(idx & my);
     const float q0 = __ldg(q + idx);
     const float qx = __ldg(q + (size_t)((i + 1) & mx) * p.ny + j);
@@ -623,6 +653,14 @@ __global__ void fvm_project_out_kernel(FvmParams p, const float* __restrict__ us
     uo[idx] = __ldg(us + idx) - (qx - q0) * p.inv_hx;
     vo[idx] = __ldg(vs + idx) - (qy - q0) * p.inv_hy;
   }
+}
+
+__global__ void fvm_project_out_kernel(FvmParams p, const float* __restrict__ us,
+                                       const float* __restrict__ vs,
+                                       const float* __restrict__ q,
+                                       float* __restrict__ uo,
+                                       float* __restrict__ vo) {
+  project_out_cells(p, blockIdx.x, gridDim.x, us, vs, q, uo, vo);
 }
 
 __global__ void divergence_kernel(FvmParams p, const float* __restrict__ u,
@@ -669,6 +707,73 @@ __global__ void max_speed_kernel(int n, const float* __restrict__ u,
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
   if ((threadIdx.x & 31) == 0) atomicMax(out, __float_as_uint(m));
+}
+
+// ---- Batched variants: the member index is the last grid axis ----
+// Buffer sets of step k: input 0 (k = 0) / 1 (k odd) / 2 (k even > 0),
+// output 1 (k even) / 2 (k odd).
+CFD_D int batch_src(int k) { return k == 0 ? 0 : ((k & 1) ? 1 : 2); }
+CFD_D int batch_dst(int k) { return (k & 1) ? 2 : 1; }
+
+template <bool PROJECT, int CONVECT>
+__global__ void __launch_bounds__(kStencilThreads)
+    fvm_batch_explicit_kernel(const FvmMember* __restrict__ mem, int k) {
+  const FvmMember& m = mem[blockIdx.z];
+  if (k >= m.steps) return;
+  const FvmParams p = m.p;
+  const int src = batch_src(k), dst = batch_dst(k);
+  explicit_tile<PROJECT, false, CONVECT>(p, blockIdx.x, blockIdx.y, m.f[src][0], m.f[src][1],
+                                         reinterpret_cast<const float*>(m.spec),
+                                         m.f[dst][0], m.f[dst][1]);
+}
+
+template <int MAXT, int MINB>
+__global__ void __launch_bounds__(MAXT, MINB)
+    fvm_batch_div_rfft_kernel(const FvmMember* __restrict__ mem, int k, int rows) {
+  const FvmMember& m = mem[blockIdx.y];
+  if (k >= m.steps) return;
+  const FvmParams p = m.p;
+  const int dst = batch_dst(k);
+  div_rfft_rows(p, blockIdx.x, rows, m.f[dst][0], m.f[dst][1], m.spec);
+}
+
+template <int MAXT, int MINB>
+__global__ void __launch_bounds__(MAXT, MINB)
+    fvm_batch_col_pinv_kernel(const FvmMember* __restrict__ mem, int k, int W, int log2W,
+                              int bstride) {
+  const FvmMember& m = mem[blockIdx.y];
+  if (k >= m.steps) return;
+  const FvmParams p = m.p;
+  col_pinv_cols(p, blockIdx.x, W, log2W, bstride, m.spec);
+}
+
+// Every block of a cluster belongs to one member (clusters span x only), so
+// an idle member's cluster leaves as a whole.
+template <int CL>
+__global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(128, 7)
+    fvm_batch_col_pinv_cluster_kernel(const FvmMember* __restrict__ mem, int k) {
+  const FvmMember& m = mem[blockIdx.y];
+  if (k >= m.steps) return;
+  const FvmParams p = m.p;
+  col_pinv_cluster_cols<CL>(p, m.spec);
+}
+
+template <int MAXT, int MINB>
+__global__ void __launch_bounds__(MAXT, MINB)
+    fvm_batch_irfft_kernel(const FvmMember* __restrict__ mem, int k, int rows) {
+  const FvmMember& m = mem[blockIdx.y];
+  if (k >= m.steps) return;
+  const FvmParams p = m.p;
+  irfft_rows(p, blockIdx.x, rows, m.spec);
+}
+
+__global__ void fvm_batch_project_out_kernel(const FvmMember* __restrict__ mem) {
+  const FvmMember& m = mem[blockIdx.y];
+  if (m.steps <= 0) return;
+  const FvmParams p = m.p;
+  const int cur = batch_dst(m.steps - 1);
+  project_out_cells(p, blockIdx.x, gridDim.x, m.f[cur][0], m.f[cur][1],
+                    reinterpret_cast<const float*>(m.spec), m.f[0][0], m.f[0][1]);
 }
 
 int fft_rows_per_block(int log2L, int nrows, int target_threads = 256) {
@@ -842,6 +947,95 @@ cudaError_t launch_max_speed(int n, const float* u, const float* v,
   cudaError_t e = cudaMemsetAsync(out_bits, 0, sizeof(unsigned int), s);
   if (e != cudaSuccess) return e;
   max_speed_kernel<<<elementwise_blocks((size_t)n), 256, 0, s>>>(n, u, v, out_bits);
+  return cudaGetLastError();
+}
+
+bool fvm_batch_shape_ok(const FvmParams& p) {
+  return p.nx % kTI == 0 && p.ny % kTJ == 0;
+}
+
+template <int MAXT, int MINB>
+static cudaError_t batch_rows_impl(const FvmParams& p, int target, const FvmMember* mem,
+                                   int count, int k, bool inverse, cudaStream_t s) {
+  const int log2L = p.log2ny - 1;
+  const int rows = fft_rows_per_block(log2L, p.nx, target);
+  const size_t smem = (size_t)rows * padded_len(p.ny / 2) * sizeof(float2);
+  const dim3 grid(p.nx / rows, count);
+  const int threads = block_threads(fft_workers(log2L, rows));
+  cudaError_t e;
+  if (inverse) {
+    if ((e = set_smem(fvm_batch_irfft_kernel<MAXT, MINB>, smem)) != cudaSuccess) return e;
+    fvm_batch_irfft_kernel<MAXT, MINB><<<grid, threads, smem, s>>>(mem, k, rows);
+  } else {
+    if ((e = set_smem(fvm_batch_div_rfft_kernel<MAXT, MINB>, smem)) != cudaSuccess) return e;
+    fvm_batch_div_rfft_kernel<MAXT, MINB><<<grid, threads, smem, s>>>(mem, k, rows);
+  }
+  return cudaGetLastError();
+}
+
+template <int MAXT, int MINB>
+static cudaError_t batch_col_impl(const FvmParams& p, int target, const FvmMember* mem,
+                                  int count, int k, cudaStream_t s) {
+  const int L = p.ny / 2;
+  int W = (16 * target) >> p.log2nx;
+  if (W < 1) W = 1;
+  if (W > L) W = L;
+  const int bstride = padded_len(p.nx) + 8;
+  const size_t smem = (size_t)W * bstride * sizeof(float2);
+  cudaError_t e = set_smem(fvm_batch_col_pinv_kernel<MAXT, MINB>, smem);
+  if (e != cudaSuccess) return e;
+  fvm_batch_col_pinv_kernel<MAXT, MINB><<<dim3(L / W, count),
+                                          block_threads(fft_workers(p.log2nx, W)), smem, s>>>(
+      mem, k, W, ilog2(W), bstride);
+  return cudaGetLastError();
+}
+
+template <int CL>
+static cudaError_t batch_col_cluster_impl(const FvmParams& p, const FvmMember* mem, int count,
+                                          int k, cudaStream_t s) {
+  const size_t smem = (size_t)padded_len(p.nx) * sizeof(float2);
+  cudaError_t e = set_smem(fvm_batch_col_pinv_cluster_kernel<CL>, smem);
+  if (e != cudaSuccess) return e;
+  fvm_batch_col_pinv_cluster_kernel<CL><<<dim3(p.ny / 2, count),
+                                          block_threads(fft_workers(p.log2nx, 1)), smem, s>>>(
+      mem, k);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fvm_batch_step(const FvmParams& p, const FvmMember* mem, int count, int k,
+                                  cudaStream_t s) {
+  if (!fvm_batch_shape_ok(p) || count < 1 || count > 65535) return cudaErrorInvalidValue;
+  const dim3 grid(p.ny / kTJ, p.nx / kTI, count);
+  if (p.convect == 0) {
+    if (k > 0) fvm_batch_explicit_kernel<true, 0><<<grid, kStencilThreads, 0, s>>>(mem, k);
+    else fvm_batch_explicit_kernel<false, 0><<<grid, kStencilThreads, 0, s>>>(mem, k);
+  } else {
+    if (k > 0) fvm_batch_explicit_kernel<true, 1><<<grid, kStencilThreads, 0, s>>>(mem, k);
+    else fvm_batch_explicit_kernel<false, 1><<<grid, kStencilThreads, 0, s>>>(mem, k);
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  e = p.fft_shape == 1 ? batch_rows_impl<64, 14>(p, 64, mem, count, k, false, s)
+                       : batch_rows_impl<256, 3>(p, 256, mem, count, k, false, s);
+  if (e != cudaSuccess) return e;
+  if (p.col_mode == 2 && col_cluster_ok(p, 8)) e = batch_col_cluster_impl<8>(p, mem, count, k, s);
+  else if (p.col_mode >= 1 && col_cluster_ok(p, 4)) e = batch_col_cluster_impl<4>(p, mem, count, k, s);
+  else e = p.fft_shape == 1 ? batch_col_impl<128, 7>(p, 128, mem, count, k, s)
+                            : batch_col_impl<256, 3>(p, 256, mem, count, k, s);
+  if (e != cudaSuccess) return e;
+  return p.fft_shape == 1 ? batch_rows_impl<64, 14>(p, 64, mem, count, k, true, s)
+                          : batch_rows_impl<256, 3>(p, 256, mem, count, k, true, s);
+}
+
+cudaError_t launch_fvm_batch_project_out(const FvmParams& p, const FvmMember* mem, int count,
+                                         cudaStream_t s) {
+  if (count < 1 || count > 65535) return cudaErrorInvalidValue;
+  const size_t n = (size_t)p.nx * p.ny;
+  int per = (int)((n + 255) / 256);
+  const int cap = (152 * 16 + count - 1) / count;
+  if (per > cap) per = cap;
+  if (per < 1) per = 1;
+  fvm_batch_project_out_kernel<<<dim3(per, count), 256, 0, s>>>(mem);
   return cudaGetLastError();
 }
 

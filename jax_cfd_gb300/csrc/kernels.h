@@ -44,6 +44,16 @@ struct FvmParams {
   int col_mode;        // column pass: 0 per-block columns, 1/2 clusters of 4/8
 };
 
+// One slot of a same-shape batch of FVM trajectories (device-resident table
+// read by the batch kernels; the member index is a grid axis).
+struct FvmMember {
+  FvmParams p;
+  float* f[3][2];  // [0] state (u, v); [1], [2] ping-pong step buffers
+  float2* spec;    // packed row spectrum / pressure q (nx * ny floats)
+  int steps;       // steps of the current chunk; 0 = idle slot
+  int pad_;
+};
+
 // Out-of-bounds / configuration errors are reported through return codes.
 cudaError_t launch_fvm_explicit(const FvmParams& p, bool project, bool out_k0,
                                 const float* ua, const float* va,
@@ -59,6 +69,16 @@ cudaError_t launch_fvm_irfft(const FvmParams& p, float2* spec, cudaStream_t s);
 cudaError_t launch_fvm_project_out(const FvmParams& p, const float* us,
                                    const float* vs, const float* q, float* uo,
                                    float* vo, cudaStream_t s);
+// Batched launches over `count` same-shape members (`shape` carries nx, ny,
+// convect and the chosen transform shapes).  Step k of a chunk reads buffer
+// set 0 (k = 0) or the previous step's output and writes set 1 (k even) or 2
+// (k odd); members with steps <= k skip.  project_out writes each member's
+// final state back into set 0.
+bool fvm_batch_shape_ok(const FvmParams& shape);
+cudaError_t launch_fvm_batch_step(const FvmParams& shape, const FvmMember* members,
+                                  int count, int k, cudaStream_t s);
+cudaError_t launch_fvm_batch_project_out(const FvmParams& shape, const FvmMember* members,
+                                         int count, cudaStream_t s);
 // Diagnostics on staggered velocity fields.
 cudaError_t launch_divergence(const FvmParams& p, const float* u,
                               const float* v, float* out, cudaStream_t s);

@@ -39,6 +39,41 @@ def require_field(t: torch.Tensor, shape, dtype=torch.float32, name='array'):
   return t
 
 
+def fvm_config(shape: Sequence[int], step: Sequence[float], *, density: float = 1.0,
+               viscosity: Optional[float] = None, dt: float = 0.0,
+               convect: int = nat.CONVECT_VAN_LEER,
+               linear_coefficient: Optional[float] = None,
+               const_forcing: int = nat.FORCE_NONE,
+               force_u: Optional[np.ndarray] = None,
+               force_v: Optional[np.ndarray] = None):
+  """The C-ABI configuration of one FVM step; returns (config, arrays the
+  config points into, which must stay alive while it is used)."""
+  cfg = nat.FvmConfig()
+  cfg.nx, cfg.ny = int(shape[0]), int(shape[1])
+  cfg.hx, cfg.hy = float(step[0]), float(step[1])
+  cfg.density = float(density)
+  cfg.has_viscosity = 0 if viscosity is None else 1
+  cfg.viscosity = 0.0 if viscosity is None else float(viscosity)
+  cfg.dt = float(dt)
+  cfg.convect = int(convect)
+  cfg.has_linear_forcing = 0 if linear_coefficient is None else 1
+  cfg.linear_coefficient = 0.0 if linear_coefficient is None else float(linear_coefficient)
+  cfg.const_forcing = int(const_forcing)
+  keep = []
+  nx, ny = cfg.nx, cfg.ny
+  lengths = {nat.FORCE_U_OF_Y: (ny, None), nat.FORCE_V_OF_X: (None, nx),
+             nat.FORCE_FULL: (nx * ny, nx * ny)}.get(int(const_forcing), (None, None))
+  for name, arr, want in (('force_u', force_u, lengths[0]), ('force_v', force_v, lengths[1])):
+    if arr is not None:
+      a = np.ascontiguousarray(arr, dtype=np.float32)
+      if want is not None and a.size != want:
+        raise ValueError(f'{name} has {a.size} values; this forcing layout on a '
+                         f'{nx}x{ny} grid needs {want}')
+      keep.append(a)
+      setattr(cfg, name, a.ctypes.data_as(ctypes.POINTER(ctypes.c_float)))
+  return cfg, keep
+
+
 class FvmPlan:
   """Native plan for the staggered-grid step and pressure projection."""
 
@@ -55,23 +90,11 @@ class FvmPlan:
     self.shape = (int(shape[0]), int(shape[1]))
     self.device = torch.device(device) if device is not None else torch.device(
         'cuda', torch.cuda.current_device())
-    cfg = nat.FvmConfig()
-    cfg.nx, cfg.ny = self.shape
-    cfg.hx, cfg.hy = float(step[0]), float(step[1])
-    cfg.density = float(density)
-    cfg.has_viscosity = 0 if viscosity is None else 1
-    cfg.viscosity = 0.0 if viscosity is None else float(viscosity)
-    cfg.dt = float(dt)
-    cfg.convect = int(convect)
-    cfg.has_linear_forcing = 0 if linear_coefficient is None else 1
-    cfg.linear_coefficient = 0.0 if linear_coefficient is None else float(linear_coefficient)
-    cfg.const_forcing = int(const_forcing)
-    self._keep = []
-    for name, arr in (('force_u', force_u), ('force_v', force_v)):
-      if arr is not None:
-        a = np.ascontiguousarray(arr, dtype=np.float32)
-        self._keep.append(a)
-        setattr(cfg, name, a.ctypes.data_as(ctypes.POINTER(ctypes.c_float)))
+    cfg, self._keep = fvm_config(self.shape, step, density=density, viscosity=viscosity,
+                                 dt=dt, convect=convect,
+                                 linear_coefficient=linear_coefficient,
+                                 const_forcing=const_forcing, force_u=force_u,
+                                 force_v=force_v)
     handle = ctypes.c_void_p()
     with torch.cuda.device(self.device):
       nat.check(nat.load().cfd_fvm_plan_create(ctypes.byref(cfg), ctypes.byref(handle)),
