@@ -329,6 +329,65 @@ def run_ensemble(dev, args, flush):
   }
 
 
+def run_serving(dev, args):
+  """Continuous-batching server on a seeded Poisson stream (FVM and spectral
+  requests, 100-step chunks, 150 GB budget); p50/p99 completion latency and
+  throughput.  A short stream over every (kind, size) warms the per-size plans
+  and the CUDA modules first; the timed server starts empty."""
+  import torch  # pylint: disable=import-outside-toplevel
+  from jax_cfd_gb300 import serving  # pylint: disable=import-outside-toplevel
+  warm = []
+  for i, (kind, n) in enumerate((kd, n) for kd in ('fvm', 'spectral') for n in serving.SIZES):
+    for k in (2, 4, 8):
+      warm.append(serving.Request(rid=10 ** 6 + 3 * i + k, kind=kind, n=n, steps=2,
+                                  viscosity=1e-3, k=k, vmax=2.0, seed=1, arrival=0.0))
+  serving.Server(device=dev, chunk=args.serve_chunk).serve(warm, realtime=False)
+  reqs = serving.poisson_requests(args.serve_rate, args.serve_seconds, seed=7)
+  server = serving.Server(device=dev, chunk=args.serve_chunk, budget_bytes=150e9)
+  t0 = time.perf_counter()
+  done = server.serve(reqs, realtime=True, timeout=args.serve_seconds + 600)
+  makespan = time.perf_counter() - t0
+  torch.cuda.synchronize(dev)
+  st = serving.Server.stats(done, makespan)
+  offered = sum(r.steps * r.n * r.n for r in reqs) / args.serve_seconds
+  # Plain loop on the same request mix: one request after another through the
+  # drop-in step (initial condition, funcutils.repeated, result to the host).
+  plain_reqs = [serving.Request(rid=r.rid, kind=r.kind, n=r.n, steps=r.steps,
+                                viscosity=r.viscosity, k=r.k, vmax=r.vmax, seed=r.seed)
+                for r in reqs[:args.serve_plain]]
+  t1 = time.perf_counter()
+  for r in plain_reqs:
+    serving.run_plain(r, dev)
+  torch.cuda.synchronize(dev)
+  plain_s = time.perf_counter() - t1
+  plain_steps = sum(r.steps for r in plain_reqs)
+  kinds = {}
+  for kind in ('fvm', 'spectral'):
+    sub = [r for r in done if r.kind == kind]
+    lat = np.array([r.latency for r in sub])
+    kinds[kind] = {'requests': len(sub),
+                   'p50_latency_s': float(np.percentile(lat, 50)),
+                   'p99_latency_s': float(np.percentile(lat, 99))}
+  return {
+      'workload': f'Poisson arrivals {args.serve_rate:g}/s for {args.serve_seconds:g} s; '
+                  'FVM or spectral 50/50; N in {64..2048} with P(N) ~ 1/N^2; horizon '
+                  'log-uniform 100-5000 steps; nu log-uniform [1e-4, 1e-2]; k in {2,4,8}; '
+                  f'{args.serve_chunk}-step chunks; 150 GB budget',
+      **st,
+      'unit': 'trajectory-steps/s',
+      'offered_cell_steps_per_s': offered,
+      'plain_loop': {'requests': len(plain_reqs), 'seconds': plain_s,
+                     'trajectory_steps_per_s': plain_steps / plain_s,
+                     'sample': f'the first {len(plain_reqs)} requests of the stream, '
+                               'one after another'},
+      'speedup_vs_plain': st['trajectory_steps_per_s'] / (plain_steps / plain_s),
+      'by_kind': kinds,
+      'pools': sum(len(p) for p in server.pools.values()),
+      'pool_bytes': server.bytes_in_use,
+      'chunk_launches': server.launches,
+  }
+
+
 def run_gb300(args):
   import torch  # pylint: disable=import-outside-toplevel
   import jax_cfd_gb300.base as cfd  # pylint: disable=import-outside-toplevel
@@ -469,6 +528,10 @@ def run_gb300(args):
   if not args.skip_ensemble:
     ensemble = run_ensemble(dev, args, flush)
 
+  served = None
+  if not args.skip_serving:
+    served = run_serving(dev, args)
+
   cpu = None
   if rank == 0 and not args.skip_cpu:
     cv, csecs, cthreads = _cpu_sample(args.cpu_steps, 1)
@@ -510,6 +573,7 @@ def run_gb300(args):
       'finite': finite,
       'spectral': spectral,
       'ensemble': ensemble,
+      'serving': served,
   })
 
 
@@ -528,6 +592,11 @@ def main():
   ap.add_argument('--skip-ensemble', action='store_true')
   ap.add_argument('--ensemble-members', type=int, default=96)
   ap.add_argument('--ensemble-steps', type=int, default=1000)
+  ap.add_argument('--skip-serving', action='store_true')
+  ap.add_argument('--serve-rate', type=float, default=200.0)
+  ap.add_argument('--serve-seconds', type=float, default=60.0)
+  ap.add_argument('--serve-chunk', type=int, default=100)
+  ap.add_argument('--serve-plain', type=int, default=150)
   args = ap.parse_args()
   if args.warmup < 3:
     ap.error('at least 3 warm-up steps are required')

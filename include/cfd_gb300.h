@@ -237,6 +237,26 @@ int cfd_irfft2(cfd_spec_plan* plan, void* stream, const float* xhat, float* x);
 int cfd_spectral_filter(cfd_spec_plan* plan, void* stream, const float* x,
                         const float* table, float* out);
 
+/* ---- Batched spectral trajectories ----
+ * The cfd_fvm_batch model for NavierStokes2D + a low-storage RK/CN
+ * integrator (spectral/equations.py:129-220, spectral/time_stepping.py:117-197):
+ * `count` slots of one grid and stage count; per-slot viscosity, drag, dt and
+ * smoothing from cfd_spec_batch_set_slot; the slot's forcing curl table is
+ * borrowed from `forcing` (a plan on the same grid after cfd_spec_set_forcing,
+ * or NULL for none), which must outlive its use.  cfd_spec_batch_state
+ * returns the slot's state (rfft of the vorticity, complex64 nx x (ny/2+1)). */
+typedef struct cfd_spec_batch cfd_spec_batch;
+int cfd_spec_batch_create(const cfd_spec_config* shape, int count, cfd_spec_batch** batch);
+int cfd_spec_batch_destroy(cfd_spec_batch* batch);
+int cfd_spec_batch_size(const cfd_spec_batch* batch);
+long long cfd_spec_batch_bytes(const cfd_spec_batch* batch);
+int cfd_spec_batch_state(cfd_spec_batch* batch, int slot, float** w);
+int cfd_spec_batch_set_slot(cfd_spec_batch* batch, int slot, const cfd_spec_config* cfg,
+                            const cfd_spec_plan* forcing);
+int cfd_spec_batch_set_steps(cfd_spec_batch* batch, int slot, int steps);
+int cfd_spec_batch_run(cfd_spec_batch* batch, void* stream, int chunk, int use_graph);
+
+
 #ifdef __cplusplus
 }
 #endif

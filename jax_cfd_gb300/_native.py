@@ -96,6 +96,15 @@ _SIGNATURES = {
                                                ctypes.POINTER(_vp)]),
     'cfd_fvm_ensemble_autotune': (ctypes.c_int, [_vp, _vp, ctypes.c_int]),
     'cfd_fvm_ensemble_step': (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_int]),
+    'cfd_spec_batch_create': (ctypes.c_int, [ctypes.POINTER(SpecConfig), ctypes.c_int,
+                                              ctypes.POINTER(_vp)]),
+    'cfd_spec_batch_destroy': (ctypes.c_int, [_vp]),
+    'cfd_spec_batch_size': (ctypes.c_int, [_vp]),
+    'cfd_spec_batch_bytes': (ctypes.c_longlong, [_vp]),
+    'cfd_spec_batch_state': (ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(_vp)]),
+    'cfd_spec_batch_set_slot': (ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(SpecConfig), _vp]),
+    'cfd_spec_batch_set_steps': (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int]),
+    'cfd_spec_batch_run': (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_int]),
     'cfd_max_speed': (ctypes.c_int, [_vp, ctypes.c_int, _vp, _vp, _vp]),
     'cfd_scale_to_max_speed': (ctypes.c_int, [_vp, ctypes.c_int, _vp, _vp, _vp, ctypes.c_double]),
     'cfd_spec_plan_create': (ctypes.c_int, [ctypes.POINTER(SpecConfig), ctypes.POINTER(_vp)]),

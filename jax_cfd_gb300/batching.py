@@ -134,6 +134,101 @@ class FvmBatch:
     return int(chosen.value)
 
 
+class SpecBatch:
+  """Slots of one grid shape running NavierStokes2D + a low-storage RK/CN
+  integrator together (``cfd_spec_batch``)."""
+
+  def __init__(self, shape: Sequence[int], step: Sequence[float], count: int, *,
+               stages: int = 5, device: Optional[torch.device] = None):
+    self.shape = (int(shape[0]), int(shape[1]))
+    self.half_shape = (self.shape[0], self.shape[1] // 2 + 1)
+    self.step = (float(step[0]), float(step[1]))
+    self.count = int(count)
+    self.stages = int(stages)
+    self.device = torch.device(device) if device is not None else torch.device(
+        'cuda', torch.cuda.current_device())
+    zeros = [0.0] * self.stages
+    cfg, _ = plans.spec_config(self.shape, self.step, alphas=[0.0] * (self.stages + 1),
+                               betas=zeros, gammas=zeros)
+    handle = ctypes.c_void_p()
+    self._lib = nat.load()
+    with torch.cuda.device(self.device):
+      nat.check(self._lib.cfd_spec_batch_create(ctypes.byref(cfg), self.count,
+                                                ctypes.byref(handle)), 'cfd_spec_batch_create')
+    self._h = handle
+    self._views = [None] * self.count
+    self._forcing = [None] * self.count
+
+  def __del__(self):
+    h = getattr(self, '_h', None)
+    if h is not None and h.value:
+      try:
+        torch.cuda.synchronize(self.device)
+        self._lib.cfd_spec_batch_destroy(h)
+      except Exception:  # pylint: disable=broad-except
+        pass
+      self._h = None
+
+  @property
+  def nbytes(self) -> int:
+    return int(self._lib.cfd_spec_batch_bytes(self._h))
+
+  def _slot(self, slot: int) -> int:
+    if not 0 <= slot < self.count:
+      raise IndexError(f'slot {slot} out of range [0, {self.count})')
+    return int(slot)
+
+  def state(self, slot: int) -> torch.Tensor:
+    """The slot's vorticity spectrum (complex64 view of batch memory)."""
+    slot = self._slot(slot)
+    if self._views[slot] is None:
+      w = ctypes.c_void_p()
+      nat.check(self._lib.cfd_spec_batch_state(self._h, slot, ctypes.byref(w)),
+                'cfd_spec_batch_state')
+      flat = _view(self, w.value, (self.half_shape[0], 2 * self.half_shape[1]), self.device)
+      self._views[slot] = flat.view(torch.complex64)
+    return self._views[slot]
+
+  def set_slot(self, slot: int, *, viscosity: float, drag: float, dt: float,
+               smooth: bool = True, alphas, betas, gammas,
+               forcing_plan: Optional[plans.SpecPlan] = None):
+    """New step parameters for a slot; the forcing curl table is borrowed from
+    `forcing_plan` (kept alive by the batch while the slot uses it)."""
+    slot = self._slot(slot)
+    cfg, keep = plans.spec_config(self.shape, self.step, viscosity=viscosity, drag=drag, dt=dt,
+                                  smooth=smooth, alphas=alphas, betas=betas, gammas=gammas)
+    fh = forcing_plan.handle if forcing_plan is not None else None
+    nat.check(self._lib.cfd_spec_batch_set_slot(self._h, slot, ctypes.byref(cfg), fh),
+              'cfd_spec_batch_set_slot')
+    self._forcing[slot] = forcing_plan
+    del keep
+
+  def set_slot_from_step(self, slot: int, step_fn):
+    """Slot parameters from a drop-in step (``crank_nicolson_rk4(eq, dt)``)."""
+    from jax_cfd_gb300.spectral import time_stepping  # pylint: disable=import-outside-toplevel
+    if not isinstance(step_fn, time_stepping.SpectralStep):
+      raise NotImplementedError('spectral slots take time_stepping.SpectralStep steps')
+    eq = step_fn.equation
+    if tuple(eq.grid.shape) != self.shape or tuple(eq.grid.step) != self.step:
+      raise ValueError('the step lives on another grid')
+    forcing = eq._plan(self.device) if eq.forcing_fn is not None else None  # pylint: disable=protected-access
+    a, b, g = step_fn.coefficients
+    self.set_slot(slot, viscosity=float(eq.viscosity), drag=float(eq.drag),
+                  dt=step_fn.time_step, smooth=eq.smooth is not None, alphas=a, betas=b,
+                  gammas=g, forcing_plan=forcing)
+
+  def set_state(self, slot: int, w_hat: torch.Tensor):
+    self.state(slot).copy_(w_hat)
+
+  def set_steps(self, slot: int, steps: int):
+    nat.check(self._lib.cfd_spec_batch_set_steps(self._h, self._slot(slot), int(steps)),
+              'cfd_spec_batch_set_steps')
+
+  def run(self, chunk: int, graph: bool = True):
+    nat.check(self._lib.cfd_spec_batch_run(self._h, plans.current_stream_ptr(self.device),
+                                           int(chunk), 1 if graph else 0), 'cfd_spec_batch_run')
+
+
 class FvmEnsemble:
   """Members of any grid shapes (``cfd_fvm_ensemble``); ``members`` are dicts
   of ``plans.fvm_config`` arguments (shape, step, dt, viscosity, ...)."""

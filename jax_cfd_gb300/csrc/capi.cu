@@ -176,6 +176,33 @@ struct cfd_fvm_ensemble {
   int graph_steps = -1;
 };
 
+// A batch of same-shape spectral trajectories (slots), like cfd_fvm_batch:
+// one device table of cfd::SpecMember entries, one slab of per-slot buffers
+// (w, h, four column fields, advection spectra: 7 half spectra per slot) and
+// the grid tables shared by every slot.
+struct cfd_spec_batch {
+  cfd::SpecParams shape;
+  double hx = 0, hy = 0;
+  int stages = 0;
+  int count = 0;
+  size_t ns = 0;  // complex entries of one half spectrum
+  float2* slab = nullptr;
+  float2* twy = nullptr;
+  float2* twpx = nullptr;
+  float2* twpy = nullptr;
+  float* kx = nullptr;
+  float* ky = nullptr;
+  std::vector<cfd::SpecMember> host;
+  std::vector<int> want;
+  cfd::SpecMember* dev = nullptr;
+  int uploaded_chunk = -1;
+  bool dirty = true;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int graph_chunk = -1;
+  long long bytes = 0;
+};
+
 struct cfd_spec_plan {
   cfd::SpecParams p;
   int stages = 0;
@@ -1014,17 +1041,17 @@ int cfd_spec_plan_destroy(cfd_spec_plan* plan) {
   return CFD_OK;
 }
 
-int cfd_spec_plan_create(const cfd_spec_config* cfg, cfd_spec_plan** out) {
-  if (!cfg || !out) return fail(CFD_ERR_INVALID_ARGUMENT, "null config or output pointer");
-  *out = nullptr;
+// Scalar parameters and stage coefficients of one spectral configuration (no
+// device tables); shared by plans and batch slots.
+static int spec_params_from_config(const cfd_spec_config* cfg, cfd::SpecParams* out,
+                                   cfd::StageCoef* coef, int* stages) {
   if (!valid_size(cfg->nx) || !valid_size(cfg->ny))
     return fail(CFD_ERR_UNSUPPORTED, "grid shape must be powers of two in [4, 4096]");
   if (cfg->num_stages < 1 || cfg->num_stages > 8 || !cfg->alphas || !cfg->betas || !cfg->gammas)
     return fail(CFD_ERR_INVALID_ARGUMENT, "num_stages must be in [1, 8] with coefficient arrays");
   if (!(cfg->hx > 0) || !(cfg->hy > 0))
     return fail(CFD_ERR_INVALID_ARGUMENT, "invalid grid step");
-  cfd_spec_plan* plan = new cfd_spec_plan();
-  cfd::SpecParams& p = plan->p;
+  cfd::SpecParams& p = *out;
   std::memset(&p, 0, sizeof(p));
   const int nx = cfg->nx, ny = cfg->ny;
   p.nx = nx;
@@ -1051,9 +1078,9 @@ int cfd_spec_plan_create(const cfd_spec_config* cfg, cfd_spec_plan** out) {
     p.filt_hi = nx + start;
     p.filt_cols = (int)(2.0 / 3.0 * (ny / 2 + 1));
   }
-  plan->stages = cfg->num_stages;
+  *stages = cfg->num_stages;
   for (int k = 0; k < cfg->num_stages; ++k) {
-    cfd::StageCoef& c = plan->coef[k];
+    cfd::StageCoef& c = coef[k];
     c.beta = (float)cfg->betas[k];
     c.gdt = (float)(cfg->gammas[k] * cfg->dt);
     c.mu = (float)(0.5 * cfg->dt * (cfg->alphas[k + 1] - cfg->alphas[k]));
@@ -1062,6 +1089,42 @@ int cfd_spec_plan_create(const cfd_spec_config* cfg, cfd_spec_plan** out) {
     c.prep_next = 1;
     c.explicit_only = 0;
   }
+  return CFD_OK;
+}
+
+// Host tables of a spectral grid: real-FFT untangling twiddles, pass tables
+// and the fftfreq / rfftfreq wavenumbers (float32 ordinals over
+// float32(step * n), grids.py:618-658 via jnp.fft.fftfreq).
+struct SpecTables {
+  std::vector<float2> twy, twpx, twpy;
+  std::vector<float> kx, ky;
+};
+static SpecTables spec_tables(const cfd::SpecParams& p) {
+  SpecTables t;
+  t.twy = twiddles(p.ny);
+  t.twpx = pass_twiddles(p.log2nx);
+  t.twpy = pass_twiddles(p.log2L);
+  t.kx.resize(p.nx);
+  t.ky.resize(p.L + 1);
+  for (int k = 0; k < p.nx; ++k) t.kx[k] = (float)(k < p.nx / 2 ? k : k - p.nx) / p.dn_x;
+  for (int k = 0; k <= p.L; ++k) t.ky[k] = (float)k / p.dn_y;
+  return t;
+}
+
+int cfd_spec_plan_create(const cfd_spec_config* cfg, cfd_spec_plan** out) {
+  if (!cfg || !out) return fail(CFD_ERR_INVALID_ARGUMENT, "null config or output pointer");
+  *out = nullptr;
+  cfd::SpecParams params;
+  cfd::StageCoef coef[8];
+  int stages = 0;
+  int rc = spec_params_from_config(cfg, &params, coef, &stages);
+  if (rc) return rc;
+  cfd_spec_plan* plan = new cfd_spec_plan();
+  cfd::SpecParams& p = plan->p;
+  p = params;
+  plan->stages = stages;
+  for (int k = 0; k < stages; ++k) plan->coef[k] = coef[k];
+  const int nx = cfg->nx;
   const size_t ns = (size_t)nx * (p.L + 1);
   cudaError_t e;
   long long bytes = 0;
@@ -1079,23 +1142,17 @@ int cfd_spec_plan_create(const cfd_spec_config* cfg, cfd_spec_plan** out) {
   CFD_ALLOC(plan->h, ns);
   CFD_ALLOC(plan->work, ns);
 #undef CFD_ALLOC
-  std::vector<float2> twy = twiddles(ny);
-  std::vector<float2> twpx = pass_twiddles(p.log2nx), twpy = pass_twiddles(p.log2L);
-  // fftfreq(n, d) / rfftfreq(n, d): float32 ordinals divided by float32(d*n)
-  // (grids.py:618-658 via jnp.fft.fftfreq).
-  std::vector<float> kxt(nx), kyt(p.L + 1);
-  for (int k = 0; k < nx; ++k) kxt[k] = (float)(k < nx / 2 ? k : k - nx) / p.dn_x;
-  for (int k = 0; k <= p.L; ++k) kyt[k] = (float)k / p.dn_y;
-  if ((e = upload(&plan->twy, twy.data(), twy.size())) != cudaSuccess ||
-      (e = upload(&plan->twpx, twpx.data(), twpx.size())) != cudaSuccess ||
-      (e = upload(&plan->twpy, twpy.data(), twpy.size())) != cudaSuccess ||
-      (e = upload(&plan->kx, kxt.data(), kxt.size())) != cudaSuccess ||
-      (e = upload(&plan->ky, kyt.data(), kyt.size())) != cudaSuccess) {
+  const SpecTables t = spec_tables(p);
+  if ((e = upload(&plan->twy, t.twy.data(), t.twy.size())) != cudaSuccess ||
+      (e = upload(&plan->twpx, t.twpx.data(), t.twpx.size())) != cudaSuccess ||
+      (e = upload(&plan->twpy, t.twpy.data(), t.twpy.size())) != cudaSuccess ||
+      (e = upload(&plan->kx, t.kx.data(), t.kx.size())) != cudaSuccess ||
+      (e = upload(&plan->ky, t.ky.data(), t.ky.size())) != cudaSuccess) {
     cfd_spec_plan_destroy(plan);
     return cuda_fail(e, "cfd_spec_plan_create: tables");
   }
-  bytes += (long long)(twy.size() + twpx.size() + twpy.size()) * 8 +
-           (long long)(kxt.size() + kyt.size()) * 4;
+  bytes += (long long)(t.twy.size() + t.twpx.size() + t.twpy.size()) * 8 +
+           (long long)(t.kx.size() + t.ky.size()) * 4;
   p.tw_y = plan->twy;
   p.twp_x = plan->twpx;
   p.twp_y = plan->twpy;
@@ -1298,6 +1355,173 @@ int cfd_spec_explicit_terms(cfd_spec_plan* plan, void* stream, const float* w,
   CFD_CHECK(cfd::launch_spec_col_update(p, c, plan->ahat, reinterpret_cast<float2*>(out),
                                         plan->h, plan->t4, s),
             "col_update");
+  return CFD_OK;
+}
+
+// ---- Same-shape spectral batches ---------------------------------------
+
+static void spec_batch_drop_graph(cfd_spec_batch* b) {
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  b->exec = nullptr;
+  b->graph = nullptr;
+  b->graph_chunk = -1;
+}
+
+int cfd_spec_batch_destroy(cfd_spec_batch* b) {
+  if (!b) return CFD_OK;
+  spec_batch_drop_graph(b);
+  void* ptrs[] = {b->slab, b->twy, b->twpx, b->twpy, b->kx, b->ky, b->dev};
+  for (void* q : ptrs)
+    if (q) cudaFree(q);
+  delete b;
+  return CFD_OK;
+}
+
+int cfd_spec_batch_create(const cfd_spec_config* shape, int count, cfd_spec_batch** out) {
+  if (!shape || !out || count < 1 || count > 65535)
+    return fail(CFD_ERR_INVALID_ARGUMENT, "cfd_spec_batch_create: bad arguments");
+  *out = nullptr;
+  cfd::SpecParams p;
+  cfd::StageCoef coef[8];
+  int stages = 0;
+  int rc = spec_params_from_config(shape, &p, coef, &stages);
+  if (rc) return rc;
+  if (p.log2L < 1) return fail(CFD_ERR_UNSUPPORTED, "batched spectral steps need ny >= 4");
+  cfd_spec_batch* b = new cfd_spec_batch();
+  b->shape = p;
+  b->hx = shape->hx;
+  b->hy = shape->hy;
+  b->stages = stages;
+  b->count = count;
+  const size_t ns = (size_t)p.nx * (p.L + 1);
+  b->ns = ns;
+  cudaError_t e = cudaMalloc((void**)&b->slab, (size_t)count * 7 * ns * sizeof(float2));
+  if (e == cudaSuccess) e = cudaMemset(b->slab, 0, (size_t)count * 7 * ns * sizeof(float2));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&b->dev, (size_t)count * sizeof(cfd::SpecMember));
+  const SpecTables t = spec_tables(p);
+  if (e == cudaSuccess) e = upload(&b->twy, t.twy.data(), t.twy.size());
+  if (e == cudaSuccess) e = upload(&b->twpx, t.twpx.data(), t.twpx.size());
+  if (e == cudaSuccess) e = upload(&b->twpy, t.twpy.data(), t.twpy.size());
+  if (e == cudaSuccess) e = upload(&b->kx, t.kx.data(), t.kx.size());
+  if (e == cudaSuccess) e = upload(&b->ky, t.ky.data(), t.ky.size());
+  if (e != cudaSuccess) {
+    cfd_spec_batch_destroy(b);
+    return cuda_fail(e, "cfd_spec_batch_create");
+  }
+  b->bytes = (long long)count * 7 * (long long)ns * 8 + (long long)count * sizeof(cfd::SpecMember);
+  b->host.assign(count, cfd::SpecMember());
+  b->want.assign(count, 0);
+  for (int i = 0; i < count; ++i) {
+    cfd::SpecMember& m = b->host[i];
+    std::memset(&m, 0, sizeof(m));
+    m.p = p;
+    m.p.tw_y = b->twy;
+    m.p.twp_x = b->twpx;
+    m.p.twp_y = b->twpy;
+    m.p.kx = b->kx;
+    m.p.ky = b->ky;
+    for (int k = 0; k < stages; ++k) m.coef[k] = coef[k];
+    m.stages = stages;
+    float2* base = b->slab + (size_t)i * 7 * ns;
+    m.w = base;
+    m.h = base + ns;
+    for (int f = 0; f < 4; ++f) m.t[f] = base + (2 + f) * ns;
+    m.ahat = base + 6 * ns;
+    m.steps = 0;
+  }
+  *out = b;
+  return CFD_OK;
+}
+
+int cfd_spec_batch_size(const cfd_spec_batch* b) { return b ? b->count : 0; }
+
+long long cfd_spec_batch_bytes(const cfd_spec_batch* b) { return b ? b->bytes : 0; }
+
+int cfd_spec_batch_state(cfd_spec_batch* b, int slot, float** w) {
+  if (!b || !w || slot < 0 || slot >= b->count)
+    return fail(CFD_ERR_INVALID_ARGUMENT, "cfd_spec_batch_state: bad arguments");
+  *w = reinterpret_cast<float*>(b->host[slot].w);
+  return CFD_OK;
+}
+
+int cfd_spec_batch_set_slot(cfd_spec_batch* b, int slot, const cfd_spec_config* cfg,
+                            const cfd_spec_plan* forcing) {
+  if (!b || !cfg || slot < 0 || slot >= b->count)
+    return fail(CFD_ERR_INVALID_ARGUMENT, "cfd_spec_batch_set_slot: bad arguments");
+  if (cfg->nx != b->shape.nx || cfg->ny != b->shape.ny || cfg->hx != b->hx || cfg->hy != b->hy ||
+      cfg->num_stages != b->stages)
+    return fail(CFD_ERR_INVALID_ARGUMENT,
+                "cfd_spec_batch_set_slot: grid, step and stage count must match the batch");
+  if (forcing && (forcing->p.nx != b->shape.nx || forcing->p.ny != b->shape.ny))
+    return fail(CFD_ERR_INVALID_ARGUMENT,
+                "cfd_spec_batch_set_slot: the forcing plan lives on another grid");
+  cfd::SpecParams p;
+  cfd::StageCoef coef[8];
+  int stages = 0;
+  int rc = spec_params_from_config(cfg, &p, coef, &stages);
+  if (rc) return rc;
+  cfd::SpecMember& m = b->host[slot];
+  p.tw_y = b->twy;
+  p.twp_x = b->twpx;
+  p.twp_y = b->twpy;
+  p.kx = b->kx;
+  p.ky = b->ky;
+  p.fc_full = forcing ? forcing->p.fc_full : nullptr;
+  p.fc_row0 = forcing ? forcing->p.fc_row0 : nullptr;
+  m.p = p;
+  for (int k = 0; k < stages; ++k) m.coef[k] = coef[k];
+  m.stages = stages;
+  b->dirty = true;
+  return CFD_OK;
+}
+
+int cfd_spec_batch_set_steps(cfd_spec_batch* b, int slot, int steps) {
+  if (!b || slot < 0 || slot >= b->count || steps < 0)
+    return fail(CFD_ERR_INVALID_ARGUMENT, "cfd_spec_batch_set_steps: bad arguments");
+  if (b->want[slot] != steps) b->dirty = true;
+  b->want[slot] = steps;
+  return CFD_OK;
+}
+
+static int spec_batch_upload(cfd_spec_batch* b, cudaStream_t s, int chunk) {
+  if (!b->dirty && b->uploaded_chunk == chunk) return CFD_OK;
+  for (int i = 0; i < b->count; ++i) b->host[i].steps = std::min(b->want[i], chunk);
+  CFD_CHECK(cudaMemcpyAsync(b->dev, b->host.data(), b->host.size() * sizeof(cfd::SpecMember),
+                            cudaMemcpyHostToDevice, s),
+            "cfd_spec_batch: slot table");
+  b->dirty = false;
+  b->uploaded_chunk = chunk;
+  return CFD_OK;
+}
+
+static int spec_batch_enqueue(cfd_spec_batch* b, cudaStream_t s, int chunk) {
+  const cfd::SpecParams& p = b->shape;
+  CFD_CHECK(cfd::launch_spec_batch_prep(p, b->dev, b->count, -1, -1, s), "batch prep");
+  for (int k = 0; k < chunk; ++k)
+    for (int st = 0; st < b->stages; ++st) {
+      CFD_CHECK(cfd::launch_spec_batch_row(p, b->dev, b->count, k, s), "batch row");
+      CFD_CHECK(cfd::launch_spec_batch_update(p, b->dev, b->count, k, st, s), "batch update");
+      CFD_CHECK(cfd::launch_spec_batch_prep(p, b->dev, b->count, k, st, s), "batch prep");
+    }
+  return CFD_OK;
+}
+
+int cfd_spec_batch_run(cfd_spec_batch* b, void* stream, int chunk, int use_graph) {
+  if (!b || chunk < 0) return fail(CFD_ERR_INVALID_ARGUMENT, "cfd_spec_batch_run: bad arguments");
+  if (chunk == 0) return CFD_OK;
+  cudaStream_t s = as_stream(stream);
+  int rc = spec_batch_upload(b, s, chunk);
+  if (rc) return rc;
+  if (!use_graph) return spec_batch_enqueue(b, s, chunk);
+  if (!b->exec || b->graph_chunk != chunk) {
+    spec_batch_drop_graph(b);
+    rc = capture_graph([&](cudaStream_t c) { return spec_batch_enqueue(b, c, chunk); },
+                       &b->graph, &b->exec);
+    if (rc) return rc;
+    b->graph_chunk = chunk;
+  }
+  CFD_CHECK(cudaGraphLaunch(b->exec, s), "cudaGraphLaunch");
   return CFD_OK;
 }
 

@@ -118,6 +118,28 @@ struct StageCoef {
   int explicit_only;  // store F(u) into the state buffer instead of updating
 };
 
+// One slot of a same-shape batch of spectral trajectories.
+struct SpecMember {
+  SpecParams p;
+  StageCoef coef[8];
+  int stages;      // low-storage RK/CN stages of this slot's integrator
+  int steps;       // steps of the current chunk; 0 = idle slot
+  float2* w;       // state: rfft of the vorticity, nx x (ny/2 + 1)
+  float2* h;       // low-storage carry
+  float2* t[4];    // column-transformed explicit-term inputs
+  float2* ahat;    // advection row spectra
+};
+
+// Batched stage launches (slot index = last grid axis); slots with steps <= k
+// skip.  A chunk is prep(k=-1) then, per step k and stage st: row(k),
+// update(k, st), prep(k, st).
+cudaError_t launch_spec_batch_prep(const SpecParams& shape, const SpecMember* mem, int count,
+                                   int k, int stage, cudaStream_t s);
+cudaError_t launch_spec_batch_row(const SpecParams& shape, const SpecMember* mem, int count,
+                                  int k, cudaStream_t s);
+cudaError_t launch_spec_batch_update(const SpecParams& shape, const SpecMember* mem, int count,
+                                     int k, int stage, cudaStream_t s);
+
 cudaError_t launch_spec_col_prep(const SpecParams& p, const float2* w,
                                  float2* const t4[4], cudaStream_t s);
 cudaError_t launch_spec_row(const SpecParams& p, const float2* const t4[4],

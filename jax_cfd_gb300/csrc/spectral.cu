@@ -67,12 +67,11 @@ struct T4 {
 // f of columns [x*W, x*W + W) from the state and writes its inverse
 // x-transform.  One transform per block keeps register use at that of a single
 // FFT.
-__global__ void __launch_bounds__(256, 3)
-    spec_col_prep_kernel(SpecParams p, int W, int log2W, int bstride,
-                         const float2* __restrict__ w, T4 t4) {
+CFD_D void col_prep_cols(const SpecParams& p, int blk, int f, int W, int log2W, int bstride,
+                          const float2* __restrict__ w, float2* __restrict__ dst) {
   extern __shared__ float2 sbuf[];
   const int N = p.nx, ncols = p.L + 1;
-  const int c0 = blockIdx.x * W, f = blockIdx.y;
+  const int c0 = blk * W;
   const int tid = threadIdx.x;
 #pragma unroll 4
   for (int e = tid; e < W * N; e += blockDim.x) {
@@ -83,7 +82,6 @@ __global__ void __launch_bounds__(256, 3)
   }
   __syncthreads();
   fft_inplace<1>(sbuf, p.log2nx, W, bstride, p.twp_x, tid);
-  float2* dst = t4.t[f];
 #pragma unroll 4
   for (int e = tid; e < W * N; e += blockDim.x) {
     const int ww = e & (W - 1), i = e >> log2W, c = c0 + ww;
@@ -91,15 +89,20 @@ __global__ void __launch_bounds__(256, 3)
   }
 }
 
+__global__ void __launch_bounds__(256, 3)
+    spec_col_prep_kernel(SpecParams p, int W, int log2W, int bstride,
+                         const float2* __restrict__ w, T4 t4) {
+  col_prep_cols(p, blockIdx.x, blockIdx.y, W, log2W, bstride, w, t4.t[blockIdx.y]);
+}
+
 // x-transform of the advection row spectra, then one low-storage RK/CN stage
 // (or, with explicit_only, just F(u)).
-__global__ void __launch_bounds__(256, 3)
-    spec_col_update_kernel(SpecParams p, StageCoef sc, int W, int log2W,
-                           int bstride, const float2* __restrict__ ahat,
-                           float2* __restrict__ wst, float2* __restrict__ hst) {
+CFD_D void col_update_cols(const SpecParams& p, const StageCoef& sc, int blk, int W,
+                            int log2W, int bstride, const float2* __restrict__ ahat,
+                            float2* __restrict__ wst, float2* __restrict__ hst) {
   extern __shared__ float2 sbuf[];
   const int N = p.nx, ncols = p.L + 1;
-  const int c0 = blockIdx.x * W;
+  const int c0 = blk * W;
   const int tid = threadIdx.x;
 #pragma unroll 4
   for (int e = tid; e < W * N; e += blockDim.x) {
@@ -147,13 +150,20 @@ __global__ void __launch_bounds__(256, 3)
 }
 
 __global__ void __launch_bounds__(256, 3)
-    spec_row_kernel(SpecParams p, int rows, const float2* __restrict__ t0,
-                    const float2* __restrict__ t1, const float2* __restrict__ t2,
-                    const float2* __restrict__ t3, float2* __restrict__ ahat) {
+    spec_col_update_kernel(SpecParams p, StageCoef sc, int W, int log2W,
+                           int bstride, const float2* __restrict__ ahat,
+                           float2* __restrict__ wst, float2* __restrict__ hst) {
+  col_update_cols(p, sc, blockIdx.x, W, log2W, bstride, ahat, wst, hst);
+}
+
+CFD_D void row_advect_rows(const SpecParams& p, int blk, int rows,
+                            const float2* __restrict__ t0, const float2* __restrict__ t1,
+                            const float2* __restrict__ t2, const float2* __restrict__ t3,
+                            float2* __restrict__ ahat) {
   extern __shared__ float2 sbuf[];
   const int L = p.L, log2L = p.log2L, ncols = L + 1, PL = padded_len(L);
   const int half = L >> 1, log2h = log2L - 1;
-  const int i0 = blockIdx.x * rows;
+  const int i0 = blk * rows;
   const float2* tf[4] = {t0, t1, t2, t3};
   // Inverse real transforms along y: build the half-length complex inputs.
   // Pairs (k, L-k) for k in [1, L/2); the k = 0 slot also does DC/Nyquist and
@@ -212,6 +222,44 @@ __global__ void __launch_bounds__(256, 3)
       out[L - k] = xm;
     }
   }
+}
+
+__global__ void __launch_bounds__(256, 3)
+    spec_row_kernel(SpecParams p, int rows, const float2* __restrict__ t0,
+                    const float2* __restrict__ t1, const float2* __restrict__ t2,
+                    const float2* __restrict__ t3, float2* __restrict__ ahat) {
+  row_advect_rows(p, blockIdx.x, rows, t0, t1, t2, t3, ahat);
+}
+
+// ---- Batched variants: the slot index is the last grid axis ----
+// Column prep after stage `stage` of step k builds the inputs of the next
+// stage (k = -1: before the first step of the chunk).
+__global__ void __launch_bounds__(256, 3)
+    spec_batch_col_prep_kernel(const SpecMember* __restrict__ mem, int k, int stage, int W,
+                               int log2W, int bstride) {
+  const SpecMember& m = mem[blockIdx.z];
+  if (m.steps <= 0 || k >= m.steps) return;
+  if (k == m.steps - 1 && stage == m.stages - 1) return;
+  const SpecParams p = m.p;
+  col_prep_cols(p, blockIdx.x, blockIdx.y, W, log2W, bstride, m.w, m.t[blockIdx.y]);
+}
+
+__global__ void __launch_bounds__(256, 3)
+    spec_batch_row_kernel(const SpecMember* __restrict__ mem, int k, int rows) {
+  const SpecMember& m = mem[blockIdx.y];
+  if (k >= m.steps) return;
+  const SpecParams p = m.p;
+  row_advect_rows(p, blockIdx.x, rows, m.t[0], m.t[1], m.t[2], m.t[3], m.ahat);
+}
+
+__global__ void __launch_bounds__(256, 3)
+    spec_batch_col_update_kernel(const SpecMember* __restrict__ mem, int k, int stage, int W,
+                                 int log2W, int bstride) {
+  const SpecMember& m = mem[blockIdx.y];
+  if (k >= m.steps) return;
+  const SpecParams p = m.p;
+  const StageCoef sc = m.coef[stage];
+  col_update_cols(p, sc, blockIdx.x, W, log2W, bstride, m.ahat, m.w, m.h);
 }
 
 // Real rows -> unpacked half spectra (rfft along y).
@@ -455,6 +503,40 @@ cudaError_t launch_spec_curl_table(const SpecParams& p, const float2* fxh,
   size_t b = (n + 255) / 256;
   if (b > 152 * 16) b = 152 * 16;
   curl_table_kernel<<<(int)b, 256, 0, s>>>(p, fxh, fyh, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_spec_batch_prep(const SpecParams& p, const SpecMember* mem, int count,
+                                   int k, int stage, cudaStream_t s) {
+  if (count < 1 || count > 65535) return cudaErrorInvalidValue;
+  const ColCfg c = col_cfg(p);
+  cudaError_t e = set_smem(spec_batch_col_prep_kernel, c.smem);
+  if (e != cudaSuccess) return e;
+  spec_batch_col_prep_kernel<<<dim3(c.blocks, 4, count), c.threads, c.smem, s>>>(
+      mem, k, stage, c.W, c.log2W, c.bstride);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_spec_batch_row(const SpecParams& p, const SpecMember* mem, int count, int k,
+                                  cudaStream_t s) {
+  if (count < 1 || count > 65535) return cudaErrorInvalidValue;
+  const int rows = rows_per_block(p.log2L, 4, p.nx);
+  const size_t smem = (size_t)rows * 4 * padded_len(p.L) * sizeof(float2);
+  cudaError_t e = set_smem(spec_batch_row_kernel, smem);
+  if (e != cudaSuccess) return e;
+  spec_batch_row_kernel<<<dim3(p.nx / rows, count), threads_for(fft_workers(p.log2L, rows * 4)),
+                          smem, s>>>(mem, k, rows);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_spec_batch_update(const SpecParams& p, const SpecMember* mem, int count,
+                                     int k, int stage, cudaStream_t s) {
+  if (count < 1 || count > 65535) return cudaErrorInvalidValue;
+  const ColCfg c = col_cfg(p);
+  cudaError_t e = set_smem(spec_batch_col_update_kernel, c.smem);
+  if (e != cudaSuccess) return e;
+  spec_batch_col_update_kernel<<<dim3(c.blocks, count), c.threads, c.smem, s>>>(
+      mem, k, stage, c.W, c.log2W, c.bstride);
   return cudaGetLastError();
 }
 

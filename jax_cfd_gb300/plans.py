@@ -211,6 +211,27 @@ def scale_to_max_speed(u, v, vmax: torch.Tensor, maximum_velocity: float):
       float(maximum_velocity)), 'cfd_scale_to_max_speed')
 
 
+def spec_config(shape: Sequence[int], step: Sequence[float], *, viscosity: float = 0.0,
+                drag: float = 0.0, dt: float = 0.0, smooth: bool = True,
+                alphas=(0., 1.), betas=(0.,), gammas=(1.,)):
+  """The C-ABI configuration of one spectral step; returns (config, arrays the
+  config points into)."""
+  coef = [np.ascontiguousarray(c, dtype=np.float64) for c in (alphas, betas, gammas)]
+  if len(coef[0]) != len(coef[1]) + 1 or len(coef[1]) != len(coef[2]):
+    raise ValueError('number of RK coefficients does not match')
+  cfg = nat.SpecConfig()
+  cfg.nx, cfg.ny = int(shape[0]), int(shape[1])
+  cfg.hx, cfg.hy = float(step[0]), float(step[1])
+  cfg.viscosity = float(viscosity)
+  cfg.drag = float(drag)
+  cfg.dt = float(dt)
+  cfg.smooth = 1 if smooth else 0
+  cfg.num_stages = len(coef[1])
+  cfg.alphas, cfg.betas, cfg.gammas = (
+      c.ctypes.data_as(ctypes.POINTER(ctypes.c_double)) for c in coef)
+  return cfg, coef
+
+
 class SpecPlan:
   """Native plan for the pseudospectral step and the 2-D real transforms."""
 
@@ -224,17 +245,8 @@ class SpecPlan:
     self.half_shape = (self.shape[0], self.shape[1] // 2 + 1)
     self.device = torch.device(device) if device is not None else torch.device(
         'cuda', torch.cuda.current_device())
-    self._coef = [np.ascontiguousarray(c, dtype=np.float64) for c in (alphas, betas, gammas)]
-    cfg = nat.SpecConfig()
-    cfg.nx, cfg.ny = self.shape
-    cfg.hx, cfg.hy = float(step[0]), float(step[1])
-    cfg.viscosity = float(viscosity)
-    cfg.drag = float(drag)
-    cfg.dt = float(dt)
-    cfg.smooth = 1 if smooth else 0
-    cfg.num_stages = len(self._coef[1])
-    cfg.alphas, cfg.betas, cfg.gammas = (
-        c.ctypes.data_as(ctypes.POINTER(ctypes.c_double)) for c in self._coef)
+    cfg, self._coef = spec_config(self.shape, step, viscosity=viscosity, drag=drag, dt=dt,
+                                  smooth=smooth, alphas=alphas, betas=betas, gammas=gammas)
     handle = ctypes.c_void_p()
     with torch.cuda.device(self.device):
       nat.check(nat.load().cfd_spec_plan_create(ctypes.byref(cfg), ctypes.byref(handle)),
@@ -250,6 +262,10 @@ class SpecPlan:
       except Exception:  # pylint: disable=broad-except
         pass
       self._h = None
+
+  @property
+  def handle(self):
+    return self._h
 
   @property
   def nbytes(self) -> int:

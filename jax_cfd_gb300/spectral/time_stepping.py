@@ -72,11 +72,18 @@ def crank_nicolson_rk3(equation, time_step: float) -> Callable:
       gammas=[1 / 3, 15 / 16, 8 / 15], equation=equation, time_step=time_step)
 
 
+# (alphas, betas, gammas) of crank_nicolson_rk4 (time_stepping.py:186-197,
+# "Carpenter-Kennedy").
+CN_RK4_COEFFICIENTS = (
+    (0, 0.1496590219993, 0.3704009573644, 0.6222557631345, 0.9582821306748, 1),
+    (0, -0.4178904745, -1.192151694643, -1.697784692471, -1.514183444257),
+    (0.1496590219993, 0.3792103129999, 0.8229550293869, 0.6994504559488, 0.1530572479681),
+)
+
+
 def crank_nicolson_rk4(equation, time_step: float) -> Callable:
   """time_stepping.py:186-197 ("Carpenter-Kennedy")."""
+  alphas, betas, gammas = CN_RK4_COEFFICIENTS
   return low_storage_runge_kutta_crank_nicolson(
-      alphas=[0, 0.1496590219993, 0.3704009573644, 0.6222557631345, 0.9582821306748, 1],
-      betas=[0, -0.4178904745, -1.192151694643, -1.697784692471, -1.514183444257],
-      gammas=[0.1496590219993, 0.3792103129999, 0.8229550293869, 0.6994504559488,
-              0.1530572479681],
+      alphas=list(alphas), betas=list(betas), gammas=list(gammas),
       equation=equation, time_step=time_step)

@@ -179,3 +179,66 @@ def test_batch_rejects_mismatched_slot(cuda_device):
     b2.set_slot(0, **kw)  # member built for 64^2 tables: forcing length mismatch is caught
   with pytest.raises(IndexError):
     b.set_steps(5, 1)
+
+
+# ---- spectral batches --------------------------------------------------
+
+def _spec_step(n, nu, k, dt):
+  from jax_cfd_gb300.base import forcings, grids
+  from jax_cfd_gb300.spectral import equations as seq
+  from jax_cfd_gb300.spectral import time_stepping as sts
+  grid = grids.Grid((n, n), domain=((0, TWO_PI), (0, TWO_PI)))
+  eq = seq.NavierStokes2D(nu, grid, drag=0.1, smooth=True,
+                          forcing_fn=lambda g: forcings.kolmogorov_forcing(
+                              g, k=k, offsets=((0, 0), (0, 0))))
+  return sts.crank_nicolson_rk4(eq, dt)
+
+
+def _vorticity_hat(n, seed, vmax, dev):
+  import jax_cfd_gb300.base as cfd
+  from jax_cfd_gb300.spectral import utils as su
+  grid = cfd.grids.Grid((n, n), domain=((0, TWO_PI), (0, TWO_PI)))
+  v0 = cfd.initial_conditions.filtered_velocity_field(seed, grid, vmax, 4, device=dev)
+  return su.rfft2(cfd.finite_differences.curl_2d(v0).data, grid)
+
+
+@pytest.mark.parametrize('graph', [False, True])
+def test_spectral_batch_slots_equal_single_steps(cuda_device, graph):
+  from jax_cfd_gb300 import batching
+  n = 64
+  draws = [(1e-3, 4, 1e-2, 61, 2.0), (1e-4, 2, 5e-3, 62, 1.0), (1e-2, 8, 2e-2, 63, 3.0)]
+  steps = [_spec_step(n, nu, k, dt) for nu, k, dt, _, _ in draws]
+  w0 = [_vorticity_hat(n, seed, vmax, cuda_device) for _, _, _, seed, vmax in draws]
+  grid_step = steps[0].equation.grid.step
+  b = batching.SpecBatch((n, n), grid_step, len(draws), device=cuda_device)
+  for i, (st, w) in enumerate(zip(steps, w0)):
+    b.set_slot_from_step(i, st)
+    b.set_state(i, w)
+    b.set_steps(i, [5, 3, 0][i])
+  b.run(5, graph=graph)
+  torch.cuda.synchronize(cuda_device)
+  for i, (st, w) in enumerate(zip(steps, w0)):
+    want = st.gb300_repeat(w, [5, 3, 0][i])
+    assert torch.equal(torch.view_as_real(b.state(i)), torch.view_as_real(want))
+
+
+def test_spectral_member_alone_equals_in_the_mix(cuda_device):
+  from jax_cfd_gb300 import batching
+  n = 128
+  draws = [(1e-3, 4, 1e-2, 71, 2.0), (3e-4, 8, 5e-3, 72, 4.0), (5e-3, 2, 1e-2, 73, 1.5)]
+  steps = [_spec_step(n, nu, k, dt) for nu, k, dt, _, _ in draws]
+  w0 = [_vorticity_hat(n, seed, vmax, cuda_device) for _, _, _, seed, vmax in draws]
+  grid_step = steps[0].equation.grid.step
+  mix = batching.SpecBatch((n, n), grid_step, 3, device=cuda_device)
+  alone = batching.SpecBatch((n, n), grid_step, 3, device=cuda_device)
+  for i in range(3):
+    mix.set_slot_from_step(i, steps[i])
+    mix.set_state(i, w0[i])
+    mix.set_steps(i, 6)
+  alone.set_slot_from_step(2, steps[2])
+  alone.set_state(2, w0[2])
+  alone.set_steps(2, 6)
+  mix.run(6)
+  alone.run(6)
+  torch.cuda.synchronize(cuda_device)
+  assert torch.equal(torch.view_as_real(mix.state(2)), torch.view_as_real(alone.state(2)))
