@@ -138,6 +138,17 @@ int cfd_fvm_projection_noalloc(void* stream, int nx, int ny, double hx,
                                double hy, const float* u, const float* v,
                                float* u_out, float* v_out);
 
+/* Adjoint of one step (no reference C counterpart: the reference gets it from
+ * jax.grad through equations.py:120-151).  For the forward step v' = step(v)
+ * at state (u, v) and a cotangent (gu, gv) of v', writes the cotangent of v
+ * to (gu_out, gv_out) (which may alias gu, gv) and, if nu_dot is not NULL,
+ * the per-cell products w . laplacian(v) with w the projected cotangent; the
+ * derivative with respect to the viscosity is dt / density * sum(nu_dot).
+ * Uses the plan's workspace like cfd_fvm_step. */
+int cfd_fvm_adjoint_step(cfd_fvm_plan* plan, void* stream, const float* u,
+                         const float* v, const float* gu, const float* gv,
+                         float* gu_out, float* gv_out, float* nu_dot);
+
 /* ---- Batched FVM trajectories ----
  * Replaces the reference's one-trajectory-at-a-time use of
  * semi_implicit_navier_stokes + funcutils.repeated (equations.py:120-151,

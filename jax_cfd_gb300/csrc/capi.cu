@@ -938,6 +938,25 @@ int cfd_fvm_ensemble_step(cfd_fvm_ensemble* ens, void* stream, int steps, int us
   return CFD_OK;
 }
 
+int cfd_fvm_adjoint_step(cfd_fvm_plan* plan, void* stream, const float* u, const float* v,
+                         const float* gu, const float* gv, float* gu_out, float* gv_out,
+                         float* nu_dot) {
+  if (!plan || !u || !v || !gu || !gv || !gu_out || !gv_out)
+    return fail(CFD_ERR_INVALID_ARGUMENT, "cfd_fvm_adjoint_step: null pointer");
+  cudaStream_t s = as_stream(stream);
+  const cfd::FvmParams& p = plan->p;
+  // w = P g into the plan's first step buffers.
+  CFD_CHECK(cfd::launch_fvm_div_rfft(p, gu, gv, plan->spec, s), "div_rfft");
+  CFD_CHECK(cfd::launch_fvm_col_pinv(p, plan->spec, s), "col_pinv");
+  CFD_CHECK(cfd::launch_fvm_irfft(p, plan->spec, s), "irfft");
+  CFD_CHECK(cfd::launch_fvm_project_out(p, gu, gv, reinterpret_cast<const float*>(plan->spec),
+                                        plan->au, plan->av, s),
+            "project_out");
+  CFD_CHECK(cfd::launch_fvm_adjoint(p, u, v, plan->au, plan->av, gu_out, gv_out, nu_dot, s),
+            "adjoint");
+  return CFD_OK;
+}
+
 int cfd_fvm_explicit_terms(cfd_fvm_plan* plan, void* stream, const float* u,
                            const float* v, float* du, float* dv) {
   if (!plan || !u || !v || !du || !dv)

@@ -79,6 +79,12 @@ cudaError_t launch_fvm_batch_step(const FvmParams& shape, const FvmMember* membe
                                   int count, int k, cudaStream_t s);
 cudaError_t launch_fvm_batch_project_out(const FvmParams& shape, const FvmMember* members,
                                          int count, cudaStream_t s);
+// Vector-Jacobian product of one FVM step at state (u, v) for the projected
+// cotangent (wu, wv) = P g: (gu, gv) = w + dt (A^T w + nu lap w + lin w) and,
+// if nu_dot is not null, nu_dot = w . lap(v) per cell.
+cudaError_t launch_fvm_adjoint(const FvmParams& p, const float* u, const float* v,
+                               const float* wu, const float* wv, float* gu, float* gv,
+                               float* nu_dot, cudaStream_t s);
 // Diagnostics on staggered velocity fields.
 cudaError_t launch_divergence(const FvmParams& p, const float* u,
                               const float* v, float* out, cudaStream_t s);

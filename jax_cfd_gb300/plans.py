@@ -158,6 +158,18 @@ class FvmPlan:
                                         ctypes.cast(ms, ctypes.c_void_p)), 'cfd_fvm_profile')
     return dict(zip(self.PROFILE_KINDS, (float(x) for x in ms)))
 
+  def adjoint_step(self, u, v, gu, gv, want_nu: bool = True):
+    """Cotangent of the state before one step, given the cotangent (gu, gv) of
+    the state after it; with want_nu also the per-cell products whose sum
+    times dt / density is the viscosity derivative."""
+    gu_out, gv_out = torch.empty_like(gu), torch.empty_like(gv)
+    nu_dot = torch.empty_like(u) if want_nu else None
+    a = self._fields(u, v, gu, gv, gu_out, gv_out)
+    nat.check(self._lib.cfd_fvm_adjoint_step(self._h, current_stream_ptr(u.device), *a,
+                                             ptr(nu_dot) if want_nu else None),
+              'cfd_fvm_adjoint_step')
+    return gu_out, gv_out, nu_dot
+
   def explicit_terms(self, u, v):
     du, dv = torch.empty_like(u), torch.empty_like(v)
     a = self._fields(u, v, du, dv)
