@@ -388,6 +388,85 @@ def run_serving(dev, args):
   }
 
 
+def run_differentiation(dev, args):
+  """Gradient of a vorticity-matching loss through 64 FVM steps at 512^2 for
+  a batch of 8 trajectories (seeds 0-7; targets from seeds 100-107 advanced
+  64 steps), with respect to the initial velocities and the viscosity, by the
+  hand-written adjoint with a checkpoint every 8 steps; timed forward +
+  backward, and a finite-difference spot check along random directions with
+  the float32 forward (eps 1e-3)."""
+  import torch  # pylint: disable=import-outside-toplevel
+  import jax_cfd_gb300.base as cfd  # pylint: disable=import-outside-toplevel
+  from jax_cfd_gb300 import adjoint  # pylint: disable=import-outside-toplevel
+  n, batch, steps, every, nu0 = 512, 8, 64, 8, 1e-3
+  grid = cfd.grids.Grid((n, n), domain=DOMAIN)
+  dt = cfd.equations.stable_time_step(MAX_VELOCITY, CFL, nu0, grid)
+  step = cfd.equations.semi_implicit_navier_stokes(
+      1.0, nu0, dt, grid, forcing=cfd.forcings.simple_turbulence_forcing(grid, 1, 4, -0.1))
+  spec = adjoint.spec_for(step, steps, checkpoint_every=every)
+
+  def ic(seed):
+    v = cfd.initial_conditions.filtered_velocity_field(seed, grid, MAX_VELOCITY, 4, device=dev)
+    return v[0].data, v[1].data
+  init = [ic(b) for b in range(batch)]
+  u0 = torch.stack([a for a, _ in init]).contiguous()
+  v0 = torch.stack([b for _, b in init]).contiguous()
+  with torch.no_grad():
+    tgt = [ic(100 + b) for b in range(batch)]
+    tu, tv = adjoint.rollout(torch.stack([a for a, _ in tgt]), torch.stack([b for _, b in tgt]),
+                             nu0, spec)
+    target = adjoint.vorticity(tu, tv, grid.step)
+
+  def loss_fn(u, v, nu):
+    a, b = adjoint.rollout(u, v, nu, spec)
+    return ((adjoint.vorticity(a, b, grid.step) - target) ** 2).mean()
+
+  stream = torch.cuda.current_stream(dev)
+  ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+  ms = []
+  for rep in range(4):
+    u = u0.clone().requires_grad_()
+    v = v0.clone().requires_grad_()
+    nu = torch.tensor(nu0, device=dev, requires_grad=True)
+    ev[0].record(stream)
+    loss = loss_fn(u, v, nu)
+    loss.backward()
+    ev[1].record(stream)
+    torch.cuda.synchronize(dev)
+    if rep:
+      ms.append(ev[0].elapsed_time(ev[1]))
+  gu, gv, gnu = u.grad, v.grad, float(nu.grad)
+  rng = np.random.default_rng(0)
+  eps = 1e-3
+  errs = []
+  with torch.no_grad():
+    for _ in range(args.diff_directions):
+      # Directions with unit RMS per cell, so that eps perturbs every cell by
+      # about eps (a unit-norm direction over 4M cells would vanish below
+      # float32 resolution).
+      du = torch.from_numpy(rng.standard_normal(u0.shape).astype(np.float32)).to(dev)
+      dv = torch.from_numpy(rng.standard_normal(v0.shape).astype(np.float32)).to(dev)
+      fd = (float(loss_fn(u0 + eps * du, v0 + eps * dv, nu0)) -
+            float(loss_fn(u0 - eps * du, v0 - eps * dv, nu0))) / (2 * eps)
+      ad = float((gu.double() * du.double()).sum() + (gv.double() * dv.double()).sum())
+      errs.append(abs(fd - ad) / max(abs(ad), 1e-30))
+    hn = 1e-6
+    fd_nu = (float(loss_fn(u0, v0, nu0 + hn)) - float(loss_fn(u0, v0, nu0 - hn))) / (2 * hn)
+  t = float(np.median(ms)) / 1000.0
+  return {
+      'workload': f'loss = MSE(vorticity after {steps} FVM steps, target) at {n}x{n}, batch '
+                  f'{batch}; gradient wrt initial velocity and viscosity; checkpoint every {every}',
+      'forward_backward_ms': t * 1000.0,
+      'trajectory_steps_per_s': batch * steps / t,
+      'cell_steps_per_s': batch * steps * n * n / t,
+      'loss': float(loss),
+      'fd_check': {'directions': len(errs), 'eps': eps, 'direction_rms': 1.0,
+                   'max_rel_err': max(errs) if errs else None,
+                   'viscosity_rel_err': abs(gnu - fd_nu) / max(abs(fd_nu), 1e-30),
+                   'forward': 'float32 GPU'},
+  }
+
+
 def run_gb300(args):
   import torch  # pylint: disable=import-outside-toplevel
   import jax_cfd_gb300.base as cfd  # pylint: disable=import-outside-toplevel
@@ -528,6 +607,10 @@ def run_gb300(args):
   if not args.skip_ensemble:
     ensemble = run_ensemble(dev, args, flush)
 
+  differentiation = None
+  if not args.skip_diff:
+    differentiation = run_differentiation(dev, args)
+
   served = None
   if not args.skip_serving:
     served = run_serving(dev, args)
@@ -574,6 +657,7 @@ def run_gb300(args):
       'spectral': spectral,
       'ensemble': ensemble,
       'serving': served,
+      'differentiation': differentiation,
   })
 
 
@@ -597,6 +681,8 @@ def main():
   ap.add_argument('--serve-seconds', type=float, default=60.0)
   ap.add_argument('--serve-chunk', type=int, default=100)
   ap.add_argument('--serve-plain', type=int, default=150)
+  ap.add_argument('--skip-diff', action='store_true')
+  ap.add_argument('--diff-directions', type=int, default=8)
   args = ap.parse_args()
   if args.warmup < 3:
     ap.error('at least 3 warm-up steps are required')

@@ -8,6 +8,7 @@ through the native kernels, the other two as device elementwise expressions.
 from __future__ import annotations
 
 import dataclasses
+import hashlib
 from typing import Callable, Optional
 
 import numpy as np
@@ -75,10 +76,27 @@ class NavierStokes2D:
     to = lambda a: None if a is None else torch.from_numpy(np.ascontiguousarray(a, np.float32)).to(device)
     return to(fu), to(fv)
 
+  def forcing_key(self, device) -> Optional[str]:
+    """Content fingerprint of the forcing fields (part of the plan cache key:
+    equations with equal forcing share plans, and a plan is never reused for
+    a different forcing)."""
+    key = getattr(self, '_forcing_key', None)
+    if key is None:
+      fields = self.forcing_fields(device)
+      if fields is None:
+        key = 'none'
+      else:
+        h = hashlib.sha1()
+        for f in fields:
+          h.update(b'-' if f is None else f.detach().float().contiguous().cpu().numpy().tobytes())
+        key = h.hexdigest()
+      self._forcing_key = key
+    return key
+
   def _plan(self, device) -> plans.SpecPlan:
     return plans.cached(
         'spec-terms', (device, self.grid.shape, self.grid.step, float(self.viscosity),
-                       float(self.drag), self.smooth is not None, id(self)),
+                       float(self.drag), self.smooth is not None, self.forcing_key(device)),
         lambda: _make_plan(self, device, 0.0, (0., 1.), (0.,), (1.,)))
 
   def explicit_terms(self, vorticity_hat: torch.Tensor) -> torch.Tensor:

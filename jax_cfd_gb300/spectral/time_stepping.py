@@ -45,7 +45,8 @@ class SpectralStep:
     eq = self.equation
     return plans.cached(
         'spec-step', (device, eq.grid.shape, eq.grid.step, float(eq.viscosity),
-                      float(eq.drag), eq.smooth is not None, id(eq), self.time_step,
+                      float(eq.drag), eq.smooth is not None, eq.forcing_key(device),
+                      self.time_step,
                       self.coefficients),
         lambda: spectral_equations._make_plan(eq, device, self.time_step,
                                               *self.coefficients))

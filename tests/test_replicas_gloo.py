@@ -32,7 +32,7 @@ def _worker(rank, world, port, out):
 
 def test_two_rank_max_over_ranks():
   world = 2
-  with mp.Manager() as m:
+  with mp.get_context('spawn').Manager() as m:
     out = m.dict()
     mp.spawn(_worker, args=(world, _free_port(), out), nprocs=world, join=True)
     assert dict(out) == {0: 2.5, 1: 2.5}
