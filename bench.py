@@ -635,9 +635,10 @@ def run_gb300(args):
                              f'{chunk} time steps per bench step',
                  'grid': [n, n], 'time_steps_per_step': chunk, 'dt': dt,
                  'l2': 'flushed (256 MiB write) between bench steps',
-                 'transform_config': {'row_blocks': ['wide', 'narrow'][shape & 1],
-                                      'column_pass': ['blocks', 'cluster4',
-                                                      'cluster8'][shape >> 1]},
+                 'launch_config': {'row_blocks': ['wide', 'narrow'][shape & 1],
+                                   'column_pass': ['blocks', 'cluster4',
+                                                   'cluster8'][(shape >> 1) % 3],
+                                   'stencil': ['tiles', 'warp_streams'][shape // 6]},
                  'parallelism': 'replicas' if world > 1 else 'single'},
       'roofline': {'kernel': dominant, 'bound': 'hbm', 'achieved': achieved, 'peak': peak,
                    'unit': 'GB/s', 'frac': achieved / peak, 'traffic': traffic,

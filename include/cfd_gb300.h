@@ -101,14 +101,19 @@ int cfd_fvm_step(cfd_fvm_plan* plan, void* stream, const float* u,
 int cfd_fvm_profile(cfd_fvm_plan* plan, void* stream, const float* u,
                     const float* v, float* u_out, float* v_out, int steps,
                     float* ms_out);
-/* Autotuner: times `steps` steps for each candidate launch configuration of
- * the transform kernels (row block shape x column-pass scheme; u, v
+/* Autotuner: times `steps` steps for each candidate launch configuration
+ * (transform row-block shape x column-pass scheme x stencil scheme; u, v
  * read-only, results go to the scratch arrays), keeps the fastest in the plan
- * and writes its index (shape + 2 * column scheme) to *chosen (may be NULL).
- * Synchronises the stream. */
+ * and writes its index (shape + 2 * column scheme + 6 * stencil scheme, 12
+ * choices) to *chosen (may be NULL).  Synchronises the stream. */
 int cfd_fvm_plan_autotune(cfd_fvm_plan* plan, void* stream, const float* u,
                           const float* v, float* u_scratch, float* v_scratch,
                           int steps, int* chosen);
+/* Pins the launch configuration (an index as cfd_fvm_plan_autotune reports:
+ * row-transform shape + 2 * column scheme + 6 * stencil scheme); results do
+ * not depend on it.  cfd_fvm_plan_get_launch returns the current one. */
+int cfd_fvm_plan_set_launch(cfd_fvm_plan* plan, int choice);
+int cfd_fvm_plan_get_launch(const cfd_fvm_plan* plan);
 /* du/dt from advection + diffusion + forcing (no projection). */
 int cfd_fvm_explicit_terms(cfd_fvm_plan* plan, void* stream, const float* u,
                            const float* v, float* du, float* dv);

@@ -85,6 +85,20 @@ cudaError_t upload(T** dev, const T* host, size_t count) {
 
 cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
+// Launch configurations of the FVM step (see cfd_fvm_plan_autotune).
+constexpr int kLaunchChoices = 12;
+bool launch_choice_ok(const cfd::FvmParams& p, int c) {
+  const int col = (c >> 1) % 3, stencil = c / 6;
+  if (col > 0 && !cfd::col_cluster_ok(p, col == 1 ? 4 : 8)) return false;
+  if (stencil == 1 && !cfd::stream_stencil_ok(p)) return false;
+  return true;
+}
+void set_launch_choice(cfd::FvmParams* p, int c) {
+  p->fft_shape = c & 1;
+  p->col_mode = (c >> 1) % 3;
+  p->stencil = c / 6;
+}
+
 // Captures `enqueue` (run on a private capture stream) into an executable graph.
 template <typename F>
 int capture_graph(F enqueue, cudaGraph_t* graph, cudaGraphExec_t* exec) {
@@ -284,6 +298,8 @@ static int fvm_params_from_config(const cfd_fvm_config* cfg, cfd::FvmParams* out
   // Narrow transform blocks keep large grids resident in one wave; the
   // autotuner can revise the choice on the device.
   p.fft_shape = (nx >= 1024 && ny >= 1024) ? 1 : 0;
+  // The warp-streaming stencil needs enough warps to fill the GPU.
+  p.stencil = ((long long)nx * ny >= (1LL << 22) && cfd::stream_stencil_ok(p)) ? 1 : 0;
   return CFD_OK;
 }
 
@@ -511,12 +527,11 @@ int cfd_fvm_plan_autotune(cfd_fvm_plan* plan, void* stream, const float* u,
   int best = -1;
   int rc = CFD_OK;
   // Candidates: transform block shape (wide, narrow) x column pass (per-block
-  // columns, clusters of 4, clusters of 8); index = shape + 2 * col_mode.
-  for (int cand = 0; cand < 6 && rc == CFD_OK; ++cand) {
-    const int shape = cand & 1, col = cand >> 1;
-    plan->p.fft_shape = shape;
-    plan->p.col_mode = col;
-    if (col > 0 && !cfd::col_cluster_ok(plan->p, col == 1 ? 4 : 8)) continue;
+  // columns, clusters of 4, clusters of 8) x stencil (shared-memory tiles,
+  // warp streams); index = shape + 2 * col_mode + 6 * stencil.
+  for (int cand = 0; cand < kLaunchChoices && rc == CFD_OK; ++cand) {
+    if (!launch_choice_ok(plan->p, cand)) continue;
+    set_launch_choice(&plan->p, cand);
     rc = cfd_fvm_step(plan, stream, u, v, u_scratch, v_scratch, 1);
     if (rc) break;
     cudaError_t e = cudaEventRecord(e0, s);
@@ -538,10 +553,23 @@ int cfd_fvm_plan_autotune(cfd_fvm_plan* plan, void* stream, const float* u,
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (best < 0) best = 0;
-  plan->p.fft_shape = best & 1;
-  plan->p.col_mode = best >> 1;
+  set_launch_choice(&plan->p, best);
   if (chosen) *chosen = best;
   return rc;
+}
+
+int cfd_fvm_plan_set_launch(cfd_fvm_plan* plan, int choice) {
+  if (!plan || choice < 0 || choice >= kLaunchChoices)
+    return fail(CFD_ERR_INVALID_ARGUMENT, "cfd_fvm_plan_set_launch: bad arguments");
+  if (!launch_choice_ok(plan->p, choice))
+    return fail(CFD_ERR_UNSUPPORTED, "cfd_fvm_plan_set_launch: choice not available on this grid");
+  set_launch_choice(&plan->p, choice);
+  return CFD_OK;
+}
+
+int cfd_fvm_plan_get_launch(const cfd_fvm_plan* plan) {
+  if (!plan) return -1;
+  return plan->p.fft_shape + 2 * plan->p.col_mode + 6 * plan->p.stencil;
 }
 
 // ---- Same-shape batches -------------------------------------------------

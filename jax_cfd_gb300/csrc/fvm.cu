@@ -202,16 +202,62 @@ __global__ void __launch_bounds__(kStencilThreads)
 CFD_D float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
 CFD_D float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
 CFD_D float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
-CFD_D float2 sub2(float2 a, float2 b) {
-  unsigned long long r;
-  const unsigned long long x = *reinterpret_cast<unsigned long long*>(&a);
-  const unsigned long long y = *reinterpret_cast<unsigned long long*>(&b);
-  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(x), "l"(y));
-  return *reinterpret_cast<float2*>(&r);
-}
+// a - b is a + (-b) exactly (IEEE subtraction is the addition of the
+// negation), so the paired add of the negation rounds like two subtractions.
+CFD_D float2 sub2(float2 a, float2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
 CFD_D float2 splat2(float a) { return make_float2(a, a); }
 CFD_D float2 sel2(bool px, bool py, float2 a, float2 b) {
   return make_float2(px ? a.x : b.x, py ? a.y : b.y);
+}
+
+// Viscosity and forcing of one cell, added to the paired explicit terms kk:
+// kk + nu lap(u) then + sum_forcings(linear, constant) / density, in the
+// reference's order (equations.py:102-110, forcings.py:125-178).  FORCE = 1
+// is the configuration of simple_turbulence_forcing (viscosity, linear drag
+// and a u-forcing over y, density 1) with its flags resolved at compile time;
+// FORCE = 0 reads them at run time.  Both evaluate the same expressions.
+template <int FORCE>
+CFD_D float2 add_diffusion_forcing(const FvmParams& p, float2 kk, float2 uv, float2 lx,
+                                   float2 ly, int i, int j) {
+  if (FORCE == 1 || p.has_visc) {
+    // finite_differences.laplacian: -2c * sum(scales) + pairs * scale
+    const float2 m2 = mul2(splat2(-2.f), uv);
+    float2 lap = fma2(lx, splat2(p.sx), mul2(m2, splat2(p.ssum)));
+    lap = fma2(ly, splat2(p.sy), lap);
+    kk = fma2(splat2(p.nu), lap, kk);
+  }
+  if (FORCE == 1) {
+    const float fu = p.lin * uv.x + __ldg(p.fu_y + j);
+    const float fv = p.lin * uv.y;
+    return make_float2(kk.x + fu, kk.y + fv);
+  }
+  if (p.has_forcing) {
+    const size_t ny = (size_t)p.ny;
+    float fu = 0.f, fv = 0.f;
+    bool any_u = false, any_v = false;
+    if (p.has_lin) {
+      fu = p.lin * uv.x;
+      fv = p.lin * uv.y;
+      any_u = any_v = true;
+    }
+    if (p.fu_y) { fu = any_u ? fu + __ldg(p.fu_y + j) : __ldg(p.fu_y + j); any_u = true; }
+    if (p.fv_x) { fv = any_v ? fv + __ldg(p.fv_x + i) : __ldg(p.fv_x + i); any_v = true; }
+    if (p.fu_full) { const float f = __ldg(p.fu_full + i * ny + j); fu = any_u ? fu + f : f; any_u = true; }
+    if (p.fv_full) { const float f = __ldg(p.fv_full + i * ny + j); fv = any_v ? fv + f : f; any_v = true; }
+    if (!p.rho_is_one) {
+      fu = fu / p.density;
+      fv = fv / p.density;
+    }
+    if (any_u) kk.x = kk.x + fu;
+    if (any_v) kk.y = kk.y + fv;
+  }
+  return kk;
+}
+
+// Whether FORCE = 1 applies.
+CFD_HD bool kolmogorov_config(const FvmParams& p) {
+  return p.has_visc && p.has_forcing && p.has_lin && p.fu_y && !p.fv_x && !p.fu_full &&
+         !p.fv_full && p.rho_is_one;
 }
 
 // Van Leer face values of two faces at once (tvd_flux in paired arithmetic).
@@ -241,7 +287,7 @@ CFD_D float2 tvd_flux2(float2 cm, float2 c0, float2 c1, float2 c2, float2 U,
 // u- and v-control volumes together, into paired shared arrays; each thread
 // then updates 4 cells of one column.
 constexpr int kBoxW = kTJ + 8;  // 72 columns: j0-4 .. j0+67
-template <bool PROJECT, bool OUT_K0, int CONVECT>
+template <bool PROJECT, bool OUT_K0, int CONVECT, int FORCE = 0>
 CFD_D void explicit_tile(const FvmParams& p, int bx, int by,
                          const float* __restrict__ ua, const float* __restrict__ va,
                          const float* __restrict__ q, float* __restrict__ uo,
@@ -352,35 +398,8 @@ CFD_D void explicit_tile(const FvmParams& p, int bx, int by,
     const float2 dx = mul2(sub2(fxg[a + 1][b], fxg[a][b]), ihx);
     float2 kk = fma2(sub2(fyg[a][b + 1], fyg[a][b]), ihy, dx);
     kk = make_float2(-kk.x, -kk.y);
-    if (p.has_visc) {
-      // finite_differences.laplacian: -2c * sum(scales) + pairs * scale
-      const float2 lx = add2(sw[r - 1][c], sw[r + 1][c]);
-      const float2 ly = add2(sw[r][c - 1], sw[r][c + 1]);
-      const float2 m2 = mul2(splat2(-2.f), uv);
-      float2 lap = fma2(lx, splat2(p.sx), mul2(m2, splat2(p.ssum)));
-      lap = fma2(ly, splat2(p.sy), lap);
-      kk = fma2(splat2(p.nu), lap, kk);
-    }
-    if (p.has_forcing) {
-      // sum_forcings(linear, constant): (0 + lin * u) + const
-      float fu = 0.f, fv = 0.f;
-      bool any_u = false, any_v = false;
-      if (p.has_lin) {
-        fu = p.lin * uv.x;
-        fv = p.lin * uv.y;
-        any_u = any_v = true;
-      }
-      if (p.fu_y) { fu = any_u ? fu + __ldg(p.fu_y + j) : __ldg(p.fu_y + j); any_u = true; }
-      if (p.fv_x) { fv = any_v ? fv + __ldg(p.fv_x + i) : __ldg(p.fv_x + i); any_v = true; }
-      if (p.fu_full) { const float f = __ldg(p.fu_full + i * ny + j); fu = any_u ? fu + f : f; any_u = true; }
-      if (p.fv_full) { const float f = __ldg(p.fv_full + i * ny + j); fv = any_v ? fv + f : f; any_v = true; }
-      if (!p.rho_is_one) {
-        fu = fu / p.density;
-        fv = fv / p.density;
-      }
-      if (any_u) kk.x = kk.x + fu;
-      if (any_v) kk.y = kk.y + fv;
-    }
+    kk = add_diffusion_forcing<FORCE>(p, kk, uv, add2(sw[r - 1][c], sw[r + 1][c]),
+                                      add2(sw[r][c - 1], sw[r][c + 1]), i, j);
     if (OUT_K0) {
       uo[i * ny + j] = kk.x;
       vo[i * ny + j] = kk.y;
@@ -392,14 +411,162 @@ CFD_D void explicit_tile(const FvmParams& p, int bx, int by,
   }
 }
 
-template <bool PROJECT, bool OUT_K0, int CONVECT>
+template <bool PROJECT, bool OUT_K0, int CONVECT, int FORCE>
 __global__ void __launch_bounds__(kStencilThreads)
     fvm_explicit_tiled_kernel(FvmParams p, const float* __restrict__ ua,
                               const float* __restrict__ va,
                               const float* __restrict__ q,
                               float* __restrict__ uo, float* __restrict__ vo) {
-  explicit_tile<PROJECT, OUT_K0, CONVECT>(p, blockIdx.x, blockIdx.y, ua, va, q, uo, vo);
+  explicit_tile<PROJECT, OUT_K0, CONVECT, FORCE>(p, blockIdx.x, blockIdx.y, ua, va, q, uo,
+                                                 vo);
 }
+
+// ---- Warp-streaming stencil ------------------------------------------------
+// The same step as explicit_tile with no shared memory and no block barrier:
+// a warp owns a strip of kSW = 28 output columns and walks down kSH = 32 rows.
+// Lane L holds column j0 - 2 + L; lanes 2..29 produce output, lanes 0, 1, 30,
+// 31 are the strip's halo.  Along x (rows) each lane keeps a five-row window
+// of projected (u, v) in registers and carries the previous x-face flux; along
+// y the neighbours' values and the left y-face flux come from warp shuffles.
+// Every expression is the one explicit_tile evaluates, in the same order, so
+// the two kernels produce identical bits.
+constexpr int kSW = 28;
+constexpr int kSH = 32;
+constexpr unsigned kFull = 0xffffffffu;
+
+CFD_D float2 shfl_down2(float2 x, int d) {
+  return make_float2(__shfl_down_sync(kFull, x.x, d), __shfl_down_sync(kFull, x.y, d));
+}
+CFD_D float2 shfl_up2(float2 x, int d) {
+  return make_float2(__shfl_up_sync(kFull, x.x, d), __shfl_up_sync(kFull, x.y, d));
+}
+
+// x-face flux pair (F, G) after row a: window rows a-1, a, a+1, a+2 and u at
+// (a, j + 1) for v's control volume.
+template <int CONVECT>
+CFD_D float2 stream_xface(const FvmParams& p, float2 cm, float2 c0, float2 c1, float2 c2,
+                          float uy1) {
+  const float2 U = mul2(splat2(0.5f), add2(splat2(c0.x), make_float2(c1.x, uy1)));
+  if (CONVECT == 0) return tvd_flux2(cm, c0, c1, c2, U, p.cfl_x);
+  const float2 cface = mul2(splat2(0.5f), add2(c0, c1));
+  return mul2(make_float2(U.x, cface.y), make_float2(U.x, U.y));
+}
+
+// Raw row data of one lane: u*, v*, q and q one column to the right.
+struct StreamRaw {
+  float u, v, q, qy;
+};
+
+template <bool PROJECT>
+CFD_D StreamRaw stream_fetch(const FvmParams& p, const float* __restrict__ ua,
+                             const float* __restrict__ va, const float* __restrict__ q,
+                             int row, int j, int j1) {
+  const size_t ny = (size_t)p.ny;
+  const size_t base = (size_t)(row & (p.nx - 1)) * ny;
+  StreamRaw r;
+  r.u = __ldg(ua + base + j);
+  r.v = __ldg(va + base + j);
+  r.q = PROJECT ? __ldg(q + base + j) : 0.f;
+  r.qy = PROJECT ? __ldg(q + base + j1) : 0.f;
+  return r;
+}
+
+// u = u* - (q[i+1] - q[i]) / hx ; v = v* - (q[j+1] - q[j]) / hy, as
+// explicit_tile evaluates it; q_next is q one row down.
+template <bool PROJECT>
+CFD_D float2 stream_project(const FvmParams& p, const StreamRaw& r, float q_next) {
+  if (!PROJECT) return make_float2(r.u, r.v);
+  return make_float2(r.u - (q_next - r.q) * p.inv_hx, r.v - (r.qy - r.q) * p.inv_hy);
+}
+
+template <bool PROJECT, int CONVECT, int FORCE>
+CFD_D void stream_row(const FvmParams& p, int i, int j, bool out, float2& w1, float2& w2,
+                      float2& w3, const float2 w4, float2& fx_prev, float* __restrict__ uo,
+                      float* __restrict__ vo) {
+  const size_t ny = (size_t)p.ny;
+  const float2 ihx = splat2(p.inv_hx), ihy = splat2(p.inv_hy);
+  // x-face after row i.
+  const float2 fx = stream_xface<CONVECT>(p, w1, w2, w3, w4, __shfl_down_sync(kFull, w2.x, 1));
+  // y-face after column j in row i: stencil columns j-1 .. j+2.
+  const float2 cm = shfl_up2(w2, 1), c1 = shfl_down2(w2, 1), c2 = shfl_down2(w2, 2);
+  const float2 V = mul2(splat2(0.5f), add2(splat2(w2.y), make_float2(w3.y, c1.y)));
+  float2 fy;
+  if (CONVECT == 0) {
+    fy = tvd_flux2(cm, w2, c1, c2, V, p.cfl_y);
+  } else {
+    const float2 cface = mul2(splat2(0.5f), add2(w2, c1));
+    fy = mul2(make_float2(cface.x, V.y), make_float2(V.x, V.y));
+  }
+  const float2 fy_left = shfl_up2(fy, 1);
+  if (out) {
+    const float2 uv = w2;
+    const float2 dx = mul2(sub2(fx, fx_prev), ihx);
+    float2 kk = fma2(sub2(fy, fy_left), ihy, dx);
+    kk = make_float2(-kk.x, -kk.y);
+    kk = add_diffusion_forcing<FORCE>(p, kk, uv, add2(w1, w3), add2(cm, c1), i, j);
+    const float2 nxt = fma2(splat2(p.dt), kk, uv);
+    uo[(size_t)i * ny + j] = nxt.x;
+    vo[(size_t)i * ny + j] = nxt.y;
+  }
+  fx_prev = fx;
+  w1 = w2;
+  w2 = w3;
+  w3 = w4;
+}
+
+// Rows are fetched four ahead of their use (a ring of raw rows in registers)
+// so that each warp keeps several row loads in flight.
+template <bool PROJECT, int CONVECT, int FORCE>
+__global__ void __launch_bounds__(128)
+    fvm_explicit_stream_kernel(FvmParams p, const float* __restrict__ ua,
+                               const float* __restrict__ va, const float* __restrict__ q,
+                               float* __restrict__ uo, float* __restrict__ vo) {
+  const int lane = threadIdx.x & 31;
+  const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int strips = (p.ny + kSW - 1) / kSW;
+  const int s = warp % strips, t = warp / strips;
+  const int r0 = t * kSH;
+  if (r0 >= p.nx) return;  // uniform per warp
+  const int my = p.ny - 1;
+  const int jl = s * kSW - 2 + lane;  // unwrapped column of this lane
+  const int j = jl & my, j1 = (jl + 1) & my;
+  const bool out = lane >= 2 && lane < 30 && jl < p.ny;
+
+  // Window rows r0-2 .. r0+1 (projected), then the ring of raw rows r0+2 .. r0+5.
+  StreamRaw ring0 = stream_fetch<PROJECT>(p, ua, va, q, r0 - 2, j, j1);
+  StreamRaw ring1 = stream_fetch<PROJECT>(p, ua, va, q, r0 - 1, j, j1);
+  StreamRaw ring2 = stream_fetch<PROJECT>(p, ua, va, q, r0, j, j1);
+  StreamRaw ring3 = stream_fetch<PROJECT>(p, ua, va, q, r0 + 1, j, j1);
+  StreamRaw nxt0 = stream_fetch<PROJECT>(p, ua, va, q, r0 + 2, j, j1);
+  const float2 w0 = stream_project<PROJECT>(p, ring0, ring1.q);
+  float2 w1 = stream_project<PROJECT>(p, ring1, ring2.q);
+  float2 w2 = stream_project<PROJECT>(p, ring2, ring3.q);
+  float2 w3 = stream_project<PROJECT>(p, ring3, nxt0.q);
+  ring0 = nxt0;
+  ring1 = stream_fetch<PROJECT>(p, ua, va, q, r0 + 3, j, j1);
+  ring2 = stream_fetch<PROJECT>(p, ua, va, q, r0 + 4, j, j1);
+  ring3 = stream_fetch<PROJECT>(p, ua, va, q, r0 + 5, j, j1);
+  float2 fx_prev = stream_xface<CONVECT>(p, w0, w1, w2, w3, __shfl_down_sync(kFull, w1.x, 1));
+  // Iteration for row i projects row i + 2 (ring slot i % 4, q from the next
+  // slot) and refills that slot with row i + 6.
+#define CFD_STREAM_ROW(K, KN)                                                          \
+  {                                                                                    \
+    const int i = r0 + a + K;                                                          \
+    const float2 w4 = stream_project<PROJECT>(p, ring##K, ring##KN.q);                 \
+    ring##K = stream_fetch<PROJECT>(p, ua, va, q, i + 6, j, j1);                       \
+    stream_row<PROJECT, CONVECT, FORCE>(p, i, j, out, w1, w2, w3, w4, fx_prev, uo, vo); \
+  }
+#pragma unroll 1
+  for (int a = 0; a < kSH; a += 4) {
+    CFD_STREAM_ROW(0, 1)
+    CFD_STREAM_ROW(1, 2)
+    CFD_STREAM_ROW(2, 3)
+    CFD_STREAM_ROW(3, 0)
+  }
+#undef CFD_STREAM_ROW
+}
+
+bool stream_ok(const FvmParams& p) { return p.ny >= 64 && p.nx % kSH == 0; }
 
 // Backward-difference divergence of (u*, v*) (finite_differences.py:95-143)
 // followed by the packed real FFT of each row along y.  Shared memory holds
@@ -799,20 +966,36 @@ cudaError_t set_smem(K kernel, size_t bytes) {
 
 }  // namespace
 
+template <bool PR, bool K0, int CV, int FO>
+static void launch_explicit_variant(const FvmParams& p, bool stream, bool tiled, dim3 grid,
+                                    const float* ua, const float* va, const float* q,
+                                    float* uo, float* vo, cudaStream_t s) {
+  if (stream) {
+    const long long warps = (long long)((p.ny + kSW - 1) / kSW) * ((p.nx + kSH - 1) / kSH);
+    fvm_explicit_stream_kernel<PR, CV, FO><<<(int)((warps + 3) / 4), 128, 0, s>>>(p, ua, va, q,
+                                                                                  uo, vo);
+  } else if (tiled) {
+    fvm_explicit_tiled_kernel<PR, K0, CV, FO><<<grid, kStencilThreads, 0, s>>>(p, ua, va, q, uo,
+                                                                               vo);
+  } else {
+    fvm_explicit_kernel<PR, K0, CV><<<grid, kStencilThreads, 0, s>>>(p, ua, va, q, uo, vo);
+  }
+}
+
 cudaError_t launch_fvm_explicit(const FvmParams& p, bool project, bool out_k0,
                                 const float* ua, const float* va,
                                 const float* q, float* uo, float* vo,
                                 cudaStream_t s) {
+  const bool stream = p.stencil == 1 && !out_k0 && stream_ok(p);
   const bool tiled = p.nx % kTI == 0 && p.ny % kTJ == 0;
   const int ti = tiled ? kTI : (p.nx < kTI ? p.nx : kTI);
   const int tj = tiled ? kTJ : (p.ny < kTJ ? p.ny : kTJ);
-  dim3 grid(p.ny / tj, p.nx / ti);
-#define CFD_EXPLICIT(PR, K0, CV)                                                         \
-  do {                                                                                   \
-    if (tiled)                                                                           \
-      fvm_explicit_tiled_kernel<PR, K0, CV><<<grid, kStencilThreads, 0, s>>>(p, ua, va, q, uo, vo); \
-    else                                                                                 \
-      fvm_explicit_kernel<PR, K0, CV><<<grid, kStencilThreads, 0, s>>>(p, ua, va, q, uo, vo);       \
+  const dim3 grid(p.ny / tj, p.nx / ti);
+  const bool ko = kolmogorov_config(p) && !out_k0;
+#define CFD_EXPLICIT(PR, K0, CV)                                                          \
+  do {                                                                                    \
+    if (ko) launch_explicit_variant<PR, K0, CV, 1>(p, stream, tiled, grid, ua, va, q, uo, vo, s); \
+    else launch_explicit_variant<PR, K0, CV, 0>(p, stream, tiled, grid, ua, va, q, uo, vo, s);    \
   } while (0)
   if (p.convect == 0) {
     if (project) {
@@ -949,6 +1132,8 @@ cudaError_t launch_max_speed(int n, const float* u, const float* v,
   max_speed_kernel<<<elementwise_blocks((size_t)n), 256, 0, s>>>(n, u, v, out_bits);
   return cudaGetLastError();
 }
+
+bool stream_stencil_ok(const FvmParams& p) { return stream_ok(p); }
 
 bool fvm_batch_shape_ok(const FvmParams& p) {
   return p.nx % kTI == 0 && p.ny % kTJ == 0;

@@ -42,6 +42,7 @@ struct FvmParams {
   const float2* twp_y;  // pass twiddle tables of the length-ny/2 row FFT
   int fft_shape;       // transform block shape: 0 wide, 1 narrow (see fvm.cu)
   int col_mode;        // column pass: 0 per-block columns, 1/2 clusters of 4/8
+  int stencil;         // explicit step: 0 shared-memory tiles, 1 warp streams
 };
 
 // One slot of a same-shape batch of FVM trajectories (device-resident table
@@ -65,6 +66,8 @@ cudaError_t launch_fvm_col_pinv(const FvmParams& p, float2* spec,
                                 cudaStream_t s);
 // Whether the cluster column pass (col_mode 1/2) applies to this grid.
 bool col_cluster_ok(const FvmParams& p, int cluster);
+// Whether the warp-streaming stencil (stencil 1) applies to this grid.
+bool stream_stencil_ok(const FvmParams& p);
 cudaError_t launch_fvm_irfft(const FvmParams& p, float2* spec, cudaStream_t s);
 cudaError_t launch_fvm_project_out(const FvmParams& p, const float* us,
                                    const float* vs, const float* q, float* uo,

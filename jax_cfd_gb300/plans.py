@@ -146,6 +146,16 @@ class FvmPlan:
               'cfd_fvm_plan_autotune')
     return int(chosen.value)
 
+  LAUNCH_CHOICES = 12
+
+  def set_launch(self, choice: int):
+    """Pins the launch configuration (see autotune); results do not change."""
+    nat.check(self._lib.cfd_fvm_plan_set_launch(self._h, int(choice)), 'cfd_fvm_plan_set_launch')
+
+  @property
+  def launch(self) -> int:
+    return int(self._lib.cfd_fvm_plan_get_launch(self._h))
+
   PROFILE_KINDS = ('explicit', 'div_rfft', 'col_pinv', 'irfft', 'project_out')
 
   def profile(self, u, v, steps: int):
