@@ -83,6 +83,10 @@ typedef struct cfd_fvm_config {
 typedef struct cfd_fvm_plan cfd_fvm_plan;
 
 const char* cfd_last_error(void);
+/* Device-side fault word: non-zero after a kernel's bounded wait on an
+ * asynchronous copy ran out (1 = bulk-copy wait); the kernel then skipped its
+ * work instead of spinning.  clear != 0 resets it.  Synchronous. */
+int cfd_device_fault(unsigned int* code, int clear);
 int cfd_version(void);
 
 int cfd_fvm_plan_create(const cfd_fvm_config* cfg, cfd_fvm_plan** plan);
@@ -102,16 +106,17 @@ int cfd_fvm_profile(cfd_fvm_plan* plan, void* stream, const float* u,
                     const float* v, float* u_out, float* v_out, int steps,
                     float* ms_out);
 /* Autotuner: times `steps` steps for each candidate launch configuration
- * (transform row-block shape x column-pass scheme x stencil scheme; u, v
- * read-only, results go to the scratch arrays), keeps the fastest in the plan
- * and writes its index (shape + 2 * column scheme + 6 * stencil scheme, 12
- * choices) to *chosen (may be NULL).  Synchronises the stream. */
+ * (transform row-block shape x column-pass scheme x stencil scheme x row
+ * feed; u, v read-only, results go to the scratch arrays), keeps the fastest
+ * in the plan and writes its index (see cfd_fvm_plan_set_launch) to *chosen
+ * (may be NULL).  Synchronises the stream. */
 int cfd_fvm_plan_autotune(cfd_fvm_plan* plan, void* stream, const float* u,
                           const float* v, float* u_scratch, float* v_scratch,
                           int steps, int* chosen);
 /* Pins the launch configuration (an index as cfd_fvm_plan_autotune reports:
- * row-transform shape + 2 * column scheme + 6 * stencil scheme); results do
- * not depend on it.  cfd_fvm_plan_get_launch returns the current one. */
+ * row-transform shape + 2 * column scheme + 6 * stencil scheme + 12 * row
+ * feed, 24 choices); results do not depend on it.  cfd_fvm_plan_get_launch
+ * returns the current one. */
 int cfd_fvm_plan_set_launch(cfd_fvm_plan* plan, int choice);
 int cfd_fvm_plan_get_launch(const cfd_fvm_plan* plan);
 /* du/dt from advection + diffusion + forcing (no projection). */

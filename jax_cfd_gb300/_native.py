@@ -76,6 +76,7 @@ _SIGNATURES = {
     'cfd_fvm_curl_2d': (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp]),
     'cfd_fvm_projection_noalloc': (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                                    ctypes.c_double, _vp, _vp, _vp, _vp]),
+    'cfd_device_fault': (ctypes.c_int, [ctypes.POINTER(ctypes.c_uint), ctypes.c_int]),
     'cfd_fvm_plan_set_launch': (ctypes.c_int, [_vp, ctypes.c_int]),
     'cfd_fvm_plan_get_launch': (ctypes.c_int, [_vp]),
     'cfd_fvm_adjoint_step': (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),

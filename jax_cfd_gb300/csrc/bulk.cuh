@@ -1,0 +1,77 @@
+// Bulk asynchronous copies (the TMA's untiled cp.async.bulk) into shared
+// memory with mbarrier completion, and bounded waits.
+//
+// Every wait on an mbarrier gives up after kBulkWaitLimit polls: the kernel
+// then records the failure in g_cfd_device_fault (read by
+// cfd_device_fault()), waits once more, with the same limit, for the copies it
+// issued, and leaves without using the data.  Nothing spins without bound.
+#pragma once
+
+#include <stdint.h>
+
+#include "common.cuh"
+
+namespace cfd {
+
+// Non-zero after a bounded wait ran out (the code of the first failure).  One
+// word per translation unit that includes this header (the library reads the
+// one of the unit that launches bulk-copy kernels).
+static __device__ unsigned int g_cfd_device_fault = 0;
+constexpr unsigned int kFaultBulkWait = 1;
+constexpr int kBulkWaitLimit = 1 << 22;
+
+CFD_D uint32_t smem_addr(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+CFD_D void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count)
+               : "memory");
+}
+
+// Makes the initialised barrier visible to the async (TMA) proxy.
+CFD_D void mbar_fence_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// One arrival that also announces `bytes` of expected transactions.
+CFD_D void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+// Global -> shared bulk copy; `bytes` and both addresses are multiples of 16.
+CFD_D void bulk_load(void* dst_smem, const void* src_global, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+          "r"(smem_addr(dst_smem)),
+      "l"(src_global), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+
+CFD_D bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(done)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+
+// Bounded wait for phase `parity`; false if the limit ran out (recorded).
+CFD_D bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  for (int k = 0; k < kBulkWaitLimit; ++k)
+    if (mbar_try_wait(bar, parity)) return true;
+  atomicCAS(&g_cfd_device_fault, 0u, kFaultBulkWait);
+  // Give the copies in flight one more bounded chance to land before the
+  // block leaves (their destination is this block's shared memory).
+  for (int k = 0; k < kBulkWaitLimit; ++k)
+    if (mbar_try_wait(bar, parity)) break;
+  return false;
+}
+
+}  // namespace cfd

@@ -86,17 +86,21 @@ cudaError_t upload(T** dev, const T* host, size_t count) {
 cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
 // Launch configurations of the FVM step (see cfd_fvm_plan_autotune).
-constexpr int kLaunchChoices = 12;
+// Index = row-transform shape + 2 * column scheme + 6 * stencil scheme
+// + 12 * row feed.
+constexpr int kLaunchChoices = 24;
 bool launch_choice_ok(const cfd::FvmParams& p, int c) {
-  const int col = (c >> 1) % 3, stencil = c / 6;
+  const int col = (c >> 1) % 3, stencil = (c / 6) & 1, feed = c / 12;
   if (col > 0 && !cfd::col_cluster_ok(p, col == 1 ? 4 : 8)) return false;
   if (stencil == 1 && !cfd::stream_stencil_ok(p)) return false;
+  if (feed == 1 && !cfd::bulk_feed_ok(p)) return false;
   return true;
 }
 void set_launch_choice(cfd::FvmParams* p, int c) {
   p->fft_shape = c & 1;
   p->col_mode = (c >> 1) % 3;
-  p->stencil = c / 6;
+  p->stencil = (c / 6) & 1;
+  p->row_feed = c / 12;
 }
 
 // Captures `enqueue` (run on a private capture stream) into an executable graph.
@@ -237,6 +241,12 @@ struct cfd_spec_plan {
 extern "C" {
 
 const char* cfd_last_error(void) { return g_last_error.c_str(); }
+
+int cfd_device_fault(unsigned int* code, int clear) {
+  if (!code) return fail(CFD_ERR_INVALID_ARGUMENT, "cfd_device_fault: null pointer");
+  CFD_CHECK(cfd::read_device_fault(code, clear != 0), "cfd_device_fault");
+  return CFD_OK;
+}
 
 int cfd_version(void) { return 1; }
 
@@ -569,7 +579,8 @@ int cfd_fvm_plan_set_launch(cfd_fvm_plan* plan, int choice) {
 
 int cfd_fvm_plan_get_launch(const cfd_fvm_plan* plan) {
   if (!plan) return -1;
-  return plan->p.fft_shape + 2 * plan->p.col_mode + 6 * plan->p.stencil;
+  return plan->p.fft_shape + 2 * plan->p.col_mode + 6 * plan->p.stencil +
+         12 * plan->p.row_feed;
 }
 
 // ---- Same-shape batches -------------------------------------------------

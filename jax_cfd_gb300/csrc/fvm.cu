@@ -16,6 +16,7 @@
 // of that packed column is untangled with the two-real-signals identity.
 #include <cooperative_groups.h>
 
+#include "bulk.cuh"
 #include "fft.cuh"
 #include "kernels.h"
 
@@ -634,6 +635,87 @@ __global__ void __launch_bounds__(MAXT, MINB)
   div_rfft_rows(p, blockIdx.x, rows, us, vs, spec);
 }
 
+// The same transform with the input rows staged by bulk copies: one thread
+// requests u rows i0-1 .. i0+R-1 and v rows i0 .. i0+R-1 straight into shared
+// memory (no registers hold data in flight), every thread waits on the
+// mbarrier, and the divergence is formed from shared memory.  Shared memory:
+// (2R + 1) rows of floats, then R padded FFT rows, then the barrier.
+CFD_HD size_t div_rfft_bulk_smem(int ny, int rows) {
+  return (size_t)(2 * rows + 1) * ny * 4 + (size_t)rows * padded_len(ny / 2) * 8 + 16;
+}
+
+CFD_D void div_rfft_rows_bulk(const FvmParams& p, int blk, int rows,
+                              const float* __restrict__ us, const float* __restrict__ vs,
+                              float2* __restrict__ spec) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int ny = p.ny, L = ny >> 1, log2L = p.log2ny - 1, PL = padded_len(L);
+  float* su = reinterpret_cast<float*>(smem_raw);
+  float* sv = su + (size_t)(rows + 1) * ny;
+  float2* sbuf = reinterpret_cast<float2*>(sv + (size_t)rows * ny);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sbuf + (size_t)rows * PL);
+  const int i0 = blk * rows, mx = p.nx - 1, my = ny - 1;
+  const uint32_t rb = (uint32_t)ny * 4u;
+  if (threadIdx.x == 0) {
+    mbar_init(bar, 1);
+    mbar_fence_init();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    mbar_arrive_expect_tx(bar, (uint32_t)(2 * rows + 1) * rb);
+    bulk_load(su, us + (size_t)((i0 - 1) & mx) * ny, rb, bar);
+    bulk_load(su + ny, us + (size_t)i0 * ny, (uint32_t)rows * rb, bar);
+    bulk_load(sv, vs + (size_t)i0 * ny, (uint32_t)rows * rb, bar);
+  }
+  const bool ok = mbar_wait(bar, 0);
+  if (__syncthreads_or(!ok)) return;
+  const int log2g = p.log2ny - 2;  // float4 groups per row
+  const int groups = rows << log2g;
+  for (int g = threadIdx.x; g < groups; g += blockDim.x) {
+    const int r = g >> log2g, jj = (g & ((1 << log2g) - 1)) << 2;
+    const float4 a = *reinterpret_cast<const float4*>(su + (size_t)(r + 1) * ny + jj);
+    const float4 b = *reinterpret_cast<const float4*>(su + (size_t)r * ny + jj);
+    const float4 c = *reinterpret_cast<const float4*>(sv + (size_t)r * ny + jj);
+    const float cm = sv[(size_t)r * ny + ((jj - 1) & my)];
+    // D = (u - u[i-1]) / hx + (v - v[j-1]) / hy
+    const float d0 = (a.x - b.x) * p.inv_hx + (c.x - cm) * p.inv_hy;
+    const float d1 = (a.y - b.y) * p.inv_hx + (c.y - c.x) * p.inv_hy;
+    const float d2 = (a.z - b.z) * p.inv_hx + (c.z - c.y) * p.inv_hy;
+    const float d3 = (a.w - b.w) * p.inv_hx + (c.w - c.z) * p.inv_hy;
+    const int n = jj >> 1;
+    float2* z = sbuf + r * PL;
+    z[pidx(n)] = make_float2(d0, d1);
+    z[pidx(n + 1)] = make_float2(d2, d3);
+  }
+  __syncthreads();
+  fft_inplace<-1>(sbuf, log2L, rows, PL, p.twp_y, threadIdx.x);
+  const int half = L >> 1, log2h = log2L - 1;
+  for (int idx = threadIdx.x; idx < (rows << log2h); idx += blockDim.x) {
+    const int r = idx >> log2h, k = idx & (half - 1);
+    float2* out = spec + (size_t)(i0 + r) * L;
+    const float2* z = sbuf + r * PL;
+    if (k == 0) {
+      const float2 z0 = z[0];
+      out[0] = make_float2(z0.x + z0.y, z0.x - z0.y);
+      float2 xk, xm;
+      const float2 zh = z[pidx(half)];
+      rfft_post_pair(zh, zh, __ldg(p.tw_y + half), &xk, &xm);
+      out[half] = xk;
+    } else {
+      float2 xk, xm;
+      rfft_post_pair(z[pidx(k)], z[pidx(L - k)], __ldg(p.tw_y + k), &xk, &xm);
+      out[k] = xk;
+      out[L - k] = xm;
+    }
+  }
+}
+
+template <int MAXT, int MINB>
+__global__ void __launch_bounds__(MAXT, MINB)
+    fvm_div_rfft_bulk_kernel(FvmParams p, int rows, const float* __restrict__ us,
+                             const float* __restrict__ vs, float2* __restrict__ spec) {
+  div_rfft_rows_bulk(p, blockIdx.x, rows, us, vs, spec);
+}
+
 // Pseudoinverse of the periodic Laplacian in the rfft basis
 // (fast_diagonalization.py:199-266): 1/lambda where |lambda| > cutoff, else 0,
 // with irfftn's 1/(nx*ny) folded in (a power of two, so exact).
@@ -802,6 +884,66 @@ template <int MAXT, int MINB>
 __global__ void __launch_bounds__(MAXT, MINB)
     fvm_irfft_kernel(FvmParams p, int rows, float2* spec) {
   irfft_rows(p, blockIdx.x, rows, spec);
+}
+
+// The inverse transform with its R spectrum rows staged by one bulk copy.
+// Shared memory: R input rows (L complex each), R padded FFT rows, barrier.
+CFD_HD size_t irfft_bulk_smem(int ny, int rows) {
+  return (size_t)rows * (ny / 2) * 8 + (size_t)rows * padded_len(ny / 2) * 8 + 16;
+}
+
+CFD_D void irfft_rows_bulk(const FvmParams& p, int blk, int rows, float2* spec) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int L = p.ny >> 1, log2L = p.log2ny - 1, PL = padded_len(L);
+  float2* sin = reinterpret_cast<float2*>(smem_raw);
+  float2* sbuf = sin + (size_t)rows * L;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sbuf + (size_t)rows * PL);
+  const int i0 = blk * rows;
+  if (threadIdx.x == 0) {
+    mbar_init(bar, 1);
+    mbar_fence_init();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const uint32_t bytes = (uint32_t)rows * (uint32_t)L * 8u;
+    mbar_arrive_expect_tx(bar, bytes);
+    bulk_load(sin, spec + (size_t)i0 * L, bytes, bar);
+  }
+  const bool ok = mbar_wait(bar, 0);
+  if (__syncthreads_or(!ok)) return;
+  const int half = L >> 1, log2h = log2L - 1;
+  for (int idx = threadIdx.x; idx < (rows << log2h); idx += blockDim.x) {
+    const int r = idx >> log2h, k = idx & (half - 1);
+    const float2* in = sin + (size_t)r * L;
+    float2* z = sbuf + r * PL;
+    if (k == 0) {
+      const float2 x0 = in[0];
+      z[0] = make_float2(x0.x + x0.y, x0.x - x0.y);
+      const float2 xh = in[half];
+      float2 zk, zm;
+      irfft_pre_pair(xh, xh, __ldg(p.tw_y + half), &zk, &zm);
+      z[pidx(half)] = zk;
+    } else {
+      float2 zk, zm;
+      irfft_pre_pair(in[k], in[L - k], __ldg(p.tw_y + k), &zk, &zm);
+      z[pidx(k)] = zk;
+      z[pidx(L - k)] = zm;
+    }
+  }
+  __syncthreads();
+  fft_inplace<1>(sbuf, log2L, rows, PL, p.twp_y, threadIdx.x);
+  const int log2p = log2L - 1;  // pairs per row
+  for (int idx = threadIdx.x; idx < (rows << log2p); idx += blockDim.x) {
+    const int r = idx >> log2p, n = (idx & ((1 << log2p) - 1)) << 1;
+    const float2 a = sbuf[r * PL + pidx(n)], b = sbuf[r * PL + pidx(n + 1)];
+    reinterpret_cast<float4*>(spec + (size_t)(i0 + r) * L)[n >> 1] = make_float4(a.x, a.y, b.x, b.y);
+  }
+}
+
+template <int MAXT, int MINB>
+__global__ void __launch_bounds__(MAXT, MINB)
+    fvm_irfft_bulk_kernel(FvmParams p, int rows, float2* spec) {
+  irfft_rows_bulk(p, blockIdx.x, rows, spec);
 }
 
 // u = u* - (q[i+1] - q[i]) / hx ; v = v* - (q[j+1] - q[j]) / hy.
@@ -1022,6 +1164,15 @@ static cudaError_t div_rfft_impl(const FvmParams& p, int target, const float* us
                                  const float* vs, float2* spec, cudaStream_t s) {
   const int log2L = p.log2ny - 1;
   const int rows = fft_rows_per_block(log2L, p.nx, target);
+  const bool aligned = (((uintptr_t)us | (uintptr_t)vs | (uintptr_t)spec) & 15) == 0;
+  if (p.row_feed == 1 && aligned) {
+    const size_t smem = div_rfft_bulk_smem(p.ny, rows);
+    cudaError_t e = set_smem(fvm_div_rfft_bulk_kernel<MAXT, MINB>, smem);
+    if (e != cudaSuccess) return e;
+    fvm_div_rfft_bulk_kernel<MAXT, MINB><<<p.nx / rows, block_threads(fft_workers(log2L, rows)),
+                                           smem, s>>>(p, rows, us, vs, spec);
+    return cudaGetLastError();
+  }
   const size_t smem = (size_t)rows * padded_len(p.ny / 2) * sizeof(float2);
   cudaError_t e = set_smem(fvm_div_rfft_kernel<MAXT, MINB>, smem);
   if (e != cudaSuccess) return e;
@@ -1084,6 +1235,14 @@ static cudaError_t irfft_impl(const FvmParams& p, int target, float2* spec,
                               cudaStream_t s) {
   const int log2L = p.log2ny - 1;
   const int rows = fft_rows_per_block(log2L, p.nx, target);
+  if (p.row_feed == 1 && (((uintptr_t)spec) & 15) == 0) {
+    const size_t smem = irfft_bulk_smem(p.ny, rows);
+    cudaError_t e = set_smem(fvm_irfft_bulk_kernel<MAXT, MINB>, smem);
+    if (e != cudaSuccess) return e;
+    fvm_irfft_bulk_kernel<MAXT, MINB><<<p.nx / rows, block_threads(fft_workers(log2L, rows)),
+                                        smem, s>>>(p, rows, spec);
+    return cudaGetLastError();
+  }
   const size_t smem = (size_t)rows * padded_len(p.ny / 2) * sizeof(float2);
   cudaError_t e = set_smem(fvm_irfft_kernel<MAXT, MINB>, smem);
   if (e != cudaSuccess) return e;
@@ -1134,6 +1293,26 @@ cudaError_t launch_max_speed(int n, const float* u, const float* v,
 }
 
 bool stream_stencil_ok(const FvmParams& p) { return stream_ok(p); }
+
+cudaError_t read_device_fault(unsigned int* code, bool clear) {
+  cudaError_t e = cudaMemcpyFromSymbol(code, g_cfd_device_fault, sizeof(unsigned int));
+  if (e == cudaSuccess && clear) {
+    const unsigned int zero = 0;
+    e = cudaMemcpyToSymbol(g_cfd_device_fault, &zero, sizeof(unsigned int));
+  }
+  return e;
+}
+
+bool bulk_feed_ok(const FvmParams& p) {
+  // Whole rows move by bulk copies: 16-byte multiples, and the staged rows of
+  // the widest block shape must fit in shared memory.
+  const int log2L = p.log2ny - 1;
+  if (p.ny < 8) return false;
+  const int rows = fft_rows_per_block(log2L, p.nx, 256);
+  // mbarrier transaction counts stay below 2^20 bytes.
+  const size_t tx = (size_t)(2 * rows + 1) * p.ny * 4;
+  return div_rfft_bulk_smem(p.ny, rows) <= 200 * 1024 && tx < (1u << 20);
+}
 
 bool fvm_batch_shape_ok(const FvmParams& p) {
   return p.nx % kTI == 0 && p.ny % kTJ == 0;

@@ -10,6 +10,9 @@ namespace cfd {
 // Records the message cfd_last_error() returns on this thread.
 void set_last_error(const std::string& msg);
 
+// Reads (and optionally clears) the device fault word that bounded waits set.
+cudaError_t read_device_fault(unsigned int* code, bool clear);
+
 // Parameters of the staggered-grid (FVM) explicit step, already rounded to
 // float32 the way the reference rounds its weakly typed Python scalars.
 struct FvmParams {
@@ -43,6 +46,7 @@ struct FvmParams {
   int fft_shape;       // transform block shape: 0 wide, 1 narrow (see fvm.cu)
   int col_mode;        // column pass: 0 per-block columns, 1/2 clusters of 4/8
   int stencil;         // explicit step: 0 shared-memory tiles, 1 warp streams
+  int row_feed;        // row transforms: 0 loads through registers, 1 bulk copies
 };
 
 // One slot of a same-shape batch of FVM trajectories (device-resident table
@@ -68,6 +72,8 @@ cudaError_t launch_fvm_col_pinv(const FvmParams& p, float2* spec,
 bool col_cluster_ok(const FvmParams& p, int cluster);
 // Whether the warp-streaming stencil (stencil 1) applies to this grid.
 bool stream_stencil_ok(const FvmParams& p);
+// Whether the bulk-copy row transforms (row_feed 1) apply to this grid.
+bool bulk_feed_ok(const FvmParams& p);
 cudaError_t launch_fvm_irfft(const FvmParams& p, float2* spec, cudaStream_t s);
 cudaError_t launch_fvm_project_out(const FvmParams& p, const float* us,
                                    const float* vs, const float* q, float* uo,

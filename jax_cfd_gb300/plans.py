@@ -146,7 +146,7 @@ class FvmPlan:
               'cfd_fvm_plan_autotune')
     return int(chosen.value)
 
-  LAUNCH_CHOICES = 12
+  LAUNCH_CHOICES = 24
 
   def set_launch(self, choice: int):
     """Pins the launch configuration (see autotune); results do not change."""
