@@ -98,6 +98,15 @@ long long cfd_fvm_plan_bytes(const cfd_fvm_plan* plan);
  * offsets (1, .5) and (.5, 1).  u_out/v_out may alias u/v. */
 int cfd_fvm_step(cfd_fvm_plan* plan, void* stream, const float* u,
                  const float* v, float* u_out, float* v_out, int steps);
+/* navier_stokes_rk (time_stepping.py:59-107) with an explicit Butcher
+ * tableau of 1-4 stages: `a` holds rows 1 .. stages-1 of the lower triangle
+ * concatenated (row i has i entries), `b` the `stages` weights; e.g.
+ * midpoint_rk2 a = {0.5}, b = {0, 1}; classic_rk4 a = {0.5, 0, 0.5, 0, 0, 1},
+ * b = {1/6, 1/3, 1/3, 1/6}.  Each stage's state is projected; the first call
+ * allocates the plan's stage buffers (make it before any stream capture). */
+int cfd_fvm_step_rk(cfd_fvm_plan* plan, void* stream, const float* u,
+                    const float* v, float* u_out, float* v_out, int steps,
+                    int stages, const double* a, const double* b);
 /* cfd_fvm_step with a CUDA event pair around every launch; synchronises the
  * stream at the end and writes the mean duration in ms of each kernel kind to
  * ms_out[5] = {explicit stencil, divergence + row rFFT, column pinv,
@@ -257,6 +266,20 @@ int cfd_irfft2(cfd_spec_plan* plan, void* stream, const float* xhat, float* x);
 /* out = irfft2(rfft2(x) * table), table real [nx, ny/2+1] on the device. */
 int cfd_spectral_filter(cfd_spec_plan* plan, void* stream, const float* x,
                         const float* table, float* out);
+
+/* Diagnostics (data/xarray_utils.py:155-167, 279-290, 370-401).
+ * cfd_energy_spectrum_shells: the isotropic kinetic-energy spectrum, binsum
+ * form, of the velocity (u, v) on the plan's grid: out[i] (nbins doubles on
+ * the device) = sum over |k| in (ks (i + 0.5), ks (i + 1.5)] of
+ * 0.5 (|fft2 u|^2 + |fft2 v|^2), with k = 2 pi fftfreq(n, d) per axis and
+ * dnx = nx * hx, dny = ny * hy.  Uses the plan's column-field workspace.
+ * cfd_enstrophy_sum: sum over cells of vorticity^2 / 2 (one double on the
+ * device); divide by nx * ny for the mean. */
+int cfd_energy_spectrum_shells(cfd_spec_plan* plan, void* stream, const float* u,
+                               const float* v, double dnx, double dny, double ks,
+                               int nbins, double* out);
+int cfd_enstrophy_sum(void* stream, int nx, int ny, double hx, double hy,
+                      const float* u, const float* v, double* out);
 
 /* ---- Batched spectral trajectories ----
  * The cfd_fvm_batch model for NavierStokes2D + a low-storage RK/CN

@@ -79,6 +79,8 @@ _SIGNATURES = {
     'cfd_device_fault': (ctypes.c_int, [ctypes.POINTER(ctypes.c_uint), ctypes.c_int]),
     'cfd_fvm_plan_set_launch': (ctypes.c_int, [_vp, ctypes.c_int]),
     'cfd_fvm_plan_get_launch': (ctypes.c_int, [_vp]),
+    'cfd_fvm_step_rk': (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_int, ctypes.c_int,
+                                        _vp, _vp]),
     'cfd_fvm_adjoint_step': (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     'cfd_fvm_batch_create': (ctypes.c_int, [ctypes.POINTER(FvmConfig), ctypes.c_int,
                                              ctypes.POINTER(_vp)]),
@@ -100,6 +102,11 @@ _SIGNATURES = {
                                                ctypes.POINTER(_vp)]),
     'cfd_fvm_ensemble_autotune': (ctypes.c_int, [_vp, _vp, ctypes.c_int]),
     'cfd_fvm_ensemble_step': (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_int]),
+    'cfd_energy_spectrum_shells': (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_double,
+                                                   ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                                                   _vp]),
+    'cfd_enstrophy_sum': (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                         ctypes.c_double, _vp, _vp, _vp]),
     'cfd_spec_batch_create': (ctypes.c_int, [ctypes.POINTER(SpecConfig), ctypes.c_int,
                                               ctypes.POINTER(_vp)]),
     'cfd_spec_batch_destroy': (ctypes.c_int, [_vp]),

@@ -80,10 +80,12 @@ class FvmStep:
   the projection of step k folded into the stencil of step k + 1.
   """
 
-  def __init__(self, grid: grids.Grid, **plan_kwargs):
+  def __init__(self, grid: grids.Grid, tableau=None, **plan_kwargs):
     self.grid = grid
     self._plan_kwargs = plan_kwargs
     self._key = tuple(sorted((k, _freeze(v)) for k, v in plan_kwargs.items()))
+    # None: the fused forward-Euler step; else (a, b) of navier_stokes_rk.
+    self.tableau = tableau
 
   def plan(self, device) -> plans.FvmPlan:
     return plans.cached('fvm-step', (device, self.grid.shape, self.grid.step, self._key),
@@ -92,7 +94,11 @@ class FvmStep:
 
   def gb300_repeat(self, v, steps: int):
     _check_state(v, self.grid)
-    uo, vo = self.plan(v[0].data.device).step(v[0].data, v[1].data, steps)
+    plan = self.plan(v[0].data.device)
+    if self.tableau is None:
+      uo, vo = plan.step(v[0].data, v[1].data, steps)
+    else:
+      uo, vo = plan.step_rk(v[0].data, v[1].data, steps, *self.tableau)
     return (GridVariable(GridArray(uo, v[0].offset, self.grid), v[0].bc),
             GridVariable(GridArray(vo, v[1].offset, self.grid), v[1].bc))
 
@@ -128,12 +134,16 @@ class _FusedEquation:
     self.pressure_projection = pressure_projection
 
   def gb300_step(self, tableau, time_step):
-    if (list(tableau.a), list(tableau.b)) != ([], [1]):
-      raise NotImplementedError(
-          'the fused GB300 step implements forward_euler (the reference default)')
     if float(time_step) != float(self.dt):
       raise NotImplementedError('time_step must equal the dt given to the equation')
-    return FvmStep(self.grid, dt=float(time_step), **self.plan_kwargs)
+    a = [list(row) for row in tableau.a]
+    b = list(tableau.b)
+    if (a, b) == ([], [1]):
+      # forward_euler: the fused step (projection folded into the next stencil).
+      return FvmStep(self.grid, dt=float(time_step), **self.plan_kwargs)
+    if not 1 <= len(b) <= 4:
+      raise NotImplementedError('the GB300 Runge-Kutta step takes tableaux of 1 to 4 stages')
+    return FvmStep(self.grid, tableau=(a, b), dt=float(time_step), **self.plan_kwargs)
 
 
 def _convect_kind(convect) -> int:

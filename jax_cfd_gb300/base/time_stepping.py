@@ -2,9 +2,11 @@
 
 ``forward_euler(equation, dt)`` applied to the equation built by
 ``equations.semi_implicit_navier_stokes`` returns the fused GB300 step
-(one native launch sequence per step).  The tableau definitions of the other
-steppers are kept for API compatibility; the fused path implements
-``forward_euler`` (time_stepping.py:109-119), which is the reference default.
+(the projection of step k folded into the stencil of step k + 1).  The other
+explicit tableaux (``midpoint_rk2``, ``heun_rk2``, ``classic_rk4`` or any
+``ButcherTableau`` of up to four stages) run ``navier_stokes_rk`` on the same
+kernels: the stencil in explicit-terms mode, the stage combinations in the
+reference's order and a projection per stage.
 """
 from __future__ import annotations
 
@@ -39,7 +41,7 @@ CLASSIC_RK4 = ButcherTableau(a=[[1 / 2], [0, 1 / 2], [0, 0, 1]],
 
 
 def navier_stokes_rk(tableau: ButcherTableau, equation, time_step: float) -> Callable:
-  """time_stepping.py:59-107; the fused path covers the forward-Euler tableau."""
+  """time_stepping.py:59-107."""
   builder = getattr(equation, 'gb300_step', None)
   if builder is None:
     raise NotImplementedError(
@@ -54,12 +56,15 @@ def forward_euler(equation, time_step: float) -> Callable:
 
 
 def midpoint_rk2(equation, time_step: float) -> Callable:
+  """time_stepping.py:121-131."""
   return navier_stokes_rk(MIDPOINT_RK2, equation, time_step)
 
 
 def heun_rk2(equation, time_step: float) -> Callable:
+  """time_stepping.py:134-144."""
   return navier_stokes_rk(HEUN_RK2, equation, time_step)
 
 
 def classic_rk4(equation, time_step: float) -> Callable:
+  """time_stepping.py:147-158."""
   return navier_stokes_rk(CLASSIC_RK4, equation, time_step)

@@ -151,6 +151,7 @@ struct cfd_fvm_plan {
   float2* twpy = nullptr;
   float* fu = nullptr;
   float* fv = nullptr;
+  float* rk = nullptr;  // Runge-Kutta stage terms k_j (u, v), allocated on first use
   long long bytes = 0;
 };
 
@@ -253,7 +254,8 @@ int cfd_version(void) { return 1; }
 int cfd_fvm_plan_destroy(cfd_fvm_plan* plan) {
   if (!plan) return CFD_OK;
   void* ptrs[] = {plan->au, plan->av, plan->bu, plan->bv, plan->spec, plan->lamx,
-                  plan->lamy, plan->twy, plan->twpx, plan->twpy, plan->fu, plan->fv};
+                  plan->lamy, plan->twy, plan->twpx, plan->twpy, plan->fu, plan->fv,
+                  plan->rk};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   delete plan;
@@ -430,6 +432,74 @@ int cfd_fvm_step(cfd_fvm_plan* plan, void* stream, const float* u,
     t = av; av = bv; bv = t;
   }
   CFD_CHECK(cfd::launch_fvm_project_out(p, au, av, q, u_out, v_out, s), "project_out");
+  return CFD_OK;
+}
+
+// navier_stokes_rk (time_stepping.py:59-107) with an arbitrary explicit
+// tableau of up to four stages: k_0 = F(u0); u_i = P(u0 + dt sum_j a_ij k_j),
+// k_i = F(u_i); u' = P(u0 + dt sum_j b_j k_j).  F is the stencil in
+// explicit-terms mode (with the projection of u_i folded into its load), P the
+// fast-diagonalisation projection.
+int cfd_fvm_step_rk(cfd_fvm_plan* plan, void* stream, const float* u, const float* v,
+                    float* u_out, float* v_out, int steps, int stages, const double* a,
+                    const double* b) {
+  if (!plan || !u || !v || !u_out || !v_out || !b || steps < 0 || stages < 1 || stages > 4 ||
+      (stages > 1 && !a))
+    return fail(CFD_ERR_INVALID_ARGUMENT, "cfd_fvm_step_rk: bad arguments");
+  cudaStream_t s = as_stream(stream);
+  const cfd::FvmParams& p = plan->p;
+  const size_t n = (size_t)p.nx * p.ny;
+  if (steps == 0) {
+    if (u_out != u) CFD_CHECK(cudaMemcpyAsync(u_out, u, n * 4, cudaMemcpyDeviceToDevice, s), "copy");
+    if (v_out != v) CFD_CHECK(cudaMemcpyAsync(v_out, v, n * 4, cudaMemcpyDeviceToDevice, s), "copy");
+    return CFD_OK;
+  }
+  if (!plan->rk) {
+    CFD_CHECK(cudaMalloc((void**)&plan->rk, 8 * n * sizeof(float)), "cfd_fvm_step_rk: cudaMalloc");
+    plan->bytes += (long long)(8 * n * sizeof(float));
+  }
+  float* K[4][2];
+  for (int j = 0; j < 4; ++j) {
+    K[j][0] = plan->rk + (size_t)(2 * j) * n;
+    K[j][1] = plan->rk + (size_t)(2 * j + 1) * n;
+  }
+  const float* q = reinterpret_cast<const float*>(plan->spec);
+  // Python coefficient rows (skipping zeros as the reference's sum does).
+  auto combo = [&](const double* coef, int count) {
+    cfd::RkCombine cb{};
+    for (int j = 0; j < count; ++j)
+      if (coef[j] != 0.0) {
+        cb.k[cb.count][0] = K[j][0];
+        cb.k[cb.count][1] = K[j][1];
+        cb.c[cb.count] = (float)coef[j];
+        ++cb.count;
+      }
+    return cb;
+  };
+  const float *cu = u, *cv = v;
+  for (int st = 0; st < steps; ++st) {
+    float* ou = (st + 1 == steps) ? u_out : plan->bu;
+    float* ov = (st + 1 == steps) ? v_out : plan->bv;
+    CFD_CHECK(cfd::launch_fvm_explicit(p, false, true, cu, cv, nullptr, K[0][0], K[0][1], s),
+              "explicit");
+    const double* row = a;
+    for (int i = 1; i < stages; ++i) {
+      CFD_CHECK(cfd::launch_fvm_rk_combine(p, cu, cv, combo(row, i), plan->au, plan->av, s),
+                "rk_combine");
+      row += i;
+      int rc = fvm_pressure(plan, s, plan->au, plan->av);
+      if (rc) return rc;
+      CFD_CHECK(cfd::launch_fvm_explicit(p, true, true, plan->au, plan->av, q, K[i][0], K[i][1], s),
+                "explicit");
+    }
+    CFD_CHECK(cfd::launch_fvm_rk_combine(p, cu, cv, combo(b, stages), plan->au, plan->av, s),
+              "rk_combine");
+    int rc = fvm_pressure(plan, s, plan->au, plan->av);
+    if (rc) return rc;
+    CFD_CHECK(cfd::launch_fvm_project_out(p, plan->au, plan->av, q, ou, ov, s), "project_out");
+    cu = ou;
+    cv = ov;
+  }
   return CFD_OK;
 }
 
@@ -1580,6 +1650,35 @@ int cfd_spec_batch_run(cfd_spec_batch* b, void* stream, int chunk, int use_graph
     b->graph_chunk = chunk;
   }
   CFD_CHECK(cudaGraphLaunch(b->exec, s), "cudaGraphLaunch");
+  return CFD_OK;
+}
+
+// ---- Diagnostics -------------------------------------------------------
+
+int cfd_energy_spectrum_shells(cfd_spec_plan* plan, void* stream, const float* u,
+                               const float* v, double dnx, double dny, double ks, int nbins,
+                               double* out) {
+  if (!plan || !u || !v || !out || nbins < 1 || !(ks > 0))
+    return fail(CFD_ERR_INVALID_ARGUMENT, "cfd_energy_spectrum_shells: bad arguments");
+  cudaStream_t s = as_stream(stream);
+  float2* uh = plan->t4[0];
+  float2* vh = plan->t4[1];
+  CFD_CHECK(cfd::launch_row_rfft(plan->p, u, uh, s), "row_rfft");
+  CFD_CHECK(cfd::launch_col_fft(plan->p, uh, -1, nullptr, s), "col_fft");
+  CFD_CHECK(cfd::launch_row_rfft(plan->p, v, vh, s), "row_rfft");
+  CFD_CHECK(cfd::launch_col_fft(plan->p, vh, -1, nullptr, s), "col_fft");
+  CFD_CHECK(cfd::launch_shell_energy(plan->p, dnx, dny, ks, nbins, uh, vh, out, s),
+            "shell_energy");
+  return CFD_OK;
+}
+
+int cfd_enstrophy_sum(void* stream, int nx, int ny, double hx, double hy, const float* u,
+                      const float* v, double* out) {
+  if (!u || !v || !out || nx < 1 || ny < 1 || !(hx > 0) || !(hy > 0))
+    return fail(CFD_ERR_INVALID_ARGUMENT, "cfd_enstrophy_sum: bad arguments");
+  CFD_CHECK(cfd::launch_enstrophy_sum(nx, ny, (float)hx, (float)hy, u, v, out,
+                                      as_stream(stream)),
+            "enstrophy_sum");
   return CFD_OK;
 }
 

@@ -972,6 +972,23 @@ __global__ void fvm_project_out_kernel(FvmParams p, const float* __restrict__ us
   project_out_cells(p, blockIdx.x, gridDim.x, us, vs, q, uo, vo);
 }
 
+// u0 + dt * sum_j c_j k_j, summed from 0 in the reference's order.
+__global__ void fvm_rk_combine_kernel(FvmParams p, const float* __restrict__ u0,
+                                      const float* __restrict__ v0, RkCombine cb,
+                                      float* __restrict__ uo, float* __restrict__ vo) {
+  const size_t n = (size_t)p.nx * p.ny;
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < n;
+       idx += (size_t)gridDim.x * blockDim.x) {
+    float au = 0.f, av = 0.f;
+    for (int j = 0; j < cb.count; ++j) {
+      au = au + cb.c[j] * __ldg(cb.k[j][0] + idx);
+      av = av + cb.c[j] * __ldg(cb.k[j][1] + idx);
+    }
+    uo[idx] = __ldg(u0 + idx) + p.dt * au;
+    vo[idx] = __ldg(v0 + idx) + p.dt * av;
+  }
+}
+
 __global__ void divergence_kernel(FvmParams p, const float* __restrict__ u,
                                   const float* __restrict__ v,
                                   float* __restrict__ out) {
@@ -1267,6 +1284,14 @@ cudaError_t launch_fvm_project_out(const FvmParams& p, const float* us,
                                    float* vo, cudaStream_t s) {
   const size_t n = (size_t)p.nx * p.ny;
   fvm_project_out_kernel<<<elementwise_blocks(n), 256, 0, s>>>(p, us, vs, q, uo, vo);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fvm_rk_combine(const FvmParams& p, const float* u0, const float* v0,
+                                  const RkCombine& cb, float* uo, float* vo, cudaStream_t s) {
+  if (cb.count < 0 || cb.count > 4) return cudaErrorInvalidValue;
+  const size_t n = (size_t)p.nx * p.ny;
+  fvm_rk_combine_kernel<<<elementwise_blocks(n), 256, 0, s>>>(p, u0, v0, cb, uo, vo);
   return cudaGetLastError();
 }
 

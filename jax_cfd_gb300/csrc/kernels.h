@@ -94,6 +94,16 @@ cudaError_t launch_fvm_batch_project_out(const FvmParams& shape, const FvmMember
 cudaError_t launch_fvm_adjoint(const FvmParams& p, const float* u, const float* v,
                                const float* wu, const float* wv, float* gu, float* gv,
                                float* nu_dot, cudaStream_t s);
+// Runge-Kutta stage combination (time_stepping.py:89-105):
+// out = u0 + dt * (0 + c[0] k[0] + c[1] k[1] + ...), coefficients in float32,
+// each product and sum rounded in that order, for the u and v fields.
+struct RkCombine {
+  const float* k[4][2];
+  float c[4];
+  int count;
+};
+cudaError_t launch_fvm_rk_combine(const FvmParams& p, const float* u0, const float* v0,
+                                  const RkCombine& cb, float* uo, float* vo, cudaStream_t s);
 // Diagnostics on staggered velocity fields.
 cudaError_t launch_divergence(const FvmParams& p, const float* u,
                               const float* v, float* out, cudaStream_t s);
@@ -171,6 +181,13 @@ cudaError_t launch_row_irfft(const SpecParams& p, const float2* X, float* x,
 // inverse; an optional real table (nx x (L+1)) multiplies the result.
 cudaError_t launch_col_fft(const SpecParams& p, float2* X, int sign,
                            const float* mult, cudaStream_t s);
+// Diagnostics: shell sums of the kinetic-energy spectrum from the rfft half
+// spectra of u and v (out: nbins doubles), and the sum of vorticity^2 / 2.
+cudaError_t launch_shell_energy(const SpecParams& p, double dnx, double dny, double ks,
+                                int nbins, const float2* uh, const float2* vh, double* out,
+                                cudaStream_t s);
+cudaError_t launch_enstrophy_sum(int nx, int ny, float hx, float hy, const float* u,
+                                 const float* v, double* out, cudaStream_t s);
 // curl table: 2 pi i (kx * fy_hat - ky * fx_hat)
 cudaError_t launch_spec_curl_table(const SpecParams& p, const float2* fxh,
                                    const float2* fyh, float2* out,

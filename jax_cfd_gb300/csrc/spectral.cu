@@ -231,6 +231,60 @@ __global__ void __launch_bounds__(256, 3)
   row_advect_rows(p, blockIdx.x, rows, t0, t1, t2, t3, ahat);
 }
 
+// Isotropic kinetic-energy spectrum, binsum form (data/xarray_utils.py:
+// 279-290, 370-401): 0.5 (|u^|^2 + |v^|^2) of the unnormalised 2-D FFTs summed
+// over shells bounds[i] < |k| <= bounds[i+1], bounds = ks (i + 0.5), with
+// |k| = 2 pi |fftfreq| formed in double.  The rfft half spectrum stands for
+// the full one: columns 1 .. L-1 have a mirror image at -ky with the same
+// energy and |k| (weight 2); columns 0 and L appear once.  Per-block shared
+// histograms in double, added to `out` (nbins doubles, zeroed by the caller).
+__global__ void shell_energy_kernel(int nx, int ny, double dnx, double dny, double ks,
+                                    int nbins, const float2* __restrict__ uh,
+                                    const float2* __restrict__ vh, double* __restrict__ out) {
+  extern __shared__ double hist[];
+  for (int b = threadIdx.x; b < nbins; b += blockDim.x) hist[b] = 0.0;
+  __syncthreads();
+  const int L = ny / 2, ncols = L + 1;
+  const size_t n = (size_t)nx * ncols;
+  const double two_pi = 6.283185307179586476925286766559;
+  for (size_t g = blockIdx.x * (size_t)blockDim.x + threadIdx.x; g < n;
+       g += (size_t)gridDim.x * blockDim.x) {
+    const int kx = (int)(g / ncols), c = (int)(g - (size_t)kx * ncols);
+    const double fx = (double)(kx < nx / 2 ? kx : kx - nx) / dnx;
+    const double fy = (double)(c < ny / 2 ? c : c - ny) / dny;
+    const double k = two_pi * sqrt(fx * fx + fy * fy);
+    const int bin = (int)ceil(k / ks - 1.5);
+    if (bin < 0 || bin >= nbins) continue;
+    const float2 a = uh[g], b = vh[g];
+    const double e = 0.5 * ((double)a.x * a.x + (double)a.y * a.y + (double)b.x * b.x +
+                            (double)b.y * b.y);
+    atomicAdd(&hist[bin], (c == 0 || c == L) ? e : 2.0 * e);
+  }
+  __syncthreads();
+  for (int b = threadIdx.x; b < nbins; b += blockDim.x)
+    if (hist[b] != 0.0) atomicAdd(&out[b], hist[b]);
+}
+
+// Sum over cells of vorticity^2 / 2 (xarray_utils.py:155-167) in double,
+// vorticity = (v[i+1] - v) / hx - (u[j+1] - u) / hy at offset (1, 1).
+__global__ void enstrophy_sum_kernel(int nx, int ny, float hx, float hy,
+                                     const float* __restrict__ u, const float* __restrict__ v,
+                                     double* __restrict__ out) {
+  const size_t n = (size_t)nx * ny;
+  double acc = 0.0;
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < n;
+       idx += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(idx / ny), j = (int)(idx - (size_t)i * ny);
+    const float dv = (__ldg(v + (size_t)((i + 1) % nx) * ny + j) - __ldg(v + idx)) / hx;
+    const float du = (__ldg(u + (size_t)i * ny + (j + 1) % ny) - __ldg(u + idx)) / hy;
+    const double w = (double)(dv - du);
+    acc += 0.5 * w * w;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) atomicAdd(out, acc);
+}
+
 // ---- Batched variants: the slot index is the last grid axis ----
 // Column prep after stage `stage` of step k builds the inputs of the next
 // stage (k = -1: before the first step of the chunk).
@@ -537,6 +591,31 @@ cudaError_t launch_spec_batch_update(const SpecParams& p, const SpecMember* mem,
   if (e != cudaSuccess) return e;
   spec_batch_col_update_kernel<<<dim3(c.blocks, count), c.threads, c.smem, s>>>(
       mem, k, stage, c.W, c.log2W, c.bstride);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_shell_energy(const SpecParams& p, double dnx, double dny, double ks,
+                                int nbins, const float2* uh, const float2* vh, double* out,
+                                cudaStream_t s) {
+  if (nbins < 1 || nbins > 8192) return cudaErrorInvalidValue;
+  cudaError_t e = cudaMemsetAsync(out, 0, (size_t)nbins * sizeof(double), s);
+  if (e != cudaSuccess) return e;
+  const size_t n = (size_t)p.nx * (p.L + 1);
+  size_t blocks = (n + 255) / 256;
+  if (blocks > 152 * 4) blocks = 152 * 4;
+  shell_energy_kernel<<<(int)blocks, 256, (size_t)nbins * sizeof(double), s>>>(
+      p.nx, p.ny, dnx, dny, ks, nbins, uh, vh, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_enstrophy_sum(int nx, int ny, float hx, float hy, const float* u,
+                                 const float* v, double* out, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(out, 0, sizeof(double), s);
+  if (e != cudaSuccess) return e;
+  const size_t n = (size_t)nx * ny;
+  size_t blocks = (n + 255) / 256;
+  if (blocks > 152 * 4) blocks = 152 * 4;
+  enstrophy_sum_kernel<<<(int)blocks, 256, 0, s>>>(nx, ny, hx, hy, u, v, out);
   return cudaGetLastError();
 }
 

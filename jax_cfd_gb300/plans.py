@@ -134,6 +134,29 @@ class FvmPlan:
               'cfd_fvm_step')
     return u_out, v_out
 
+  def step_rk(self, u, v, steps: int, a, b, u_out=None, v_out=None):
+    """navier_stokes_rk with Butcher tableau (a, b) (time_stepping.py:59-107)."""
+    if steps < 0:
+      raise ValueError('steps must be non-negative')
+    stages = len(b)
+    if not 1 <= stages <= 4 or len(a) + 1 != stages:
+      raise NotImplementedError('the GB300 Runge-Kutta step takes tableaux of 1 to 4 stages')
+    if any(len(row) > i + 1 for i, row in enumerate(a)):
+      raise ValueError('explicit tableaux only: row i has at most i + 1 entries')
+    # Row i of the lower triangle, padded with zeros (which the reference's
+    # sum skips, like the native combination).
+    flat = [float(x) for i, row in enumerate(a)
+            for x in list(row) + [0.0] * (i + 1 - len(row))]
+    ca = (ctypes.c_double * len(flat))(*flat) if flat else None
+    cb = (ctypes.c_double * stages)(*[float(x) for x in b])
+    u_out = torch.empty_like(u) if u_out is None else u_out
+    v_out = torch.empty_like(v) if v_out is None else v_out
+    ptrs = self._fields(u, v, u_out, v_out)
+    nat.check(self._lib.cfd_fvm_step_rk(self._h, current_stream_ptr(u.device), *ptrs, int(steps),
+                                        stages, ctypes.cast(ca, ctypes.c_void_p) if ca else None,
+                                        ctypes.cast(cb, ctypes.c_void_p)), 'cfd_fvm_step_rk')
+    return u_out, v_out
+
   def autotune(self, u, v, steps: int = 20) -> int:
     """Times each transform launch configuration on (u, v) and keeps the
     fastest; returns its index (row block shape + 2 * column-pass scheme).

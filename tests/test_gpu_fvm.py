@@ -228,3 +228,37 @@ def test_every_launch_configuration_gives_the_same_bits(cuda_device, shape):
   assert 0 in results and 6 in results
   for choice, (a, b) in results.items():
     assert torch.equal(a, results[0][0]) and torch.equal(b, results[0][1]), choice
+
+
+@pytest.mark.parametrize('name', ['midpoint_rk2', 'heun_rk2', 'classic_rk4'])
+@pytest.mark.parametrize('shape', [(64, 64), (128, 64)])
+def test_runge_kutta_tableaux_match_oracle(cuda_device, name, shape):
+  """time_stepping.py:121-158 on the same kernels: one step and a 10-step
+  chunk against the oracle's navier_stokes_rk."""
+  import jax_cfd_gb300.base as cfd
+  from oracle import fvm as ofvm
+  tableau = {'midpoint_rk2': ofvm.MIDPOINT_RK2, 'heun_rk2': ofvm.HEUN_RK2,
+             'classic_rk4': ofvm.CLASSIC_RK4}[name]
+  og, v0 = _setup(shape, seed=8)
+  grid = cfd.grids.Grid(shape, domain=((0, TWO_PI), (0, TWO_PI)))
+  dt = ofvm.stable_time_step(2.0, 0.5, 1e-3, og)
+  step = cfd.equations.semi_implicit_navier_stokes(
+      1.0, 1e-3, dt, grid, forcing=cfd.forcings.simple_turbulence_forcing(grid, 1, 4, -0.1),
+      time_stepper=getattr(cfd.time_stepping, name))
+  ref_step = ofvm.semi_implicit_navier_stokes(
+      1.0, 1e-3, dt, og, forcing=ofvm.simple_turbulence_forcing(og, 1, 4, -0.1),
+      tableau=tableau)
+  v = _to_gpu(v0, grid, cuda_device)
+  for g, w in zip(_np(step(v)), ref_step(v0)):
+    assert rel_l2(g, w) <= STEP_TOL
+  chunk = cfd.funcutils.repeated(step, 10)(v)
+  single = v
+  for _ in range(10):
+    single = step(single)
+  for x, y in zip(chunk, single):
+    assert torch.equal(x.data, y.data)
+  ref = ofvm.repeated(ref_step, 10)([a.copy() for a in v0])
+  for g, w in zip(_np(chunk), ref):
+    assert rel_l2(g, w) <= 10 * STEP_TOL
+  div = ofvm.divergence(_np(chunk), og.step)
+  assert np.abs(div).max() <= 1e-4

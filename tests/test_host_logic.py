@@ -104,9 +104,12 @@ def test_unsupported_options_raise_not_implemented():
   with pytest.raises(NotImplementedError):
     cfd.equations.semi_implicit_navier_stokes(1.0, 1e-3, 1e-3, g,
                                               pressure_solve=cfd.pressure.solve_cg)
+  five = cfd.time_stepping.ButcherTableau(a=[[1], [0, 1], [0, 0, 1], [0, 0, 0, 1]],
+                                          b=[0.2] * 5)
   with pytest.raises(NotImplementedError):
-    cfd.equations.semi_implicit_navier_stokes(1.0, 1e-3, 1e-3, g,
-                                              time_stepper=cfd.time_stepping.classic_rk4)
+    cfd.equations.semi_implicit_navier_stokes(
+        1.0, 1e-3, 1e-3, g,
+        time_stepper=lambda eq, dt: cfd.time_stepping.navier_stokes_rk(five, eq, dt))
   with pytest.raises(NotImplementedError):
     cfd.equations.semi_implicit_navier_stokes(1.0, 1e-3, 1e-3, g, diffuse=lambda c, nu: c)
   three = cfd.forcings.sum_forcings(cfd.forcings.linear_forcing(g, 1.0),
@@ -153,3 +156,15 @@ def test_brick_wall_filter_mirror():
     g = grids.Grid((n, n))
     got = su.brick_wall_filter_2d(g, device='cpu').numpy()
     np.testing.assert_array_equal(got, ospec.brick_wall_filter_2d(fvm.Grid.make((n, n))))
+
+
+def test_other_tableaux_build_rk_steps():
+  import jax_cfd_gb300.base as cfd
+  g = _grid()
+  for stepper, stages in ((cfd.time_stepping.midpoint_rk2, 2), (cfd.time_stepping.heun_rk2, 2),
+                          (cfd.time_stepping.classic_rk4, 4)):
+    step = cfd.equations.semi_implicit_navier_stokes(1.0, 1e-3, 1e-3, g, time_stepper=stepper)
+    assert isinstance(step, cfd.equations.FvmStep)
+    assert len(step.tableau[1]) == stages
+  euler = cfd.equations.semi_implicit_navier_stokes(1.0, 1e-3, 1e-3, g)
+  assert euler.tableau is None
