@@ -244,6 +244,11 @@ typedef struct cfd_spec_plan cfd_spec_plan;
 int cfd_spec_plan_create(const cfd_spec_config* cfg, cfd_spec_plan** plan);
 int cfd_spec_plan_destroy(cfd_spec_plan* plan);
 long long cfd_spec_plan_bytes(const cfd_spec_plan* plan);
+/* Launch configuration of the column passes: 0 per-block columns (default),
+ * 1 clusters of four one-column blocks exchanging rows through distributed
+ * shared memory (256 <= nx <= 2048).  Results are bit-for-bit the same. */
+int cfd_spec_plan_set_launch(cfd_spec_plan* plan, int choice);
+int cfd_spec_plan_get_launch(const cfd_spec_plan* plan);
 /* Velocity-independent forcing (fx, fy real [nx, ny] on the device, either may
  * be NULL): stores 2 pi i (kx rfft2(fy) - ky rfft2(fx)).  Synchronises the
  * stream once to decide whether the table lives only in row kx = 0. */

@@ -121,6 +121,8 @@ _SIGNATURES = {
     'cfd_spec_plan_create': (ctypes.c_int, [ctypes.POINTER(SpecConfig), ctypes.POINTER(_vp)]),
     'cfd_spec_plan_destroy': (ctypes.c_int, [_vp]),
     'cfd_spec_plan_bytes': (ctypes.c_longlong, [_vp]),
+    'cfd_spec_plan_set_launch': (ctypes.c_int, [_vp, ctypes.c_int]),
+    'cfd_spec_plan_get_launch': (ctypes.c_int, [_vp]),
     'cfd_spec_set_forcing': (ctypes.c_int, [_vp, _vp, _vp, _vp]),
     'cfd_spec_step': (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_int]),
     'cfd_spec_profile': (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_int, _vp]),

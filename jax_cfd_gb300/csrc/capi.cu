@@ -10,6 +10,7 @@
 #include "../../include/cfd_gb300.h"
 #include "kernels.h"
 #include "fft.cuh"
+#include "wfft.cuh"
 
 namespace {
 
@@ -46,7 +47,17 @@ std::vector<float2> twiddles(int n) {
 // fft.cuh): entry [r-1][k] of the pass with span Ns and radix R is
 // exp(-2 pi i r k / (Ns R)), computed in double and rounded once.
 std::vector<float2> pass_twiddles(int log2L) {
-  std::vector<float2> t(cfd::fft_pass_table_size(log2L) > 0 ? cfd::fft_pass_table_size(log2L) : 1);
+  const int stockham = cfd::fft_pass_table_size(log2L);
+  std::vector<float2> t(std::max(1, stockham + cfd::wfft_table_size(log2L)));
+  // The one-warp 1024-point transform's table follows the pass tables:
+  // entry [k2 * 32 + n1] = exp(-2 pi i n1 k2 / 1024).
+  if (cfd::wfft_table_size(log2L) > 0)
+    for (int k2 = 0; k2 < 32; ++k2)
+      for (int n1 = 0; n1 < 32; ++n1) {
+        const double a = -2.0 * M_PI * (double)(n1 * k2) / 1024.0;
+        t[cfd::wfft_table_offset(log2L) + k2 * 32 + n1] =
+            make_float2((float)std::cos(a), (float)std::sin(a));
+      }
   int off = 0, ns = 1;
   for (int q = 0; q < cfd::fft_num_passes(log2L); ++q) {
     const int R = cfd::fft_pass_radix(log2L, q);
@@ -1250,6 +1261,8 @@ int cfd_spec_plan_create(const cfd_spec_config* cfg, cfd_spec_plan** out) {
   cfd_spec_plan* plan = new cfd_spec_plan();
   cfd::SpecParams& p = plan->p;
   p = params;
+  // Clustered column passes measured faster at 256^2 and 512^2 (GB300).
+  p.col_mode = (cfg->nx >= 256 && cfg->nx <= 512) ? 1 : 0;
   plan->stages = stages;
   for (int k = 0; k < stages; ++k) plan->coef[k] = coef[k];
   const int nx = cfg->nx;
@@ -1292,6 +1305,19 @@ int cfd_spec_plan_create(const cfd_spec_config* cfg, cfd_spec_plan** out) {
 }
 
 long long cfd_spec_plan_bytes(const cfd_spec_plan* plan) { return plan ? plan->bytes : 0; }
+
+int cfd_spec_plan_set_launch(cfd_spec_plan* plan, int choice) {
+  if (!plan || choice < 0 || choice > 1)
+    return fail(CFD_ERR_INVALID_ARGUMENT, "cfd_spec_plan_set_launch: bad arguments");
+  cfd::SpecParams q = plan->p;
+  q.col_mode = choice;
+  if (choice == 1 && !cfd::spec_cluster_ok(q))
+    return fail(CFD_ERR_UNSUPPORTED, "cfd_spec_plan_set_launch: choice not available on this grid");
+  plan->p.col_mode = choice;
+  return CFD_OK;
+}
+
+int cfd_spec_plan_get_launch(const cfd_spec_plan* plan) { return plan ? plan->p.col_mode : -1; }
 
 int cfd_rfft2(cfd_spec_plan* plan, void* stream, const float* x, float* xhat) {
   if (!plan || !x || !xhat) return fail(CFD_ERR_INVALID_ARGUMENT, "cfd_rfft2: null pointer");

@@ -12,13 +12,14 @@
 // step's stencil load, or into project_out at the end of a chunk.
 //
 // The half spectrum of a row of M reals is stored "packed" as M/2 complex
-// numbers: element 0 holds (X[0], X[M/2]), both real.  The x-axis transform
-// of that packed column is untangled with the two-real-signals identity.
+// numbers: element 0 holds (X[0], X[M/2]), both real.  The x-axis transforms
+// of the DC and Nyquist columns run as two separate real sequences.
 #include <cooperative_groups.h>
 
 #include "bulk.cuh"
 #include "fft.cuh"
 #include "kernels.h"
+#include "wfft.cuh"
 
 namespace cg = cooperative_groups;
 
@@ -724,45 +725,52 @@ CFD_D float pinv_diag(const FvmParams& p, int kx, int ky) {
   return fabsf(lam) > p.cutoff ? p.pinv_scale / lam : 0.f;
 }
 
+// Column pass of the packed row spectra.  Row element 0 holds the real DC and
+// Nyquist values (X_0, X_L) of the row transform; their columns are
+// transformed as two separate real sequences: the block of column 0 takes the
+// DC column (imaginary parts zero) and one extra block past the last column
+// group takes the Nyquist column.  (Transforming them together as one complex
+// column A + iB would put the rounding error of the large DC column, whose
+// low modes pinv amplifies, into the small Nyquist column: the projected
+// field's divergence then grows tenfold at 2048 rows.)  Each writes back only
+// its own float of element 0.
 CFD_D void col_pinv_cols(const FvmParams& p, int blk, int W, int log2W, int bstride,
                           float2* __restrict__ spec) {
   extern __shared__ float2 sbuf[];
   const int L = p.ny >> 1, N = p.nx;
   const int c0 = blk * W;
+  const bool nyq = c0 >= L;  // the extra block: Nyquist column in slot 0
+  float* specf = reinterpret_cast<float*>(spec);
   const int tid = threadIdx.x;
 #pragma unroll 4
   for (int idx = tid; idx < W * N; idx += blockDim.x) {
-    const int w = idx & (W - 1), i = idx >> log2W;
-    sbuf[w * bstride + pidx(i)] = spec[(size_t)i * L + c0 + w];
+    const int w = idx & (W - 1), i = idx >> log2W, c = c0 + w;
+    float2 x;
+    if (nyq) x = make_float2(w == 0 ? specf[(size_t)i * L * 2 + 1] : 0.f, 0.f);
+    else if (c == 0) x = make_float2(specf[(size_t)i * L * 2], 0.f);
+    else x = spec[(size_t)i * L + c];
+    sbuf[w * bstride + pidx(i)] = x;
   }
   __syncthreads();
   fft_inplace<-1>(sbuf, p.log2nx, W, bstride, p.twp_x, tid);
   for (int idx = tid; idx < W * N; idx += blockDim.x) {
     const int w = idx & (W - 1), kx = idx >> log2W;
-    const int c = c0 + w;
-    if (c == 0) continue;
     float2* e = sbuf + w * bstride + pidx(kx);
-    *e = c_scale(*e, pinv_diag(p, kx, c));
-  }
-  if (c0 == 0) {
-    // Packed column: Z = A + iB with A, B the x-transforms of the DC and
-    // Nyquist columns.  Z' = d0 A + i dN B
-    //                      = (d0 + dN)/2 Z[k] + (d0 - dN)/2 conj Z[-k].
-    for (int k = tid; k <= N / 2; k += blockDim.x) {
-      const int m = (N - k) & (N - 1);
-      const float d0 = pinv_diag(p, k, 0), dn = pinv_diag(p, k, L);
-      const float al = 0.5f * (d0 + dn), be = 0.5f * (d0 - dn);
-      const float2 zk = sbuf[pidx(k)], zm = sbuf[pidx(m)];
-      sbuf[pidx(k)] = c_add(c_scale(zk, al), c_scale(c_conj(zm), be));
-      if (m != k) sbuf[pidx(m)] = c_add(c_scale(zm, al), c_scale(c_conj(zk), be));
-    }
+    *e = c_scale(*e, pinv_diag(p, kx, nyq ? L : c0 + w));
   }
   __syncthreads();
   fft_inplace<1>(sbuf, p.log2nx, W, bstride, p.twp_x, tid);
 #pragma unroll 4
   for (int idx = tid; idx < W * N; idx += blockDim.x) {
-    const int w = idx & (W - 1), i = idx >> log2W;
-    spec[(size_t)i * L + c0 + w] = sbuf[w * bstride + pidx(i)];
+    const int w = idx & (W - 1), i = idx >> log2W, c = c0 + w;
+    const float2 x = sbuf[w * bstride + pidx(i)];
+    if (nyq) {
+      if (w == 0) specf[(size_t)i * L * 2 + 1] = x.x;
+    } else if (c == 0) {
+      specf[(size_t)i * L * 2] = x.x;
+    } else {
+      spec[(size_t)i * L + c] = x;
+    }
   }
 }
 
@@ -779,6 +787,14 @@ __global__ void __launch_bounds__(MAXT, MINB)
 // block `rank` of the cluster moves rows [rank*nx/CL, (rank+1)*nx/CL) of all
 // CL columns between global memory and the owning blocks' shared memory, and
 // each block transforms its own column.
+// The column pass with one column per block and CL adjacent columns per
+// thread-block cluster.  Global memory is read and written in CL-column row
+// segments (32 or 64 bytes: whole sectors) through distributed shared memory:
+// block `rank` of the cluster moves rows [rank*nx/CL, (rank+1)*nx/CL) of all
+// CL columns between global memory and the owning blocks' shared memory, and
+// each block transforms its own column.  As in col_pinv_cols, column 0 is the
+// DC column alone and one extra cluster (first column L) carries the Nyquist
+// column in its block 0 (its other blocks transform zeros and store nothing).
 template <int CL>
 CFD_D void col_pinv_cluster_cols(const FvmParams& p, float2* __restrict__ spec) {
   extern __shared__ float2 sbuf[];
@@ -787,6 +803,8 @@ CFD_D void col_pinv_cluster_cols(const FvmParams& p, float2* __restrict__ spec) 
   const int L = p.ny >> 1, N = p.nx;
   const int c0 = blockIdx.x - rank;  // first column of this cluster
   const int c = c0 + rank;
+  const bool nyq = c0 >= L;
+  float* specf = reinterpret_cast<float*>(spec);
   const int tid = threadIdx.x;
   const int rows_per = N / CL, r0 = rank * rows_per;
   float2* dsm[CL];
@@ -795,44 +813,58 @@ CFD_D void col_pinv_cluster_cols(const FvmParams& p, float2* __restrict__ spec) 
   // Every block of the cluster must be running before any block touches a
   // peer's shared memory.
   cluster.sync();
+  if (nyq) {
+    for (int row = r0 + tid; row < r0 + rows_per; row += blockDim.x) {
+      dsm[0][pidx(row)] = make_float2(specf[(size_t)row * L * 2 + 1], 0.f);
+#pragma unroll
+      for (int r = 1; r < CL; ++r) dsm[r][pidx(row)] = make_float2(0.f, 0.f);
+    }
+  } else {
 #pragma unroll 2
-  for (int row = r0 + tid; row < r0 + rows_per; row += blockDim.x) {
-    const float4* src = reinterpret_cast<const float4*>(spec + (size_t)row * L + c0);
-    float4 v[CL / 2];
+    for (int row = r0 + tid; row < r0 + rows_per; row += blockDim.x) {
+      const float4* src = reinterpret_cast<const float4*>(spec + (size_t)row * L + c0);
+      float4 v[CL / 2];
 #pragma unroll
-    for (int h = 0; h < CL / 2; ++h) v[h] = src[h];
+      for (int h = 1; h < CL / 2; ++h) v[h] = src[h];
+      if (c0 == 0) {
+        // DC value only: the Nyquist float belongs to the extra cluster.
+        const float2 b = spec[(size_t)row * L + 1];
+        v[0] = make_float4(specf[(size_t)row * L * 2], 0.f, b.x, b.y);
+      } else {
+        v[0] = src[0];
+      }
 #pragma unroll
-    for (int h = 0; h < CL / 2; ++h) {
-      dsm[2 * h][pidx(row)] = make_float2(v[h].x, v[h].y);
-      dsm[2 * h + 1][pidx(row)] = make_float2(v[h].z, v[h].w);
+      for (int h = 0; h < CL / 2; ++h) {
+        dsm[2 * h][pidx(row)] = make_float2(v[h].x, v[h].y);
+        dsm[2 * h + 1][pidx(row)] = make_float2(v[h].z, v[h].w);
+      }
     }
   }
   cluster.sync();
   fft_inplace<-1>(sbuf, p.log2nx, 1, padded_len(N), p.twp_x, tid);
-  if (c != 0) {
-    for (int kx = tid; kx < N; kx += blockDim.x)
-      sbuf[pidx(kx)] = c_scale(sbuf[pidx(kx)], pinv_diag(p, kx, c));
-  } else {
-    // Packed DC/Nyquist column (see fvm_col_pinv_kernel).
-    for (int k = tid; k <= N / 2; k += blockDim.x) {
-      const int m = (N - k) & (N - 1);
-      const float d0 = pinv_diag(p, k, 0), dn = pinv_diag(p, k, L);
-      const float al = 0.5f * (d0 + dn), be = 0.5f * (d0 - dn);
-      const float2 zk = sbuf[pidx(k)], zm = sbuf[pidx(m)];
-      sbuf[pidx(k)] = c_add(c_scale(zk, al), c_scale(c_conj(zm), be));
-      if (m != k) sbuf[pidx(m)] = c_add(c_scale(zm, al), c_scale(c_conj(zk), be));
-    }
-  }
+  const int cp = nyq ? L : c;  // pinv column index
+  for (int kx = tid; kx < N; kx += blockDim.x)
+    sbuf[pidx(kx)] = c_scale(sbuf[pidx(kx)], pinv_diag(p, kx, cp));
   __syncthreads();
   fft_inplace<1>(sbuf, p.log2nx, 1, padded_len(N), p.twp_x, tid);
   cluster.sync();
+  if (nyq) {
+    for (int row = r0 + tid; row < r0 + rows_per; row += blockDim.x)
+      specf[(size_t)row * L * 2 + 1] = dsm[0][pidx(row)].x;
+  } else {
 #pragma unroll 2
-  for (int row = r0 + tid; row < r0 + rows_per; row += blockDim.x) {
-    float4* dst = reinterpret_cast<float4*>(spec + (size_t)row * L + c0);
+    for (int row = r0 + tid; row < r0 + rows_per; row += blockDim.x) {
+      float4* dst = reinterpret_cast<float4*>(spec + (size_t)row * L + c0);
 #pragma unroll
-    for (int h = 0; h < CL / 2; ++h) {
-      const float2 a = dsm[2 * h][pidx(row)], b = dsm[2 * h + 1][pidx(row)];
-      dst[h] = make_float4(a.x, a.y, b.x, b.y);
+      for (int h = 0; h < CL / 2; ++h) {
+        const float2 a = dsm[2 * h][pidx(row)], b = dsm[2 * h + 1][pidx(row)];
+        if (h == 0 && c0 == 0) {
+          specf[(size_t)row * L * 2] = a.x;
+          spec[(size_t)row * L + 1] = b;
+        } else {
+          dst[h] = make_float4(a.x, a.y, b.x, b.y);
+        }
+      }
     }
   }
   // No block may leave while a peer still reads its shared memory.
@@ -944,6 +976,96 @@ template <int MAXT, int MINB>
 __global__ void __launch_bounds__(MAXT, MINB)
     fvm_irfft_bulk_kernel(FvmParams p, int rows, float2* spec) {
   irfft_rows_bulk(p, blockIdx.x, rows, spec);
+}
+
+// ---- One warp per row (ny = 2048: L = 1024 packed complex values) ----
+// The row transforms of the pressure solve with the four-step warp FFT of
+// wfft.cuh: lane l reads complex elements l + 32 m straight from global
+// memory (coalesced), transforms in registers with one shared-memory
+// transpose, and writes elements l + 32 k1 (coalesced).  The real-FFT
+// untangling pairs X[k] with X[L - k] through a shuffle: for lane l >= 1 the
+// partner lives in lane 32 - l, register 31 - k1; for lane 0 in lane 0,
+// register 32 - k1.
+
+CFD_HD bool warp_rows_ok(const FvmParams& p) { return p.log2ny - 1 == kWarpFftLog2; }
+constexpr int kWarpRows = 4;  // rows (warps) per block
+
+CFD_D float2 shfl_idx2(float2 x, int src) {
+  return make_float2(__shfl_sync(kFull, x.x, src), __shfl_sync(kFull, x.y, src));
+}
+
+// Z[L - k] for k = lane + 32 k1, from the warp FFT's output registers.
+CFD_D float2 wfft_mirror(const float2 (&v)[32], int k1, int lane) {
+  float2 zp = shfl_idx2(v[wfft_slot(31 - k1)], (32 - lane) & 31);
+  if (lane == 0) zp = v[wfft_slot((32 - k1) & 31)];
+  return zp;
+}
+
+CFD_D void div_rfft_row_warp(const FvmParams& p, int i, const float* __restrict__ us,
+                             const float* __restrict__ vs, float2* __restrict__ spec,
+                             float2* tile) {
+  const int lane = threadIdx.x & 31;
+  const int L = p.ny >> 1, mx = p.nx - 1, my = p.ny - 1;
+  const size_t ny = (size_t)p.ny;
+  const float2* ua = reinterpret_cast<const float2*>(us + i * ny);
+  const float2* ub = reinterpret_cast<const float2*>(us + ((i - 1) & mx) * ny);
+  const float2* vc = reinterpret_cast<const float2*>(vs + i * ny);
+  float2 v[32];
+#pragma unroll
+  for (int m = 0; m < 32; ++m) {
+    const int n = lane + 32 * m;
+    const float2 a = __ldg(ua + n), b = __ldg(ub + n), c = __ldg(vc + n);
+    const float cm = __ldg(vs + i * ny + ((2 * n - 1) & my));
+    // D = (u - u[i-1]) / hx + (v - v[j-1]) / hy, as in div_rfft_rows
+    v[m] = make_float2((a.x - b.x) * p.inv_hx + (c.x - cm) * p.inv_hy,
+                       (a.y - b.y) * p.inv_hx + (c.y - c.x) * p.inv_hy);
+  }
+  warp_fft1024<-1>(v, tile, p.twp_y + wfft_table_offset(kWarpFftLog2));
+  float2* out = spec + (size_t)i * L;
+#pragma unroll
+  for (int k1 = 0; k1 < 32; ++k1) {
+    const int k = lane + 32 * k1;
+    const float2 z = v[wfft_slot(k1)], zp = wfft_mirror(v, k1, lane);
+    float2 xk, xm;
+    rfft_post_pair(z, zp, __ldg(p.tw_y + k), &xk, &xm);
+    // element 0 packs the real DC and Nyquist values
+    out[k] = k == 0 ? make_float2(z.x + z.y, z.x - z.y) : xk;
+  }
+}
+
+CFD_D void irfft_row_warp(const FvmParams& p, int i, float2* spec, float2* tile) {
+  const int lane = threadIdx.x & 31;
+  const int L = p.ny >> 1;
+  float2* row = spec + (size_t)i * L;
+  float2 v[32];
+#pragma unroll
+  for (int m = 0; m < 32; ++m) {
+    const int k = lane + 32 * m;
+    const float2 x = row[k], xm = row[(L - k) & (L - 1)];
+    float2 zk, zm;
+    irfft_pre_pair(x, xm, __ldg(p.tw_y + k), &zk, &zm);
+    v[m] = k == 0 ? make_float2(x.x + x.y, x.x - x.y) : zk;
+  }
+  warp_fft1024<1>(v, tile, p.twp_y + wfft_table_offset(kWarpFftLog2));
+  // q[2n], q[2n+1] = z[n] over the same row (every load above has completed:
+  // the transform depends on all of them).
+#pragma unroll
+  for (int k1 = 0; k1 < 32; ++k1) row[lane + 32 * k1] = v[wfft_slot(k1)];
+}
+
+__global__ void __launch_bounds__(32 * kWarpRows)
+    fvm_div_rfft_warp_kernel(FvmParams p, const float* __restrict__ us,
+                             const float* __restrict__ vs, float2* __restrict__ spec) {
+  __shared__ float2 tiles[kWarpRows][kWarpFftTile];
+  const int w = threadIdx.x >> 5;
+  div_rfft_row_warp(p, blockIdx.x * kWarpRows + w, us, vs, spec, tiles[w]);
+}
+
+__global__ void __launch_bounds__(32 * kWarpRows)
+    fvm_irfft_warp_kernel(FvmParams p, float2* spec) {
+  __shared__ float2 tiles[kWarpRows][kWarpFftTile];
+  const int w = threadIdx.x >> 5;
+  irfft_row_warp(p, blockIdx.x * kWarpRows + w, spec, tiles[w]);
 }
 
 // u = u* - (q[i+1] - q[i]) / hx ; v = v* - (q[j+1] - q[j]) / hy.
@@ -1093,6 +1215,26 @@ __global__ void __launch_bounds__(MAXT, MINB)
   irfft_rows(p, blockIdx.x, rows, m.spec);
 }
 
+__global__ void __launch_bounds__(32 * kWarpRows)
+    fvm_batch_div_rfft_warp_kernel(const FvmMember* __restrict__ mem, int k) {
+  __shared__ float2 tiles[kWarpRows][kWarpFftTile];
+  const FvmMember& m = mem[blockIdx.y];
+  if (k >= m.steps) return;
+  const FvmParams p = m.p;
+  const int dst = batch_dst(k), w = threadIdx.x >> 5;
+  div_rfft_row_warp(p, blockIdx.x * kWarpRows + w, m.f[dst][0], m.f[dst][1], m.spec, tiles[w]);
+}
+
+__global__ void __launch_bounds__(32 * kWarpRows)
+    fvm_batch_irfft_warp_kernel(const FvmMember* __restrict__ mem, int k) {
+  __shared__ float2 tiles[kWarpRows][kWarpFftTile];
+  const FvmMember& m = mem[blockIdx.y];
+  if (k >= m.steps) return;
+  const FvmParams p = m.p;
+  const int w = threadIdx.x >> 5;
+  irfft_row_warp(p, blockIdx.x * kWarpRows + w, m.spec, tiles[w]);
+}
+
 __global__ void fvm_batch_project_out_kernel(const FvmMember* __restrict__ mem) {
   const FvmMember& m = mem[blockIdx.y];
   if (m.steps <= 0) return;
@@ -1180,6 +1322,10 @@ template <int MAXT, int MINB>
 static cudaError_t div_rfft_impl(const FvmParams& p, int target, const float* us,
                                  const float* vs, float2* spec, cudaStream_t s) {
   const int log2L = p.log2ny - 1;
+  if (warp_rows_ok(p)) {
+    fvm_div_rfft_warp_kernel<<<p.nx / kWarpRows, 32 * kWarpRows, 0, s>>>(p, us, vs, spec);
+    return cudaGetLastError();
+  }
   const int rows = fft_rows_per_block(log2L, p.nx, target);
   const bool aligned = (((uintptr_t)us | (uintptr_t)vs | (uintptr_t)spec) & 15) == 0;
   if (p.row_feed == 1 && aligned) {
@@ -1218,7 +1364,8 @@ static cudaError_t col_pinv_impl(const FvmParams& p, int target, float2* spec,
   const size_t smem = (size_t)W * bstride * sizeof(float2);
   cudaError_t e = set_smem(fvm_col_pinv_kernel<MAXT, MINB>, smem);
   if (e != cudaSuccess) return e;
-  fvm_col_pinv_kernel<MAXT, MINB><<<L / W, block_threads(fft_workers(p.log2nx, W)), smem,
+  // L / W column groups plus the Nyquist block
+  fvm_col_pinv_kernel<MAXT, MINB><<<L / W + 1, block_threads(fft_workers(p.log2nx, W)), smem,
                                     s>>>(p, W, ilog2(W), bstride, spec);
   return cudaGetLastError();
 }
@@ -1229,7 +1376,9 @@ static cudaError_t col_pinv_cluster_impl(const FvmParams& p, float2* spec, cudaS
   const size_t smem = (size_t)padded_len(p.nx) * sizeof(float2);
   cudaError_t e = set_smem(fvm_col_pinv_cluster_kernel<CL>, smem);
   if (e != cudaSuccess) return e;
-  fvm_col_pinv_cluster_kernel<CL><<<L, block_threads(fft_workers(p.log2nx, 1)), smem, s>>>(p, spec);
+  // L columns plus the Nyquist cluster
+  fvm_col_pinv_cluster_kernel<CL><<<L + CL, block_threads(fft_workers(p.log2nx, 1)), smem, s>>>(
+      p, spec);
   return cudaGetLastError();
 }
 
@@ -1251,6 +1400,10 @@ template <int MAXT, int MINB>
 static cudaError_t irfft_impl(const FvmParams& p, int target, float2* spec,
                               cudaStream_t s) {
   const int log2L = p.log2ny - 1;
+  if (warp_rows_ok(p)) {
+    fvm_irfft_warp_kernel<<<p.nx / kWarpRows, 32 * kWarpRows, 0, s>>>(p, spec);
+    return cudaGetLastError();
+  }
   const int rows = fft_rows_per_block(log2L, p.nx, target);
   if (p.row_feed == 1 && (((uintptr_t)spec) & 15) == 0) {
     const size_t smem = irfft_bulk_smem(p.ny, rows);
@@ -1332,7 +1485,7 @@ bool bulk_feed_ok(const FvmParams& p) {
   // Whole rows move by bulk copies: 16-byte multiples, and the staged rows of
   // the widest block shape must fit in shared memory.
   const int log2L = p.log2ny - 1;
-  if (p.ny < 8) return false;
+  if (p.ny < 8 || warp_rows_ok(p)) return false;
   const int rows = fft_rows_per_block(log2L, p.nx, 256);
   // mbarrier transaction counts stay below 2^20 bytes.
   const size_t tx = (size_t)(2 * rows + 1) * p.ny * 4;
@@ -1347,6 +1500,12 @@ template <int MAXT, int MINB>
 static cudaError_t batch_rows_impl(const FvmParams& p, int target, const FvmMember* mem,
                                    int count, int k, bool inverse, cudaStream_t s) {
   const int log2L = p.log2ny - 1;
+  if (warp_rows_ok(p)) {
+    const dim3 wgrid(p.nx / kWarpRows, count);
+    if (inverse) fvm_batch_irfft_warp_kernel<<<wgrid, 32 * kWarpRows, 0, s>>>(mem, k);
+    else fvm_batch_div_rfft_warp_kernel<<<wgrid, 32 * kWarpRows, 0, s>>>(mem, k);
+    return cudaGetLastError();
+  }
   const int rows = fft_rows_per_block(log2L, p.nx, target);
   const size_t smem = (size_t)rows * padded_len(p.ny / 2) * sizeof(float2);
   const dim3 grid(p.nx / rows, count);
@@ -1373,7 +1532,7 @@ static cudaError_t batch_col_impl(const FvmParams& p, int target, const FvmMembe
   const size_t smem = (size_t)W * bstride * sizeof(float2);
   cudaError_t e = set_smem(fvm_batch_col_pinv_kernel<MAXT, MINB>, smem);
   if (e != cudaSuccess) return e;
-  fvm_batch_col_pinv_kernel<MAXT, MINB><<<dim3(L / W, count),
+  fvm_batch_col_pinv_kernel<MAXT, MINB><<<dim3(L / W + 1, count),
                                           block_threads(fft_workers(p.log2nx, W)), smem, s>>>(
       mem, k, W, ilog2(W), bstride);
   return cudaGetLastError();
@@ -1385,7 +1544,7 @@ static cudaError_t batch_col_cluster_impl(const FvmParams& p, const FvmMember* m
   const size_t smem = (size_t)padded_len(p.nx) * sizeof(float2);
   cudaError_t e = set_smem(fvm_batch_col_pinv_cluster_kernel<CL>, smem);
   if (e != cudaSuccess) return e;
-  fvm_batch_col_pinv_cluster_kernel<CL><<<dim3(p.ny / 2, count),
+  fvm_batch_col_pinv_cluster_kernel<CL><<<dim3(p.ny / 2 + CL, count),
                                           block_threads(fft_workers(p.log2nx, 1)), smem, s>>>(
       mem, k);
   return cudaGetLastError();

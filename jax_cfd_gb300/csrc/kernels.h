@@ -116,7 +116,7 @@ cudaError_t launch_max_speed(int n, const float* u, const float* v,
 struct SpecParams {
   int nx, ny, L;        // L = ny / 2; rfft half spectrum has L + 1 columns
   int log2nx, log2ny, log2L;
-  float inv_dn_x;       // unused placeholder for alignment
+  int col_mode;         // column passes: 0 per-block columns, 1 clusters of 4
   float dn_x, dn_y;     // float32(step * n): fftfreq denominators
   float two_pi;         // float32(2 pi)
   float lap_coef;       // float32((2 pi i)^2) = -4 pi^2
@@ -132,6 +132,9 @@ struct SpecParams {
   const float* kx;      // fftfreq(nx, hx) in float32 (nx)
   const float* ky;      // rfftfreq(ny, hy) in float32 (L + 1)
 };
+
+// Whether the clustered spectral column passes (col_mode 1) apply to this grid.
+bool spec_cluster_ok(const SpecParams& p);
 
 struct StageCoef {
   float beta;     // float32(beta_k), multiplies the previous h

@@ -17,8 +17,12 @@
 // Multiplying by a function of ky commutes with the x transforms, so the ky
 // factors are applied on the row side.  All transforms are unnormalised; the
 // irfftn 1/(nx*ny) is a power of two applied once to the product.
+#include <cooperative_groups.h>
+
 #include "fft.cuh"
 #include "kernels.h"
+
+namespace cg = cooperative_groups;
 
 namespace cfd {
 namespace {
@@ -97,6 +101,44 @@ __global__ void __launch_bounds__(256, 3)
 
 // x-transform of the advection row spectra, then one low-storage RK/CN stage
 // (or, with explicit_only, just F(u)).
+// Element (kx, c) of one low-storage RK/CN stage given the x-transformed
+// advection spectrum a (spectral/equations.py:160-190,
+// spectral/time_stepping.py:163-169), or just F(u) with explicit_only.
+CFD_D void stage_update_at(const SpecParams& p, const StageCoef& sc, int kx, int c, float2 a,
+                           float2* __restrict__ wst, float2* __restrict__ hst) {
+  const int ncols = p.L + 1;
+  const size_t g = (size_t)kx * ncols + c;
+  // explicit_terms: rfftn(advection) * filter (+ forcing curl)
+  float2 F = a;
+  if (p.filt_on) {
+    const float fl = filt(p, kx, c);
+    F = make_float2(a.x * fl, a.y * fl);
+  }
+  if (p.fc_full) F = c_add(F, __ldg(p.fc_full + g));
+  else if (p.fc_row0 && kx == 0) F = c_add(F, __ldg(p.fc_row0 + c));
+  if (sc.explicit_only) {
+    wst[g] = F;
+    return;
+  }
+  // h = F(u) + beta_k h
+  float2 h = F;
+  if (sc.has_h_in) {
+    const float2 ho = hst[g];
+    h = c_add(F, make_float2(sc.beta * ho.x, sc.beta * ho.y));
+  }
+  // linear_term = nu * laplace - drag; laplace = (2 pi i)^2 |k|^2
+  const float kxf = kx_of(p, kx), kyf = ky_of(p, c);
+  const float lin = p.nu * (p.lap_coef * (kxf * kxf + kyf * kyf)) - p.drag;
+  const float2 u = wst[g];
+  // u + gamma dt h + mu G(u), G(u) = linear_term * u
+  const float2 x = make_float2((u.x + sc.gdt * h.x) + sc.mu * (lin * u.x),
+                               (u.y + sc.gdt * h.y) + sc.mu * (lin * u.y));
+  // implicit_solve: 1 / (1 - mu * linear_term) * x
+  const float inv = __frcp_rn(1.f - sc.mu * lin);
+  wst[g] = make_float2(inv * x.x, inv * x.y);
+  if (sc.write_h) hst[g] = h;
+}
+
 CFD_D void col_update_cols(const SpecParams& p, const StageCoef& sc, int blk, int W,
                             int log2W, int bstride, const float2* __restrict__ ahat,
                             float2* __restrict__ wst, float2* __restrict__ hst) {
@@ -115,37 +157,7 @@ CFD_D void col_update_cols(const SpecParams& p, const StageCoef& sc, int blk, in
   for (int e = tid; e < W * N; e += blockDim.x) {
     const int w = e & (W - 1), kx = e >> log2W, c = c0 + w;
     if (c >= ncols) continue;
-    const size_t g = (size_t)kx * ncols + c;
-    // explicit_terms: rfftn(advection) * filter (+ forcing curl)
-    const float2 a = sbuf[w * bstride + pidx(kx)];
-    float2 F = a;
-    if (p.filt_on) {
-      const float fl = filt(p, kx, c);
-      F = make_float2(a.x * fl, a.y * fl);
-    }
-    if (p.fc_full) F = c_add(F, __ldg(p.fc_full + g));
-    else if (p.fc_row0 && kx == 0) F = c_add(F, __ldg(p.fc_row0 + c));
-    if (sc.explicit_only) {
-      wst[g] = F;
-      continue;
-    }
-    // h = F(u) + beta_k h
-    float2 h = F;
-    if (sc.has_h_in) {
-      const float2 ho = hst[g];
-      h = c_add(F, make_float2(sc.beta * ho.x, sc.beta * ho.y));
-    }
-    // linear_term = nu * laplace - drag; laplace = (2 pi i)^2 |k|^2
-    const float kxf = kx_of(p, kx), kyf = ky_of(p, c);
-    const float lin = p.nu * (p.lap_coef * (kxf * kxf + kyf * kyf)) - p.drag;
-    const float2 u = wst[g];
-    // u + gamma dt h + mu G(u), G(u) = linear_term * u
-    const float2 x = make_float2((u.x + sc.gdt * h.x) + sc.mu * (lin * u.x),
-                                 (u.y + sc.gdt * h.y) + sc.mu * (lin * u.y));
-    // implicit_solve: 1 / (1 - mu * linear_term) * x
-    const float inv = __frcp_rn(1.f - sc.mu * lin);
-    wst[g] = make_float2(inv * x.x, inv * x.y);
-    if (sc.write_h) hst[g] = h;
+    stage_update_at(p, sc, kx, c, sbuf[w * bstride + pidx(kx)], wst, hst);
   }
 }
 
@@ -283,6 +295,84 @@ __global__ void enstrophy_sum_kernel(int nx, int ny, float hx, float hy,
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
   if ((threadIdx.x & 31) == 0) atomicAdd(out, acc);
+}
+
+// Clustered column passes, the scheme of the FVM column pass: clusters of CL
+// one-column blocks; block `rank` moves rows [rank N/CL, (rank+1) N/CL) of the
+// cluster's CL columns (CL consecutive complex values per row) between global
+// memory and the owning blocks' shared memory, and each block transforms its
+// own column.  Columns past the last one (ncols = L + 1 is odd) transform
+// zeros and store nothing.  Each block's arithmetic is that of the per-block
+// kernels, so both give the same bits.
+template <int CL>
+__global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(128, 7)
+    spec_col_prep_cluster_kernel(SpecParams p, const float2* __restrict__ w, T4 t4) {
+  extern __shared__ float2 sbuf[];
+  cg::cluster_group cluster = cg::this_cluster();
+  const int rank = (int)cluster.block_rank();
+  const int N = p.nx, ncols = p.L + 1, f = blockIdx.y;
+  const int c0 = blockIdx.x - rank;
+  const int tid = threadIdx.x;
+  const int rows_per = N / CL, r0 = rank * rows_per;
+  // Every block of the cluster runs before any block touches a peer.
+  cluster.sync();
+  for (int row = r0 + tid; row < r0 + rows_per; row += blockDim.x) {
+#pragma unroll
+    for (int q = 0; q < CL; ++q) {
+      const int col = c0 + q;
+      cluster.map_shared_rank(sbuf, q)[pidx(row)] =
+          col < ncols ? prep_factor(p, f, row, col, w[(size_t)row * ncols + col])
+                      : make_float2(0.f, 0.f);
+    }
+  }
+  cluster.sync();
+  fft_inplace<1>(sbuf, p.log2nx, 1, padded_len(N), p.twp_x, tid);
+  cluster.sync();
+  float2* dst = t4.t[f];
+  for (int row = r0 + tid; row < r0 + rows_per; row += blockDim.x) {
+#pragma unroll
+    for (int q = 0; q < CL; ++q) {
+      const int col = c0 + q;
+      if (col < ncols) dst[(size_t)row * ncols + col] = cluster.map_shared_rank(sbuf, q)[pidx(row)];
+    }
+  }
+  // No block may leave while a peer still reads its shared memory.
+  cluster.sync();
+}
+
+template <int CL>
+__global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(128, 7)
+    spec_col_update_cluster_kernel(SpecParams p, StageCoef sc, const float2* __restrict__ ahat,
+                                   float2* __restrict__ wst, float2* __restrict__ hst) {
+  extern __shared__ float2 sbuf[];
+  cg::cluster_group cluster = cg::this_cluster();
+  const int rank = (int)cluster.block_rank();
+  const int N = p.nx, ncols = p.L + 1;
+  const int c0 = blockIdx.x - rank;
+  const int tid = threadIdx.x;
+  const int rows_per = N / CL, r0 = rank * rows_per;
+  cluster.sync();
+  for (int row = r0 + tid; row < r0 + rows_per; row += blockDim.x) {
+#pragma unroll
+    for (int q = 0; q < CL; ++q) {
+      const int col = c0 + q;
+      cluster.map_shared_rank(sbuf, q)[pidx(row)] =
+          col < ncols ? ahat[(size_t)row * ncols + col] : make_float2(0.f, 0.f);
+    }
+  }
+  cluster.sync();
+  fft_inplace<-1>(sbuf, p.log2nx, 1, padded_len(N), p.twp_x, tid);
+  cluster.sync();
+  // The stage update on this block's row range, in row order (coalesced).
+  for (int row = r0 + tid; row < r0 + rows_per; row += blockDim.x) {
+#pragma unroll
+    for (int q = 0; q < CL; ++q) {
+      const int col = c0 + q;
+      if (col < ncols)
+        stage_update_at(p, sc, row, col, cluster.map_shared_rank(sbuf, q)[pidx(row)], wst, hst);
+    }
+  }
+  cluster.sync();
 }
 
 // ---- Batched variants: the slot index is the last grid axis ----
@@ -475,8 +565,25 @@ cudaError_t set_smem(K kernel, size_t bytes) {
 
 }  // namespace
 
+constexpr int kSpecCluster = 4;
+
+bool spec_cluster_ok(const SpecParams& p) {
+  return p.col_mode == 1 && p.nx >= 256 && p.nx <= 2048;
+}
+
 cudaError_t launch_spec_col_prep(const SpecParams& p, const float2* w,
                                  float2* const t4[4], cudaStream_t s) {
+  T4 tt{{t4[0], t4[1], t4[2], t4[3]}};
+  if (spec_cluster_ok(p)) {
+    const int ncols = p.L + 1;
+    const int gx = (ncols + kSpecCluster - 1) / kSpecCluster * kSpecCluster;
+    const size_t smem = (size_t)padded_len(p.nx) * sizeof(float2);
+    cudaError_t e = set_smem(spec_col_prep_cluster_kernel<kSpecCluster>, smem);
+    if (e != cudaSuccess) return e;
+    spec_col_prep_cluster_kernel<kSpecCluster><<<dim3(gx, 4), threads_for(fft_workers(p.log2nx, 1)),
+                                                 smem, s>>>(p, w, tt);
+    return cudaGetLastError();
+  }
   const ColCfg c = col_cfg(p);
   cudaError_t e = set_smem(spec_col_prep_kernel, c.smem);
   if (e != cudaSuccess) return e;
@@ -489,11 +596,22 @@ cudaError_t launch_spec_col_prep(const SpecParams& p, const float2* w,
 cudaError_t launch_spec_col_update(const SpecParams& p, const StageCoef& sc,
                                    const float2* ahat, float2* w, float2* h,
                                    float2* const t4[4], cudaStream_t s) {
-  const ColCfg c = col_cfg(p);
-  cudaError_t e = set_smem(spec_col_update_kernel, c.smem);
-  if (e != cudaSuccess) return e;
-  spec_col_update_kernel<<<c.blocks, c.threads, c.smem, s>>>(
-      p, sc, c.W, c.log2W, c.bstride, ahat, w, h);
+  cudaError_t e;
+  if (spec_cluster_ok(p)) {
+    const int ncols = p.L + 1;
+    const int gx = (ncols + kSpecCluster - 1) / kSpecCluster * kSpecCluster;
+    const size_t smem = (size_t)padded_len(p.nx) * sizeof(float2);
+    e = set_smem(spec_col_update_cluster_kernel<kSpecCluster>, smem);
+    if (e != cudaSuccess) return e;
+    spec_col_update_cluster_kernel<kSpecCluster><<<gx, threads_for(fft_workers(p.log2nx, 1)),
+                                                   smem, s>>>(p, sc, ahat, w, h);
+  } else {
+    const ColCfg c = col_cfg(p);
+    e = set_smem(spec_col_update_kernel, c.smem);
+    if (e != cudaSuccess) return e;
+    spec_col_update_kernel<<<c.blocks, c.threads, c.smem, s>>>(
+        p, sc, c.W, c.log2W, c.bstride, ahat, w, h);
+  }
   e = cudaGetLastError();
   if (e != cudaSuccess || !sc.prep_next || sc.explicit_only) return e;
   return launch_spec_col_prep(p, w, t4, s);

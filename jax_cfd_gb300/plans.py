@@ -316,6 +316,17 @@ class SpecPlan:
   def nbytes(self) -> int:
     return int(self._lib.cfd_spec_plan_bytes(self._h))
 
+  LAUNCH_CHOICES = 2
+
+  def set_launch(self, choice: int):
+    """Column passes: 0 per-block columns, 1 clusters of four one-column
+    blocks (256 <= nx <= 2048).  Results do not change."""
+    nat.check(self._lib.cfd_spec_plan_set_launch(self._h, int(choice)), 'cfd_spec_plan_set_launch')
+
+  @property
+  def launch(self) -> int:
+    return int(self._lib.cfd_spec_plan_get_launch(self._h))
+
   def _real(self, t, name='x'):
     return require_field(t, self.shape, name=name)
 

@@ -120,3 +120,30 @@ def test_taylor_green_spectral_analytic(cuda_device):
   got = np.fft.irfftn(out.cpu().numpy(), s=(n, n), axes=(0, 1))
   want = ofvm.curl_2d(tg(steps * dt), og.step)
   assert np.abs(got - want).max() <= 1e-3
+
+
+@pytest.mark.parametrize('shape', [(256, 256), (512, 256), (2048, 2048)])
+@pytest.mark.parametrize('forcing', ['smooth', 'kolmogorov'])
+def test_cluster_column_passes_are_bitwise(cuda_device, shape, forcing):
+  """Clustered column passes (launch 1) give exactly the per-block bits."""
+  import jax_cfd_gb300.base as cfd
+  from jax_cfd_gb300.spectral import equations as seq
+  from jax_cfd_gb300.spectral import time_stepping as sts
+  _, w0 = _vorticity_hat(shape, seed=3)
+  grid = cfd.grids.Grid(shape, domain=((0, TWO_PI), (0, TWO_PI)))
+  if forcing == 'smooth':
+    eq = seq.ForcedNavierStokes2D(1e-3, grid, smooth=True)
+  else:
+    eq = seq.NavierStokes2D(1e-3, grid, forcing_fn=cfd.forcings.kolmogorov_forcing, drag=0.1)
+  plan = sts.crank_nicolson_rk4(eq, 1e-3).plan(cuda_device)
+  w = torch.from_numpy(w0.astype(np.complex64)).to(cuda_device)
+  default = plan.launch
+  try:
+    plan.set_launch(0)
+    base = plan.step(w, 3)
+    plan.set_launch(1)
+    assert plan.launch == 1
+    got = plan.step(w, 3)
+  finally:
+    plan.set_launch(default)
+  assert torch.equal(torch.view_as_real(got), torch.view_as_real(base))
