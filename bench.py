@@ -501,7 +501,11 @@ def run_gb300(args):
   # the speed dt was chosen for, and the reference algorithm overflows near
   # t = 0.9 at 2048^2 -- the oracle and this path blow up at the same step.)
   plan = step.plan(dev)
-  shape = plan.autotune(v0[0].data, v0[1].data, 20)
+  if args.launch >= 0:
+    plan.set_launch(args.launch)
+    shape = args.launch
+  else:
+    shape = plan.autotune(v0[0].data, v0[1].data, 20)
   v = v0
   for _ in range(args.warmup):
     v = run(v0)
@@ -571,6 +575,9 @@ def run_gb300(args):
     w0 = su.rfft2(cfd.finite_differences.curl_2d(v0).data, grid)
     eq = seq.ForcedNavierStokes2D(VISCOSITY, grid, smooth=True)
     sstep = sts.crank_nicolson_rk4(eq, 1e-3)
+    splan = sstep.plan(dev)
+    s_launch = splan.autotune(w0, 4) if args.spectral_launch < 0 else args.spectral_launch
+    splan.set_launch(s_launch)
     srun = cfd.funcutils.repeated(sstep, args.spectral_chunk)
     for _ in range(3):
       w = srun(w0)
@@ -598,6 +605,7 @@ def run_gb300(args):
                           'peak': peak, 'unit': 'GB/s',
                           'frac': SPEC_STEP_BYTES_PER_CELL * s_value / 1e9 / peak},
         'kernel_ms': sk,
+        'column_pass': ['blocks', 'cluster4', 'pipelined4', 'pipelined2'][s_launch],
         'roofline': {'kernel': s_dom, 'bound': 'hbm', 'achieved': s_ach, 'peak': peak,
                      'unit': 'GB/s', 'frac': s_ach / peak},
         'finite': bool(torch.isfinite(torch.view_as_real(w)).all()),
@@ -636,9 +644,10 @@ def run_gb300(args):
                  'grid': [n, n], 'time_steps_per_step': chunk, 'dt': dt,
                  'l2': 'flushed (256 MiB write) between bench steps',
                  'launch_config': {'row_blocks': ['wide', 'narrow'][shape & 1],
-                                   'column_pass': ['blocks', 'cluster4',
-                                                   'cluster8'][(shape >> 1) % 3],
-                                   'stencil': ['tiles', 'warp_streams'][shape // 6]},
+                                   'column_pass': ['blocks', 'cluster4', 'cluster8',
+                                                   'pipelined4', 'pipelined2'][(shape >> 1) % 5],
+                                   'stencil': ['tiles', 'warp_streams'][(shape // 10) & 1],
+                                   'row_feed': ['registers', 'bulk_copy'][shape // 20]},
                  'parallelism': 'replicas' if world > 1 else 'single'},
       'roofline': {'kernel': dominant, 'bound': 'hbm', 'achieved': achieved, 'peak': peak,
                    'unit': 'GB/s', 'frac': achieved / peak, 'traffic': traffic,
@@ -670,7 +679,11 @@ def main():
   ap.add_argument('--impl', choices=['gb300', 'reference'], default='gb300')
   ap.add_argument('--size', type=int, default=N)
   ap.add_argument('--chunk', type=int, default=200)
+  ap.add_argument('--launch', type=int, default=-1,
+                  help='pin the FVM launch configuration (default: autotune)')
   ap.add_argument('--spectral-chunk', type=int, default=20)
+  ap.add_argument('--spectral-launch', type=int, default=-1,
+                  help='pin the spectral column-pass scheme (default: autotune)')
   ap.add_argument('--cpu-steps', type=int, default=5)
   ap.add_argument('--skip-cpu', action='store_true')
   ap.add_argument('--skip-spectral', action='store_true')

@@ -123,8 +123,11 @@ int cfd_fvm_plan_autotune(cfd_fvm_plan* plan, void* stream, const float* u,
                           const float* v, float* u_scratch, float* v_scratch,
                           int steps, int* chosen);
 /* Pins the launch configuration (an index as cfd_fvm_plan_autotune reports:
- * row-transform shape + 2 * column scheme + 6 * stencil scheme + 12 * row
- * feed, 24 choices); results do not depend on it.  cfd_fvm_plan_get_launch
+ * row-transform shape (0 wide, 1 narrow) + 2 * column scheme (0 blocks,
+ * 1/2 clusters of 4/8, 3/4 persistent pipelined groups of 4/2 columns)
+ * + 10 * stencil scheme (0 shared-memory tiles, 1 warp streams) + 20 * row
+ * feed (0 registers, 1 bulk copies): 40 choices); results do not depend on
+ * it.  cfd_fvm_plan_get_launch
  * returns the current one. */
 int cfd_fvm_plan_set_launch(cfd_fvm_plan* plan, int choice);
 int cfd_fvm_plan_get_launch(const cfd_fvm_plan* plan);
@@ -244,9 +247,11 @@ typedef struct cfd_spec_plan cfd_spec_plan;
 int cfd_spec_plan_create(const cfd_spec_config* cfg, cfd_spec_plan** plan);
 int cfd_spec_plan_destroy(cfd_spec_plan* plan);
 long long cfd_spec_plan_bytes(const cfd_spec_plan* plan);
-/* Launch configuration of the column passes: 0 per-block columns (default),
- * 1 clusters of four one-column blocks exchanging rows through distributed
- * shared memory (256 <= nx <= 2048).  Results are bit-for-bit the same. */
+/* Launch configuration of the column passes: 0 per-block columns, 1 clusters
+ * of four one-column blocks exchanging rows through distributed shared memory
+ * (256 <= nx <= 2048), 2/3 persistent blocks that stage the next group of
+ * 4/2 columns with cp.async while transforming the current one in registers
+ * (512 <= nx <= 4096).  Results are bit-for-bit the same. */
 int cfd_spec_plan_set_launch(cfd_spec_plan* plan, int choice);
 int cfd_spec_plan_get_launch(const cfd_spec_plan* plan);
 /* Velocity-independent forcing (fx, fy real [nx, ny] on the device, either may

@@ -97,21 +97,22 @@ cudaError_t upload(T** dev, const T* host, size_t count) {
 cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
 // Launch configurations of the FVM step (see cfd_fvm_plan_autotune).
-// Index = row-transform shape + 2 * column scheme + 6 * stencil scheme
-// + 12 * row feed.
-constexpr int kLaunchChoices = 24;
+// Index = row-transform shape + 2 * column scheme + 10 * stencil scheme
+// + 20 * row feed.
+constexpr int kLaunchChoices = 40;
 bool launch_choice_ok(const cfd::FvmParams& p, int c) {
-  const int col = (c >> 1) % 3, stencil = (c / 6) & 1, feed = c / 12;
-  if (col > 0 && !cfd::col_cluster_ok(p, col == 1 ? 4 : 8)) return false;
+  const int col = (c >> 1) % 5, stencil = (c / 10) & 1, feed = c / 20;
+  if ((col == 1 || col == 2) && !cfd::col_cluster_ok(p, col == 1 ? 4 : 8)) return false;
+  if (col >= 3 && !cfd::col_pipe_ok(p, col == 4)) return false;
   if (stencil == 1 && !cfd::stream_stencil_ok(p)) return false;
   if (feed == 1 && !cfd::bulk_feed_ok(p)) return false;
   return true;
 }
 void set_launch_choice(cfd::FvmParams* p, int c) {
   p->fft_shape = c & 1;
-  p->col_mode = (c >> 1) % 3;
-  p->stencil = (c / 6) & 1;
-  p->row_feed = c / 12;
+  p->col_mode = (c >> 1) % 5;
+  p->stencil = (c / 10) & 1;
+  p->row_feed = c / 20;
 }
 
 // Captures `enqueue` (run on a private capture stream) into an executable graph.
@@ -323,6 +324,8 @@ static int fvm_params_from_config(const cfd_fvm_config* cfg, cfd::FvmParams* out
   p.fft_shape = (nx >= 1024 && ny >= 1024) ? 1 : 0;
   // The warp-streaming stencil needs enough warps to fill the GPU.
   p.stencil = ((long long)nx * ny >= (1LL << 22) && cfd::stream_stencil_ok(p)) ? 1 : 0;
+  // The persistent column pass measured fastest from 1024 rows up (GB300).
+  p.col_mode = (nx >= 1024 && cfd::col_pipe_ok(p, 0)) ? 3 : 0;
   return CFD_OK;
 }
 
@@ -618,8 +621,10 @@ int cfd_fvm_plan_autotune(cfd_fvm_plan* plan, void* stream, const float* u,
   int best = -1;
   int rc = CFD_OK;
   // Candidates: transform block shape (wide, narrow) x column pass (per-block
-  // columns, clusters of 4, clusters of 8) x stencil (shared-memory tiles,
-  // warp streams); index = shape + 2 * col_mode + 6 * stencil.
+  // columns, clusters of 4, clusters of 8, persistent pipelined groups of 4
+  // or 2 columns) x
+  // stencil (shared-memory tiles, warp streams) x row feed; index as in
+  // set_launch_choice.
   for (int cand = 0; cand < kLaunchChoices && rc == CFD_OK; ++cand) {
     if (!launch_choice_ok(plan->p, cand)) continue;
     set_launch_choice(&plan->p, cand);
@@ -660,8 +665,8 @@ int cfd_fvm_plan_set_launch(cfd_fvm_plan* plan, int choice) {
 
 int cfd_fvm_plan_get_launch(const cfd_fvm_plan* plan) {
   if (!plan) return -1;
-  return plan->p.fft_shape + 2 * plan->p.col_mode + 6 * plan->p.stencil +
-         12 * plan->p.row_feed;
+  return plan->p.fft_shape + 2 * plan->p.col_mode + 10 * plan->p.stencil +
+         20 * plan->p.row_feed;
 }
 
 // ---- Same-shape batches -------------------------------------------------
@@ -1261,8 +1266,13 @@ int cfd_spec_plan_create(const cfd_spec_config* cfg, cfd_spec_plan** out) {
   cfd_spec_plan* plan = new cfd_spec_plan();
   cfd::SpecParams& p = plan->p;
   p = params;
-  // Clustered column passes measured faster at 256^2 and 512^2 (GB300).
+  // Clustered column passes measured faster at 256^2 and 512^2, the
+  // persistent pipelined ones at 2048^2 (GB300).
   p.col_mode = (cfg->nx >= 256 && cfg->nx <= 512) ? 1 : 0;
+  if (cfg->nx >= 1024) {
+    p.col_mode = 2;
+    if (!cfd::spec_pipe_ok(p)) p.col_mode = 0;
+  }
   plan->stages = stages;
   for (int k = 0; k < stages; ++k) plan->coef[k] = coef[k];
   const int nx = cfg->nx;
@@ -1307,11 +1317,11 @@ int cfd_spec_plan_create(const cfd_spec_config* cfg, cfd_spec_plan** out) {
 long long cfd_spec_plan_bytes(const cfd_spec_plan* plan) { return plan ? plan->bytes : 0; }
 
 int cfd_spec_plan_set_launch(cfd_spec_plan* plan, int choice) {
-  if (!plan || choice < 0 || choice > 1)
+  if (!plan || choice < 0 || choice > 3)
     return fail(CFD_ERR_INVALID_ARGUMENT, "cfd_spec_plan_set_launch: bad arguments");
   cfd::SpecParams q = plan->p;
   q.col_mode = choice;
-  if (choice == 1 && !cfd::spec_cluster_ok(q))
+  if ((choice == 1 && !cfd::spec_cluster_ok(q)) || (choice >= 2 && !cfd::spec_pipe_ok(q)))
     return fail(CFD_ERR_UNSUPPORTED, "cfd_spec_plan_set_launch: choice not available on this grid");
   plan->p.col_mode = choice;
   return CFD_OK;

@@ -1,0 +1,123 @@
+#pragma once
+
+#include "common.cuh"
+#include "fft.cuh"
+
+namespace cfd {
+
+// Persistent column passes with register-resident Stockham passes, shared by
+// the FVM pressure solve and the spectral stage kernels.
+//
+// A block owns CG adjacent columns at a time (a group), walks its work items
+// with the grid as its stride, and copies the next item's input into shared
+// memory (cp.async, each thread its own points) while it transforms the
+// current one, so the global traffic of one item overlaps the arithmetic of
+// the other.  Worker t of a column holds the 16 points x[t + (N/16) r] that
+// the first Stockham pass of fft_inplace gives it; every pass runs the same
+// butterflies on the same twiddles as fft_inplace (so results are bit for bit
+// those of the shared-memory engine), with shared memory used only to
+// exchange data between passes: two buffers written alternately, one barrier
+// per exchange.  The last pass leaves X[t + (N/16) m] in the worker's
+// registers, which are exactly the first inverse pass's inputs, so a scaling
+// between a forward and an inverse transform needs no exchange at all.
+template <int LOG2N>
+struct ColPipe {
+  static constexpr int N = 1 << LOG2N;
+  static constexpr int NTHR = N / 16;     // workers per column
+  static constexpr int N16 = LOG2N >> 2;  // radix-16 passes
+  static constexpr int REM = LOG2N & 3;   // radix 2^REM of the last pass (0: none)
+  static constexpr int PASSES = N16 + (REM ? 1 : 0);
+};
+
+// Float2 slots per column buffer: the padded sequence plus 16/CG slots, so
+// the CG columns a half warp touches start in different banks.
+template <int LOG2N, int CG>
+CFD_HD int col_pipe_bstride() {
+  return padded_len(1 << LOG2N) + 16 / CG;
+}
+
+// Two exchange buffers per column, then 16 staging slots per thread.
+template <int LOG2N, int CG>
+CFD_HD size_t col_pipe_smem() {
+  return ((size_t)2 * CG * col_pipe_bstride<LOG2N, CG>() + (size_t)CG * (1 << LOG2N)) *
+         sizeof(float2);
+}
+
+// One transform of sign SIGN of the calling worker's column.  v: the pass-0
+// inputs x[t + NTHR r] on entry, X[t + NTHR m] in v[m] on return.  buf[0],
+// buf[1]: this column's two exchange buffers; the k-th exchange of the
+// transform writes buf[(FIRST + k) & 1].  Called by every thread of the block
+// (it contains barriers).
+template <int LOG2N, int SIGN, int FIRST>
+CFD_D void col_pipe_fft(float2 (&v)[16], float2* const (&buf)[2], int t,
+                        const float2* __restrict__ twp) {
+  using P = ColPipe<LOG2N>;
+  int wsel = FIRST;
+  int tw_off = 0;
+#pragma unroll
+  for (int q = 0; q < P::N16; ++q) {
+    const int Ns = 1 << (4 * q);
+    if (q > 0) {
+      const float2* in = buf[wsel ^ 1];
+#pragma unroll
+      for (int r = 0; r < 16; ++r) v[r] = in[pidx(t + P::NTHR * r)];
+    }
+    const int k = t & (Ns - 1);
+    if (Ns > 1) apply_twiddles<16, SIGN>(v, twp + tw_off, Ns, k);
+    Dft<16, SIGN>::run(v);
+    if (q > 0) tw_off += 15 << (4 * q);
+    const bool last = q == P::N16 - 1 && P::REM == 0;
+    if (!last) {
+      float2* out = buf[wsel];
+      const int o = ((t - k) << 4) + k;
+#pragma unroll
+      for (int r = 0; r < 16; ++r) out[pidx(o + r * Ns)] = v[r];
+      wsel ^= 1;
+      __syncthreads();
+    }
+  }
+  if constexpr (P::REM > 0) {
+    constexpr int R = 1 << P::REM, NB = 16 / R;
+    constexpr int Ns = P::N / R;  // = N / R: the final span
+    const float2* in = buf[wsel ^ 1];
+    float2 vv[NB][R];
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+      const int j = t + P::NTHR * b;
+#pragma unroll
+      for (int r = 0; r < R; ++r) vv[b][r] = in[pidx(j + Ns * r)];
+    }
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+      const int j = t + P::NTHR * b;
+      apply_twiddles<R, SIGN>(vv[b], twp + tw_off, Ns, j);
+      Dft<R, SIGN>::run(vv[b]);
+      // X[j + Ns r] = X[t + NTHR (b + NB r)]
+#pragma unroll
+      for (int r = 0; r < R; ++r) v[b + NB * r] = vv[b][r];
+    }
+  }
+}
+
+// Asynchronous 8-byte global -> shared copy (cp.async, L1-allocating).
+CFD_D void cp_async8(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+CFD_D void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+CFD_D void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// Multiprocessors of the current device (host side; 1 if the query fails).
+static inline int col_pipe_device_sms() {
+  int dev = 0, n = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n < 1)
+    return 1;
+  return n;
+}
+
+// Register cap of 128 at every block size (512 threads per multiprocessor or
+// more), for __launch_bounds__(T, col_pipe_min_blocks(T)).
+constexpr int col_pipe_min_blocks(int threads) { return threads >= 512 ? 1 : 512 / threads; }
+
+}  // namespace cfd

@@ -17,6 +17,7 @@
 #include <cooperative_groups.h>
 
 #include "bulk.cuh"
+#include "colpipe.cuh"
 #include "fft.cuh"
 #include "kernels.h"
 #include "wfft.cuh"
@@ -877,6 +878,104 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(128, 7)
   col_pinv_cluster_cols<CL>(p, spec);
 }
 
+// ---- Persistent FVM column pass (engine in colpipe.cuh) ----
+// Requests worker t's pass-0 points of group g into its own staging slots
+// stage[r * T + tid] (T threads per block).  Column c = g * CG + w; the
+// Nyquist group's slot 0 reads row element 0 (its imaginary part is the
+// Nyquist value), its other slots read nothing.
+template <int LOG2N, int CG>
+CFD_D void col_pipe_prefetch(const float2* __restrict__ spec, int L, int g, int w, int t,
+                             float2* __restrict__ stage) {
+  constexpr int NTHR = ColPipe<LOG2N>::NTHR, T = CG * NTHR;
+  const bool nyq = g * CG >= L;
+  if (nyq && w != 0) return;
+  const int c = nyq ? 0 : g * CG + w;
+  const int tid = t * CG + w;
+#pragma unroll
+  for (int r = 0; r < 16; ++r) cp_async8(stage + r * T + tid, spec + (size_t)(t + NTHR * r) * L + c);
+}
+
+// Worker t's pass-0 points from its staging slots: the DC column (c == 0)
+// takes the real parts of row element 0, the Nyquist column their imaginary
+// parts, both as real sequences; the Nyquist group's other slots are zeros.
+template <int LOG2N, int CG>
+CFD_D void col_pipe_take(const float2* __restrict__ stage, int L, int g, int w, int t,
+                         float2 (&v)[16]) {
+  constexpr int NTHR = ColPipe<LOG2N>::NTHR, T = CG * NTHR;
+  const int c = g * CG + w;
+  const bool nyq = g * CG >= L;
+  const int tid = t * CG + w;
+  if (!nyq && c != 0) {
+#pragma unroll
+    for (int r = 0; r < 16; ++r) v[r] = stage[r * T + tid];
+  } else {
+#pragma unroll
+    for (int r = 0; r < 16; ++r) {
+      const float2 x = stage[r * T + tid];
+      v[r] = make_float2(nyq ? (w == 0 ? x.y : 0.f) : x.x, 0.f);
+    }
+  }
+}
+
+template <int LOG2N, int CG>
+CFD_D void col_pipe_store(float2* __restrict__ spec, int L, int g, int w, int t,
+                          const float2 (&v)[16]) {
+  constexpr int NTHR = ColPipe<LOG2N>::NTHR;
+  const int c = g * CG + w;
+  const bool nyq = g * CG >= L;
+  if (!nyq && c != 0) {
+#pragma unroll
+    for (int r = 0; r < 16; ++r) spec[(size_t)(t + NTHR * r) * L + c] = v[r];
+  } else if (!nyq || w == 0) {
+    float* specf = reinterpret_cast<float*>(spec);
+    const int off = nyq ? 1 : 0;
+#pragma unroll
+    for (int r = 0; r < 16; ++r) specf[(size_t)(t + NTHR * r) * L * 2 + off] = v[r].x;
+  }
+}
+
+template <int LOG2N, int CG>
+CFD_D void col_pinv_pipe_cols(const FvmParams& p, float2* __restrict__ spec, int g0,
+                              int gstep) {
+  using P = ColPipe<LOG2N>;
+  extern __shared__ float2 sbuf[];
+  const int L = p.ny >> 1;
+  const int groups = L / CG + 1;
+  const int w = threadIdx.x % CG, t = threadIdx.x / CG;
+  const int bstride = col_pipe_bstride<LOG2N, CG>();
+  float2* const buf[2] = {sbuf + w * bstride, sbuf + (CG + w) * bstride};
+  float2* const stage = sbuf + 2 * CG * bstride;  // 16 * T slots
+  constexpr int INV_FIRST = (P::PASSES - 1) & 1;
+  if (g0 >= groups) return;  // uniform per block
+  float2 v[16];
+  col_pipe_prefetch<LOG2N, CG>(spec, L, g0, w, t, stage);
+  cp_async_commit();
+#pragma unroll 1
+  for (int g = g0; g < groups; g += gstep) {
+    // Each thread reads back only the slots it requested itself, so its own
+    // wait is the only ordering needed before it reuses them.
+    cp_async_wait_all();
+    col_pipe_take<LOG2N, CG>(stage, L, g, w, t, v);
+    const int gn = g + gstep;
+    if (gn < groups) col_pipe_prefetch<LOG2N, CG>(spec, L, gn, w, t, stage);
+    cp_async_commit();
+    col_pipe_fft<LOG2N, -1, 0>(v, buf, t, p.twp_x);
+    const int cp = g * CG >= L ? L : g * CG + w;  // pinv column index
+#pragma unroll
+    for (int m = 0; m < 16; ++m) v[m] = c_scale(v[m], pinv_diag(p, t + P::NTHR * m, cp));
+    col_pipe_fft<LOG2N, 1, INV_FIRST>(v, buf, t, p.twp_x);
+    col_pipe_store<LOG2N, CG>(spec, L, g, w, t, v);
+  }
+  cp_async_wait_all();
+}
+
+template <int LOG2N, int CG>
+__global__ void __launch_bounds__(CG * (1 << LOG2N) / 16,
+                                  col_pipe_min_blocks(CG * (1 << LOG2N) / 16))
+    fvm_col_pinv_pipe_kernel(FvmParams p, float2* __restrict__ spec) {
+  col_pinv_pipe_cols<LOG2N, CG>(p, spec, blockIdx.x, gridDim.x);
+}
+
 // Inverse packed real FFT of each row, in place: q^ rows -> q rows (floats).
 CFD_D void irfft_rows(const FvmParams& p, int blk, int rows, float2* spec) {
   extern __shared__ float2 sbuf[];
@@ -1387,11 +1486,63 @@ bool col_cluster_ok(const FvmParams& p, int cl) {
   return p.nx >= 256 && p.nx <= 2048 && (p.ny / 2) % cl == 0;
 }
 
-// col_mode 1/2: clusters of 4/8 single-column blocks.
+// Persistent column pass: as many blocks as fit on the device at once (one
+// per multiprocessor at 2048 rows), never more than there are groups.
+template <int LOG2N, int CG>
+static cudaError_t col_pinv_pipe_impl(const FvmParams& p, float2* spec, cudaStream_t s) {
+  const size_t smem = col_pipe_smem<LOG2N, CG>();
+  const int threads = CG * (1 << LOG2N) / 16;
+  auto kern = fvm_col_pinv_pipe_kernel<LOG2N, CG>;
+  cudaError_t e = set_smem(kern, smem);
+  if (e != cudaSuccess) return e;
+  static int per_sm = 0;  // same value for every device of one kind
+  if (per_sm == 0) {
+    int nb = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, threads, smem);
+    if (e != cudaSuccess) return e;
+    per_sm = nb > 0 ? nb : 1;
+  }
+  const int groups = p.ny / 2 / CG + 1;
+  const int slots = col_pipe_device_sms() * per_sm;
+  kern<<<groups < slots ? groups : slots, threads, smem, s>>>(p, spec);
+  return cudaGetLastError();
+}
+
+// Column groups of the persistent pass: 4 columns per block (wide, col_mode
+// 3; 2 at 4096 rows) or 2 (narrow, col_mode 4: two independent blocks per
+// multiprocessor at 2048 rows, so their barriers do not stall one another).
+bool col_pipe_ok(const FvmParams& p, int narrow) {
+  const int cg = (narrow || p.log2nx == 12) ? 2 : 4;
+  return p.log2nx >= 8 && p.log2nx <= 12 && (p.ny / 2) % cg == 0;
+}
+
+static cudaError_t col_pinv_pipe_launch(const FvmParams& p, float2* spec, cudaStream_t s) {
+  if (p.col_mode == 4) {
+    switch (p.log2nx) {
+      case 8: return col_pinv_pipe_impl<8, 2>(p, spec, s);
+      case 9: return col_pinv_pipe_impl<9, 2>(p, spec, s);
+      case 10: return col_pinv_pipe_impl<10, 2>(p, spec, s);
+      case 11: return col_pinv_pipe_impl<11, 2>(p, spec, s);
+      default: return col_pinv_pipe_impl<12, 2>(p, spec, s);
+    }
+  }
+  switch (p.log2nx) {
+    case 8: return col_pinv_pipe_impl<8, 4>(p, spec, s);
+    case 9: return col_pinv_pipe_impl<9, 4>(p, spec, s);
+    case 10: return col_pinv_pipe_impl<10, 4>(p, spec, s);
+    case 11: return col_pinv_pipe_impl<11, 4>(p, spec, s);
+    default: return col_pinv_pipe_impl<12, 2>(p, spec, s);
+  }
+}
+
+// col_mode 1/2: clusters of 4/8 single-column blocks; 3/4: the persistent
+// register-pipelined pass with 4 / 2 columns per block.
 cudaError_t launch_fvm_col_pinv(const FvmParams& p, float2* spec,
                                 cudaStream_t s) {
+  if (p.col_mode >= 3 && col_pipe_ok(p, p.col_mode == 4)) return col_pinv_pipe_launch(p, spec, s);
   if (p.col_mode == 2 && col_cluster_ok(p, 8)) return col_pinv_cluster_impl<8>(p, spec, s);
-  if (p.col_mode >= 1 && col_cluster_ok(p, 4)) return col_pinv_cluster_impl<4>(p, spec, s);
+  if ((p.col_mode == 1 || p.col_mode == 2) && col_cluster_ok(p, 4))
+    return col_pinv_cluster_impl<4>(p, spec, s);
   return p.fft_shape == 1 ? col_pinv_impl<128, 7>(p, 128, spec, s)
                           : col_pinv_impl<256, 3>(p, 256, spec, s);
 }

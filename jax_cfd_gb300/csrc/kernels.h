@@ -44,7 +44,8 @@ struct FvmParams {
   const float2* twp_x;  // pass twiddle tables of the length-nx column FFT
   const float2* twp_y;  // pass twiddle tables of the length-ny/2 row FFT
   int fft_shape;       // transform block shape: 0 wide, 1 narrow (see fvm.cu)
-  int col_mode;        // column pass: 0 per-block columns, 1/2 clusters of 4/8
+  int col_mode;        // column pass: 0 per-block columns, 1/2 clusters of 4/8,
+                       // 3/4 persistent register-pipelined groups of 4/2 columns
   int stencil;         // explicit step: 0 shared-memory tiles, 1 warp streams
   int row_feed;        // row transforms: 0 loads through registers, 1 bulk copies
 };
@@ -70,6 +71,9 @@ cudaError_t launch_fvm_col_pinv(const FvmParams& p, float2* spec,
                                 cudaStream_t s);
 // Whether the cluster column pass (col_mode 1/2) applies to this grid.
 bool col_cluster_ok(const FvmParams& p, int cluster);
+// Whether the persistent column pass (col_mode 3, or 4 with narrow != 0)
+// applies to this grid.
+bool col_pipe_ok(const FvmParams& p, int narrow);
 // Whether the warp-streaming stencil (stencil 1) applies to this grid.
 bool stream_stencil_ok(const FvmParams& p);
 // Whether the bulk-copy row transforms (row_feed 1) apply to this grid.
@@ -116,7 +120,8 @@ cudaError_t launch_max_speed(int n, const float* u, const float* v,
 struct SpecParams {
   int nx, ny, L;        // L = ny / 2; rfft half spectrum has L + 1 columns
   int log2nx, log2ny, log2L;
-  int col_mode;         // column passes: 0 per-block columns, 1 clusters of 4
+  int col_mode;         // column passes: 0 per-block columns, 1 clusters of 4,
+                        // 2/3 persistent register-pipelined groups of 4/2 columns
   float dn_x, dn_y;     // float32(step * n): fftfreq denominators
   float two_pi;         // float32(2 pi)
   float lap_coef;       // float32((2 pi i)^2) = -4 pi^2
@@ -135,6 +140,8 @@ struct SpecParams {
 
 // Whether the clustered spectral column passes (col_mode 1) apply to this grid.
 bool spec_cluster_ok(const SpecParams& p);
+// Whether the persistent spectral column passes (col_mode 2/3) apply to this grid.
+bool spec_pipe_ok(const SpecParams& p);
 
 struct StageCoef {
   float beta;     // float32(beta_k), multiplies the previous h

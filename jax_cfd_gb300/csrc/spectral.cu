@@ -19,6 +19,7 @@
 // irfftn 1/(nx*ny) is a power of two applied once to the product.
 #include <cooperative_groups.h>
 
+#include "colpipe.cuh"
 #include "fft.cuh"
 #include "kernels.h"
 
@@ -104,8 +105,10 @@ __global__ void __launch_bounds__(256, 3)
 // Element (kx, c) of one low-storage RK/CN stage given the x-transformed
 // advection spectrum a (spectral/equations.py:160-190,
 // spectral/time_stepping.py:163-169), or just F(u) with explicit_only.
-CFD_D void stage_update_at(const SpecParams& p, const StageCoef& sc, int kx, int c, float2 a,
-                           float2* __restrict__ wst, float2* __restrict__ hst) {
+// The stage arithmetic of one element from its loaded state u and register h
+// (ho, read only when sc.has_h_in): returns the new state, sets *h_new.
+CFD_D float2 stage_update_core(const SpecParams& p, const StageCoef& sc, int kx, int c,
+                               float2 a, float2 u, float2 ho, float2* h_new) {
   const int ncols = p.L + 1;
   const size_t g = (size_t)kx * ncols + c;
   // explicit_terms: rfftn(advection) * filter (+ forcing curl)
@@ -117,25 +120,34 @@ CFD_D void stage_update_at(const SpecParams& p, const StageCoef& sc, int kx, int
   if (p.fc_full) F = c_add(F, __ldg(p.fc_full + g));
   else if (p.fc_row0 && kx == 0) F = c_add(F, __ldg(p.fc_row0 + c));
   if (sc.explicit_only) {
-    wst[g] = F;
-    return;
+    *h_new = F;
+    return F;
   }
   // h = F(u) + beta_k h
   float2 h = F;
-  if (sc.has_h_in) {
-    const float2 ho = hst[g];
-    h = c_add(F, make_float2(sc.beta * ho.x, sc.beta * ho.y));
-  }
+  if (sc.has_h_in) h = c_add(F, make_float2(sc.beta * ho.x, sc.beta * ho.y));
   // linear_term = nu * laplace - drag; laplace = (2 pi i)^2 |k|^2
   const float kxf = kx_of(p, kx), kyf = ky_of(p, c);
   const float lin = p.nu * (p.lap_coef * (kxf * kxf + kyf * kyf)) - p.drag;
-  const float2 u = wst[g];
   // u + gamma dt h + mu G(u), G(u) = linear_term * u
   const float2 x = make_float2((u.x + sc.gdt * h.x) + sc.mu * (lin * u.x),
                                (u.y + sc.gdt * h.y) + sc.mu * (lin * u.y));
   // implicit_solve: 1 / (1 - mu * linear_term) * x
   const float inv = __frcp_rn(1.f - sc.mu * lin);
-  wst[g] = make_float2(inv * x.x, inv * x.y);
+  *h_new = h;
+  return make_float2(inv * x.x, inv * x.y);
+}
+
+CFD_D void stage_update_at(const SpecParams& p, const StageCoef& sc, int kx, int c, float2 a,
+                           float2* __restrict__ wst, float2* __restrict__ hst) {
+  const size_t g = (size_t)kx * (p.L + 1) + c;
+  float2 h;
+  if (sc.explicit_only) {
+    wst[g] = stage_update_core(p, sc, kx, c, a, a, a, &h);
+    return;
+  }
+  const float2 ho = sc.has_h_in ? hst[g] : make_float2(0.f, 0.f);
+  wst[g] = stage_update_core(p, sc, kx, c, a, wst[g], ho, &h);
   if (sc.write_h) hst[g] = h;
 }
 
@@ -375,6 +387,120 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(128, 7)
   cluster.sync();
 }
 
+// ---- Persistent column passes (engine in colpipe.cuh) ----
+// Work items of the update pass are groups of CG of the ncols = L + 1
+// half-spectrum columns (the last group padded with zero columns that store
+// nothing); items of the prep pass are (group, field) pairs, one inverse
+// transform each.  Every item reads its column inputs through the staging
+// slots while the previous item is transformed.  Each element is computed by
+// the expressions col_update_cols / col_prep_cols evaluate, after the same
+// butterflies, so all column schemes give the same bits.  One transform makes
+// two exchanges at 512 to 4096 rows, so every item starts on buffer 0.
+template <int LOG2N, int CG>
+CFD_D void spec_pipe_prefetch(const float2* __restrict__ src, int ncols, int c, int t,
+                              float2* __restrict__ stage) {
+  constexpr int NTHR = ColPipe<LOG2N>::NTHR, T = CG * NTHR;
+  if (c >= ncols) return;
+  const int tid = t * CG + (c % CG);
+#pragma unroll
+  for (int r = 0; r < 16; ++r)
+    cp_async8(stage + r * T + tid, src + (size_t)(t + NTHR * r) * ncols + c);
+}
+
+template <int LOG2N, int CG>
+__global__ void __launch_bounds__(CG * (1 << LOG2N) / 16,
+                                  col_pipe_min_blocks(CG * (1 << LOG2N) / 16))
+    spec_col_update_pipe_kernel(SpecParams p, StageCoef sc, const float2* __restrict__ ahat,
+                                float2* __restrict__ wst, float2* __restrict__ hst) {
+  using P = ColPipe<LOG2N>;
+  constexpr int T = CG * P::NTHR;
+  extern __shared__ float2 sbuf[];
+  const int ncols = p.L + 1, groups = (ncols + CG - 1) / CG;
+  const int w = threadIdx.x % CG, t = threadIdx.x / CG, tid = threadIdx.x;
+  const int bstride = col_pipe_bstride<LOG2N, CG>();
+  float2* const buf[2] = {sbuf + w * bstride, sbuf + (CG + w) * bstride};
+  float2* const stage = sbuf + 2 * CG * bstride;
+  int g = blockIdx.x;
+  if (g >= groups) return;  // uniform per block
+  spec_pipe_prefetch<LOG2N, CG>(ahat, ncols, g * CG + w, t, stage);
+  cp_async_commit();
+  float2 v[16], us[16], hs[16];
+#pragma unroll 1
+  for (; g < groups; g += gridDim.x) {
+    const int c = g * CG + w;
+    cp_async_wait_all();
+#pragma unroll
+    for (int r = 0; r < 16; ++r) v[r] = c < ncols ? stage[r * T + tid] : make_float2(0.f, 0.f);
+    const int gn = g + gridDim.x;
+    if (gn < groups) spec_pipe_prefetch<LOG2N, CG>(ahat, ncols, gn * CG + w, t, stage);
+    cp_async_commit();
+    if (c < ncols && !sc.explicit_only) {
+      // All of this column's state and h values are requested before any is
+      // used (each element is read and written by this thread only).
+#pragma unroll
+      for (int m = 0; m < 16; ++m) {
+        const size_t gi = (size_t)(t + P::NTHR * m) * ncols + c;
+        us[m] = wst[gi];
+        hs[m] = sc.has_h_in ? hst[gi] : make_float2(0.f, 0.f);
+      }
+    }
+    col_pipe_fft<LOG2N, -1, 0>(v, buf, t, p.twp_x);
+    if (c < ncols) {
+#pragma unroll
+      for (int m = 0; m < 16; ++m) {
+        const int kx = t + P::NTHR * m;
+        const size_t gi = (size_t)kx * ncols + c;
+        if (sc.explicit_only) {
+          stage_update_at(p, sc, kx, c, v[m], wst, hst);
+        } else {
+          float2 h;
+          wst[gi] = stage_update_core(p, sc, kx, c, v[m], us[m], hs[m], &h);
+          if (sc.write_h) hst[gi] = h;
+        }
+      }
+    }
+  }
+  cp_async_wait_all();
+}
+
+template <int LOG2N, int CG>
+__global__ void __launch_bounds__(CG * (1 << LOG2N) / 16,
+                                  col_pipe_min_blocks(CG * (1 << LOG2N) / 16))
+    spec_col_prep_pipe_kernel(SpecParams p, const float2* __restrict__ wst, T4 t4) {
+  using P = ColPipe<LOG2N>;
+  constexpr int T = CG * P::NTHR;
+  extern __shared__ float2 sbuf[];
+  const int ncols = p.L + 1, items = 4 * ((ncols + CG - 1) / CG);
+  const int w = threadIdx.x % CG, t = threadIdx.x / CG, tid = threadIdx.x;
+  const int bstride = col_pipe_bstride<LOG2N, CG>();
+  float2* const buf[2] = {sbuf + w * bstride, sbuf + (CG + w) * bstride};
+  float2* const stage = sbuf + 2 * CG * bstride;
+  int it = blockIdx.x;
+  if (it >= items) return;  // uniform per block
+  spec_pipe_prefetch<LOG2N, CG>(wst, ncols, (it >> 2) * CG + w, t, stage);
+  cp_async_commit();
+  float2 v[16];
+#pragma unroll 1
+  for (; it < items; it += gridDim.x) {
+    const int f = it & 3, c = (it >> 2) * CG + w;
+    cp_async_wait_all();
+#pragma unroll
+    for (int r = 0; r < 16; ++r)
+      v[r] = c < ncols ? prep_factor(p, f, t + P::NTHR * r, c, stage[r * T + tid])
+                       : make_float2(0.f, 0.f);
+    const int in = it + gridDim.x;
+    if (in < items) spec_pipe_prefetch<LOG2N, CG>(wst, ncols, (in >> 2) * CG + w, t, stage);
+    cp_async_commit();
+    col_pipe_fft<LOG2N, 1, 0>(v, buf, t, p.twp_x);
+    if (c < ncols) {
+      float2* dst = f == 0 ? t4.t[0] : f == 1 ? t4.t[1] : f == 2 ? t4.t[2] : t4.t[3];
+#pragma unroll
+      for (int m = 0; m < 16; ++m) dst[(size_t)(t + P::NTHR * m) * ncols + c] = v[m];
+    }
+  }
+  cp_async_wait_all();
+}
+
 // ---- Batched variants: the slot index is the last grid axis ----
 // Column prep after stage `stage` of step k builds the inputs of the next
 // stage (k = -1: before the first step of the chunk).
@@ -571,9 +697,77 @@ bool spec_cluster_ok(const SpecParams& p) {
   return p.col_mode == 1 && p.nx >= 256 && p.nx <= 2048;
 }
 
+// col_mode 2: groups of 4 columns per block (2 at 4096 rows); 3: groups of 2.
+bool spec_pipe_ok(const SpecParams& p) {
+  return (p.col_mode == 2 || p.col_mode == 3) && p.log2nx >= 9 && p.log2nx <= 12;
+}
+
+// Persistent column passes: as many blocks as fit on the device at once,
+// never more than there are work items.
+template <int LOG2N, int CG, typename K>
+static cudaError_t spec_pipe_grid(K kern, int items, int* grid, size_t* smem, int* threads) {
+  *smem = col_pipe_smem<LOG2N, CG>();
+  *threads = CG * (1 << LOG2N) / 16;
+  cudaError_t e = set_smem(kern, *smem);
+  if (e != cudaSuccess) return e;
+  static int per_sm = 0;  // per instantiation; same for every device of one kind
+  if (per_sm == 0) {
+    int nb = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, *threads, *smem);
+    if (e != cudaSuccess) return e;
+    per_sm = nb > 0 ? nb : 1;
+  }
+  const int slots = col_pipe_device_sms() * per_sm;
+  *grid = items < slots ? items : slots;
+  return cudaSuccess;
+}
+
+template <int LOG2N, int CG>
+static cudaError_t spec_prep_pipe_impl(const SpecParams& p, const float2* w, const T4& tt,
+                                       cudaStream_t s) {
+  int grid, threads;
+  size_t smem;
+  auto kern = spec_col_prep_pipe_kernel<LOG2N, CG>;
+  cudaError_t e = spec_pipe_grid<LOG2N, CG>(kern, 4 * ((p.L + 1 + CG - 1) / CG), &grid, &smem,
+                                            &threads);
+  if (e != cudaSuccess) return e;
+  kern<<<grid, threads, smem, s>>>(p, w, tt);
+  return cudaGetLastError();
+}
+
+template <int LOG2N, int CG>
+static cudaError_t spec_update_pipe_impl(const SpecParams& p, const StageCoef& sc,
+                                         const float2* ahat, float2* w, float2* h,
+                                         cudaStream_t s) {
+  int grid, threads;
+  size_t smem;
+  auto kern = spec_col_update_pipe_kernel<LOG2N, CG>;
+  cudaError_t e = spec_pipe_grid<LOG2N, CG>(kern, (p.L + 1 + CG - 1) / CG, &grid, &smem,
+                                            &threads);
+  if (e != cudaSuccess) return e;
+  kern<<<grid, threads, smem, s>>>(p, sc, ahat, w, h);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_spec_col_prep(const SpecParams& p, const float2* w,
                                  float2* const t4[4], cudaStream_t s) {
   T4 tt{{t4[0], t4[1], t4[2], t4[3]}};
+  if (spec_pipe_ok(p) && p.col_mode == 3) {
+    switch (p.log2nx) {
+      case 9: return spec_prep_pipe_impl<9, 2>(p, w, tt, s);
+      case 10: return spec_prep_pipe_impl<10, 2>(p, w, tt, s);
+      case 11: return spec_prep_pipe_impl<11, 2>(p, w, tt, s);
+      default: return spec_prep_pipe_impl<12, 2>(p, w, tt, s);
+    }
+  }
+  if (spec_pipe_ok(p)) {
+    switch (p.log2nx) {
+      case 9: return spec_prep_pipe_impl<9, 4>(p, w, tt, s);
+      case 10: return spec_prep_pipe_impl<10, 4>(p, w, tt, s);
+      case 11: return spec_prep_pipe_impl<11, 4>(p, w, tt, s);
+      default: return spec_prep_pipe_impl<12, 2>(p, w, tt, s);
+    }
+  }
   if (spec_cluster_ok(p)) {
     const int ncols = p.L + 1;
     const int gx = (ncols + kSpecCluster - 1) / kSpecCluster * kSpecCluster;
@@ -597,7 +791,23 @@ cudaError_t launch_spec_col_update(const SpecParams& p, const StageCoef& sc,
                                    const float2* ahat, float2* w, float2* h,
                                    float2* const t4[4], cudaStream_t s) {
   cudaError_t e;
-  if (spec_cluster_ok(p)) {
+  if (spec_pipe_ok(p) && p.col_mode == 3) {
+    switch (p.log2nx) {
+      case 9: e = spec_update_pipe_impl<9, 2>(p, sc, ahat, w, h, s); break;
+      case 10: e = spec_update_pipe_impl<10, 2>(p, sc, ahat, w, h, s); break;
+      case 11: e = spec_update_pipe_impl<11, 2>(p, sc, ahat, w, h, s); break;
+      default: e = spec_update_pipe_impl<12, 2>(p, sc, ahat, w, h, s); break;
+    }
+    if (e != cudaSuccess) return e;
+  } else if (spec_pipe_ok(p)) {
+    switch (p.log2nx) {
+      case 9: e = spec_update_pipe_impl<9, 4>(p, sc, ahat, w, h, s); break;
+      case 10: e = spec_update_pipe_impl<10, 4>(p, sc, ahat, w, h, s); break;
+      case 11: e = spec_update_pipe_impl<11, 4>(p, sc, ahat, w, h, s); break;
+      default: e = spec_update_pipe_impl<12, 2>(p, sc, ahat, w, h, s); break;
+    }
+    if (e != cudaSuccess) return e;
+  } else if (spec_cluster_ok(p)) {
     const int ncols = p.L + 1;
     const int gx = (ncols + kSpecCluster - 1) / kSpecCluster * kSpecCluster;
     const size_t smem = (size_t)padded_len(p.nx) * sizeof(float2);

@@ -159,8 +159,8 @@ class FvmPlan:
 
   def autotune(self, u, v, steps: int = 20) -> int:
     """Times each transform launch configuration on (u, v) and keeps the
-    fastest; returns its index (row block shape + 2 * column-pass scheme).
-    Synchronises the stream."""
+    fastest; returns its index (row block shape + 2 * column-pass scheme +
+    10 * stencil scheme + 20 * row feed).  Synchronises the stream."""
     us, vs = torch.empty_like(u), torch.empty_like(v)
     chosen = ctypes.c_int(-1)
     a = self._fields(u, v, us, vs)
@@ -169,7 +169,7 @@ class FvmPlan:
               'cfd_fvm_plan_autotune')
     return int(chosen.value)
 
-  LAUNCH_CHOICES = 24
+  LAUNCH_CHOICES = 40
 
   def set_launch(self, choice: int):
     """Pins the launch configuration (see autotune); results do not change."""
@@ -316,16 +316,41 @@ class SpecPlan:
   def nbytes(self) -> int:
     return int(self._lib.cfd_spec_plan_bytes(self._h))
 
-  LAUNCH_CHOICES = 2
+  LAUNCH_CHOICES = 4
 
   def set_launch(self, choice: int):
     """Column passes: 0 per-block columns, 1 clusters of four one-column
-    blocks (256 <= nx <= 2048).  Results do not change."""
+    blocks (256 <= nx <= 2048), 2/3 persistent register-pipelined groups of
+    4/2 columns (512 <= nx <= 4096).  Results do not change."""
     nat.check(self._lib.cfd_spec_plan_set_launch(self._h, int(choice)), 'cfd_spec_plan_set_launch')
 
   @property
   def launch(self) -> int:
     return int(self._lib.cfd_spec_plan_get_launch(self._h))
+
+  def autotune(self, w_hat: torch.Tensor, steps: int = 4) -> int:
+    """Times `steps` steps from w_hat under each column-pass scheme this grid
+    supports (CUDA events on the current stream, one untimed step first) and
+    keeps the fastest; returns its index.  Synchronises the stream."""
+    stream = torch.cuda.current_stream(w_hat.device)
+    best, best_ms = self.launch, None
+    for choice in range(self.LAUNCH_CHOICES):
+      try:
+        self.set_launch(choice)
+      except NotImplementedError:
+        continue
+      self.step(w_hat, 1)
+      e0 = torch.cuda.Event(enable_timing=True)
+      e1 = torch.cuda.Event(enable_timing=True)
+      e0.record(stream)
+      self.step(w_hat, steps)
+      e1.record(stream)
+      e1.synchronize()
+      ms = e0.elapsed_time(e1)
+      if best_ms is None or ms < best_ms:
+        best, best_ms = choice, ms
+    self.set_launch(best)
+    return best
 
   def _real(self, t, name='x'):
     return require_field(t, self.shape, name=name)

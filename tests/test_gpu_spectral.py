@@ -125,7 +125,8 @@ def test_taylor_green_spectral_analytic(cuda_device):
 @pytest.mark.parametrize('shape', [(256, 256), (512, 256), (2048, 2048)])
 @pytest.mark.parametrize('forcing', ['smooth', 'kolmogorov'])
 def test_cluster_column_passes_are_bitwise(cuda_device, shape, forcing):
-  """Clustered column passes (launch 1) give exactly the per-block bits."""
+  """Clustered (launch 1) and persistent pipelined (launch 2) column passes
+  give exactly the per-block bits."""
   import jax_cfd_gb300.base as cfd
   from jax_cfd_gb300.spectral import equations as seq
   from jax_cfd_gb300.spectral import time_stepping as sts
@@ -138,12 +139,17 @@ def test_cluster_column_passes_are_bitwise(cuda_device, shape, forcing):
   plan = sts.crank_nicolson_rk4(eq, 1e-3).plan(cuda_device)
   w = torch.from_numpy(w0.astype(np.complex64)).to(cuda_device)
   default = plan.launch
+  results = {}
   try:
-    plan.set_launch(0)
-    base = plan.step(w, 3)
-    plan.set_launch(1)
-    assert plan.launch == 1
-    got = plan.step(w, 3)
+    for choice in range(plan.LAUNCH_CHOICES):
+      try:
+        plan.set_launch(choice)
+      except NotImplementedError:
+        continue
+      assert plan.launch == choice
+      results[choice] = plan.step(w, 3)
   finally:
     plan.set_launch(default)
-  assert torch.equal(torch.view_as_real(got), torch.view_as_real(base))
+  assert 0 in results and 1 in results
+  for choice, got in results.items():
+    assert torch.equal(torch.view_as_real(got), torch.view_as_real(results[0])), choice
