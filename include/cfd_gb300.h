@@ -98,6 +98,24 @@ long long cfd_fvm_plan_bytes(const cfd_fvm_plan* plan);
  * offsets (1, .5) and (.5, 1).  u_out/v_out may alias u/v. */
 int cfd_fvm_step(cfd_fvm_plan* plan, void* stream, const float* u,
                  const float* v, float* u_out, float* v_out, int steps);
+/* diffusion.solve_fast_diag (jax_cfd/base/diffusion.py:166-212) for periodic
+ * velocity components: u_out = u + irfftn(func(lambda) * rfftn(u)) with
+ * func(x) = (dt nu) x / (1 - (dt nu) x) on the eigenvalues of the periodic
+ * Laplacian (fast_diagonalization.py:199-225), same for v.  u_out/v_out may
+ * alias u/v.  Uses the plan's grid, spectrum buffer and column scheme. */
+int cfd_fvm_diffusion_solve(cfd_fvm_plan* plan, void* stream, const float* u,
+                            const float* v, float* u_out, float* v_out,
+                            double nu, double dt);
+/* `steps` steps of implicit_diffusion_navier_stokes
+ * (jax_cfd/base/equations.py:154-195, diffusion_solve = pressure_solve =
+ * solve_fast_diag): convection + forcing / density explicitly, forward Euler
+ * with the plan's dt, projection, then the implicit diffusion solve with
+ * `viscosity`.  The plan must be created with has_viscosity = 0 (the
+ * explicit terms of this step have no diffusion); CFD_ERR_UNSUPPORTED
+ * otherwise.  u_out/v_out may alias u/v. */
+int cfd_fvm_step_implicit(cfd_fvm_plan* plan, void* stream, const float* u,
+                          const float* v, float* u_out, float* v_out, int steps,
+                          double viscosity);
 /* navier_stokes_rk (time_stepping.py:59-107) with an explicit Butcher
  * tableau of 1-4 stages: `a` holds rows 1 .. stages-1 of the lower triangle
  * concatenated (row i has i entries), `b` the `stages` weights; e.g.

@@ -1,8 +1,8 @@
 """Navier-Stokes equations, mirroring ``jax_cfd/base/equations.py``.
 
-``semi_implicit_navier_stokes`` keeps the reference signature
-(equations.py:120-151) and returns a step function backed by the fused
-GB300 kernels.  The arguments are pattern-matched onto the kernels: the
+``semi_implicit_navier_stokes`` (equations.py:120-151) and
+``implicit_diffusion_navier_stokes`` (154-195) keep the reference signatures
+and return step functions backed by the fused GB300 kernels.  The arguments are pattern-matched onto the kernels: the
 default Van Leer convection (or ``advection.convect_linear``),
 ``diffusion.diffuse``, ``pressure.solve_fast_diag``, forcings built by
 ``forcings`` and ``time_stepping.forward_euler``.  Anything else raises
@@ -80,12 +80,16 @@ class FvmStep:
   the projection of step k folded into the stencil of step k + 1.
   """
 
-  def __init__(self, grid: grids.Grid, tableau=None, **plan_kwargs):
+  def __init__(self, grid: grids.Grid, tableau=None, implicit_viscosity=None,
+               **plan_kwargs):
     self.grid = grid
     self._plan_kwargs = plan_kwargs
     self._key = tuple(sorted((k, _freeze(v)) for k, v in plan_kwargs.items()))
     # None: the fused forward-Euler step; else (a, b) of navier_stokes_rk.
     self.tableau = tableau
+    # Not None: implicit_diffusion_navier_stokes with this viscosity (the
+    # plan's explicit terms then carry no diffusion).
+    self.implicit_viscosity = implicit_viscosity
 
   def plan(self, device) -> plans.FvmPlan:
     return plans.cached('fvm-step', (device, self.grid.shape, self.grid.step, self._key),
@@ -95,7 +99,9 @@ class FvmStep:
   def gb300_repeat(self, v, steps: int):
     _check_state(v, self.grid)
     plan = self.plan(v[0].data.device)
-    if self.tableau is None:
+    if self.implicit_viscosity is not None:
+      uo, vo = plan.step_implicit(v[0].data, v[1].data, steps, self.implicit_viscosity)
+    elif self.tableau is None:
       uo, vo = plan.step(v[0].data, v[1].data, steps)
     else:
       uo, vo = plan.step_rk(v[0].data, v[1].data, steps, *self.tableau)
@@ -194,6 +200,17 @@ def semi_implicit_navier_stokes(density: float, viscosity: float, dt: float,
   return time_stepper(eq, dt)
 
 
-def implicit_diffusion_navier_stokes(*args, **kwargs):
-  """equations.py:154-195 is outside the GB300 hot path."""
-  raise NotImplementedError('implicit_diffusion_navier_stokes is outside the GB300 hot path')
+def implicit_diffusion_navier_stokes(density: float, viscosity: float, dt: float,
+                                     grid: grids.Grid, convect=None,
+                                     diffusion_solve: Callable = diffusion.solve_fast_diag,
+                                     pressure_solve: Callable = pressure.solve_fast_diag,
+                                     forcing=None) -> Callable:
+  """equations.py:154-195: v + dt (convection + forcing / density), the
+  projection, then diffusion_solve(v, viscosity, dt), as one native step
+  (cfd_fvm_step_implicit)."""
+  if diffusion_solve is not diffusion.solve_fast_diag:
+    raise NotImplementedError('diffusion_solve must be diffusion.solve_fast_diag on the GB300 path')
+  if pressure_solve is not pressure.solve_fast_diag:
+    raise NotImplementedError('pressure_solve must be pressure.solve_fast_diag on the GB300 path')
+  kw = _plan_kwargs(density, None, convect, diffusion.diffuse, forcing)
+  return FvmStep(grid, implicit_viscosity=float(viscosity), dt=float(dt), **kw)

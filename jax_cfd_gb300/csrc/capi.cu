@@ -164,6 +164,7 @@ struct cfd_fvm_plan {
   float* fu = nullptr;
   float* fv = nullptr;
   float* rk = nullptr;  // Runge-Kutta stage terms k_j (u, v), allocated on first use
+  double dt = 0;        // the configuration's dt (double, as the reference's Python float)
   long long bytes = 0;
 };
 
@@ -338,6 +339,7 @@ int cfd_fvm_plan_create(const cfd_fvm_config* cfg, cfd_fvm_plan** out) {
   cfd_fvm_plan* plan = new cfd_fvm_plan();
   cfd::FvmParams& p = plan->p;
   p = params;
+  plan->dt = cfg->dt;
   const int nx = cfg->nx, ny = cfg->ny;
 
   const size_t n = (size_t)nx * ny;
@@ -446,6 +448,75 @@ int cfd_fvm_step(cfd_fvm_plan* plan, void* stream, const float* u,
     t = av; av = bv; bv = t;
   }
   CFD_CHECK(cfd::launch_fvm_project_out(p, au, av, q, u_out, v_out, s), "project_out");
+  return CFD_OK;
+}
+
+// diffusion.solve_fast_diag (diffusion.py:166-212) on periodic fields, in
+// place on (u, v): u + irfftn(func(lambda) rfftn(u)) per component, func(x) =
+// (dt nu) x / (1 - (dt nu) x) on the summed eigenvalues of the periodic 1-D
+// Laplacians (the same circulant for both staggered offsets).  Uses the
+// plan's spectrum buffer and column-pass scheme.
+static int fvm_diffuse_implicit(cfd_fvm_plan* plan, cudaStream_t s, float* u, float* v,
+                                double nu, double dt) {
+  cfd::FvmParams pd = plan->p;
+  pd.col_diag = 1;
+  pd.dtnu = (float)(dt * nu);
+  const size_t n = (size_t)pd.nx * pd.ny;
+  const float* w = reinterpret_cast<const float*>(plan->spec);
+  for (float* c : {u, v}) {
+    CFD_CHECK(cfd::launch_fvm_field_rfft(pd, c, plan->spec, s), "field_rfft");
+    CFD_CHECK(cfd::launch_fvm_col_pinv(pd, plan->spec, s), "col_diffuse");
+    CFD_CHECK(cfd::launch_fvm_irfft(pd, plan->spec, s), "irfft");
+    CFD_CHECK(cfd::launch_fvm_add(n, w, c, s), "add");
+  }
+  return CFD_OK;
+}
+
+int cfd_fvm_diffusion_solve(cfd_fvm_plan* plan, void* stream, const float* u, const float* v,
+                            float* u_out, float* v_out, double nu, double dt) {
+  if (!plan || !u || !v || !u_out || !v_out)
+    return fail(CFD_ERR_INVALID_ARGUMENT, "cfd_fvm_diffusion_solve: null pointer");
+  cudaStream_t s = as_stream(stream);
+  const size_t bytes = (size_t)plan->p.nx * plan->p.ny * sizeof(float);
+  if (u_out != u) CFD_CHECK(cudaMemcpyAsync(u_out, u, bytes, cudaMemcpyDeviceToDevice, s), "copy");
+  if (v_out != v) CFD_CHECK(cudaMemcpyAsync(v_out, v, bytes, cudaMemcpyDeviceToDevice, s), "copy");
+  return fvm_diffuse_implicit(plan, s, u_out, v_out, nu, dt);
+}
+
+// implicit_diffusion_navier_stokes (equations.py:154-195) with
+// diffusion_solve = pressure_solve = solve_fast_diag: u* = u + dt (convection
+// + forcing / density) (the stencil without its viscosity term), projection,
+// then the implicit diffusion solve with the plan's dt.  The plan must be
+// made without explicit viscosity.
+int cfd_fvm_step_implicit(cfd_fvm_plan* plan, void* stream, const float* u, const float* v,
+                          float* u_out, float* v_out, int steps, double viscosity) {
+  if (!plan || !u || !v || !u_out || !v_out || steps < 0)
+    return fail(CFD_ERR_INVALID_ARGUMENT, "cfd_fvm_step_implicit: bad arguments");
+  const cfd::FvmParams& p = plan->p;
+  if (p.has_visc)
+    return fail(CFD_ERR_UNSUPPORTED,
+                "cfd_fvm_step_implicit: the plan's explicit terms must not include viscosity");
+  cudaStream_t s = as_stream(stream);
+  const size_t bytes = (size_t)p.nx * p.ny * sizeof(float);
+  if (steps == 0) {
+    if (u_out != u) CFD_CHECK(cudaMemcpyAsync(u_out, u, bytes, cudaMemcpyDeviceToDevice, s), "copy");
+    if (v_out != v) CFD_CHECK(cudaMemcpyAsync(v_out, v, bytes, cudaMemcpyDeviceToDevice, s), "copy");
+    return CFD_OK;
+  }
+  const float* q = reinterpret_cast<const float*>(plan->spec);
+  const float *cu = u, *cv = v;
+  for (int k = 0; k < steps; ++k) {
+    CFD_CHECK(cfd::launch_fvm_explicit(p, false, false, cu, cv, nullptr, plan->au, plan->av, s),
+              "explicit");
+    int rc = fvm_pressure(plan, s, plan->au, plan->av);
+    if (rc) return rc;
+    CFD_CHECK(cfd::launch_fvm_project_out(p, plan->au, plan->av, q, u_out, v_out, s),
+              "project_out");
+    rc = fvm_diffuse_implicit(plan, s, u_out, v_out, viscosity, plan->dt);
+    if (rc) return rc;
+    cu = u_out;
+    cv = v_out;
+  }
   return CFD_OK;
 }
 

@@ -592,6 +592,13 @@ CFD_D void div_rfft_rows(const FvmParams& p, int blk, int rows,
     const int r = g >> log2g, jj = (g & ((1 << log2g) - 1)) << 2;
     const int i = i0 + r, im = (i - 1) & mx;
     const float4 a = __ldg(reinterpret_cast<const float4*>(us + i * ny + jj));
+    if (p.row_field) {
+      // The field itself (implicit diffusion's rfftn(u)).
+      float2* z = sbuf + r * PL;
+      z[pidx(jj >> 1)] = make_float2(a.x, a.y);
+      z[pidx((jj >> 1) + 1)] = make_float2(a.z, a.w);
+      continue;
+    }
     const float4 b = __ldg(reinterpret_cast<const float4*>(us + im * ny + jj));
     const float4 c = __ldg(reinterpret_cast<const float4*>(vs + i * ny + jj));
     const float cm = __ldg(vs + i * ny + ((jj - 1) & my));
@@ -718,11 +725,17 @@ __global__ void __launch_bounds__(MAXT, MINB)
   div_rfft_rows_bulk(p, blockIdx.x, rows, us, vs, spec);
 }
 
-// Pseudoinverse of the periodic Laplacian in the rfft basis
-// (fast_diagonalization.py:199-266): 1/lambda where |lambda| > cutoff, else 0,
-// with irfftn's 1/(nx*ny) folded in (a power of two, so exact).
+// Diagonal of the column pass in the rfft basis, with irfftn's 1/(nx*ny)
+// folded in (a power of two, so exact).  col_diag 0: the pseudoinverse of the
+// periodic Laplacian (fast_diagonalization.py:199-266), 1/lambda where
+// |lambda| > cutoff, else 0.  col_diag 1: implicit diffusion's
+// func(lambda) = x / (1 - x), x = (dt nu) lambda (diffusion.py:176-182).
 CFD_D float pinv_diag(const FvmParams& p, int kx, int ky) {
   const float lam = __ldg(p.lamx + kx) + __ldg(p.lamy + ky);
+  if (p.col_diag == 1) {
+    const float x = p.dtnu * lam;
+    return p.pinv_scale * (x / (1.f - x));
+  }
   return fabsf(lam) > p.cutoff ? p.pinv_scale / lam : 0.f;
 }
 
@@ -1185,6 +1198,14 @@ CFD_D void project_out_cells(const FvmParams& p, int blk, int nblk,
   }
 }
 
+// u += w: the last sum of diffusion.solve_fast_diag, u_interior +
+// u_dt_diffused (diffusion.py:203-210).
+__global__ void fvm_add_kernel(size_t n, const float* __restrict__ w, float* __restrict__ u) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    u[i] = u[i] + w[i];
+}
+
 __global__ void fvm_project_out_kernel(FvmParams p, const float* __restrict__ us,
                                        const float* __restrict__ vs,
                                        const float* __restrict__ q,
@@ -1443,6 +1464,20 @@ static cudaError_t div_rfft_impl(const FvmParams& p, int target, const float* us
   return cudaGetLastError();
 }
 
+cudaError_t launch_fvm_field_rfft(const FvmParams& p, const float* f, float2* spec,
+                                  cudaStream_t s) {
+  FvmParams q = p;
+  q.row_field = 1;
+  const int log2L = q.log2ny - 1;
+  const int rows = fft_rows_per_block(log2L, q.nx, 256);
+  const size_t smem = (size_t)rows * padded_len(q.ny / 2) * sizeof(float2);
+  cudaError_t e = set_smem(fvm_div_rfft_kernel<256, 3>, smem);
+  if (e != cudaSuccess) return e;
+  fvm_div_rfft_kernel<256, 3><<<q.nx / rows, block_threads(fft_workers(log2L, rows)), smem, s>>>(
+      q, rows, f, f, spec);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_fvm_div_rfft(const FvmParams& p, const float* us,
                                 const float* vs, float2* spec, cudaStream_t s) {
   return p.fft_shape == 1 ? div_rfft_impl<64, 14>(p, 64, us, vs, spec, s)
@@ -1588,6 +1623,11 @@ cudaError_t launch_fvm_project_out(const FvmParams& p, const float* us,
                                    float* vo, cudaStream_t s) {
   const size_t n = (size_t)p.nx * p.ny;
   fvm_project_out_kernel<<<elementwise_blocks(n), 256, 0, s>>>(p, us, vs, q, uo, vo);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fvm_add(size_t n, const float* w, float* u, cudaStream_t s) {
+  fvm_add_kernel<<<elementwise_blocks(n), 256, 0, s>>>(n, w, u);
   return cudaGetLastError();
 }
 

@@ -48,6 +48,10 @@ struct FvmParams {
                        // 3/4 persistent register-pipelined groups of 4/2 columns
   int stencil;         // explicit step: 0 shared-memory tiles, 1 warp streams
   int row_feed;        // row transforms: 0 loads through registers, 1 bulk copies
+  // Implicit diffusion (diffusion.solve_fast_diag) on the same transforms:
+  int row_field;       // forward row transform of the field us itself, not div
+  int col_diag;        // column-pass diagonal: 0 pinv(lambda), 1 x / (1 - x), x = dtnu lambda
+  float dtnu;          // float32(dt * viscosity) for col_diag = 1
 };
 
 // One slot of a same-shape batch of FVM trajectories (device-resident table
@@ -79,6 +83,12 @@ bool stream_stencil_ok(const FvmParams& p);
 // Whether the bulk-copy row transforms (row_feed 1) apply to this grid.
 bool bulk_feed_ok(const FvmParams& p);
 cudaError_t launch_fvm_irfft(const FvmParams& p, float2* spec, cudaStream_t s);
+// Forward packed row rFFT of one field (row_field mode of the divergence
+// transform, shared-memory engine).
+cudaError_t launch_fvm_field_rfft(const FvmParams& p, const float* f, float2* spec,
+                                  cudaStream_t s);
+// u[i] += w[i] over n floats.
+cudaError_t launch_fvm_add(size_t n, const float* w, float* u, cudaStream_t s);
 cudaError_t launch_fvm_project_out(const FvmParams& p, const float* us,
                                    const float* vs, const float* q, float* uo,
                                    float* vo, cudaStream_t s);

@@ -134,6 +134,29 @@ class FvmPlan:
               'cfd_fvm_step')
     return u_out, v_out
 
+  def step_implicit(self, u, v, steps: int, viscosity: float, u_out=None, v_out=None):
+    """implicit_diffusion_navier_stokes (equations.py:154-195); the plan is
+    made without explicit viscosity."""
+    if steps < 0:
+      raise ValueError('steps must be non-negative')
+    u_out = torch.empty_like(u) if u_out is None else u_out
+    v_out = torch.empty_like(v) if v_out is None else v_out
+    a = self._fields(u, v, u_out, v_out)
+    nat.check(self._lib.cfd_fvm_step_implicit(self._h, current_stream_ptr(u.device), *a,
+                                              int(steps), float(viscosity)),
+              'cfd_fvm_step_implicit')
+    return u_out, v_out
+
+  def diffusion_solve(self, u, v, nu: float, dt: float, u_out=None, v_out=None):
+    """diffusion.solve_fast_diag (diffusion.py:166-212) on periodic (u, v)."""
+    u_out = torch.empty_like(u) if u_out is None else u_out
+    v_out = torch.empty_like(v) if v_out is None else v_out
+    a = self._fields(u, v, u_out, v_out)
+    nat.check(self._lib.cfd_fvm_diffusion_solve(self._h, current_stream_ptr(u.device), *a,
+                                                float(nu), float(dt)),
+              'cfd_fvm_diffusion_solve')
+    return u_out, v_out
+
   def step_rk(self, u, v, steps: int, a, b, u_out=None, v_out=None):
     """navier_stokes_rk with Butcher tableau (a, b) (time_stepping.py:59-107)."""
     if steps < 0:

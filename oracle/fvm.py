@@ -419,6 +419,37 @@ def projection(v, grid: Grid, diag=None):
 
 
 # ---------------------------------------------------------------------------
+# Implicit diffusion (diffusion.py, fast_diagonalization.py)
+# ---------------------------------------------------------------------------
+def diffusion_diagonal(grid: Grid, nu, dt, dtype=np.float32) -> np.ndarray:
+  """diffusion.py:176-182 ``func`` on the summed eigenvalues of the periodic
+  Laplacians (fast_diagonalization.py:199-225): ``x = (dt * nu) * lambda``,
+  ``x / (1 - x)`` in float64, then cast to the complex dtype."""
+  ops = [laplacian_matrix(n, s) for n, s in zip(grid.shape, grid.step)]
+  eig = [np.fft.fft(op[:, 0]) for op in ops[:-1]] + [np.fft.rfft(ops[-1][:, 0])]
+  summed = eig[0]
+  for e in eig[1:]:
+    summed = np.add.outer(summed, e)
+  dt_nu_x = (dt * nu) * summed
+  diag = dt_nu_x / (1 - dt_nu_x)
+  cdtype = np.complex64 if dtype == np.float32 else np.complex128
+  return diag.astype(cdtype)
+
+
+def diffusion_solve_fast_diag(v, nu, dt, grid: Grid, diag=None):
+  """diffusion.py:166-212 for periodic components: u + irfftn(diag * rfftn(u))
+  (the 'rfft' transform, fast_diagonalization.py:199-225)."""
+  if diag is None:
+    diag = diffusion_diagonal(grid, nu, dt, v[0].dtype)
+  out = []
+  for u in v:
+    axes = tuple(range(u.ndim))
+    w = np.fft.irfftn(diag * np.fft.rfftn(u), s=u.shape, axes=axes).astype(u.dtype)
+    out.append(u + w)
+  return tuple(out)
+
+
+# ---------------------------------------------------------------------------
 # Equations and time stepping (equations.py, time_stepping.py)
 # ---------------------------------------------------------------------------
 ButcherTableau = Tuple[Sequence[Sequence[float]], Sequence[float]]
@@ -495,6 +526,26 @@ def semi_implicit_navier_stokes(density, viscosity, dt, grid: Grid,
       d = cache[key]
     return projection(v, grid, d)
   return navier_stokes_rk(tableau, F, P, dt)
+
+
+def implicit_diffusion_navier_stokes(density, viscosity, dt, grid: Grid,
+                                     convect='van_leer', forcing=None):
+  """equations.py:154-195 with diffusion_solve = pressure_solve =
+  solve_fast_diag: v + dvdt * dt with dvdt = convection + forcing / density
+  (sum_fields from 0), projection, then the implicit diffusion solve."""
+  F = explicit_terms_fn(density, None, dt, grid, convect, forcing)
+  cache = {}
+
+  def step(v):
+    dvdt = F(v)
+    v = tuple(u + d * dt for u, d in zip(v, dvdt))
+    key = v[0].dtype
+    if key not in cache:
+      cache[key] = (pinv_diagonal(grid, key), diffusion_diagonal(grid, viscosity, dt, key))
+    pd, dd = cache[key]
+    v = projection(v, grid, pd)
+    return diffusion_solve_fast_diag(v, viscosity, dt, grid, dd)
+  return step
 
 
 def repeated(f, steps):

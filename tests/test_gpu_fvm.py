@@ -271,3 +271,73 @@ def test_runge_kutta_tableaux_match_oracle(cuda_device, name, shape):
     assert rel_l2(g, w) <= 10 * STEP_TOL
   div = ofvm.divergence(_np(chunk), og.step)
   assert np.abs(div).max() <= 1e-4
+
+
+# --- implicit_diffusion_navier_stokes / diffusion.solve_fast_diag ----------
+@pytest.mark.parametrize('shape', [(64, 64), (128, 64), (2048, 256)])
+def test_diffusion_solve_matches_oracle(cuda_device, shape):
+  """diffusion.py:166-212 on the native transforms: the diffused fields and
+  the small diffusive increment both match the oracle."""
+  import jax_cfd_gb300.base as cfd
+  from oracle import fvm as ofvm
+  og, v0 = _setup(shape, seed=5)
+  grid = cfd.grids.Grid(shape, domain=((0, TWO_PI), (0, TWO_PI)))
+  nu, dt = 1e-2, 0.05
+  got = _np(cfd.diffusion.solve_fast_diag(_to_gpu(v0, grid, cuda_device), nu, dt))
+  want = ofvm.diffusion_solve_fast_diag(v0, nu, dt, og)
+  for g, w, u in zip(got, want, v0):
+    assert rel_l2(g, w) <= STEP_TOL
+    assert rel_l2(g - u, w - u) <= 1e-4
+
+
+def test_diffusion_solve_keeps_constant_field(cuda_device):
+  """diffusion_test.py:58-80 on a power-of-two grid."""
+  import jax_cfd_gb300.base as cfd
+  grid = cfd.grids.Grid((128, 128), step=1)
+  bc = cfd.boundaries.periodic_boundary_conditions(2)
+  ones = torch.ones((128, 128), dtype=torch.float32, device=cuda_device)
+  v = tuple(cfd.grids.GridVariable(cfd.grids.GridArray(ones, o, grid), bc) for o in grid.cell_faces)
+  for out in cfd.diffusion.solve_fast_diag(v, 1.0, 0.1):
+    assert torch.allclose(out.data, ones, atol=1e-6)
+
+
+@pytest.mark.parametrize('shape', [(64, 64), (128, 64)])
+@pytest.mark.parametrize('convect', ['van_leer', 'linear'])
+def test_implicit_diffusion_step_matches_oracle(cuda_device, shape, convect):
+  """equations.py:154-195: one step and a 10-step chunk against the oracle."""
+  import jax_cfd_gb300.base as cfd
+  from oracle import fvm as ofvm
+  og, v0 = _setup(shape, seed=7)
+  grid = cfd.grids.Grid(shape, domain=((0, TWO_PI), (0, TWO_PI)))
+  nu = 1e-3
+  dt = ofvm.stable_time_step(2.0, 0.5, nu, og, implicit_diffusion=True)
+  kw = {} if convect == 'van_leer' else {'convect': cfd.advection.convect_linear}
+  step = cfd.equations.implicit_diffusion_navier_stokes(
+      1.0, nu, dt, grid, forcing=cfd.forcings.simple_turbulence_forcing(grid, 1, 4, -0.1), **kw)
+  ostep = ofvm.implicit_diffusion_navier_stokes(
+      1.0, nu, dt, og, convect=convect, forcing=ofvm.simple_turbulence_forcing(og, 1, 4, -0.1))
+  v = _to_gpu(v0, grid, cuda_device)
+  one = _np(cfd.funcutils.repeated(step, 1)(v))
+  for g, w in zip(one, ostep(v0)):
+    assert rel_l2(g, w) <= STEP_TOL
+  ten = _np(cfd.funcutils.repeated(step, 10)(v))
+  for g, w in zip(ten, ofvm.repeated(ostep, 10)(v0)):
+    assert rel_l2(g, w) <= 1e-4
+  assert np.abs(ofvm.divergence(ten, og.step)).max() <= 1e-3
+
+
+def test_implicit_sinusoidal_divergence_and_momentum(cuda_device):
+  """equations_test.py:196-258 (implicit_sinusoidal_velocity_fast_diag) on a
+  128 x 128 grid (power of two), 1000 steps."""
+  import jax_cfd_gb300.base as cfd
+  from oracle import fvm as ofvm
+  from tests.test_oracle_pins import sinusoidal_velocity_field
+  og = ofvm.Grid.make((128, 128), step=(1., 1.))
+  v0 = sinusoidal_velocity_field(og)
+  grid = cfd.grids.Grid((128, 128), step=1)
+  step = cfd.equations.implicit_diffusion_navier_stokes(
+      1., 1e-4, 5e-3, grid, convect=cfd.advection.convect_linear)
+  out = _np(cfd.funcutils.repeated(step, 1000)(_to_gpu(v0, grid, cuda_device)))
+  assert np.max(ofvm.divergence(out, og.step)) < 1e-3
+  momentum = lambda v: np.array(v).sum() * np.prod(og.step)
+  np.testing.assert_allclose(momentum(out), momentum(v0), atol=1e-3)

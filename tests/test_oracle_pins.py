@@ -154,6 +154,42 @@ def test_taylor_green_linear_convection():
     assert np.abs(a - b).max() <= 5e-5
 
 
+# --- diffusion_test.py:58-80 and 31-42 (implicit diffusion, periodic) -------
+def test_implicit_diffusion_constant_field_unchanged():
+  g = fvm.Grid.make((100, 100), step=(1., 1.))
+  ones = np.ones((100, 100), np.float32)
+  for out in fvm.diffusion_solve_fast_diag((ones, ones), 1.0, 0.1, g):
+    np.testing.assert_allclose(out, ones, atol=1e-6)
+
+
+def test_implicit_diffusion_inverts_one_minus_nu_dt_laplacian():
+  # diffusion_setup: the solution x of the solve satisfies x - nu dt lap(x) = b.
+  g = fvm.Grid.make((4, 4), domain=((0, 4), (0, 4)))
+  b = np.random.RandomState(0).randn(4, 4).astype(np.float32)
+  x = fvm.diffusion_solve_fast_diag((b, b), 1.0, 0.5, g)[0]
+  np.testing.assert_allclose(x - 1.0 * 0.5 * fvm.laplacian(x, g.step), b, atol=1e-5)
+
+
+def sinusoidal_velocity_field(g):
+  """equations_test.py:42-50: sin(2 pi x_d / L_d) at cell centres, rotated
+  one component (u gets the y profile, v the x profile)."""
+  mesh_size = np.array(g.shape) * np.array(g.step)
+  vs = tuple(np.sin(2. * np.pi * m / sz).astype(np.float32)
+             for m, sz in zip(g.mesh(), mesh_size))
+  return vs[1:] + vs[:1]
+
+
+# --- equations_test.py:196-258 (implicit_sinusoidal_velocity_fast_diag) ----
+def test_implicit_sinusoidal_divergence_and_momentum():
+  g = fvm.Grid.make((100, 100), step=(1., 1.))
+  v0 = sinusoidal_velocity_field(g)
+  step = fvm.implicit_diffusion_navier_stokes(1., 1e-4, 5e-3, g, convect='linear')
+  out = fvm.repeated(step, 1000)(v0)
+  assert np.max(fvm.divergence(out, g.step)) < 1e-3
+  momentum = lambda v: np.array(v).sum() * 1. * np.prod(g.step)
+  np.testing.assert_allclose(momentum(out), momentum(v0), atol=1e-3)
+
+
 # --- spectral/time_stepping_test.py:42-196 (CN-RK4 on closed forms, x64) ----
 class _ODE:
 
