@@ -269,7 +269,9 @@ long long cfd_spec_plan_bytes(const cfd_spec_plan* plan);
  * of four one-column blocks exchanging rows through distributed shared memory
  * (256 <= nx <= 2048), 2/3 persistent blocks that stage the next group of
  * 4/2 columns with cp.async while transforming the current one in registers
- * (512 <= nx <= 4096).  Results are bit-for-bit the same. */
+ * (512 <= nx <= 4096), 4 as 2 with each stage's column update and the next
+ * stage's column prep fused into one pass.  Results are bit-for-bit the
+ * same. */
 int cfd_spec_plan_set_launch(cfd_spec_plan* plan, int choice);
 int cfd_spec_plan_get_launch(const cfd_spec_plan* plan);
 /* Velocity-independent forcing (fx, fy real [nx, ny] on the device, either may
@@ -281,8 +283,9 @@ int cfd_spec_set_forcing(cfd_spec_plan* plan, void* stream, const float* fx,
  * w_out may alias w_in. */
 int cfd_spec_step(cfd_spec_plan* plan, void* stream, const float* w_in,
                   float* w_out, int steps);
-/* cfd_spec_step with event pairs; ms_out[3] = {row pass, column update,
- * column prep} mean durations in ms.  Synchronises the stream. */
+/* cfd_spec_step with event pairs; ms_out[4] = {row pass, column update,
+ * column prep, fused column update + prep (column scheme 4)} mean durations
+ * in ms (0 for a kind that did not run).  Synchronises the stream. */
 int cfd_spec_profile(cfd_spec_plan* plan, void* stream, const float* w_in,
                      float* w_out, int steps, float* ms_out);
 /* Explicit terms F(w) of NavierStokes2D (advection, filter, forcing). */

@@ -1338,10 +1338,10 @@ int cfd_spec_plan_create(const cfd_spec_config* cfg, cfd_spec_plan** out) {
   cfd::SpecParams& p = plan->p;
   p = params;
   // Clustered column passes measured faster at 256^2 and 512^2, the
-  // persistent pipelined ones at 2048^2 (GB300).
+  // persistent pipelined ones with the fused update + prep at 2048^2 (GB300).
   p.col_mode = (cfg->nx >= 256 && cfg->nx <= 512) ? 1 : 0;
   if (cfg->nx >= 1024) {
-    p.col_mode = 2;
+    p.col_mode = 4;
     if (!cfd::spec_pipe_ok(p)) p.col_mode = 0;
   }
   plan->stages = stages;
@@ -1388,7 +1388,7 @@ int cfd_spec_plan_create(const cfd_spec_config* cfg, cfd_spec_plan** out) {
 long long cfd_spec_plan_bytes(const cfd_spec_plan* plan) { return plan ? plan->bytes : 0; }
 
 int cfd_spec_plan_set_launch(cfd_spec_plan* plan, int choice) {
-  if (!plan || choice < 0 || choice > 3)
+  if (!plan || choice < 0 || choice > 4)
     return fail(CFD_ERR_INVALID_ARGUMENT, "cfd_spec_plan_set_launch: bad arguments");
   cfd::SpecParams q = plan->p;
   q.col_mode = choice;
@@ -1529,6 +1529,7 @@ int cfd_spec_profile(cfd_spec_plan* plan, void* stream, const float* w_in,
     CFD_CHECK(cudaMemcpyAsync(w_out, w_in, ns * sizeof(float2), cudaMemcpyDeviceToDevice, s),
               "copy");
   const int launches = 1 + steps * plan->stages * 3;
+  const bool fused = p.col_mode == 4 && cfd::spec_pipe_ok(p);
   std::vector<cudaEvent_t> ev(2 * launches);
   std::vector<int> kind;
   for (auto& e : ev) CFD_CHECK(cudaEventCreate(&e), "cudaEventCreate");
@@ -1551,6 +1552,14 @@ int cfd_spec_profile(cfd_spec_plan* plan, void* stream, const float* w_in,
       rec(0, false);
       cfd::StageCoef c = plan->coef[k];
       const bool prep = !(st + 1 == steps && k + 1 == plan->stages);
+      if (prep && fused) {
+        // Update and the next stage's prep in one launch.
+        c.prep_next = 1;
+        rec(3, true);
+        if (e == cudaSuccess) e = cfd::launch_spec_col_update(p, c, plan->ahat, w, plan->h, plan->t4, s);
+        rec(3, false);
+        continue;
+      }
       c.prep_next = 0;
       rec(1, true);
       if (e == cudaSuccess) e = cfd::launch_spec_col_update(p, c, plan->ahat, w, plan->h, plan->t4, s);
@@ -1563,8 +1572,8 @@ int cfd_spec_profile(cfd_spec_plan* plan, void* stream, const float* w_in,
     }
   }
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-  double sum[3] = {0, 0, 0};
-  int cnt[3] = {0, 0, 0};
+  double sum[4] = {0, 0, 0, 0};
+  int cnt[4] = {0, 0, 0, 0};
   for (int i = 0; i < li && e == cudaSuccess; ++i) {
     float ms = 0.f;
     e = cudaEventElapsedTime(&ms, ev[2 * i], ev[2 * i + 1]);
@@ -1573,7 +1582,7 @@ int cfd_spec_profile(cfd_spec_plan* plan, void* stream, const float* w_in,
   }
   for (auto& x : ev) cudaEventDestroy(x);
   if (e != cudaSuccess) return cuda_fail(e, "cfd_spec_profile");
-  for (int k = 0; k < 3; ++k) ms_out[k] = cnt[k] ? (float)(sum[k] / cnt[k]) : 0.f;
+  for (int k = 0; k < 4; ++k) ms_out[k] = cnt[k] ? (float)(sum[k] / cnt[k]) : 0.f;
   return CFD_OK;
 }
 

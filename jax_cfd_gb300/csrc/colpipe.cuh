@@ -36,14 +36,59 @@ CFD_HD int col_pipe_bstride() {
   return padded_len(1 << LOG2N) + 16 / CG;
 }
 
-// Two exchange buffers per column, then 16 staging slots per thread.
+// Up to 2048 rows the block also keeps the pass twiddle table and one
+// length-N float table (eigenvalues or wavenumbers) in shared memory: with
+// the exchange buffers and staging slots taking most of the 227 KB, the L1
+// left over cannot hold them next to the staged traffic.
+template <int LOG2N>
+constexpr bool col_pipe_smem_tables() { return LOG2N <= 11; }
+
+// Two exchange buffers per column, then 16 staging slots per thread, then
+// (col_pipe_smem_tables) the twiddle table and the float table.
 template <int LOG2N, int CG>
 CFD_HD size_t col_pipe_smem() {
-  return ((size_t)2 * CG * col_pipe_bstride<LOG2N, CG>() + (size_t)CG * (1 << LOG2N)) *
-         sizeof(float2);
+  size_t b = ((size_t)2 * CG * col_pipe_bstride<LOG2N, CG>() + (size_t)CG * (1 << LOG2N)) *
+             sizeof(float2);
+  if (col_pipe_smem_tables<LOG2N>())
+    b += (size_t)fft_pass_table_size(LOG2N) * sizeof(float2) + (size_t)(1 << LOG2N) * sizeof(float);
+  return b;
 }
 
-// One transform of sign SIGN of the calling worker's column.  v: the pass-0
+// The tables' place in shared memory, after the staging slots.
+template <int LOG2N, int CG>
+CFD_D float2* col_pipe_tw_smem(float2* sbuf) {
+  return sbuf + 2 * CG * col_pipe_bstride<LOG2N, CG>() + CG * (1 << LOG2N);
+}
+template <int LOG2N, int CG>
+CFD_D float* col_pipe_tab_smem(float2* sbuf) {
+  return reinterpret_cast<float*>(col_pipe_tw_smem<LOG2N, CG>(sbuf) +
+                                  fft_pass_table_size(LOG2N));
+}
+
+// Copies the twiddle table and the float table `tab` (N entries) into shared
+// memory when col_pipe_smem_tables; returns the pointers the block reads
+// them through (shared copies or the global tables).  Ends with a barrier.
+template <int LOG2N, int CG>
+CFD_D void col_pipe_tables(float2* sbuf, const float2* __restrict__ twp,
+                           const float* __restrict__ tab, const float2** tw_out,
+                           const float** tab_out) {
+  if (col_pipe_smem_tables<LOG2N>()) {
+    float2* tw = col_pipe_tw_smem<LOG2N, CG>(sbuf);
+    float* tb = col_pipe_tab_smem<LOG2N, CG>(sbuf);
+    const int ntw = fft_pass_table_size(LOG2N);
+    for (int i = threadIdx.x; i < ntw; i += blockDim.x) tw[i] = __ldg(twp + i);
+    for (int i = threadIdx.x; i < (1 << LOG2N); i += blockDim.x) tb[i] = __ldg(tab + i);
+    *tw_out = tw;
+    *tab_out = tb;
+  } else {
+    *tw_out = twp;
+    *tab_out = tab;
+  }
+  __syncthreads();
+}
+
+// One transform of sign SIGN of the calling worker's column; twp is the pass
+// table as col_pipe_tables returned it.  v: the pass-0
 // inputs x[t + NTHR r] on entry, X[t + NTHR m] in v[m] on return.  buf[0],
 // buf[1]: this column's two exchange buffers; the k-th exchange of the
 // transform writes buf[(FIRST + k) & 1].  Called by every thread of the block
@@ -51,6 +96,7 @@ CFD_HD size_t col_pipe_smem() {
 template <int LOG2N, int SIGN, int FIRST>
 CFD_D void col_pipe_fft(float2 (&v)[16], float2* const (&buf)[2], int t,
                         const float2* __restrict__ twp) {
+  constexpr bool LDG = !col_pipe_smem_tables<LOG2N>();  // twp: global or a shared copy
   using P = ColPipe<LOG2N>;
   int wsel = FIRST;
   int tw_off = 0;
@@ -63,7 +109,7 @@ CFD_D void col_pipe_fft(float2 (&v)[16], float2* const (&buf)[2], int t,
       for (int r = 0; r < 16; ++r) v[r] = in[pidx(t + P::NTHR * r)];
     }
     const int k = t & (Ns - 1);
-    if (Ns > 1) apply_twiddles<16, SIGN>(v, twp + tw_off, Ns, k);
+    if (Ns > 1) apply_twiddles<16, SIGN, LDG>(v, twp + tw_off, Ns, k);
     Dft<16, SIGN>::run(v);
     if (q > 0) tw_off += 15 << (4 * q);
     const bool last = q == P::N16 - 1 && P::REM == 0;
@@ -90,7 +136,7 @@ CFD_D void col_pipe_fft(float2 (&v)[16], float2* const (&buf)[2], int t,
 #pragma unroll
     for (int b = 0; b < NB; ++b) {
       const int j = t + P::NTHR * b;
-      apply_twiddles<R, SIGN>(vv[b], twp + tw_off, Ns, j);
+      apply_twiddles<R, SIGN, LDG>(vv[b], twp + tw_off, Ns, j);
       Dft<R, SIGN>::run(vv[b]);
       // X[j + Ns r] = X[t + NTHR (b + NB r)]
 #pragma unroll

@@ -149,33 +149,35 @@ CFD_HD int fft_pass_table_size(int log2L) {
 // rounded once from double); the others are one product of two table values,
 // r = 4b + a -> w^(4b k) * w^(a k), so no twiddle is more than one complex
 // rounding away from the correctly rounded value.
-template <int R, int SIGN>
+// LDG: the table is in global memory (read through the read-only path);
+// otherwise it is read with plain loads (a copy in shared memory).
+template <int R, int SIGN, bool LDG = true>
 CFD_D float2 load_tw(const float2* __restrict__ twp, int Ns, int r, int k) {
-  float2 w = __ldg(twp + (r - 1) * Ns + k);
+  float2 w = LDG ? __ldg(twp + (r - 1) * Ns + k) : twp[(r - 1) * Ns + k];
   if (SIGN > 0) w.y = -w.y;
   return w;
 }
 
-template <int R, int SIGN>
+template <int R, int SIGN, bool LDG = true>
 CFD_D void apply_twiddles(float2* v, const float2* __restrict__ twp, int Ns,
                           int k) {
-  const float2 w1 = load_tw<R, SIGN>(twp, Ns, 1, k);
+  const float2 w1 = load_tw<R, SIGN, LDG>(twp, Ns, 1, k);
   if (R == 2) {
     v[1] = c_mul(v[1], w1);
     return;
   }
-  const float2 w2 = load_tw<R, SIGN>(twp, Ns, 2, k);
-  const float2 w3 = load_tw<R, SIGN>(twp, Ns, 3, k);
+  const float2 w2 = load_tw<R, SIGN, LDG>(twp, Ns, 2, k);
+  const float2 w3 = load_tw<R, SIGN, LDG>(twp, Ns, 3, k);
   v[1] = c_mul(v[1], w1);
   v[2] = c_mul(v[2], w2);
   v[3] = c_mul(v[3], w3);
   if (R == 4) return;
   float2 wb[4];
   wb[0] = make_float2(1.f, 0.f);
-  wb[1] = load_tw<R, SIGN>(twp, Ns, 4, k);
+  wb[1] = load_tw<R, SIGN, LDG>(twp, Ns, 4, k);
   if (R == 16) {
-    wb[2] = load_tw<R, SIGN>(twp, Ns, 8, k);
-    wb[3] = load_tw<R, SIGN>(twp, Ns, 12, k);
+    wb[2] = load_tw<R, SIGN, LDG>(twp, Ns, 8, k);
+    wb[3] = load_tw<R, SIGN, LDG>(twp, Ns, 12, k);
   }
   const float2 wa[4] = {make_float2(1.f, 0.f), w1, w2, w3};
 #pragma unroll

@@ -730,13 +730,16 @@ __global__ void __launch_bounds__(MAXT, MINB)
 // periodic Laplacian (fast_diagonalization.py:199-266), 1/lambda where
 // |lambda| > cutoff, else 0.  col_diag 1: implicit diffusion's
 // func(lambda) = x / (1 - x), x = (dt nu) lambda (diffusion.py:176-182).
-CFD_D float pinv_diag(const FvmParams& p, int kx, int ky) {
-  const float lam = __ldg(p.lamx + kx) + __ldg(p.lamy + ky);
+CFD_D float pinv_diag_at(const FvmParams& p, float lamx, int ky) {
+  const float lam = lamx + __ldg(p.lamy + ky);
   if (p.col_diag == 1) {
     const float x = p.dtnu * lam;
     return p.pinv_scale * (x / (1.f - x));
   }
   return fabsf(lam) > p.cutoff ? p.pinv_scale / lam : 0.f;
+}
+CFD_D float pinv_diag(const FvmParams& p, int kx, int ky) {
+  return pinv_diag_at(p, __ldg(p.lamx + kx), ky);
 }
 
 // Column pass of the packed row spectra.  Row element 0 holds the real DC and
@@ -963,6 +966,9 @@ CFD_D void col_pinv_pipe_cols(const FvmParams& p, float2* __restrict__ spec, int
   float2 v[16];
   col_pipe_prefetch<LOG2N, CG>(spec, L, g0, w, t, stage);
   cp_async_commit();
+  const float2* tw;
+  const float* lamx;
+  col_pipe_tables<LOG2N, CG>(sbuf, p.twp_x, p.lamx, &tw, &lamx);
 #pragma unroll 1
   for (int g = g0; g < groups; g += gstep) {
     // Each thread reads back only the slots it requested itself, so its own
@@ -972,11 +978,12 @@ CFD_D void col_pinv_pipe_cols(const FvmParams& p, float2* __restrict__ spec, int
     const int gn = g + gstep;
     if (gn < groups) col_pipe_prefetch<LOG2N, CG>(spec, L, gn, w, t, stage);
     cp_async_commit();
-    col_pipe_fft<LOG2N, -1, 0>(v, buf, t, p.twp_x);
+    col_pipe_fft<LOG2N, -1, 0>(v, buf, t, tw);
     const int cp = g * CG >= L ? L : g * CG + w;  // pinv column index
 #pragma unroll
-    for (int m = 0; m < 16; ++m) v[m] = c_scale(v[m], pinv_diag(p, t + P::NTHR * m, cp));
-    col_pipe_fft<LOG2N, 1, INV_FIRST>(v, buf, t, p.twp_x);
+    for (int m = 0; m < 16; ++m)
+      v[m] = c_scale(v[m], pinv_diag_at(p, lamx[t + P::NTHR * m], cp));
+    col_pipe_fft<LOG2N, 1, INV_FIRST>(v, buf, t, tw);
     col_pipe_store<LOG2N, CG>(spec, L, g, w, t, v);
   }
   cp_async_wait_all();

@@ -41,8 +41,9 @@ CFD_D float filt(const SpecParams& p, int kx, int c) {
 
 // The four column-transformed inputs of the explicit terms for element
 // (kx, c) of the state u.
-CFD_D float2 prep_factor(const SpecParams& p, int f, int kx, int c, float2 u) {
-  const float kxf = kx_of(p, kx), kyf = ky_of(p, c);
+// kxf: the kx wavenumber of row kx (from the table, wherever it is read).
+CFD_D float2 prep_factor_k(const SpecParams& p, int f, int kx, float kxf, int c, float2 u) {
+  const float kyf = ky_of(p, c);
   if (f == 3) return u;
   const float ax = p.two_pi * kxf;
   if (f == 2) return make_float2(ax * u.x, ax * u.y);
@@ -54,6 +55,10 @@ CFD_D float2 prep_factor(const SpecParams& p, int f, int kx, int c, float2 u) {
   const float2 psi = make_float2(pm * u.x, pm * u.y);
   if (f == 0) return psi;
   return make_float2(ax * psi.x, ax * psi.y);
+}
+
+CFD_D float2 prep_factor(const SpecParams& p, int f, int kx, int c, float2 u) {
+  return prep_factor_k(p, f, kx, kx_of(p, kx), c, u);
 }
 
 // ky-side factors: vx = i ay A, vy = -i B, gx = i C, gy = i ay D.
@@ -107,8 +112,8 @@ __global__ void __launch_bounds__(256, 3)
 // spectral/time_stepping.py:163-169), or just F(u) with explicit_only.
 // The stage arithmetic of one element from its loaded state u and register h
 // (ho, read only when sc.has_h_in): returns the new state, sets *h_new.
-CFD_D float2 stage_update_core(const SpecParams& p, const StageCoef& sc, int kx, int c,
-                               float2 a, float2 u, float2 ho, float2* h_new) {
+CFD_D float2 stage_update_core_k(const SpecParams& p, const StageCoef& sc, int kx, float kxf,
+                                 int c, float2 a, float2 u, float2 ho, float2* h_new) {
   const int ncols = p.L + 1;
   const size_t g = (size_t)kx * ncols + c;
   // explicit_terms: rfftn(advection) * filter (+ forcing curl)
@@ -127,7 +132,7 @@ CFD_D float2 stage_update_core(const SpecParams& p, const StageCoef& sc, int kx,
   float2 h = F;
   if (sc.has_h_in) h = c_add(F, make_float2(sc.beta * ho.x, sc.beta * ho.y));
   // linear_term = nu * laplace - drag; laplace = (2 pi i)^2 |k|^2
-  const float kxf = kx_of(p, kx), kyf = ky_of(p, c);
+  const float kyf = ky_of(p, c);
   const float lin = p.nu * (p.lap_coef * (kxf * kxf + kyf * kyf)) - p.drag;
   // u + gamma dt h + mu G(u), G(u) = linear_term * u
   const float2 x = make_float2((u.x + sc.gdt * h.x) + sc.mu * (lin * u.x),
@@ -136,6 +141,11 @@ CFD_D float2 stage_update_core(const SpecParams& p, const StageCoef& sc, int kx,
   const float inv = __frcp_rn(1.f - sc.mu * lin);
   *h_new = h;
   return make_float2(inv * x.x, inv * x.y);
+}
+
+CFD_D float2 stage_update_core(const SpecParams& p, const StageCoef& sc, int kx, int c,
+                               float2 a, float2 u, float2 ho, float2* h_new) {
+  return stage_update_core_k(p, sc, kx, kx_of(p, kx), c, a, u, ho, h_new);
 }
 
 CFD_D void stage_update_at(const SpecParams& p, const StageCoef& sc, int kx, int c, float2 a,
@@ -424,6 +434,9 @@ __global__ void __launch_bounds__(CG * (1 << LOG2N) / 16,
   if (g >= groups) return;  // uniform per block
   spec_pipe_prefetch<LOG2N, CG>(ahat, ncols, g * CG + w, t, stage);
   cp_async_commit();
+  const float2* tw;
+  const float* kxt;
+  col_pipe_tables<LOG2N, CG>(sbuf, p.twp_x, p.kx, &tw, &kxt);
   float2 v[16], us[16], hs[16];
 #pragma unroll 1
   for (; g < groups; g += gridDim.x) {
@@ -444,7 +457,7 @@ __global__ void __launch_bounds__(CG * (1 << LOG2N) / 16,
         hs[m] = sc.has_h_in ? hst[gi] : make_float2(0.f, 0.f);
       }
     }
-    col_pipe_fft<LOG2N, -1, 0>(v, buf, t, p.twp_x);
+    col_pipe_fft<LOG2N, -1, 0>(v, buf, t, tw);
     if (c < ncols) {
 #pragma unroll
       for (int m = 0; m < 16; ++m) {
@@ -454,9 +467,85 @@ __global__ void __launch_bounds__(CG * (1 << LOG2N) / 16,
           stage_update_at(p, sc, kx, c, v[m], wst, hst);
         } else {
           float2 h;
-          wst[gi] = stage_update_core(p, sc, kx, c, v[m], us[m], hs[m], &h);
+          wst[gi] = stage_update_core_k(p, sc, kx, kxt[kx], c, v[m], us[m], hs[m], &h);
           if (sc.write_h) hst[gi] = h;
         }
+      }
+    }
+  }
+  cp_async_wait_all();
+}
+
+// Column update fused with the next stage's column prep: after the forward
+// transform and the stage update, the thread holds the new state of its
+// column at kx = t + (N/16) m, which are exactly the first inverse pass's
+// input positions, so the four prep fields are formed in registers and
+// transformed without re-reading the state.  Every value is the one the
+// separate update and prep passes compute, so the bits are the same.  One
+// item makes ten exchanges (five transforms), so items start on buffer 0.
+template <int LOG2N, int CG>
+__global__ void __launch_bounds__(CG * (1 << LOG2N) / 16,
+                                  col_pipe_min_blocks(CG * (1 << LOG2N) / 16))
+    spec_col_stage_pipe_kernel(SpecParams p, StageCoef sc, const float2* __restrict__ ahat,
+                               float2* __restrict__ wst, float2* __restrict__ hst, T4 t4) {
+  using P = ColPipe<LOG2N>;
+  constexpr int T = CG * P::NTHR;
+  extern __shared__ float2 sbuf[];
+  const int ncols = p.L + 1, groups = (ncols + CG - 1) / CG;
+  const int w = threadIdx.x % CG, t = threadIdx.x / CG, tid = threadIdx.x;
+  const int bstride = col_pipe_bstride<LOG2N, CG>();
+  float2* const buf[2] = {sbuf + w * bstride, sbuf + (CG + w) * bstride};
+  float2* const stage = sbuf + 2 * CG * bstride;
+  int g = blockIdx.x;
+  if (g >= groups) return;  // uniform per block
+  spec_pipe_prefetch<LOG2N, CG>(ahat, ncols, g * CG + w, t, stage);
+  cp_async_commit();
+  const float2* tw;
+  const float* kxt;
+  col_pipe_tables<LOG2N, CG>(sbuf, p.twp_x, p.kx, &tw, &kxt);
+  float2 v[16], u[16], hs[16];
+#pragma unroll 1
+  for (; g < groups; g += gridDim.x) {
+    const int c = g * CG + w;
+    const bool live = c < ncols;
+    cp_async_wait_all();
+#pragma unroll
+    for (int r = 0; r < 16; ++r) v[r] = live ? stage[r * T + tid] : make_float2(0.f, 0.f);
+    const int gn = g + gridDim.x;
+    if (gn < groups) spec_pipe_prefetch<LOG2N, CG>(ahat, ncols, gn * CG + w, t, stage);
+    cp_async_commit();
+    // The column's state and h values are requested before the transform
+    // (each element is read and written by this thread only).
+#pragma unroll
+    for (int m = 0; m < 16; ++m) {
+      const size_t gi = (size_t)(t + P::NTHR * m) * ncols + c;
+      u[m] = live ? wst[gi] : make_float2(0.f, 0.f);
+      hs[m] = (live && sc.has_h_in) ? hst[gi] : make_float2(0.f, 0.f);
+    }
+    col_pipe_fft<LOG2N, -1, 0>(v, buf, t, tw);
+    if (live) {
+#pragma unroll
+      for (int m = 0; m < 16; ++m) {
+        const int kx = t + P::NTHR * m;
+        const size_t gi = (size_t)kx * ncols + c;
+        float2 h;
+        u[m] = stage_update_core_k(p, sc, kx, kxt[kx], c, v[m], u[m], hs[m], &h);
+        wst[gi] = u[m];
+        if (sc.write_h) hst[gi] = h;
+      }
+    }
+#pragma unroll 1
+    for (int f = 0; f < 4; ++f) {
+#pragma unroll
+      for (int r = 0; r < 16; ++r) {
+        const int kx = t + P::NTHR * r;
+        v[r] = live ? prep_factor_k(p, f, kx, kxt[kx], c, u[r]) : make_float2(0.f, 0.f);
+      }
+      col_pipe_fft<LOG2N, 1, 0>(v, buf, t, tw);
+      if (live) {
+        float2* dst = f == 0 ? t4.t[0] : f == 1 ? t4.t[1] : f == 2 ? t4.t[2] : t4.t[3];
+#pragma unroll
+        for (int m = 0; m < 16; ++m) dst[(size_t)(t + P::NTHR * m) * ncols + c] = v[m];
       }
     }
   }
@@ -479,19 +568,24 @@ __global__ void __launch_bounds__(CG * (1 << LOG2N) / 16,
   if (it >= items) return;  // uniform per block
   spec_pipe_prefetch<LOG2N, CG>(wst, ncols, (it >> 2) * CG + w, t, stage);
   cp_async_commit();
+  const float2* tw;
+  const float* kxt;
+  col_pipe_tables<LOG2N, CG>(sbuf, p.twp_x, p.kx, &tw, &kxt);
   float2 v[16];
 #pragma unroll 1
   for (; it < items; it += gridDim.x) {
     const int f = it & 3, c = (it >> 2) * CG + w;
     cp_async_wait_all();
 #pragma unroll
-    for (int r = 0; r < 16; ++r)
-      v[r] = c < ncols ? prep_factor(p, f, t + P::NTHR * r, c, stage[r * T + tid])
+    for (int r = 0; r < 16; ++r) {
+      const int kx = t + P::NTHR * r;
+      v[r] = c < ncols ? prep_factor_k(p, f, kx, kxt[kx], c, stage[r * T + tid])
                        : make_float2(0.f, 0.f);
+    }
     const int in = it + gridDim.x;
     if (in < items) spec_pipe_prefetch<LOG2N, CG>(wst, ncols, (in >> 2) * CG + w, t, stage);
     cp_async_commit();
-    col_pipe_fft<LOG2N, 1, 0>(v, buf, t, p.twp_x);
+    col_pipe_fft<LOG2N, 1, 0>(v, buf, t, tw);
     if (c < ncols) {
       float2* dst = f == 0 ? t4.t[0] : f == 1 ? t4.t[1] : f == 2 ? t4.t[2] : t4.t[3];
 #pragma unroll
@@ -697,9 +791,10 @@ bool spec_cluster_ok(const SpecParams& p) {
   return p.col_mode == 1 && p.nx >= 256 && p.nx <= 2048;
 }
 
-// col_mode 2: groups of 4 columns per block (2 at 4096 rows); 3: groups of 2.
+// col_mode 2: groups of 4 columns per block (2 at 4096 rows); 3: groups of 2;
+// 4: groups of 4 with the update and the next stage's prep fused.
 bool spec_pipe_ok(const SpecParams& p) {
-  return (p.col_mode == 2 || p.col_mode == 3) && p.log2nx >= 9 && p.log2nx <= 12;
+  return p.col_mode >= 2 && p.col_mode <= 4 && p.log2nx >= 9 && p.log2nx <= 12;
 }
 
 // Persistent column passes: as many blocks as fit on the device at once,
@@ -732,6 +827,20 @@ static cudaError_t spec_prep_pipe_impl(const SpecParams& p, const float2* w, con
                                             &threads);
   if (e != cudaSuccess) return e;
   kern<<<grid, threads, smem, s>>>(p, w, tt);
+  return cudaGetLastError();
+}
+
+template <int LOG2N, int CG>
+static cudaError_t spec_stage_pipe_impl(const SpecParams& p, const StageCoef& sc,
+                                        const float2* ahat, float2* w, float2* h, const T4& tt,
+                                        cudaStream_t s) {
+  int grid, threads;
+  size_t smem;
+  auto kern = spec_col_stage_pipe_kernel<LOG2N, CG>;
+  cudaError_t e = spec_pipe_grid<LOG2N, CG>(kern, (p.L + 1 + CG - 1) / CG, &grid, &smem,
+                                            &threads);
+  if (e != cudaSuccess) return e;
+  kern<<<grid, threads, smem, s>>>(p, sc, ahat, w, h, tt);
   return cudaGetLastError();
 }
 
@@ -791,6 +900,16 @@ cudaError_t launch_spec_col_update(const SpecParams& p, const StageCoef& sc,
                                    const float2* ahat, float2* w, float2* h,
                                    float2* const t4[4], cudaStream_t s) {
   cudaError_t e;
+  if (spec_pipe_ok(p) && p.col_mode == 4 && sc.prep_next && !sc.explicit_only) {
+    // Update and the next stage's prep in one pass.
+    T4 tt{{t4[0], t4[1], t4[2], t4[3]}};
+    switch (p.log2nx) {
+      case 9: return spec_stage_pipe_impl<9, 4>(p, sc, ahat, w, h, tt, s);
+      case 10: return spec_stage_pipe_impl<10, 4>(p, sc, ahat, w, h, tt, s);
+      case 11: return spec_stage_pipe_impl<11, 4>(p, sc, ahat, w, h, tt, s);
+      default: return spec_stage_pipe_impl<12, 2>(p, sc, ahat, w, h, tt, s);
+    }
+  }
   if (spec_pipe_ok(p) && p.col_mode == 3) {
     switch (p.log2nx) {
       case 9: e = spec_update_pipe_impl<9, 2>(p, sc, ahat, w, h, s); break;

@@ -339,12 +339,13 @@ class SpecPlan:
   def nbytes(self) -> int:
     return int(self._lib.cfd_spec_plan_bytes(self._h))
 
-  LAUNCH_CHOICES = 4
+  LAUNCH_CHOICES = 5
 
   def set_launch(self, choice: int):
     """Column passes: 0 per-block columns, 1 clusters of four one-column
     blocks (256 <= nx <= 2048), 2/3 persistent register-pipelined groups of
-    4/2 columns (512 <= nx <= 4096).  Results do not change."""
+    4/2 columns (512 <= nx <= 4096), 4 as 2 with each stage's update and the
+    next stage's prep fused.  Results do not change."""
     nat.check(self._lib.cfd_spec_plan_set_launch(self._h, int(choice)), 'cfd_spec_plan_set_launch')
 
   @property
@@ -401,13 +402,13 @@ class SpecPlan:
                                       ptr(out), int(steps)), 'cfd_spec_step')
     return out
 
-  PROFILE_KINDS = ('row', 'col_update', 'col_prep')
+  PROFILE_KINDS = ('row', 'col_update', 'col_prep', 'col_stage')
 
   def profile(self, w_hat: torch.Tensor, steps: int):
     """Mean per-launch duration (ms) of each spectral kernel kind."""
     self._half(w_hat, 'vorticity_hat')
     out = torch.empty_like(w_hat)
-    ms = (ctypes.c_float * 3)()
+    ms = (ctypes.c_float * 4)()
     nat.check(self._lib.cfd_spec_profile(self._h, current_stream_ptr(w_hat.device), ptr(w_hat),
                                          ptr(out), int(steps), ctypes.cast(ms, ctypes.c_void_p)),
               'cfd_spec_profile')
