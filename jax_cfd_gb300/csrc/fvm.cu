@@ -1109,17 +1109,6 @@ __global__ void __launch_bounds__(MAXT, MINB)
 CFD_HD bool warp_rows_ok(const FvmParams& p) { return p.log2ny - 1 == kWarpFftLog2; }
 constexpr int kWarpRows = 4;  // rows (warps) per block
 
-CFD_D float2 shfl_idx2(float2 x, int src) {
-  return make_float2(__shfl_sync(kFull, x.x, src), __shfl_sync(kFull, x.y, src));
-}
-
-// Z[L - k] for k = lane + 32 k1, from the warp FFT's output registers.
-CFD_D float2 wfft_mirror(const float2 (&v)[32], int k1, int lane) {
-  float2 zp = shfl_idx2(v[wfft_slot(31 - k1)], (32 - lane) & 31);
-  if (lane == 0) zp = v[wfft_slot((32 - k1) & 31)];
-  return zp;
-}
-
 CFD_D void div_rfft_row_warp(const FvmParams& p, int i, const float* __restrict__ us,
                              const float* __restrict__ vs, float2* __restrict__ spec,
                              float2* tile) {

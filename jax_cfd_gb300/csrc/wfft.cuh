@@ -114,4 +114,17 @@ CFD_D void warp_fft1024(float2 (&v)[32], float2* __restrict__ tile,
   dft32<SIGN>(v);
 }
 
+CFD_D float2 wfft_shfl_idx2(float2 x, int src) {
+  return make_float2(__shfl_sync(0xffffffffu, x.x, src), __shfl_sync(0xffffffffu, x.y, src));
+}
+
+// Z[L - k] for k = lane + 32 k1 (L = 1024), from warp_fft1024's output
+// registers: for lane l >= 1 the partner lives in lane 32 - l, register
+// 31 - k1; for lane 0 in lane 0, register 32 - k1.
+CFD_D float2 wfft_mirror(const float2 (&v)[32], int k1, int lane) {
+  float2 zp = wfft_shfl_idx2(v[wfft_slot(31 - k1)], (32 - lane) & 31);
+  if (lane == 0) zp = v[wfft_slot((32 - k1) & 31)];
+  return zp;
+}
+
 }  // namespace cfd

@@ -208,11 +208,13 @@ def _vorticity_hat(n, seed, vmax, dev):
 
 
 @pytest.mark.parametrize('graph', [False, True])
-def test_spectral_batch_slots_equal_single_steps(cuda_device, graph):
+@pytest.mark.parametrize('n', [64, 2048])
+def test_spectral_batch_slots_equal_single_steps(cuda_device, graph, n):
+  """Slots of a batch equal the single-trajectory step bit for bit."""
   from jax_cfd_gb300 import batching
-  n = 64
   draws = [(1e-3, 4, 1e-2, 61, 2.0), (1e-4, 2, 5e-3, 62, 1.0), (1e-2, 8, 2e-2, 63, 3.0)]
-  steps = [_spec_step(n, nu, k, dt) for nu, k, dt, _, _ in draws]
+  # dt chosen for 64^2; scaled with the grid step to keep the Courant number.
+  steps = [_spec_step(n, nu, k, dt * 64 / n) for nu, k, dt, _, _ in draws]
   w0 = [_vorticity_hat(n, seed, vmax, cuda_device) for _, _, _, seed, vmax in draws]
   grid_step = steps[0].equation.grid.step
   b = batching.SpecBatch((n, n), grid_step, len(draws), device=cuda_device)
@@ -224,6 +226,7 @@ def test_spectral_batch_slots_equal_single_steps(cuda_device, graph):
   torch.cuda.synchronize(cuda_device)
   for i, (st, w) in enumerate(zip(steps, w0)):
     want = st.gb300_repeat(w, [5, 3, 0][i])
+    assert torch.isfinite(torch.view_as_real(want)).all()
     assert torch.equal(torch.view_as_real(b.state(i)), torch.view_as_real(want))
 
 

@@ -36,7 +36,7 @@ def test_rfft2_irfft2(cuda_device, shape):
   assert rel_l2(back, x) <= 1e-6
 
 
-@pytest.mark.parametrize('shape', [(16, 16), (64, 64), (128, 64)])
+@pytest.mark.parametrize('shape', [(16, 16), (64, 64), (128, 64), (64, 2048)])
 @pytest.mark.parametrize('forced', [False, True])
 def test_explicit_terms_match_oracle(cuda_device, shape, forced):
   import jax_cfd_gb300.base as cfd
@@ -54,7 +54,7 @@ def test_explicit_terms_match_oracle(cuda_device, shape, forced):
   assert rel_l2(got, oeq.explicit_terms(w0)) <= STEP_TOL
 
 
-@pytest.mark.parametrize('shape', [(16, 16), (64, 64), (256, 256), (64, 128)])
+@pytest.mark.parametrize('shape', [(16, 16), (64, 64), (256, 256), (64, 128), (256, 2048)])
 def test_cn_rk4_step_matches_oracle(cuda_device, shape):
   import jax_cfd_gb300.base as cfd
   from jax_cfd_gb300.spectral import equations as seq
