@@ -2,6 +2,7 @@
 // grid; entry points enqueue the kernels of kernels.h on the caller's stream.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -327,6 +328,10 @@ static int fvm_params_from_config(const cfd_fvm_config* cfg, cfd::FvmParams* out
   p.stencil = ((long long)nx * ny >= (1LL << 22) && cfd::stream_stencil_ok(p)) ? 1 : 0;
   // The persistent column pass measured fastest from 1024 rows up (GB300).
   p.col_mode = (nx >= 1024 && cfd::col_pipe_ok(p, 0)) ? 3 : 0;
+  // The step's kernels start as programmatic dependents of their predecessor
+  // (CFD_GB300_PDL=0 in the environment turns this off, for comparison).
+  const char* pdl = std::getenv("CFD_GB300_PDL");
+  p.pdl = (pdl && pdl[0] == '0') ? 0 : 1;
   return CFD_OK;
 }
 

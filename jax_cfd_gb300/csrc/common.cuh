@@ -34,3 +34,31 @@ CFD_HD int ilog2(int x) {
 }
 
 CFD_HD bool is_pow2(int x) { return x > 0 && (x & (x - 1)) == 0; }
+
+// Programmatic dependent launch (sm_90+).  A kernel launched with
+// cudaLaunchAttributeProgrammaticStreamSerialization may start while the
+// previous kernel in the stream is still running; pdl_wait() blocks until
+// that kernel has completed and its writes are visible, so it must precede
+// every read of the previous kernel's output.  pdl_trigger() lets the next
+// kernel be launched once every block of this one is running.  Without the
+// attribute both are no-ops.
+CFD_D void pdl_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
+CFD_D void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;\n" :::); }
+
+// Launches `kern` on stream s, as a programmatic dependent of the previous
+// kernel when pdl != 0.
+template <typename... KArgs, typename... Args>
+cudaError_t launch_maybe_pdl(bool pdl, void (*kern)(KArgs...), dim3 grid, dim3 block,
+                             size_t smem, cudaStream_t s, Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = pdl ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, kern, static_cast<KArgs>(args)...);
+}

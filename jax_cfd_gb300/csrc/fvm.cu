@@ -524,6 +524,8 @@ __global__ void __launch_bounds__(128)
     fvm_explicit_stream_kernel(FvmParams p, const float* __restrict__ ua,
                                const float* __restrict__ va, const float* __restrict__ q,
                                float* __restrict__ uo, float* __restrict__ vo) {
+  pdl_wait();
+  pdl_trigger();
   const int lane = threadIdx.x & 31;
   const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
   const int strips = (p.ny + kSW - 1) / kSW;
@@ -964,11 +966,15 @@ CFD_D void col_pinv_pipe_cols(const FvmParams& p, float2* __restrict__ spec, int
   constexpr int INV_FIRST = (P::PASSES - 1) & 1;
   if (g0 >= groups) return;  // uniform per block
   float2 v[16];
-  col_pipe_prefetch<LOG2N, CG>(spec, L, g0, w, t, stage);
-  cp_async_commit();
+  // The constant tables first: under a programmatic launch this overlaps the
+  // previous kernel's tail.
   const float2* tw;
   const float* lamx;
   col_pipe_tables<LOG2N, CG>(sbuf, p.twp_x, p.lamx, &tw, &lamx);
+  pdl_wait();
+  pdl_trigger();
+  col_pipe_prefetch<LOG2N, CG>(spec, L, g0, w, t, stage);
+  cp_async_commit();
 #pragma unroll 1
   for (int g = g0; g < groups; g += gstep) {
     // Each thread reads back only the slots it requested itself, so its own
@@ -1164,6 +1170,8 @@ CFD_D void irfft_row_warp(const FvmParams& p, int i, float2* spec, float2* tile)
 __global__ void __launch_bounds__(32 * kWarpRows)
     fvm_div_rfft_warp_kernel(FvmParams p, const float* __restrict__ us,
                              const float* __restrict__ vs, float2* __restrict__ spec) {
+  pdl_wait();
+  pdl_trigger();
   __shared__ float2 tiles[kWarpRows][kWarpFftTile];
   const int w = threadIdx.x >> 5;
   div_rfft_row_warp(p, blockIdx.x * kWarpRows + w, us, vs, spec, tiles[w]);
@@ -1171,6 +1179,8 @@ __global__ void __launch_bounds__(32 * kWarpRows)
 
 __global__ void __launch_bounds__(32 * kWarpRows)
     fvm_irfft_warp_kernel(FvmParams p, float2* spec) {
+  pdl_wait();
+  pdl_trigger();
   __shared__ float2 tiles[kWarpRows][kWarpFftTile];
   const int w = threadIdx.x >> 5;
   irfft_row_warp(p, blockIdx.x * kWarpRows + w, spec, tiles[w]);
@@ -1207,6 +1217,8 @@ __global__ void fvm_project_out_kernel(FvmParams p, const float* __restrict__ us
                                        const float* __restrict__ q,
                                        float* __restrict__ uo,
                                        float* __restrict__ vo) {
+  pdl_wait();
+  pdl_trigger();
   project_out_cells(p, blockIdx.x, gridDim.x, us, vs, q, uo, vo);
 }
 
@@ -1389,8 +1401,8 @@ static void launch_explicit_variant(const FvmParams& p, bool stream, bool tiled,
                                     float* uo, float* vo, cudaStream_t s) {
   if (stream) {
     const long long warps = (long long)((p.ny + kSW - 1) / kSW) * ((p.nx + kSH - 1) / kSH);
-    fvm_explicit_stream_kernel<PR, CV, FO><<<(int)((warps + 3) / 4), 128, 0, s>>>(p, ua, va, q,
-                                                                                  uo, vo);
+    launch_maybe_pdl(p.pdl, fvm_explicit_stream_kernel<PR, CV, FO>, dim3((int)((warps + 3) / 4)),
+                     dim3(128), 0, s, p, ua, va, q, uo, vo);
   } else if (tiled) {
     fvm_explicit_tiled_kernel<PR, K0, CV, FO><<<grid, kStencilThreads, 0, s>>>(p, ua, va, q, uo,
                                                                                vo);
@@ -1439,8 +1451,8 @@ static cudaError_t div_rfft_impl(const FvmParams& p, int target, const float* us
                                  const float* vs, float2* spec, cudaStream_t s) {
   const int log2L = p.log2ny - 1;
   if (warp_rows_ok(p)) {
-    fvm_div_rfft_warp_kernel<<<p.nx / kWarpRows, 32 * kWarpRows, 0, s>>>(p, us, vs, spec);
-    return cudaGetLastError();
+    return launch_maybe_pdl(p.pdl, fvm_div_rfft_warp_kernel, dim3(p.nx / kWarpRows),
+                            dim3(32 * kWarpRows), 0, s, p, us, vs, spec);
   }
   const int rows = fft_rows_per_block(log2L, p.nx, target);
   const bool aligned = (((uintptr_t)us | (uintptr_t)vs | (uintptr_t)spec) & 15) == 0;
@@ -1535,8 +1547,8 @@ static cudaError_t col_pinv_pipe_impl(const FvmParams& p, float2* spec, cudaStre
   }
   const int groups = p.ny / 2 / CG + 1;
   const int slots = col_pipe_device_sms() * per_sm;
-  kern<<<groups < slots ? groups : slots, threads, smem, s>>>(p, spec);
-  return cudaGetLastError();
+  return launch_maybe_pdl(p.pdl, kern, dim3(groups < slots ? groups : slots), dim3(threads), smem,
+                          s, p, spec);
 }
 
 // Column groups of the persistent pass: 4 columns per block (wide, col_mode
@@ -1583,8 +1595,8 @@ static cudaError_t irfft_impl(const FvmParams& p, int target, float2* spec,
                               cudaStream_t s) {
   const int log2L = p.log2ny - 1;
   if (warp_rows_ok(p)) {
-    fvm_irfft_warp_kernel<<<p.nx / kWarpRows, 32 * kWarpRows, 0, s>>>(p, spec);
-    return cudaGetLastError();
+    return launch_maybe_pdl(p.pdl, fvm_irfft_warp_kernel, dim3(p.nx / kWarpRows),
+                            dim3(32 * kWarpRows), 0, s, p, spec);
   }
   const int rows = fft_rows_per_block(log2L, p.nx, target);
   if (p.row_feed == 1 && (((uintptr_t)spec) & 15) == 0) {
@@ -1618,8 +1630,8 @@ cudaError_t launch_fvm_project_out(const FvmParams& p, const float* us,
                                    const float* vs, const float* q, float* uo,
                                    float* vo, cudaStream_t s) {
   const size_t n = (size_t)p.nx * p.ny;
-  fvm_project_out_kernel<<<elementwise_blocks(n), 256, 0, s>>>(p, us, vs, q, uo, vo);
-  return cudaGetLastError();
+  return launch_maybe_pdl(p.pdl, fvm_project_out_kernel, dim3(elementwise_blocks(n)), dim3(256),
+                          0, s, p, us, vs, q, uo, vo);
 }
 
 cudaError_t launch_fvm_add(size_t n, const float* w, float* u, cudaStream_t s) {

@@ -52,6 +52,7 @@ struct FvmParams {
   int row_field;       // forward row transform of the field us itself, not div
   int col_diag;        // column-pass diagonal: 0 pinv(lambda), 1 x / (1 - x), x = dtnu lambda
   float dtnu;          // float32(dt * viscosity) for col_diag = 1
+  int pdl;             // launch the step's kernels as programmatic dependents
 };
 
 // One slot of a same-shape batch of FVM trajectories (device-resident table
