@@ -147,6 +147,7 @@ struct SpecParams {
   const float2* twp_y;  // pass twiddle tables of the length-ny/2 row FFT
   const float* kx;      // fftfreq(nx, hx) in float32 (nx)
   const float* ky;      // rfftfreq(ny, hy) in float32 (L + 1)
+  int pdl;              // launch the stage kernels as programmatic dependents
 };
 
 // Whether the clustered spectral column passes (col_mode 1) apply to this grid.

@@ -262,6 +262,8 @@ __global__ void __launch_bounds__(256, 3)
     spec_row_kernel(SpecParams p, int rows, const float2* __restrict__ t0,
                     const float2* __restrict__ t1, const float2* __restrict__ t2,
                     const float2* __restrict__ t3, float2* __restrict__ ahat) {
+  pdl_wait();
+  pdl_trigger();
   row_advect_rows(p, blockIdx.x, rows, t0, t1, t2, t3, ahat);
 }
 
@@ -432,11 +434,15 @@ __global__ void __launch_bounds__(CG * (1 << LOG2N) / 16,
   float2* const stage = sbuf + 2 * CG * bstride;
   int g = blockIdx.x;
   if (g >= groups) return;  // uniform per block
-  spec_pipe_prefetch<LOG2N, CG>(ahat, ncols, g * CG + w, t, stage);
-  cp_async_commit();
+  // The constant tables first: under a programmatic launch this overlaps the
+  // previous kernel's tail.
   const float2* tw;
   const float* kxt;
   col_pipe_tables<LOG2N, CG>(sbuf, p.twp_x, p.kx, &tw, &kxt);
+  pdl_wait();
+  pdl_trigger();
+  spec_pipe_prefetch<LOG2N, CG>(ahat, ncols, g * CG + w, t, stage);
+  cp_async_commit();
   float2 v[16], us[16], hs[16];
 #pragma unroll 1
   for (; g < groups; g += gridDim.x) {
@@ -498,11 +504,15 @@ __global__ void __launch_bounds__(CG * (1 << LOG2N) / 16,
   float2* const stage = sbuf + 2 * CG * bstride;
   int g = blockIdx.x;
   if (g >= groups) return;  // uniform per block
-  spec_pipe_prefetch<LOG2N, CG>(ahat, ncols, g * CG + w, t, stage);
-  cp_async_commit();
+  // The constant tables first: under a programmatic launch this overlaps the
+  // previous kernel's tail.
   const float2* tw;
   const float* kxt;
   col_pipe_tables<LOG2N, CG>(sbuf, p.twp_x, p.kx, &tw, &kxt);
+  pdl_wait();
+  pdl_trigger();
+  spec_pipe_prefetch<LOG2N, CG>(ahat, ncols, g * CG + w, t, stage);
+  cp_async_commit();
   float2 v[16], u[16], hs[16];
 #pragma unroll 1
   for (; g < groups; g += gridDim.x) {
@@ -566,11 +576,13 @@ __global__ void __launch_bounds__(CG * (1 << LOG2N) / 16,
   float2* const stage = sbuf + 2 * CG * bstride;
   int it = blockIdx.x;
   if (it >= items) return;  // uniform per block
-  spec_pipe_prefetch<LOG2N, CG>(wst, ncols, (it >> 2) * CG + w, t, stage);
-  cp_async_commit();
   const float2* tw;
   const float* kxt;
   col_pipe_tables<LOG2N, CG>(sbuf, p.twp_x, p.kx, &tw, &kxt);
+  pdl_wait();
+  pdl_trigger();
+  spec_pipe_prefetch<LOG2N, CG>(wst, ncols, (it >> 2) * CG + w, t, stage);
+  cp_async_commit();
   float2 v[16];
 #pragma unroll 1
   for (; it < items; it += gridDim.x) {
@@ -826,8 +838,7 @@ static cudaError_t spec_prep_pipe_impl(const SpecParams& p, const float2* w, con
   cudaError_t e = spec_pipe_grid<LOG2N, CG>(kern, 4 * ((p.L + 1 + CG - 1) / CG), &grid, &smem,
                                             &threads);
   if (e != cudaSuccess) return e;
-  kern<<<grid, threads, smem, s>>>(p, w, tt);
-  return cudaGetLastError();
+  return launch_maybe_pdl(p.pdl, kern, dim3(grid), dim3(threads), smem, s, p, w, tt);
 }
 
 template <int LOG2N, int CG>
@@ -840,8 +851,8 @@ static cudaError_t spec_stage_pipe_impl(const SpecParams& p, const StageCoef& sc
   cudaError_t e = spec_pipe_grid<LOG2N, CG>(kern, (p.L + 1 + CG - 1) / CG, &grid, &smem,
                                             &threads);
   if (e != cudaSuccess) return e;
-  kern<<<grid, threads, smem, s>>>(p, sc, ahat, w, h, tt);
-  return cudaGetLastError();
+  return launch_maybe_pdl(p.pdl, kern, dim3(grid), dim3(threads), smem, s, p, sc, ahat, w, h,
+                          tt);
 }
 
 template <int LOG2N, int CG>
@@ -854,8 +865,7 @@ static cudaError_t spec_update_pipe_impl(const SpecParams& p, const StageCoef& s
   cudaError_t e = spec_pipe_grid<LOG2N, CG>(kern, (p.L + 1 + CG - 1) / CG, &grid, &smem,
                                             &threads);
   if (e != cudaSuccess) return e;
-  kern<<<grid, threads, smem, s>>>(p, sc, ahat, w, h);
-  return cudaGetLastError();
+  return launch_maybe_pdl(p.pdl, kern, dim3(grid), dim3(threads), smem, s, p, sc, ahat, w, h);
 }
 
 cudaError_t launch_spec_col_prep(const SpecParams& p, const float2* w,
@@ -952,9 +962,9 @@ cudaError_t launch_spec_row(const SpecParams& p, const float2* const t4[4],
   const size_t smem = (size_t)rows * 4 * padded_len(p.L) * sizeof(float2);
   cudaError_t e = set_smem(spec_row_kernel, smem);
   if (e != cudaSuccess) return e;
-  spec_row_kernel<<<p.nx / rows, threads_for(fft_workers(p.log2L, rows * 4)),
-                    smem, s>>>(p, rows, t4[0], t4[1], t4[2], t4[3], ahat);
-  return cudaGetLastError();
+  return launch_maybe_pdl(p.pdl, spec_row_kernel, dim3(p.nx / rows),
+                          dim3(threads_for(fft_workers(p.log2L, rows * 4))), smem, s, p, rows,
+                          t4[0], t4[1], t4[2], t4[3], ahat);
 }
 
 cudaError_t launch_row_rfft(const SpecParams& p, const float* x, float2* X,
