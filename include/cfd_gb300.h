@@ -218,10 +218,17 @@ int cfd_fvm_batch_set_slot(cfd_fvm_batch* batch, void* stream, int slot,
                            const cfd_fvm_config* cfg);
 int cfd_fvm_batch_set_steps(cfd_fvm_batch* batch, int slot, int steps);
 int cfd_fvm_batch_run(cfd_fvm_batch* batch, void* stream, int chunk, int use_graph);
-/* Times the transform launch configurations on a `steps`-step chunk of the
- * current slots, restores their states and keeps the fastest (index as in
- * cfd_fvm_plan_autotune).  Synchronises. */
+/* Times the launch configurations on a `steps`-step chunk of the current
+ * slots, restores their states and keeps the fastest; *chosen = row-transform
+ * shape (0 wide, 1 narrow) + 2 * column scheme (0 blocks, 1/2 clusters of
+ * 4/8, 3 persistent pipelined groups of 4 columns over all slots) + 8 *
+ * stencil (0 shared-memory tiles, 1 warp streams).  Every configuration gives
+ * the same bits.  Synchronises. */
 int cfd_fvm_batch_autotune(cfd_fvm_batch* batch, void* stream, int steps, int* chosen);
+/* Pins the batch's launch configuration (index as cfd_fvm_batch_autotune
+ * reports); CFD_ERR_UNSUPPORTED for a configuration the grid cannot take.
+ * Results do not depend on it. */
+int cfd_fvm_batch_set_launch(cfd_fvm_batch* batch, int choice);
 
 /* A ragged ensemble: members of any grid shapes, grouped into one batch per
  * (shape, step, convection).  cfd_fvm_ensemble_step advances every member by

@@ -89,6 +89,7 @@ _SIGNATURES = {
     'cfd_fvm_batch_create': (ctypes.c_int, [ctypes.POINTER(FvmConfig), ctypes.c_int,
                                              ctypes.POINTER(_vp)]),
     'cfd_fvm_batch_destroy': (ctypes.c_int, [_vp]),
+    'cfd_fvm_batch_set_launch': (ctypes.c_int, [_vp, ctypes.c_int]),
     'cfd_fvm_batch_size': (ctypes.c_int, [_vp]),
     'cfd_fvm_batch_bytes': (ctypes.c_longlong, [_vp]),
     'cfd_fvm_batch_state': (ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(_vp),

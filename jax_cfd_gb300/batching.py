@@ -127,11 +127,20 @@ class FvmBatch:
                                           int(chunk), 1 if graph else 0), 'cfd_fvm_batch_run')
 
   def autotune(self, steps: int = 10) -> int:
+    """Times the launch configurations and keeps the fastest; returns its
+    index (row shape + 2 * column scheme + 8 * stencil)."""
     chosen = ctypes.c_int(-1)
     nat.check(self._lib.cfd_fvm_batch_autotune(self._h, plans.current_stream_ptr(self.device),
                                                int(steps), ctypes.byref(chosen)),
               'cfd_fvm_batch_autotune')
     return int(chosen.value)
+
+  LAUNCH_CHOICES = 16
+
+  def set_launch(self, choice: int):
+    """Pins the launch configuration (see autotune); results do not change."""
+    nat.check(self._lib.cfd_fvm_batch_set_launch(self._h, int(choice)),
+              'cfd_fvm_batch_set_launch')
 
 
 class SpecBatch:

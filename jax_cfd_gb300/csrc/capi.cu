@@ -774,6 +774,10 @@ int cfd_fvm_batch_create(const cfd_fvm_config* shape, int count, cfd_fvm_batch**
   if (rc) return rc;
   if (!cfd::fvm_batch_shape_ok(p))
     return fail(CFD_ERR_UNSUPPORTED, "batched steps need nx % 16 == 0 and ny % 64 == 0");
+  // Batches launch their kernels plainly: several batches run concurrently in
+  // an ensemble graph, and programmatic launch (blocks waiting early) measured
+  // slower there (197k against 206k trajectory-steps/s, 96-member ensemble).
+  p.pdl = 0;
   cfd_fvm_batch* b = new cfd_fvm_batch();
   b->shape = p;
   b->hx = shape->hx;
@@ -926,6 +930,32 @@ int cfd_fvm_batch_run(cfd_fvm_batch* b, void* stream, int chunk, int use_graph) 
 // Times every transform launch configuration on a `steps`-step chunk of all
 // slots (with their current parameters and steps = `steps`), restores the
 // slot states afterwards and keeps the fastest configuration.  Synchronises.
+// Whether batch launch configuration c (index as in cfd_fvm_batch_autotune)
+// applies to the batch's grid; sets it in `shape` when it does.
+static bool batch_launch_choice(cfd::FvmParams* shape, int c) {
+  if (c < 0 || c >= 16) return false;
+  cfd::FvmParams q = *shape;
+  q.fft_shape = c & 1;
+  q.col_mode = (c >> 1) & 3;
+  q.stencil = c >> 3;
+  if ((q.col_mode == 1 || q.col_mode == 2) && !cfd::col_cluster_ok(q, q.col_mode == 1 ? 4 : 8))
+    return false;
+  if (q.col_mode == 3 && !cfd::col_pipe_ok(q, 0)) return false;
+  if (q.stencil == 1 && !cfd::stream_stencil_ok(q)) return false;
+  *shape = q;
+  return true;
+}
+
+int cfd_fvm_batch_set_launch(cfd_fvm_batch* b, int choice) {
+  if (!b || choice < 0 || choice >= 16)
+    return fail(CFD_ERR_INVALID_ARGUMENT, "cfd_fvm_batch_set_launch: bad arguments");
+  if (!batch_launch_choice(&b->shape, choice))
+    return fail(CFD_ERR_UNSUPPORTED, "cfd_fvm_batch_set_launch: choice not available on this grid");
+  b->dirty = true;
+  batch_drop_graph(b);
+  return CFD_OK;
+}
+
 int cfd_fvm_batch_autotune(cfd_fvm_batch* b, void* stream, int steps, int* chosen) {
   if (!b || steps < 1) return fail(CFD_ERR_INVALID_ARGUMENT, "cfd_fvm_batch_autotune: bad arguments");
   cudaStream_t s = as_stream(stream);
@@ -958,11 +988,11 @@ int cfd_fvm_batch_autotune(cfd_fvm_batch* b, void* stream, int steps, int* chose
   b->dirty = true;
   int rc = CFD_OK, best = -1;
   float best_ms = 0.f;
-  for (int cand = 0; cand < 6 && rc == CFD_OK; ++cand) {
-    b->shape.fft_shape = cand & 1;
-    b->shape.col_mode = cand >> 1;
-    if (b->shape.col_mode > 0 && !cfd::col_cluster_ok(b->shape, b->shape.col_mode == 1 ? 4 : 8))
-      continue;
+  // Candidates: index = row-transform shape + 2 * column scheme (0 blocks, 1/2
+  // clusters of 4/8, 3 persistent pipelined groups) + 8 * stencil (0 tiles,
+  // 1 warp streams).
+  for (int cand = 0; cand < 16 && rc == CFD_OK; ++cand) {
+    if (!batch_launch_choice(&b->shape, cand)) continue;
     b->dirty = true;
     rc = cfd_fvm_batch_run(b, stream, 1, 0);  // warm-up (and per-kernel smem setup)
     if (rc) break;
@@ -991,9 +1021,10 @@ int cfd_fvm_batch_autotune(cfd_fvm_batch* b, void* stream, int steps, int* chose
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   cudaFree(backup);
-  if (best < 0) best = 0;
-  b->shape.fft_shape = best & 1;
-  b->shape.col_mode = best >> 1;
+  if (best < 0 || !batch_launch_choice(&b->shape, best)) {
+    best = 0;
+    batch_launch_choice(&b->shape, 0);
+  }
   b->want = want;
   b->dirty = true;
   batch_drop_graph(b);

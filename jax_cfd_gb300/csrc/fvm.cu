@@ -519,15 +519,13 @@ CFD_D void stream_row(const FvmParams& p, int i, int j, bool out, float2& w1, fl
 
 // Rows are fetched four ahead of their use (a ring of raw rows in registers)
 // so that each warp keeps several row loads in flight.
+// bx: the block's index among the (ny / 28) x (nx / 32) / 4 blocks of a grid.
 template <bool PROJECT, int CONVECT, int FORCE>
-__global__ void __launch_bounds__(128)
-    fvm_explicit_stream_kernel(FvmParams p, const float* __restrict__ ua,
-                               const float* __restrict__ va, const float* __restrict__ q,
-                               float* __restrict__ uo, float* __restrict__ vo) {
-  pdl_wait();
-  pdl_trigger();
+CFD_D void explicit_stream_body(const FvmParams& p, int bx, const float* __restrict__ ua,
+                                const float* __restrict__ va, const float* __restrict__ q,
+                                float* __restrict__ uo, float* __restrict__ vo) {
   const int lane = threadIdx.x & 31;
-  const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int warp = (int)((bx * blockDim.x + threadIdx.x) >> 5);
   const int strips = (p.ny + kSW - 1) / kSW;
   const int s = warp % strips, t = warp / strips;
   const int r0 = t * kSH;
@@ -569,6 +567,16 @@ __global__ void __launch_bounds__(128)
     CFD_STREAM_ROW(3, 0)
   }
 #undef CFD_STREAM_ROW
+}
+
+template <bool PROJECT, int CONVECT, int FORCE>
+__global__ void __launch_bounds__(128)
+    fvm_explicit_stream_kernel(FvmParams p, const float* __restrict__ ua,
+                               const float* __restrict__ va, const float* __restrict__ q,
+                               float* __restrict__ uo, float* __restrict__ vo) {
+  pdl_wait();
+  pdl_trigger();
+  explicit_stream_body<PROJECT, CONVECT, FORCE>(p, blockIdx.x, ua, va, q, uo, vo);
 }
 
 bool stream_ok(const FvmParams& p) { return p.ny >= 64 && p.nx % kSH == 0; }
@@ -1002,6 +1010,61 @@ __global__ void __launch_bounds__(CG * (1 << LOG2N) / 16,
   col_pinv_pipe_cols<LOG2N, CG>(p, spec, blockIdx.x, gridDim.x);
 }
 
+// The persistent column pass over a same-shape batch: the work items are the
+// (member, group) pairs of the members that take this step, walked with the
+// grid as stride, so many members keep every block's staging pipeline full.
+// The grid tables are the batch's (member 0's pointers); the pinv scalars are
+// each member's, equal across a batch.
+template <int LOG2N, int CG>
+__global__ void __launch_bounds__(CG * (1 << LOG2N) / 16,
+                                  col_pipe_min_blocks(CG * (1 << LOG2N) / 16))
+    fvm_batch_col_pinv_pipe_kernel(const FvmMember* __restrict__ mem, int count, int k) {
+  using P = ColPipe<LOG2N>;
+  extern __shared__ float2 sbuf[];
+  const int L = mem[0].p.ny >> 1;
+  const int groups = L / CG + 1, items = count * groups;
+  const int w = threadIdx.x % CG, t = threadIdx.x / CG;
+  const int bstride = col_pipe_bstride<LOG2N, CG>();
+  float2* const buf[2] = {sbuf + w * bstride, sbuf + (CG + w) * bstride};
+  float2* const stage = sbuf + 2 * CG * bstride;
+  constexpr int INV_FIRST = (P::PASSES - 1) & 1;
+  const float2* tw;
+  const float* lamx;
+  col_pipe_tables<LOG2N, CG>(sbuf, mem[0].p.twp_x, mem[0].p.lamx, &tw, &lamx);
+  pdl_wait();
+  pdl_trigger();
+  // Next item at or after `it` (stride gridDim.x) whose member takes step k;
+  // the same for every thread of the block.
+  auto next_active = [&](int it) {
+    while (it < items && k >= mem[it / groups].steps) it += gridDim.x;
+    return it;
+  };
+  int it = next_active(blockIdx.x);
+  if (it >= items) return;  // uniform per block
+  col_pipe_prefetch<LOG2N, CG>(mem[it / groups].spec, L, it % groups, w, t, stage);
+  cp_async_commit();
+  float2 v[16];
+#pragma unroll 1
+  while (it < items) {
+    const FvmMember& m = mem[it / groups];
+    const int g = it % groups;
+    cp_async_wait_all();
+    col_pipe_take<LOG2N, CG>(stage, L, g, w, t, v);
+    const int nit = next_active(it + gridDim.x);
+    if (nit < items) col_pipe_prefetch<LOG2N, CG>(mem[nit / groups].spec, L, nit % groups, w, t, stage);
+    cp_async_commit();
+    col_pipe_fft<LOG2N, -1, 0>(v, buf, t, tw);
+    const int cp = g * CG >= L ? L : g * CG + w;  // pinv column index
+#pragma unroll
+    for (int mm = 0; mm < 16; ++mm)
+      v[mm] = c_scale(v[mm], pinv_diag_at(m.p, lamx[t + P::NTHR * mm], cp));
+    col_pipe_fft<LOG2N, 1, INV_FIRST>(v, buf, t, tw);
+    col_pipe_store<LOG2N, CG>(m.spec, L, g, w, t, v);
+    it = nit;
+  }
+  cp_async_wait_all();
+}
+
 // Inverse packed real FFT of each row, in place: q^ rows -> q rows (floats).
 CFD_D void irfft_rows(const FvmParams& p, int blk, int rows, float2* spec) {
   extern __shared__ float2 sbuf[];
@@ -1294,6 +1357,8 @@ CFD_D int batch_dst(int k) { return (k & 1) ? 2 : 1; }
 template <bool PROJECT, int CONVECT>
 __global__ void __launch_bounds__(kStencilThreads)
     fvm_batch_explicit_kernel(const FvmMember* __restrict__ mem, int k) {
+  pdl_wait();
+  pdl_trigger();
   const FvmMember& m = mem[blockIdx.z];
   if (k >= m.steps) return;
   const FvmParams p = m.p;
@@ -1303,9 +1368,28 @@ __global__ void __launch_bounds__(kStencilThreads)
                                          m.f[dst][0], m.f[dst][1]);
 }
 
+// The warp-streaming stencil over a batch (member on grid axis y); the
+// forcing flags are read at run time (members may differ in them), which
+// evaluates the same expressions as the tiles.
+template <bool PROJECT, int CONVECT>
+__global__ void __launch_bounds__(128)
+    fvm_batch_explicit_stream_kernel(const FvmMember* __restrict__ mem, int k) {
+  pdl_wait();
+  pdl_trigger();
+  const FvmMember& m = mem[blockIdx.y];
+  if (k >= m.steps) return;
+  const FvmParams p = m.p;
+  const int src = batch_src(k), dst = batch_dst(k);
+  explicit_stream_body<PROJECT, CONVECT, 0>(p, blockIdx.x, m.f[src][0], m.f[src][1],
+                                            reinterpret_cast<const float*>(m.spec),
+                                            m.f[dst][0], m.f[dst][1]);
+}
+
 template <int MAXT, int MINB>
 __global__ void __launch_bounds__(MAXT, MINB)
     fvm_batch_div_rfft_kernel(const FvmMember* __restrict__ mem, int k, int rows) {
+  pdl_wait();
+  pdl_trigger();
   const FvmMember& m = mem[blockIdx.y];
   if (k >= m.steps) return;
   const FvmParams p = m.p;
@@ -1317,6 +1401,8 @@ template <int MAXT, int MINB>
 __global__ void __launch_bounds__(MAXT, MINB)
     fvm_batch_col_pinv_kernel(const FvmMember* __restrict__ mem, int k, int W, int log2W,
                               int bstride) {
+  pdl_wait();
+  pdl_trigger();
   const FvmMember& m = mem[blockIdx.y];
   if (k >= m.steps) return;
   const FvmParams p = m.p;
@@ -1328,6 +1414,8 @@ __global__ void __launch_bounds__(MAXT, MINB)
 template <int CL>
 __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(128, 7)
     fvm_batch_col_pinv_cluster_kernel(const FvmMember* __restrict__ mem, int k) {
+  pdl_wait();
+  pdl_trigger();
   const FvmMember& m = mem[blockIdx.y];
   if (k >= m.steps) return;
   const FvmParams p = m.p;
@@ -1337,6 +1425,8 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(128, 7)
 template <int MAXT, int MINB>
 __global__ void __launch_bounds__(MAXT, MINB)
     fvm_batch_irfft_kernel(const FvmMember* __restrict__ mem, int k, int rows) {
+  pdl_wait();
+  pdl_trigger();
   const FvmMember& m = mem[blockIdx.y];
   if (k >= m.steps) return;
   const FvmParams p = m.p;
@@ -1345,6 +1435,8 @@ __global__ void __launch_bounds__(MAXT, MINB)
 
 __global__ void __launch_bounds__(32 * kWarpRows)
     fvm_batch_div_rfft_warp_kernel(const FvmMember* __restrict__ mem, int k) {
+  pdl_wait();
+  pdl_trigger();
   __shared__ float2 tiles[kWarpRows][kWarpFftTile];
   const FvmMember& m = mem[blockIdx.y];
   if (k >= m.steps) return;
@@ -1355,6 +1447,8 @@ __global__ void __launch_bounds__(32 * kWarpRows)
 
 __global__ void __launch_bounds__(32 * kWarpRows)
     fvm_batch_irfft_warp_kernel(const FvmMember* __restrict__ mem, int k) {
+  pdl_wait();
+  pdl_trigger();
   __shared__ float2 tiles[kWarpRows][kWarpFftTile];
   const FvmMember& m = mem[blockIdx.y];
   if (k >= m.steps) return;
@@ -1364,6 +1458,8 @@ __global__ void __launch_bounds__(32 * kWarpRows)
 }
 
 __global__ void fvm_batch_project_out_kernel(const FvmMember* __restrict__ mem) {
+  pdl_wait();
+  pdl_trigger();
   const FvmMember& m = mem[blockIdx.y];
   if (m.steps <= 0) return;
   const FvmParams p = m.p;
@@ -1701,8 +1797,11 @@ static cudaError_t batch_rows_impl(const FvmParams& p, int target, const FvmMemb
   const int log2L = p.log2ny - 1;
   if (warp_rows_ok(p)) {
     const dim3 wgrid(p.nx / kWarpRows, count);
-    if (inverse) fvm_batch_irfft_warp_kernel<<<wgrid, 32 * kWarpRows, 0, s>>>(mem, k);
-    else fvm_batch_div_rfft_warp_kernel<<<wgrid, 32 * kWarpRows, 0, s>>>(mem, k);
+    if (inverse)
+      launch_maybe_pdl(p.pdl, fvm_batch_irfft_warp_kernel, wgrid, dim3(32 * kWarpRows), 0, s, mem, k);
+    else
+      launch_maybe_pdl(p.pdl, fvm_batch_div_rfft_warp_kernel, wgrid, dim3(32 * kWarpRows), 0, s, mem,
+                       k);
     return cudaGetLastError();
   }
   const int rows = fft_rows_per_block(log2L, p.nx, target);
@@ -1712,10 +1811,12 @@ static cudaError_t batch_rows_impl(const FvmParams& p, int target, const FvmMemb
   cudaError_t e;
   if (inverse) {
     if ((e = set_smem(fvm_batch_irfft_kernel<MAXT, MINB>, smem)) != cudaSuccess) return e;
-    fvm_batch_irfft_kernel<MAXT, MINB><<<grid, threads, smem, s>>>(mem, k, rows);
+    launch_maybe_pdl(p.pdl, fvm_batch_irfft_kernel<MAXT, MINB>, grid, dim3(threads), smem, s, mem, k,
+                     rows);
   } else {
     if ((e = set_smem(fvm_batch_div_rfft_kernel<MAXT, MINB>, smem)) != cudaSuccess) return e;
-    fvm_batch_div_rfft_kernel<MAXT, MINB><<<grid, threads, smem, s>>>(mem, k, rows);
+    launch_maybe_pdl(p.pdl, fvm_batch_div_rfft_kernel<MAXT, MINB>, grid, dim3(threads), smem, s, mem,
+                     k, rows);
   }
   return cudaGetLastError();
 }
@@ -1731,9 +1832,9 @@ static cudaError_t batch_col_impl(const FvmParams& p, int target, const FvmMembe
   const size_t smem = (size_t)W * bstride * sizeof(float2);
   cudaError_t e = set_smem(fvm_batch_col_pinv_kernel<MAXT, MINB>, smem);
   if (e != cudaSuccess) return e;
-  fvm_batch_col_pinv_kernel<MAXT, MINB><<<dim3(L / W + 1, count),
-                                          block_threads(fft_workers(p.log2nx, W)), smem, s>>>(
-      mem, k, W, ilog2(W), bstride);
+  launch_maybe_pdl(p.pdl, fvm_batch_col_pinv_kernel<MAXT, MINB>, dim3(L / W + 1, count),
+                   dim3(block_threads(fft_workers(p.log2nx, W))), smem, s, mem, k, W, ilog2(W),
+                   bstride);
   return cudaGetLastError();
 }
 
@@ -1743,30 +1844,79 @@ static cudaError_t batch_col_cluster_impl(const FvmParams& p, const FvmMember* m
   const size_t smem = (size_t)padded_len(p.nx) * sizeof(float2);
   cudaError_t e = set_smem(fvm_batch_col_pinv_cluster_kernel<CL>, smem);
   if (e != cudaSuccess) return e;
-  fvm_batch_col_pinv_cluster_kernel<CL><<<dim3(p.ny / 2 + CL, count),
-                                          block_threads(fft_workers(p.log2nx, 1)), smem, s>>>(
-      mem, k);
+  launch_maybe_pdl(p.pdl, fvm_batch_col_pinv_cluster_kernel<CL>, dim3(p.ny / 2 + CL, count),
+                   dim3(block_threads(fft_workers(p.log2nx, 1))), smem, s, mem, k);
   return cudaGetLastError();
+}
+
+template <int LOG2N, int CG>
+static cudaError_t batch_col_pipe_impl(const FvmParams& p, const FvmMember* mem, int count,
+                                       int k, cudaStream_t s) {
+  const size_t smem = col_pipe_smem<LOG2N, CG>();
+  const int threads = CG * (1 << LOG2N) / 16;
+  auto kern = fvm_batch_col_pinv_pipe_kernel<LOG2N, CG>;
+  cudaError_t e = set_smem(kern, smem);
+  if (e != cudaSuccess) return e;
+  static int per_sm = 0;
+  if (per_sm == 0) {
+    int nb = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, threads, smem);
+    if (e != cudaSuccess) return e;
+    per_sm = nb > 0 ? nb : 1;
+  }
+  const long long items = (long long)count * (p.ny / 2 / CG + 1);
+  const long long slots = (long long)col_pipe_device_sms() * per_sm;
+  return launch_maybe_pdl(p.pdl, kern, dim3((int)(items < slots ? items : slots)), dim3(threads),
+                          smem, s, mem, count, k);
+}
+
+static cudaError_t batch_col_pipe_launch(const FvmParams& p, const FvmMember* mem, int count,
+                                         int k, cudaStream_t s) {
+  switch (p.log2nx) {
+    case 8: return batch_col_pipe_impl<8, 4>(p, mem, count, k, s);
+    case 9: return batch_col_pipe_impl<9, 4>(p, mem, count, k, s);
+    case 10: return batch_col_pipe_impl<10, 4>(p, mem, count, k, s);
+    case 11: return batch_col_pipe_impl<11, 4>(p, mem, count, k, s);
+    default: return batch_col_pipe_impl<12, 2>(p, mem, count, k, s);
+  }
 }
 
 cudaError_t launch_fvm_batch_step(const FvmParams& p, const FvmMember* mem, int count, int k,
                                   cudaStream_t s) {
   if (!fvm_batch_shape_ok(p) || count < 1 || count > 65535) return cudaErrorInvalidValue;
-  const dim3 grid(p.ny / kTJ, p.nx / kTI, count);
-  if (p.convect == 0) {
-    if (k > 0) fvm_batch_explicit_kernel<true, 0><<<grid, kStencilThreads, 0, s>>>(mem, k);
-    else fvm_batch_explicit_kernel<false, 0><<<grid, kStencilThreads, 0, s>>>(mem, k);
+  if (p.stencil == 1 && stream_ok(p)) {
+    const long long warps = (long long)((p.ny + kSW - 1) / kSW) * ((p.nx + kSH - 1) / kSH);
+    const dim3 sg((unsigned)((warps + 3) / 4), count);
+    if (p.convect == 0) {
+      if (k > 0) launch_maybe_pdl(p.pdl, fvm_batch_explicit_stream_kernel<true, 0>, sg, dim3(128), 0, s, mem, k);
+      else launch_maybe_pdl(p.pdl, fvm_batch_explicit_stream_kernel<false, 0>, sg, dim3(128), 0, s, mem, k);
+    } else {
+      if (k > 0) launch_maybe_pdl(p.pdl, fvm_batch_explicit_stream_kernel<true, 1>, sg, dim3(128), 0, s, mem, k);
+      else launch_maybe_pdl(p.pdl, fvm_batch_explicit_stream_kernel<false, 1>, sg, dim3(128), 0, s, mem, k);
+    }
   } else {
-    if (k > 0) fvm_batch_explicit_kernel<true, 1><<<grid, kStencilThreads, 0, s>>>(mem, k);
-    else fvm_batch_explicit_kernel<false, 1><<<grid, kStencilThreads, 0, s>>>(mem, k);
+    const dim3 grid(p.ny / kTJ, p.nx / kTI, count);
+    if (p.convect == 0) {
+      if (k > 0) launch_maybe_pdl(p.pdl, fvm_batch_explicit_kernel<true, 0>, grid, dim3(kStencilThreads), 0, s,
+                         mem, k);
+      else launch_maybe_pdl(p.pdl, fvm_batch_explicit_kernel<false, 0>, grid, dim3(kStencilThreads), 0, s,
+                         mem, k);
+    } else {
+      if (k > 0) launch_maybe_pdl(p.pdl, fvm_batch_explicit_kernel<true, 1>, grid, dim3(kStencilThreads), 0, s,
+                         mem, k);
+      else launch_maybe_pdl(p.pdl, fvm_batch_explicit_kernel<false, 1>, grid, dim3(kStencilThreads), 0, s,
+                         mem, k);
+    }
   }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   e = p.fft_shape == 1 ? batch_rows_impl<64, 14>(p, 64, mem, count, k, false, s)
                        : batch_rows_impl<256, 3>(p, 256, mem, count, k, false, s);
   if (e != cudaSuccess) return e;
-  if (p.col_mode == 2 && col_cluster_ok(p, 8)) e = batch_col_cluster_impl<8>(p, mem, count, k, s);
-  else if (p.col_mode >= 1 && col_cluster_ok(p, 4)) e = batch_col_cluster_impl<4>(p, mem, count, k, s);
+  if (p.col_mode == 3 && col_pipe_ok(p, 0)) e = batch_col_pipe_launch(p, mem, count, k, s);
+  else if (p.col_mode == 2 && col_cluster_ok(p, 8)) e = batch_col_cluster_impl<8>(p, mem, count, k, s);
+  else if ((p.col_mode == 1 || p.col_mode == 2) && col_cluster_ok(p, 4))
+    e = batch_col_cluster_impl<4>(p, mem, count, k, s);
   else e = p.fft_shape == 1 ? batch_col_impl<128, 7>(p, 128, mem, count, k, s)
                             : batch_col_impl<256, 3>(p, 256, mem, count, k, s);
   if (e != cudaSuccess) return e;
@@ -1782,8 +1932,8 @@ cudaError_t launch_fvm_batch_project_out(const FvmParams& p, const FvmMember* me
   const int cap = (152 * 16 + count - 1) / count;
   if (per > cap) per = cap;
   if (per < 1) per = 1;
-  fvm_batch_project_out_kernel<<<dim3(per, count), 256, 0, s>>>(mem);
-  return cudaGetLastError();
+  return launch_maybe_pdl(p.pdl, fvm_batch_project_out_kernel, dim3(per, count), dim3(256), 0, s,
+                          mem);
 }
 
 }  // namespace cfd

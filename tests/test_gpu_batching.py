@@ -79,6 +79,34 @@ def test_batch_slots_equal_single_trajectories(cuda_device, graph, shape):
       assert torch.equal(got, w)
 
 
+@pytest.mark.parametrize('shape', [(256, 256), (1024, 128)])
+def test_every_batch_launch_configuration_gives_the_same_bits(cuda_device, shape):
+  """Tiles vs warp-streaming stencil, wide vs narrow row blocks, per-block,
+  cluster and persistent pipelined column passes over a batch with an idle
+  slot: identical results, equal to the single trajectories."""
+  draws = [(shape, 21, 1e-3, 4, 2.0), (shape, 22, 1e-4, 2, 1.0), (shape, 23, 1e-3, 8, 3.0)]
+  pairs = [_member(*d) for d in draws]
+  b = _batch([m for m, _ in pairs], cuda_device)
+  results = {}
+  for choice in range(b.LAUNCH_CHOICES):
+    try:
+      b.set_launch(choice)
+    except NotImplementedError:
+      continue
+    for i, (_, v0) in enumerate(pairs):
+      _load(b, i, v0, cuda_device)
+      b.set_steps(i, [5, 0, 3][i])
+    b.run(5, graph=choice % 2 == 0)
+    torch.cuda.synchronize(cuda_device)
+    results[choice] = [tuple(t.clone() for t in b.state(i)) for i in range(len(pairs))]
+  assert 0 in results and 6 in results and 14 in results
+  for i, (m, v0) in enumerate(pairs):
+    want = _single(m, v0, [5, 0, 3][i], cuda_device)
+    for choice, states in results.items():
+      for got, w in zip(states[i], want):
+        assert torch.equal(got, w), (choice, i)
+
+
 def test_ragged_steps_and_idle_slots(cuda_device):
   draws = [((128, 64), 21, 1e-3, 4, 2.0), ((128, 64), 22, 3e-3, 2, 3.0),
            ((128, 64), 23, 1e-3, 8, 1.5)]
