@@ -608,7 +608,8 @@ def run_gb300(args):
                           'frac': SPEC_STEP_BYTES_PER_CELL * s_value / 1e9 / peak},
         'kernel_ms': sk,
         'column_pass': ['blocks', 'cluster4', 'pipelined4', 'pipelined2',
-                                        'pipelined4_fused'][s_launch],
+                        'pipelined4_fused'][s_launch % 5],
+        'row_pass': ['shared_memory', 'register_passes'][s_launch // 5],
         'roofline': {'kernel': s_dom, 'bound': 'hbm', 'achieved': s_ach, 'peak': peak,
                      'unit': 'GB/s', 'frac': s_ach / peak},
         'finite': bool(torch.isfinite(torch.view_as_real(w)).all()),

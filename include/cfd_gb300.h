@@ -277,8 +277,9 @@ long long cfd_spec_plan_bytes(const cfd_spec_plan* plan);
  * (256 <= nx <= 2048), 2/3 persistent blocks that stage the next group of
  * 4/2 columns with cp.async while transforming the current one in registers
  * (512 <= nx <= 4096), 4 as 2 with each stage's column update and the next
- * stage's column prep fused into one pass.  Results are bit-for-bit the
- * same. */
+ * stage's column prep fused into one pass; plus 5 x the row scheme: 0 the
+ * shared-memory row pass, 1 the register-pass row pass (512 <= ny <= 4096).
+ * Results are bit-for-bit the same for every choice. */
 int cfd_spec_plan_set_launch(cfd_spec_plan* plan, int choice);
 int cfd_spec_plan_get_launch(const cfd_spec_plan* plan);
 /* Velocity-independent forcing (fx, fy real [nx, ny] on the device, either may

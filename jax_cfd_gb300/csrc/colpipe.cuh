@@ -93,36 +93,42 @@ CFD_D void col_pipe_tables(float2* sbuf, const float2* __restrict__ twp,
 // buf[1]: this column's two exchange buffers; the k-th exchange of the
 // transform writes buf[(FIRST + k) & 1].  Called by every thread of the block
 // (it contains barriers).
-template <int LOG2N, int SIGN, int FIRST>
+// LDG: twp is the global table (else a shared copy).  A thread with
+// active == false computes nothing but takes part in every barrier.
+template <int LOG2N, int SIGN, int FIRST, bool LDG = !col_pipe_smem_tables<LOG2N>()>
 CFD_D void col_pipe_fft(float2 (&v)[16], float2* const (&buf)[2], int t,
-                        const float2* __restrict__ twp) {
-  constexpr bool LDG = !col_pipe_smem_tables<LOG2N>();  // twp: global or a shared copy
+                        const float2* __restrict__ twp, bool active = true) {
   using P = ColPipe<LOG2N>;
   int wsel = FIRST;
   int tw_off = 0;
 #pragma unroll
   for (int q = 0; q < P::N16; ++q) {
     const int Ns = 1 << (4 * q);
-    if (q > 0) {
-      const float2* in = buf[wsel ^ 1];
-#pragma unroll
-      for (int r = 0; r < 16; ++r) v[r] = in[pidx(t + P::NTHR * r)];
-    }
     const int k = t & (Ns - 1);
-    if (Ns > 1) apply_twiddles<16, SIGN, LDG>(v, twp + tw_off, Ns, k);
-    Dft<16, SIGN>::run(v);
+    if (active) {
+      if (q > 0) {
+        const float2* in = buf[wsel ^ 1];
+#pragma unroll
+        for (int r = 0; r < 16; ++r) v[r] = in[pidx(t + P::NTHR * r)];
+      }
+      if (Ns > 1) apply_twiddles<16, SIGN, LDG>(v, twp + tw_off, Ns, k);
+      Dft<16, SIGN>::run(v);
+    }
     if (q > 0) tw_off += 15 << (4 * q);
     const bool last = q == P::N16 - 1 && P::REM == 0;
     if (!last) {
-      float2* out = buf[wsel];
-      const int o = ((t - k) << 4) + k;
+      if (active) {
+        float2* out = buf[wsel];
+        const int o = ((t - k) << 4) + k;
 #pragma unroll
-      for (int r = 0; r < 16; ++r) out[pidx(o + r * Ns)] = v[r];
+        for (int r = 0; r < 16; ++r) out[pidx(o + r * Ns)] = v[r];
+      }
       wsel ^= 1;
       __syncthreads();
     }
   }
   if constexpr (P::REM > 0) {
+    if (!active) return;
     constexpr int R = 1 << P::REM, NB = 16 / R;
     constexpr int Ns = P::N / R;  // = N / R: the final span
     const float2* in = buf[wsel ^ 1];

@@ -148,12 +148,15 @@ struct SpecParams {
   const float* kx;      // fftfreq(nx, hx) in float32 (nx)
   const float* ky;      // rfftfreq(ny, hy) in float32 (L + 1)
   int pdl;              // launch the stage kernels as programmatic dependents
+  int row_mode;         // row pass: 0 shared-memory engine, 1 register passes
 };
 
 // Whether the clustered spectral column passes (col_mode 1) apply to this grid.
 bool spec_cluster_ok(const SpecParams& p);
 // Whether the persistent spectral column passes (col_mode 2/3) apply to this grid.
 bool spec_pipe_ok(const SpecParams& p);
+// Whether the register-pass row pass (row_mode 1) applies to this grid.
+bool spec_row_pipe_ok(const SpecParams& p);
 
 struct StageCoef {
   float beta;     // float32(beta_k), multiplies the previous h

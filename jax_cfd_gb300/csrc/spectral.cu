@@ -607,6 +607,113 @@ __global__ void __launch_bounds__(CG * (1 << LOG2N) / 16,
   cp_async_wait_all();
 }
 
+// ---- Row pass with register-resident Stockham passes ----
+// One row per block.  Thread (f, t) -- field f = threadIdx.x / (L/16), worker
+// t -- builds the 16 inputs of field f's inverse real transform that the first
+// Stockham pass gives worker t straight from global memory, with the
+// pre-untangling of row_advect_rows (for k > L/2 as the second output of the
+// pair (L - k, k), so each element rounds as there), and runs the passes of
+// colpipe.cuh.  The four fields' samples meet in shared memory for the
+// advection product, which the field-0 threads form at exactly the forward
+// transform's first-pass positions; the post-untangling partners again come
+// from shared memory.  Same butterflies, twiddles and element formulas as
+// row_advect_rows, so the same bits, with one barrier per exchange and no
+// shared-memory round trip around the transforms' global loads and stores.
+template <int LOG2L>
+__global__ void __launch_bounds__(4 * (1 << LOG2L) / 16, 512 / (4 * (1 << LOG2L) / 16))
+    spec_row_pipe_kernel(SpecParams p, const float2* __restrict__ t0,
+                         const float2* __restrict__ t1, const float2* __restrict__ t2,
+                         const float2* __restrict__ t3, float2* __restrict__ ahat) {
+  using P = ColPipe<LOG2L>;
+  constexpr int NTHR = P::NTHR, L = P::N, half = L / 2;
+  extern __shared__ float2 sbuf[];
+  pdl_wait();
+  pdl_trigger();
+  const int f = threadIdx.x / NTHR, t = threadIdx.x % NTHR;
+  const int ncols = L + 1;
+  const int bstride = padded_len(L);
+  float2* const buf[2] = {sbuf + f * bstride, sbuf + (4 + f) * bstride};
+  const float2* in = (f == 0 ? t0 : f == 1 ? t1 : f == 2 ? t2 : t3) + (size_t)blockIdx.x * ncols;
+  float2 v[16];
+#pragma unroll
+  for (int r = 0; r < 16; ++r) {
+    const int k = t + NTHR * r;
+    float2 zk, zm;
+    if (k == 0) {
+      const float2 x0 = row_factor(p, f, 0, in[0]);
+      const float2 xl = row_factor(p, f, L, in[L]);
+      v[r] = make_float2(x0.x + xl.x, x0.x - xl.x);
+    } else if (k == half) {
+      const float2 xh = row_factor(p, f, half, in[half]);
+      irfft_pre_pair(xh, xh, __ldg(p.tw_y + half), &zk, &zm);
+      v[r] = zk;
+    } else if (k < half) {
+      const float2 xk = row_factor(p, f, k, in[k]);
+      const float2 xm = row_factor(p, f, L - k, in[L - k]);
+      irfft_pre_pair(xk, xm, __ldg(p.tw_y + k), &zk, &zm);
+      v[r] = zk;
+    } else {
+      const int kp = L - k;
+      const float2 xk = row_factor(p, f, kp, in[kp]);
+      const float2 xm = row_factor(p, f, k, in[k]);
+      irfft_pre_pair(xk, xm, __ldg(p.tw_y + kp), &zk, &zm);
+      v[r] = zm;
+    }
+  }
+  col_pipe_fft<LOG2L, 1, 0, true>(v, buf, t, p.twp_y);
+  // Samples n = t + NTHR m of every field into its first buffer (free: its
+  // last reader was the transform's second pass).
+#pragma unroll
+  for (int m = 0; m < 16; ++m) buf[0][pidx(t + NTHR * m)] = v[m];
+  __syncthreads();
+  const bool lead = f == 0;
+  if (lead) {
+    // advection = -(gx * vx + gy * vy), each field scaled by 1/(nx*ny).
+    const float s2 = p.scale * p.scale;
+    const float2* vyb = sbuf + 1 * bstride;
+    const float2* gxb = sbuf + 2 * bstride;
+    const float2* gyb = sbuf + 3 * bstride;
+#pragma unroll
+    for (int m = 0; m < 16; ++m) {
+      const int n = pidx(t + NTHR * m);
+      const float2 vx = v[m], vy = vyb[n], gx = gxb[n], gy = gyb[n];
+      v[m] = make_float2(-(gx.x * vx.x + gy.x * vy.x) * s2, -(gx.y * vx.y + gy.y * vy.y) * s2);
+    }
+  }
+  // Forward transform of the advection (field-0 threads); it starts on the
+  // second buffers, which nobody reads any more, while the first buffers of
+  // fields 1-3 may still be read above.
+  col_pipe_fft<LOG2L, -1, 1, true>(v, buf, t, p.twp_y, lead);
+  // Z[k] into field 0's second buffer (its last reader was the forward
+  // transform's first read), then each output from the pair (k, L - k).
+  if (lead) {
+#pragma unroll
+    for (int m = 0; m < 16; ++m) buf[1][pidx(t + NTHR * m)] = v[m];
+  }
+  __syncthreads();
+  if (!lead) return;
+  float2* out = ahat + (size_t)blockIdx.x * ncols;
+#pragma unroll
+  for (int m = 0; m < 16; ++m) {
+    const int k = t + NTHR * m;
+    const float2 z = v[m];
+    float2 xk, xm;
+    if (k == 0) {
+      out[0] = make_float2(z.x + z.y, 0.f);
+      out[L] = make_float2(z.x - z.y, 0.f);
+    } else if (k == half) {
+      rfft_post_pair(z, z, __ldg(p.tw_y + half), &xk, &xm);
+      out[half] = xk;
+    } else if (k < half) {
+      rfft_post_pair(z, buf[1][pidx(L - k)], __ldg(p.tw_y + k), &xk, &xm);
+      out[k] = xk;
+    } else {
+      rfft_post_pair(buf[1][pidx(L - k)], z, __ldg(p.tw_y + L - k), &xk, &xm);
+      out[k] = xm;
+    }
+  }
+}
+
 // ---- Batched variants: the slot index is the last grid axis ----
 // Column prep after stage `stage` of step k builds the inputs of the next
 // stage (k = -1: before the first step of the chunk).
@@ -956,8 +1063,29 @@ cudaError_t launch_spec_col_update(const SpecParams& p, const StageCoef& sc,
   return launch_spec_col_prep(p, w, t4, s);
 }
 
+template <int LOG2L>
+static cudaError_t spec_row_pipe_impl(const SpecParams& p, const float2* const t4[4],
+                                      float2* ahat, cudaStream_t s) {
+  const size_t smem = (size_t)8 * padded_len(1 << LOG2L) * sizeof(float2);
+  auto kern = spec_row_pipe_kernel<LOG2L>;
+  cudaError_t e = set_smem(kern, smem);
+  if (e != cudaSuccess) return e;
+  return launch_maybe_pdl(p.pdl, kern, dim3(p.nx), dim3(4 * (1 << LOG2L) / 16), smem, s, p,
+                          t4[0], t4[1], t4[2], t4[3], ahat);
+}
+
+bool spec_row_pipe_ok(const SpecParams& p) { return p.log2L >= 8 && p.log2L <= 11; }
+
 cudaError_t launch_spec_row(const SpecParams& p, const float2* const t4[4],
                             float2* ahat, cudaStream_t s) {
+  if (p.row_mode == 1 && spec_row_pipe_ok(p)) {
+    switch (p.log2L) {
+      case 8: return spec_row_pipe_impl<8>(p, t4, ahat, s);
+      case 9: return spec_row_pipe_impl<9>(p, t4, ahat, s);
+      case 10: return spec_row_pipe_impl<10>(p, t4, ahat, s);
+      default: return spec_row_pipe_impl<11>(p, t4, ahat, s);
+    }
+  }
   const int rows = rows_per_block(p.log2L, 4, p.nx);
   const size_t smem = (size_t)rows * 4 * padded_len(p.L) * sizeof(float2);
   cudaError_t e = set_smem(spec_row_kernel, smem);

@@ -339,13 +339,15 @@ class SpecPlan:
   def nbytes(self) -> int:
     return int(self._lib.cfd_spec_plan_bytes(self._h))
 
-  LAUNCH_CHOICES = 5
+  LAUNCH_CHOICES = 10
 
   def set_launch(self, choice: int):
-    """Column passes: 0 per-block columns, 1 clusters of four one-column
-    blocks (256 <= nx <= 2048), 2/3 persistent register-pipelined groups of
-    4/2 columns (512 <= nx <= 4096), 4 as 2 with each stage's update and the
-    next stage's prep fused.  Results do not change."""
+    """choice = column scheme + 5 * row scheme.  Column passes: 0 per-block
+    columns, 1 clusters of four one-column blocks (256 <= nx <= 2048), 2/3
+    persistent register-pipelined groups of 4/2 columns (512 <= nx <= 4096),
+    4 as 2 with each stage's update and the next stage's prep fused.  Row
+    pass: 0 shared-memory engine, 1 register passes (512 <= ny <= 4096).
+    Results do not change."""
     nat.check(self._lib.cfd_spec_plan_set_launch(self._h, int(choice)), 'cfd_spec_plan_set_launch')
 
   @property

@@ -125,8 +125,8 @@ def test_taylor_green_spectral_analytic(cuda_device):
 @pytest.mark.parametrize('shape', [(256, 256), (512, 256), (2048, 2048)])
 @pytest.mark.parametrize('forcing', ['smooth', 'kolmogorov'])
 def test_cluster_column_passes_are_bitwise(cuda_device, shape, forcing):
-  """Clustered (launch 1) and persistent pipelined (launch 2) column passes
-  give exactly the per-block bits."""
+  """Every column scheme (per-block, clusters, persistent pipelined, fused
+  update + prep) and both row passes give exactly the per-block bits."""
   import jax_cfd_gb300.base as cfd
   from jax_cfd_gb300.spectral import equations as seq
   from jax_cfd_gb300.spectral import time_stepping as sts
