@@ -620,20 +620,17 @@ __global__ void __launch_bounds__(CG * (1 << LOG2N) / 16,
 // row_advect_rows, so the same bits, with one barrier per exchange and no
 // shared-memory round trip around the transforms' global loads and stores.
 template <int LOG2L>
-__global__ void __launch_bounds__(4 * (1 << LOG2L) / 16, 512 / (4 * (1 << LOG2L) / 16))
-    spec_row_pipe_kernel(SpecParams p, const float2* __restrict__ t0,
-                         const float2* __restrict__ t1, const float2* __restrict__ t2,
-                         const float2* __restrict__ t3, float2* __restrict__ ahat) {
+CFD_D void spec_row_pipe_body(const SpecParams& p, int row, const float2* __restrict__ t0,
+                              const float2* __restrict__ t1, const float2* __restrict__ t2,
+                              const float2* __restrict__ t3, float2* __restrict__ ahat) {
   using P = ColPipe<LOG2L>;
   constexpr int NTHR = P::NTHR, L = P::N, half = L / 2;
   extern __shared__ float2 sbuf[];
-  pdl_wait();
-  pdl_trigger();
   const int f = threadIdx.x / NTHR, t = threadIdx.x % NTHR;
   const int ncols = L + 1;
   const int bstride = padded_len(L);
   float2* const buf[2] = {sbuf + f * bstride, sbuf + (4 + f) * bstride};
-  const float2* in = (f == 0 ? t0 : f == 1 ? t1 : f == 2 ? t2 : t3) + (size_t)blockIdx.x * ncols;
+  const float2* in = (f == 0 ? t0 : f == 1 ? t1 : f == 2 ? t2 : t3) + (size_t)row * ncols;
   float2 v[16];
 #pragma unroll
   for (int r = 0; r < 16; ++r) {
@@ -692,7 +689,7 @@ __global__ void __launch_bounds__(4 * (1 << LOG2L) / 16, 512 / (4 * (1 << LOG2L)
   }
   __syncthreads();
   if (!lead) return;
-  float2* out = ahat + (size_t)blockIdx.x * ncols;
+  float2* out = ahat + (size_t)row * ncols;
 #pragma unroll
   for (int m = 0; m < 16; ++m) {
     const int k = t + NTHR * m;
@@ -712,6 +709,162 @@ __global__ void __launch_bounds__(4 * (1 << LOG2L) / 16, 512 / (4 * (1 << LOG2L)
       out[k] = xm;
     }
   }
+}
+
+template <int LOG2L>
+__global__ void __launch_bounds__(4 * (1 << LOG2L) / 16, 512 / (4 * (1 << LOG2L) / 16))
+    spec_row_pipe_kernel(SpecParams p, const float2* __restrict__ t0,
+                         const float2* __restrict__ t1, const float2* __restrict__ t2,
+                         const float2* __restrict__ t3, float2* __restrict__ ahat) {
+  pdl_wait();
+  pdl_trigger();
+  spec_row_pipe_body<LOG2L>(p, blockIdx.x, t0, t1, t2, t3, ahat);
+}
+
+// The register-pass row pass over a batch (slot on grid axis y).
+template <int LOG2L>
+__global__ void __launch_bounds__(4 * (1 << LOG2L) / 16, 512 / (4 * (1 << LOG2L) / 16))
+    spec_batch_row_pipe_kernel(const SpecMember* __restrict__ mem, int k) {
+  const SpecMember& m = mem[blockIdx.y];
+  if (k >= m.steps) return;
+  const SpecParams p = m.p;
+  spec_row_pipe_body<LOG2L>(p, blockIdx.x, m.t[0], m.t[1], m.t[2], m.t[3], m.ahat);
+}
+
+// Batched persistent column passes: the work items are (slot, group) pairs
+// -- (slot, group, field) for the prep before a chunk's first step -- of the
+// slots that take step k, walked with the grid as stride.  The grid tables
+// are the batch's (slot 0's pointers); coefficients and pointers are each
+// slot's.  The update item also builds the slot's next-stage fields unless
+// this is the slot's last stage of its last step, as the per-block update
+// and prep passes do, so the bits are theirs.
+template <int LOG2N, int CG>
+__global__ void __launch_bounds__(CG * (1 << LOG2N) / 16,
+                                  col_pipe_min_blocks(CG * (1 << LOG2N) / 16))
+    spec_batch_col_stage_pipe_kernel(const SpecMember* __restrict__ mem, int count, int k,
+                                     int stage) {
+  using P = ColPipe<LOG2N>;
+  constexpr int T = CG * P::NTHR;
+  extern __shared__ float2 sbuf[];
+  const int ncols = mem[0].p.L + 1, groups = (ncols + CG - 1) / CG, items = count * groups;
+  const int w = threadIdx.x % CG, t = threadIdx.x / CG, tid = threadIdx.x;
+  const int bstride = col_pipe_bstride<LOG2N, CG>();
+  float2* const buf[2] = {sbuf + w * bstride, sbuf + (CG + w) * bstride};
+  float2* const stg = sbuf + 2 * CG * bstride;
+  const float2* tw;
+  const float* kxt;
+  col_pipe_tables<LOG2N, CG>(sbuf, mem[0].p.twp_x, mem[0].p.kx, &tw, &kxt);
+  auto next_active = [&](int it) {
+    while (it < items && k >= mem[it / groups].steps) it += gridDim.x;
+    return it;
+  };
+  int it = next_active(blockIdx.x);
+  if (it >= items) return;  // uniform per block
+  spec_pipe_prefetch<LOG2N, CG>(mem[it / groups].ahat, ncols, (it % groups) * CG + w, t, stg);
+  cp_async_commit();
+  float2 v[16], u[16], hs[16];
+#pragma unroll 1
+  while (it < items) {
+    const SpecMember& m = mem[it / groups];
+    const SpecParams& p = m.p;
+    const StageCoef sc = m.coef[stage];
+    const int c = (it % groups) * CG + w;
+    const bool live = c < ncols;
+    const bool prep = !(k == m.steps - 1 && stage == m.stages - 1);
+    cp_async_wait_all();
+#pragma unroll
+    for (int r = 0; r < 16; ++r) v[r] = live ? stg[r * T + tid] : make_float2(0.f, 0.f);
+    const int nit = next_active(it + gridDim.x);
+    if (nit < items)
+      spec_pipe_prefetch<LOG2N, CG>(mem[nit / groups].ahat, ncols, (nit % groups) * CG + w, t, stg);
+    cp_async_commit();
+#pragma unroll
+    for (int mm = 0; mm < 16; ++mm) {
+      const size_t gi = (size_t)(t + P::NTHR * mm) * ncols + c;
+      u[mm] = live ? m.w[gi] : make_float2(0.f, 0.f);
+      hs[mm] = (live && sc.has_h_in) ? m.h[gi] : make_float2(0.f, 0.f);
+    }
+    col_pipe_fft<LOG2N, -1, 0>(v, buf, t, tw);
+    if (live) {
+#pragma unroll
+      for (int mm = 0; mm < 16; ++mm) {
+        const int kx = t + P::NTHR * mm;
+        const size_t gi = (size_t)kx * ncols + c;
+        float2 h;
+        u[mm] = stage_update_core_k(p, sc, kx, kxt[kx], c, v[mm], u[mm], hs[mm], &h);
+        m.w[gi] = u[mm];
+        if (sc.write_h) m.h[gi] = h;
+      }
+    }
+    if (prep) {
+#pragma unroll 1
+      for (int f = 0; f < 4; ++f) {
+#pragma unroll
+        for (int r = 0; r < 16; ++r) {
+          const int kx = t + P::NTHR * r;
+          v[r] = live ? prep_factor_k(p, f, kx, kxt[kx], c, u[r]) : make_float2(0.f, 0.f);
+        }
+        col_pipe_fft<LOG2N, 1, 0>(v, buf, t, tw);
+        if (live) {
+          float2* dst = m.t[f];
+#pragma unroll
+          for (int mm = 0; mm < 16; ++mm) dst[(size_t)(t + P::NTHR * mm) * ncols + c] = v[mm];
+        }
+      }
+    }
+    it = nit;
+  }
+  cp_async_wait_all();
+}
+
+template <int LOG2N, int CG>
+__global__ void __launch_bounds__(CG * (1 << LOG2N) / 16,
+                                  col_pipe_min_blocks(CG * (1 << LOG2N) / 16))
+    spec_batch_col_prep_pipe_kernel(const SpecMember* __restrict__ mem, int count) {
+  using P = ColPipe<LOG2N>;
+  constexpr int T = CG * P::NTHR;
+  extern __shared__ float2 sbuf[];
+  const int ncols = mem[0].p.L + 1, per = 4 * ((ncols + CG - 1) / CG), items = count * per;
+  const int w = threadIdx.x % CG, t = threadIdx.x / CG, tid = threadIdx.x;
+  const int bstride = col_pipe_bstride<LOG2N, CG>();
+  float2* const buf[2] = {sbuf + w * bstride, sbuf + (CG + w) * bstride};
+  float2* const stg = sbuf + 2 * CG * bstride;
+  const float2* tw;
+  const float* kxt;
+  col_pipe_tables<LOG2N, CG>(sbuf, mem[0].p.twp_x, mem[0].p.kx, &tw, &kxt);
+  auto next_active = [&](int it) {
+    while (it < items && mem[it / per].steps <= 0) it += gridDim.x;
+    return it;
+  };
+  int it = next_active(blockIdx.x);
+  if (it >= items) return;  // uniform per block
+  spec_pipe_prefetch<LOG2N, CG>(mem[it / per].w, ncols, ((it % per) >> 2) * CG + w, t, stg);
+  cp_async_commit();
+  float2 v[16];
+#pragma unroll 1
+  while (it < items) {
+    const SpecMember& m = mem[it / per];
+    const int f = (it % per) & 3, c = ((it % per) >> 2) * CG + w;
+    cp_async_wait_all();
+#pragma unroll
+    for (int r = 0; r < 16; ++r) {
+      const int kx = t + P::NTHR * r;
+      v[r] = c < ncols ? prep_factor_k(m.p, f, kx, kxt[kx], c, stg[r * T + tid])
+                       : make_float2(0.f, 0.f);
+    }
+    const int nit = next_active(it + gridDim.x);
+    if (nit < items)
+      spec_pipe_prefetch<LOG2N, CG>(mem[nit / per].w, ncols, ((nit % per) >> 2) * CG + w, t, stg);
+    cp_async_commit();
+    col_pipe_fft<LOG2N, 1, 0>(v, buf, t, tw);
+    if (c < ncols) {
+      float2* dst = m.t[f];
+#pragma unroll
+      for (int mm = 0; mm < 16; ++mm) dst[(size_t)(t + P::NTHR * mm) * ncols + c] = v[mm];
+    }
+    it = nit;
+  }
+  cp_async_wait_all();
 }
 
 // ---- Batched variants: the slot index is the last grid axis ----
@@ -1145,9 +1298,49 @@ cudaError_t launch_spec_curl_table(const SpecParams& p, const float2* fxh,
   return cudaGetLastError();
 }
 
+// Batched pipelined passes (column scheme 4 and the register row pass).
+template <int LOG2N, int CG>
+static cudaError_t spec_batch_stage_pipe_impl(const SpecParams& p, const SpecMember* mem,
+                                              int count, int k, int stage, cudaStream_t s) {
+  int grid, threads;
+  size_t smem;
+  auto kern = spec_batch_col_stage_pipe_kernel<LOG2N, CG>;
+  const long long items = (long long)count * ((p.L + 1 + CG - 1) / CG);
+  cudaError_t e = spec_pipe_grid<LOG2N, CG>(kern, (int)(items < (1 << 30) ? items : (1 << 30)),
+                                            &grid, &smem, &threads);
+  if (e != cudaSuccess) return e;
+  kern<<<grid, threads, smem, s>>>(mem, count, k, stage);
+  return cudaGetLastError();
+}
+
+template <int LOG2N, int CG>
+static cudaError_t spec_batch_prep_pipe_impl(const SpecParams& p, const SpecMember* mem,
+                                             int count, cudaStream_t s) {
+  int grid, threads;
+  size_t smem;
+  auto kern = spec_batch_col_prep_pipe_kernel<LOG2N, CG>;
+  const long long items = (long long)count * 4 * ((p.L + 1 + CG - 1) / CG);
+  cudaError_t e = spec_pipe_grid<LOG2N, CG>(kern, (int)(items < (1 << 30) ? items : (1 << 30)),
+                                            &grid, &smem, &threads);
+  if (e != cudaSuccess) return e;
+  kern<<<grid, threads, smem, s>>>(mem, count);
+  return cudaGetLastError();
+}
+
+static bool spec_batch_fused(const SpecParams& p) { return p.col_mode == 4 && spec_pipe_ok(p); }
+
 cudaError_t launch_spec_batch_prep(const SpecParams& p, const SpecMember* mem, int count,
                                    int k, int stage, cudaStream_t s) {
   if (count < 1 || count > 65535) return cudaErrorInvalidValue;
+  if (spec_batch_fused(p)) {
+    if (k >= 0) return cudaSuccess;  // built by the fused update pass
+    switch (p.log2nx) {
+      case 9: return spec_batch_prep_pipe_impl<9, 4>(p, mem, count, s);
+      case 10: return spec_batch_prep_pipe_impl<10, 4>(p, mem, count, s);
+      case 11: return spec_batch_prep_pipe_impl<11, 4>(p, mem, count, s);
+      default: return spec_batch_prep_pipe_impl<12, 2>(p, mem, count, s);
+    }
+  }
   const ColCfg c = col_cfg(p);
   cudaError_t e = set_smem(spec_batch_col_prep_kernel, c.smem);
   if (e != cudaSuccess) return e;
@@ -1156,9 +1349,28 @@ cudaError_t launch_spec_batch_prep(const SpecParams& p, const SpecMember* mem, i
   return cudaGetLastError();
 }
 
+template <int LOG2L>
+static cudaError_t spec_batch_row_pipe_impl(const SpecParams& p, const SpecMember* mem, int count,
+                                            int k, cudaStream_t s) {
+  const size_t smem = (size_t)8 * padded_len(1 << LOG2L) * sizeof(float2);
+  auto kern = spec_batch_row_pipe_kernel<LOG2L>;
+  cudaError_t e = set_smem(kern, smem);
+  if (e != cudaSuccess) return e;
+  kern<<<dim3(p.nx, count), 4 * (1 << LOG2L) / 16, smem, s>>>(mem, k);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_spec_batch_row(const SpecParams& p, const SpecMember* mem, int count, int k,
                                   cudaStream_t s) {
   if (count < 1 || count > 65535) return cudaErrorInvalidValue;
+  if (p.row_mode == 1 && spec_row_pipe_ok(p)) {
+    switch (p.log2L) {
+      case 8: return spec_batch_row_pipe_impl<8>(p, mem, count, k, s);
+      case 9: return spec_batch_row_pipe_impl<9>(p, mem, count, k, s);
+      case 10: return spec_batch_row_pipe_impl<10>(p, mem, count, k, s);
+      default: return spec_batch_row_pipe_impl<11>(p, mem, count, k, s);
+    }
+  }
   const int rows = rows_per_block(p.log2L, 4, p.nx);
   const size_t smem = (size_t)rows * 4 * padded_len(p.L) * sizeof(float2);
   cudaError_t e = set_smem(spec_batch_row_kernel, smem);
@@ -1171,6 +1383,14 @@ cudaError_t launch_spec_batch_row(const SpecParams& p, const SpecMember* mem, in
 cudaError_t launch_spec_batch_update(const SpecParams& p, const SpecMember* mem, int count,
                                      int k, int stage, cudaStream_t s) {
   if (count < 1 || count > 65535) return cudaErrorInvalidValue;
+  if (spec_batch_fused(p)) {
+    switch (p.log2nx) {
+      case 9: return spec_batch_stage_pipe_impl<9, 4>(p, mem, count, k, stage, s);
+      case 10: return spec_batch_stage_pipe_impl<10, 4>(p, mem, count, k, stage, s);
+      case 11: return spec_batch_stage_pipe_impl<11, 4>(p, mem, count, k, stage, s);
+      default: return spec_batch_stage_pipe_impl<12, 2>(p, mem, count, k, stage, s);
+    }
+  }
   const ColCfg c = col_cfg(p);
   cudaError_t e = set_smem(spec_batch_col_update_kernel, c.smem);
   if (e != cudaSuccess) return e;
