@@ -20,7 +20,8 @@ pass over the same workload and the HBM bandwidth in MEASURED_PEAKS.json.
 
 `--impl reference` times the reference algorithm on the host CPU (the NumPy
 restatement of jax-cfd's step; JAX cannot be installed here) on a bounded
-sample of the same workload.
+sample of the same workload: one 2048^2 trajectory per host core, in spawned
+processes timed together.
 
 Multi-GPU: replicas only (each rank advances its own trajectory; no
 collective on the data path); value sums the ranks' cell-steps.
@@ -172,23 +173,54 @@ def max_over_ranks(x: float) -> float:
 # ---------------------------------------------------------------------------
 # Reference arm: the jax-cfd algorithm on the host CPU.
 # ---------------------------------------------------------------------------
-def _cpu_sample(steps: int, warmup: int, n: int = N):
-  """Times the NumPy restatement of the reference step on a bounded sample
-  (`steps` FVM steps at n x n); returns (cell-steps/s, seconds, threads)."""
+def _cpu_step(n: int, seed: int):
+  """The NumPy restatement of the reference step at n x n and a seeded
+  velocity field of unit-scale noise (the step's cost does not depend on the
+  values)."""
   from oracle import fvm as ofvm  # pylint: disable=import-outside-toplevel
   og = ofvm.Grid.make((n, n), domain=DOMAIN)
-  rng = np.random.default_rng(0)
+  rng = np.random.default_rng(seed)
   v = tuple((0.5 * rng.standard_normal((n, n))).astype(np.float32) for _ in range(2))
   dt = ofvm.stable_time_step(MAX_VELOCITY, CFL, VISCOSITY, og)
   step = ofvm.semi_implicit_navier_stokes(
       1.0, VISCOSITY, dt, og, forcing=ofvm.simple_turbulence_forcing(og, 1, 4, -0.1))
+  return step, v
+
+
+def _cpu_worker(index: int, steps: int, warmup: int, n: int, barrier, results):
+  """One host process of the CPU sample: warm up, wait for every process,
+  then time `steps` steps (monotonic clock, comparable across processes)."""
+  step, v = _cpu_step(n, index)
   for _ in range(warmup):
     v = step(v)
+  barrier.wait()
   t0 = time.perf_counter()
   for _ in range(steps):
     v = step(v)
-  dt_s = time.perf_counter() - t0
-  return n * n * steps / dt_s, dt_s, 1
+  results.put((t0, time.perf_counter()))
+
+
+def _cpu_sample(steps: int, warmup: int, n: int = N, procs: int = 0):
+  """Times the NumPy restatement of the reference step on a bounded sample:
+  `procs` host processes (default: one per host core, started with spawn),
+  each advancing its own n x n trajectory by `steps` steps after `warmup`;
+  returns (cell-steps/s over all processes, seconds of the timed region,
+  processes).  The restatement is single-threaded, so one trajectory per core
+  is how it uses every core."""
+  import multiprocessing  # pylint: disable=import-outside-toplevel
+  procs = procs or os.cpu_count() or 1
+  ctx = multiprocessing.get_context('spawn')
+  barrier = ctx.Barrier(procs)
+  results = ctx.Queue()
+  workers = [ctx.Process(target=_cpu_worker, args=(i, steps, warmup, n, barrier, results))
+             for i in range(procs)]
+  for w in workers:
+    w.start()
+  spans = [results.get() for _ in range(procs)]
+  for w in workers:
+    w.join()
+  secs = max(t1 for _, t1 in spans) - min(t0 for t0, _ in spans)
+  return procs * n * n * steps / secs, secs, procs
 
 
 def run_reference(args):
@@ -200,7 +232,8 @@ def run_reference(args):
   # Each reference "step" is one FVM time step of the 2048^2 workload (a
   # bounded sample: the full 2000-step run would take about an hour on CPU).
   value, secs, threads = _cpu_sample(k, w)
-  sample = f'{k} FVM steps at {N}x{N} after {w} warm-up steps ({secs:.1f} s)'
+  sample = (f'{threads} host processes (one per core), each {k} FVM steps of its own '
+            f'{N}x{N} trajectory after {w} warm-up steps ({secs:.1f} s)')
   _json_line({
       'metric': 'FVM cell-steps/s at 2048^2', 'value': value, 'unit': 'cell-steps/s',
       'impl': 'reference', 'n_gpus': world, 'steps': k, 'warmup': w,
@@ -631,8 +664,9 @@ def run_gb300(args):
   if rank == 0 and not args.skip_cpu:
     cv, csecs, cthreads = _cpu_sample(args.cpu_steps, 1)
     cpu = {'value': cv, 'unit': 'cell-steps/s', 'cores': cthreads, 'kind': 'port',
-           'sample': f'{args.cpu_steps} FVM steps at {N}x{N} of the NumPy restatement '
-                     f'after 1 warm-up step ({csecs:.1f} s)'}
+           'sample': f'{cthreads} host processes (one per core), each {args.cpu_steps} FVM '
+                     f'steps of its own {N}x{N} trajectory of the NumPy restatement after 1 '
+                     f'warm-up step ({csecs:.1f} s)'}
 
   if rank != 0:
     return

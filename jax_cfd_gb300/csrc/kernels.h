@@ -40,7 +40,7 @@ struct FvmParams {
   const float* lamy;   // eigenvalues along y, rfft half (ny/2 + 1)
   float cutoff;        // 10 * eps(float32)
   float pinv_scale;    // 1 / (nx * ny), folds irfftn's normalisation
-  const float2* tw_y;  // exp(-2 pi i k / ny), k <= ny/4: real-FFT untangling
+  const float2* tw_y;  // exp(-2 pi i k / ny), 0 <= k < ny: real-FFT untangling
   const float2* twp_x;  // pass twiddle tables of the length-nx column FFT
   const float2* twp_y;  // pass twiddle tables of the length-ny/2 row FFT
   int fft_shape;       // transform block shape: 0 wide, 1 narrow (see fvm.cu)
