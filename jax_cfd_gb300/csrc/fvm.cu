@@ -1187,15 +1187,24 @@ CFD_D void div_rfft_row_warp(const FvmParams& p, int i, const float* __restrict_
   const float2* ua = reinterpret_cast<const float2*>(us + i * ny);
   const float2* ub = reinterpret_cast<const float2*>(us + ((i - 1) & mx) * ny);
   const float2* vc = reinterpret_cast<const float2*>(vs + i * ny);
-  float2 v[32];
+  float2 v[32], c[32];
+#pragma unroll
+  for (int m = 0; m < 32; ++m) c[m] = __ldg(vc + lane + 32 * m);
+  // v[j - 1] for j = 2n is the odd half of element n - 1, held by lane - 1 in
+  // the same slot; for lane 0 by lane 31 in the previous slot (cyclically).
+  // Every lane passes its own slot-m value down one lane, and lane 0 keeps
+  // what arrives for its next slot.
+  float recv[32];
+#pragma unroll
+  for (int m = 0; m < 32; ++m) recv[m] = __shfl_sync(kFull, c[m].y, (lane - 1) & 31);
 #pragma unroll
   for (int m = 0; m < 32; ++m) {
     const int n = lane + 32 * m;
-    const float2 a = __ldg(ua + n), b = __ldg(ub + n), c = __ldg(vc + n);
-    const float cm = __ldg(vs + i * ny + ((2 * n - 1) & my));
+    const float2 a = __ldg(ua + n), b = __ldg(ub + n);
+    const float cm = lane == 0 ? recv[(m - 1) & 31] : recv[m];
     // D = (u - u[i-1]) / hx + (v - v[j-1]) / hy, as in div_rfft_rows
-    v[m] = make_float2((a.x - b.x) * p.inv_hx + (c.x - cm) * p.inv_hy,
-                       (a.y - b.y) * p.inv_hx + (c.y - c.x) * p.inv_hy);
+    v[m] = make_float2((a.x - b.x) * p.inv_hx + (c[m].x - cm) * p.inv_hy,
+                       (a.y - b.y) * p.inv_hx + (c[m].y - c[m].x) * p.inv_hy);
   }
   warp_fft1024<-1>(v, tile, p.twp_y + wfft_table_offset(kWarpFftLog2));
   float2* out = spec + (size_t)i * L;

@@ -341,3 +341,18 @@ def test_implicit_sinusoidal_divergence_and_momentum(cuda_device):
   assert np.max(ofvm.divergence(out, og.step)) < 1e-3
   momentum = lambda v: np.array(v).sum() * np.prod(og.step)
   np.testing.assert_allclose(momentum(out), momentum(v0), atol=1e-3)
+
+
+@pytest.mark.parametrize('shape', [(1024, 2048), (2048, 256)])
+def test_programmatic_launch_keeps_bits(cuda_device, monkeypatch, shape):
+  """The step's kernels launched as programmatic dependents of their
+  predecessor (the default) and launched plainly give the same bits."""
+  from tests.test_gpu_batching import _member, _single
+  member, v0 = _member(shape, 31, 1e-3, 4, 2.0)
+  with_pdl = _single(member, v0, 6, cuda_device)
+  monkeypatch.setenv('CFD_GB300_PDL', '0')
+  plain = _single(member, v0, 6, cuda_device)
+  torch.cuda.synchronize(cuda_device)
+  for a, b in zip(with_pdl, plain):
+    assert torch.isfinite(a).all()
+    assert torch.equal(a, b)
