@@ -494,7 +494,7 @@ def run_differentiation(dev, args):
       'forward_backward_ms': t * 1000.0,
       'trajectory_steps_per_s': batch * steps / t,
       'cell_steps_per_s': batch * steps * n * n / t,
-      'loss': float(loss),
+      'loss': float(loss.detach()),
       'fd_check': {'directions': len(errs), 'eps': eps, 'direction_rms': 1.0,
                    'max_rel_err': max(errs) if errs else None,
                    'viscosity_rel_err': abs(gnu - fd_nu) / max(abs(fd_nu), 1e-30),
