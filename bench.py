@@ -683,9 +683,10 @@ def run_gb300(args):
                  'l2': 'flushed (256 MiB write) between bench steps',
                  'launch_config': {'row_blocks': ['wide', 'narrow'][shape & 1],
                                    'column_pass': ['blocks', 'cluster4', 'cluster8',
-                                                   'pipelined4', 'pipelined2'][(shape >> 1) % 5],
-                                   'stencil': ['tiles', 'warp_streams'][(shape // 10) & 1],
-                                   'row_feed': ['registers', 'bulk_copy'][shape // 20]},
+                                                   'pipelined4', 'pipelined2',
+                                                   'pipelined4_tma'][(shape >> 1) % 6],
+                                   'stencil': ['tiles', 'warp_streams'][(shape // 12) & 1],
+                                   'row_feed': ['registers', 'bulk_copy'][shape // 24]},
                  'parallelism': 'replicas' if world > 1 else 'single'},
       'roofline': {'kernel': dominant, 'bound': 'hbm', 'achieved': achieved, 'peak': peak,
                    'unit': 'GB/s', 'frac': achieved / peak, 'traffic': traffic,

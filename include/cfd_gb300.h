@@ -142,10 +142,10 @@ int cfd_fvm_plan_autotune(cfd_fvm_plan* plan, void* stream, const float* u,
                           int steps, int* chosen);
 /* Pins the launch configuration (an index as cfd_fvm_plan_autotune reports:
  * row-transform shape (0 wide, 1 narrow) + 2 * column scheme (0 blocks,
- * 1/2 clusters of 4/8, 3/4 persistent pipelined groups of 4/2 columns)
- * + 10 * stencil scheme (0 shared-memory tiles, 1 warp streams) + 20 * row
- * feed (0 registers, 1 bulk copies): 40 choices); results do not depend on
- * it.  cfd_fvm_plan_get_launch
+ * 1/2 clusters of 4/8, 3/4 persistent pipelined groups of 4/2 columns, 5
+ * groups of 4 staged by TMA tensor loads) + 12 * stencil scheme (0
+ * shared-memory tiles, 1 warp streams) + 24 * row feed (0 registers, 1 bulk
+ * copies): 48 choices); results do not depend on it.  cfd_fvm_plan_get_launch
  * returns the current one. */
 int cfd_fvm_plan_set_launch(cfd_fvm_plan* plan, int choice);
 int cfd_fvm_plan_get_launch(const cfd_fvm_plan* plan);

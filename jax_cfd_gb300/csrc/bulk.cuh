@@ -50,6 +50,21 @@ CFD_D void bulk_load(void* dst_smem, const void* src_global, uint32_t bytes, uin
       : "memory");
 }
 
+// Tiled 2-D TMA load of one box of the tensor map `tmap` (the generic
+// address of a __grid_constant__ CUtensorMap) at element coordinates (x, y)
+// into shared memory; x times the element size must be a multiple of 16 B.
+CFD_D void tma_load_2d(void* dst_smem, const void* tmap, int x, int y, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes "
+      "[%0], [%1, {%2, %3}], [%4];" ::"r"(smem_addr(dst_smem)),
+      "l"(tmap), "r"(x), "r"(y), "r"(smem_addr(bar))
+      : "memory");
+}
+
+// Orders this thread's earlier generic-proxy accesses to shared memory before
+// its later async-proxy (TMA) accesses.
+CFD_D void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
 CFD_D bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   uint32_t done;
   asm volatile(

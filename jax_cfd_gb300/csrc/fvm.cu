@@ -15,6 +15,7 @@
 // numbers: element 0 holds (X[0], X[M/2]), both real.  The x-axis transforms
 // of the DC and Nyquist columns run as two separate real sequences.
 #include <cooperative_groups.h>
+#include <cuda.h>
 
 #include "bulk.cuh"
 #include "colpipe.cuh"
@@ -1010,6 +1011,75 @@ __global__ void __launch_bounds__(CG * (1 << LOG2N) / 16,
   col_pinv_pipe_cols<LOG2N, CG>(p, spec, blockIdx.x, gridDim.x);
 }
 
+// The persistent column pass with each group staged by TMA: one thread
+// issues the group's tiled tensor loads (boxes of 4 columns x 256 rows) onto
+// an mbarrier, and the box layout in shared memory, row-major over the 4
+// columns, is exactly the per-thread staging layout of col_pinv_pipe_cols
+// (worker t of column w reads rows t + (N/16) r at r * T + 4 t + w), so the
+// transform code is shared and the bits are the same.  The next group's
+// loads are issued after a block barrier (every thread has read the staged
+// group) and an async-proxy fence.  Waits are bounded: a copy that never
+// lands records g_cfd_device_fault and the block leaves.
+template <int LOG2N>
+__global__ void __launch_bounds__(4 * (1 << LOG2N) / 16, col_pipe_min_blocks(4 * (1 << LOG2N) / 16))
+    fvm_col_pinv_tma_kernel(FvmParams p, float2* __restrict__ spec,
+                            const __grid_constant__ CUtensorMap tmap) {
+  constexpr int CG = 4;
+  using P = ColPipe<LOG2N>;
+  constexpr int N = P::N, BOX = N < 256 ? N : 256, NBOX = N / BOX;
+  constexpr uint32_t kGroupBytes = (uint32_t)N * CG * sizeof(float2);
+  extern __shared__ float2 sbuf[];  // no static shared memory: 128-byte aligned
+  const int L = p.ny >> 1, groups = L / CG + 1;
+  const int w = threadIdx.x % CG, t = threadIdx.x / CG;
+  const int bstride = col_pipe_bstride<LOG2N, CG>();
+  float2* const buf[2] = {sbuf + w * bstride, sbuf + (CG + w) * bstride};
+  float2* const stage = sbuf + 2 * CG * bstride;
+  uint64_t* const bar =
+      reinterpret_cast<uint64_t*>(reinterpret_cast<char*>(sbuf) + col_pipe_smem<LOG2N, CG>());
+  constexpr int INV_FIRST = (P::PASSES - 1) & 1;
+  int g = blockIdx.x;
+  if (g >= groups) return;  // uniform per block
+  const float2* tw;
+  const float* lamx;
+  col_pipe_tables<LOG2N, CG>(sbuf, p.twp_x, p.lamx, &tw, &lamx);
+  if (threadIdx.x == 0) {
+    mbar_init(bar, 1);
+    mbar_fence_init();
+  }
+  __syncthreads();
+  pdl_wait();
+  pdl_trigger();
+  // Group gg's columns start at float 8 gg of a row; the Nyquist group reads
+  // row element 0 (its imaginary part), like the first group.
+  auto issue = [&](int gg) {
+    const int x = gg * CG >= L ? 0 : 2 * CG * gg;
+    mbar_arrive_expect_tx(bar, kGroupBytes);
+#pragma unroll
+    for (int b = 0; b < NBOX; ++b) tma_load_2d(stage + b * BOX * CG, &tmap, x, b * BOX, bar);
+  };
+  if (threadIdx.x == 0) issue(g);
+  uint32_t phase = 0;
+  float2 v[16];
+#pragma unroll 1
+  for (; g < groups; g += gridDim.x) {
+    if (!mbar_wait(bar, phase)) return;
+    phase ^= 1u;
+    col_pipe_take<LOG2N, CG>(stage, L, g, w, t, v);
+    __syncthreads();  // the staged group is read
+    if (threadIdx.x == 0 && g + gridDim.x < groups) {
+      fence_proxy_async_smem();
+      issue(g + gridDim.x);
+    }
+    col_pipe_fft<LOG2N, -1, 0>(v, buf, t, tw);
+    const int cp = g * CG >= L ? L : g * CG + w;  // pinv column index
+#pragma unroll
+    for (int m = 0; m < 16; ++m)
+      v[m] = c_scale(v[m], pinv_diag_at(p, lamx[t + P::NTHR * m], cp));
+    col_pipe_fft<LOG2N, 1, INV_FIRST>(v, buf, t, tw);
+    col_pipe_store<LOG2N, CG>(spec, L, g, w, t, v);
+  }
+}
+
 // The persistent column pass over a same-shape batch: the work items are the
 // (member, group) pairs of the members that take this step, walked with the
 // grid as stride, so many members keep every block's staging pipeline full.
@@ -1664,6 +1734,40 @@ bool col_pipe_ok(const FvmParams& p, int narrow) {
   return p.log2nx >= 8 && p.log2nx <= 12 && (p.ny / 2) % cg == 0;
 }
 
+bool col_tma_grid_ok(const FvmParams& p) {
+  return p.log2nx >= 8 && p.log2nx <= 11 && (p.ny / 2) % 4 == 0;
+}
+
+template <int LOG2N>
+static cudaError_t col_pinv_tma_impl(const FvmParams& p, float2* spec, cudaStream_t s) {
+  const size_t smem = col_pipe_smem<LOG2N, 4>() + 16;  // + the mbarrier
+  const int threads = 4 * (1 << LOG2N) / 16;
+  auto kern = fvm_col_pinv_tma_kernel<LOG2N>;
+  cudaError_t e = set_smem(kern, smem);
+  if (e != cudaSuccess) return e;
+  static int per_sm = 0;  // same value for every device of one kind
+  if (per_sm == 0) {
+    int nb = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, threads, smem);
+    if (e != cudaSuccess) return e;
+    per_sm = nb > 0 ? nb : 1;
+  }
+  const int groups = p.ny / 2 / 4 + 1;
+  const int slots = col_pipe_device_sms() * per_sm;
+  const CUtensorMap map = *static_cast<const CUtensorMap*>(p.col_tmap);
+  return launch_maybe_pdl(p.pdl, kern, dim3(groups < slots ? groups : slots), dim3(threads), smem,
+                          s, p, spec, map);
+}
+
+static cudaError_t col_pinv_tma_launch(const FvmParams& p, float2* spec, cudaStream_t s) {
+  switch (p.log2nx) {
+    case 8: return col_pinv_tma_impl<8>(p, spec, s);
+    case 9: return col_pinv_tma_impl<9>(p, spec, s);
+    case 10: return col_pinv_tma_impl<10>(p, spec, s);
+    default: return col_pinv_tma_impl<11>(p, spec, s);
+  }
+}
+
 static cudaError_t col_pinv_pipe_launch(const FvmParams& p, float2* spec, cudaStream_t s) {
   if (p.col_mode == 4) {
     switch (p.log2nx) {
@@ -1687,7 +1791,10 @@ static cudaError_t col_pinv_pipe_launch(const FvmParams& p, float2* spec, cudaSt
 // register-pipelined pass with 4 / 2 columns per block.
 cudaError_t launch_fvm_col_pinv(const FvmParams& p, float2* spec,
                                 cudaStream_t s) {
-  if (p.col_mode >= 3 && col_pipe_ok(p, p.col_mode == 4)) return col_pinv_pipe_launch(p, spec, s);
+  if (p.col_mode == 5 && p.col_tmap && p.col_tmap_spec == spec && col_tma_grid_ok(p))
+    return col_pinv_tma_launch(p, spec, s);
+  if ((p.col_mode == 3 || p.col_mode == 4) && col_pipe_ok(p, p.col_mode == 4))
+    return col_pinv_pipe_launch(p, spec, s);
   if (p.col_mode == 2 && col_cluster_ok(p, 8)) return col_pinv_cluster_impl<8>(p, spec, s);
   if ((p.col_mode == 1 || p.col_mode == 2) && col_cluster_ok(p, 4))
     return col_pinv_cluster_impl<4>(p, spec, s);

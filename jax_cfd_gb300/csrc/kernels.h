@@ -45,7 +45,8 @@ struct FvmParams {
   const float2* twp_y;  // pass twiddle tables of the length-ny/2 row FFT
   int fft_shape;       // transform block shape: 0 wide, 1 narrow (see fvm.cu)
   int col_mode;        // column pass: 0 per-block columns, 1/2 clusters of 4/8,
-                       // 3/4 persistent register-pipelined groups of 4/2 columns
+                       // 3/4 persistent register-pipelined groups of 4/2 columns,
+                       // 5 as 3 with the groups staged by TMA tensor loads
   int stencil;         // explicit step: 0 shared-memory tiles, 1 warp streams
   int row_feed;        // row transforms: 0 loads through registers, 1 bulk copies
   // Implicit diffusion (diffusion.solve_fast_diag) on the same transforms:
@@ -53,6 +54,9 @@ struct FvmParams {
   int col_diag;        // column-pass diagonal: 0 pinv(lambda), 1 x / (1 - x), x = dtnu lambda
   float dtnu;          // float32(dt * viscosity) for col_diag = 1
   int pdl;             // launch the step's kernels as programmatic dependents
+  const void* col_tmap;  // HOST pointer to the plan's CUtensorMap of its spectrum
+  const void* col_tmap_spec;  // the spectrum buffer col_tmap describes
+                         // (col_mode 5), or null
 };
 
 // One slot of a same-shape batch of FVM trajectories (device-resident table
@@ -79,6 +83,9 @@ bool col_cluster_ok(const FvmParams& p, int cluster);
 // Whether the persistent column pass (col_mode 3, or 4 with narrow != 0)
 // applies to this grid.
 bool col_pipe_ok(const FvmParams& p, int narrow);
+// Whether the TMA-staged column pass (col_mode 5) can run on this grid (a
+// tensor map of the spectrum is then needed in col_tmap).
+bool col_tma_grid_ok(const FvmParams& p);
 // Whether the warp-streaming stencil (stencil 1) applies to this grid.
 bool stream_stencil_ok(const FvmParams& p);
 // Whether the bulk-copy row transforms (row_feed 1) apply to this grid.

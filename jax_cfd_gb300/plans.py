@@ -183,7 +183,7 @@ class FvmPlan:
   def autotune(self, u, v, steps: int = 20) -> int:
     """Times each transform launch configuration on (u, v) and keeps the
     fastest; returns its index (row block shape + 2 * column-pass scheme +
-    10 * stencil scheme + 20 * row feed).  Synchronises the stream."""
+    12 * stencil scheme + 24 * row feed).  Synchronises the stream."""
     us, vs = torch.empty_like(u), torch.empty_like(v)
     chosen = ctypes.c_int(-1)
     a = self._fields(u, v, us, vs)
@@ -192,7 +192,7 @@ class FvmPlan:
               'cfd_fvm_plan_autotune')
     return int(chosen.value)
 
-  LAUNCH_CHOICES = 40
+  LAUNCH_CHOICES = 48
 
   def set_launch(self, choice: int):
     """Pins the launch configuration (see autotune); results do not change."""
