@@ -1019,7 +1019,7 @@ __global__ void __launch_bounds__(CG * (1 << LOG2N) / 16,
 // transform code is shared and the bits are the same.  The next group's
 // loads are issued after a block barrier (every thread has read the staged
 // group) and an async-proxy fence.  Waits are bounded: a copy that never
-// lands records g_cfd_device_fault and the block leaves.
+// lands records g_cfd_device_fault and the whole block leaves together.
 template <int LOG2N>
 __global__ void __launch_bounds__(4 * (1 << LOG2N) / 16, col_pipe_min_blocks(4 * (1 << LOG2N) / 16))
     fvm_col_pinv_tma_kernel(FvmParams p, float2* __restrict__ spec,
@@ -1062,10 +1062,12 @@ __global__ void __launch_bounds__(4 * (1 << LOG2N) / 16, col_pipe_min_blocks(4 *
   float2 v[16];
 #pragma unroll 1
   for (; g < groups; g += gridDim.x) {
-    if (!mbar_wait(bar, phase)) return;
+    const bool landed = mbar_wait(bar, phase);
     phase ^= 1u;
-    col_pipe_take<LOG2N, CG>(stage, L, g, w, t, v);
-    __syncthreads();  // the staged group is read
+    if (landed) col_pipe_take<LOG2N, CG>(stage, L, g, w, t, v);
+    // The staged group is read; a wait that gave up on any thread ends the
+    // whole block here (no copy is then issued, none other is in flight).
+    if (__syncthreads_or(!landed)) return;
     if (threadIdx.x == 0 && g + gridDim.x < groups) {
       fence_proxy_async_smem();
       issue(g + gridDim.x);
