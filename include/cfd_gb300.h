@@ -221,9 +221,10 @@ int cfd_fvm_batch_run(cfd_fvm_batch* batch, void* stream, int chunk, int use_gra
 /* Times the launch configurations on a `steps`-step chunk of the current
  * slots, restores their states and keeps the fastest; *chosen = row-transform
  * shape (0 wide, 1 narrow) + 2 * column scheme (0 blocks, 1/2 clusters of
- * 4/8, 3 persistent pipelined groups of 4 columns over all slots) + 8 *
- * stencil (0 shared-memory tiles, 1 warp streams).  Every configuration gives
- * the same bits.  Synchronises. */
+ * 4/8, 3 persistent pipelined groups of 4 columns over all slots staged by
+ * cp.async, 4 the same staged by TMA tensor loads) + 10 * stencil (0
+ * shared-memory tiles, 1 warp streams): 20 choices.  Every configuration
+ * gives the same bits.  Synchronises. */
 int cfd_fvm_batch_autotune(cfd_fvm_batch* batch, void* stream, int steps, int* chosen);
 /* Pins the batch's launch configuration (index as cfd_fvm_batch_autotune
  * reports); CFD_ERR_UNSUPPORTED for a configuration the grid cannot take.

@@ -61,6 +61,15 @@ CFD_D void tma_load_2d(void* dst_smem, const void* tmap, int x, int y, uint64_t*
       : "memory");
 }
 
+// The same for a 3-D tensor map at element coordinates (x, y, z).
+CFD_D void tma_load_3d(void* dst_smem, const void* tmap, int x, int y, int z, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes "
+      "[%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_addr(dst_smem)),
+      "l"(tmap), "r"(x), "r"(y), "r"(z), "r"(smem_addr(bar))
+      : "memory");
+}
+
 // Orders this thread's earlier generic-proxy accesses to shared memory before
 // its later async-proxy (TMA) accesses.
 CFD_D void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }

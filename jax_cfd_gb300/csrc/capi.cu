@@ -199,6 +199,8 @@ struct cfd_fvm_batch {
   cudaGraphExec_t exec = nullptr;
   int graph_chunk = -1;
   long long bytes = 0;
+  // 3-D tensor map of every slot's spectrum for the TMA-staged column pass.
+  alignas(64) CUtensorMap spec_map;
 };
 
 // Several batches (one per grid shape) stepped together: a chunk forks one
@@ -341,9 +343,11 @@ static int fvm_params_from_config(const cfd_fvm_config* cfg, cfd::FvmParams* out
   return CFD_OK;
 }
 
-// Tensor map of a packed row spectrum viewed as nx rows of ny float32
-// (2 floats per complex value), boxes of 8 floats x min(nx, 256) rows.
-static bool encode_spec_map(CUtensorMap* map, float2* spec, int nx, int ny) {
+// Tensor map of `count` packed row spectra, each nx rows of ny float32 (2
+// floats per complex value), spectrum z at spec + z * member_floats floats;
+// boxes of 8 floats x min(nx, 256) rows x 1 spectrum.
+static bool encode_spec_map(CUtensorMap* map, float2* spec, int nx, int ny, int count = 1,
+                            size_t member_floats = 0) {
   static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
   if (!encode) {
     void* fn = nullptr;
@@ -354,11 +358,14 @@ static bool encode_spec_map(CUtensorMap* map, float2* spec, int nx, int ny) {
       return false;
     encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
   }
-  const cuuint64_t dims[2] = {(cuuint64_t)ny, (cuuint64_t)nx};
-  const cuuint64_t strides[1] = {(cuuint64_t)ny * sizeof(float)};
-  const cuuint32_t box[2] = {8, (cuuint32_t)(nx < 256 ? nx : 256)};
-  const cuuint32_t estride[2] = {1, 1};
-  return encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, spec, dims, strides, box, estride,
+  const cuuint64_t dims[3] = {(cuuint64_t)ny, (cuuint64_t)nx, (cuuint64_t)count};
+  const cuuint64_t strides[2] = {(cuuint64_t)ny * sizeof(float),
+                                 (cuuint64_t)member_floats * sizeof(float)};
+  const cuuint32_t box[3] = {8, (cuuint32_t)(nx < 256 ? nx : 256), 1};
+  const cuuint32_t estride[3] = {1, 1, 1};
+  if (count > 1 && (member_floats * sizeof(float)) % 16 != 0) return false;
+  return encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, count > 1 ? 3 : 2, spec, dims, strides,
+                box, estride,
                 CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                 CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) ==
          CUDA_SUCCESS;
@@ -861,6 +868,13 @@ int cfd_fvm_batch_create(const cfd_fvm_config* shape, int count, cfd_fvm_batch**
     m.spec = reinterpret_cast<float2*>(base + 6 * n);
     m.steps = 0;
   }
+  // Every slot's spectrum at one stride (7 n floats): one 3-D map covers
+  // them for the TMA-staged column pass, the default where it encodes.
+  if (cfd::col_tma_grid_ok(b->shape) &&
+      encode_spec_map(&b->spec_map, b->host[0].spec, nx, ny, count, 7 * n)) {
+    b->shape.col_tmap = &b->spec_map;
+    if (b->shape.col_mode == 3) b->shape.col_mode = 5;
+  }
   *out = b;
   return CFD_OK;
 }
@@ -968,22 +982,28 @@ int cfd_fvm_batch_run(cfd_fvm_batch* b, void* stream, int chunk, int use_graph) 
 // slot states afterwards and keeps the fastest configuration.  Synchronises.
 // Whether batch launch configuration c (index as in cfd_fvm_batch_autotune)
 // applies to the batch's grid; sets it in `shape` when it does.
+// Index = row shape + 2 * column scheme (0 blocks, 1/2 clusters of 4/8, 3
+// pipelined groups of 4 staged by cp.async, 4 the same staged by TMA, run as
+// col_mode 5) + 10 * stencil.
+constexpr int kBatchLaunchChoices = 20;
 static bool batch_launch_choice(cfd::FvmParams* shape, int c) {
-  if (c < 0 || c >= 16) return false;
+  if (c < 0 || c >= kBatchLaunchChoices) return false;
   cfd::FvmParams q = *shape;
+  const int col = (c >> 1) % 5;
   q.fft_shape = c & 1;
-  q.col_mode = (c >> 1) & 3;
-  q.stencil = c >> 3;
+  q.col_mode = col == 4 ? 5 : col;
+  q.stencil = c / 10;
   if ((q.col_mode == 1 || q.col_mode == 2) && !cfd::col_cluster_ok(q, q.col_mode == 1 ? 4 : 8))
     return false;
   if (q.col_mode == 3 && !cfd::col_pipe_ok(q, 0)) return false;
+  if (q.col_mode == 5 && !(q.col_tmap && cfd::col_tma_grid_ok(q))) return false;
   if (q.stencil == 1 && !cfd::stream_stencil_ok(q)) return false;
   *shape = q;
   return true;
 }
 
 int cfd_fvm_batch_set_launch(cfd_fvm_batch* b, int choice) {
-  if (!b || choice < 0 || choice >= 16)
+  if (!b || choice < 0 || choice >= kBatchLaunchChoices)
     return fail(CFD_ERR_INVALID_ARGUMENT, "cfd_fvm_batch_set_launch: bad arguments");
   if (!batch_launch_choice(&b->shape, choice))
     return fail(CFD_ERR_UNSUPPORTED, "cfd_fvm_batch_set_launch: choice not available on this grid");
@@ -1027,7 +1047,7 @@ int cfd_fvm_batch_autotune(cfd_fvm_batch* b, void* stream, int steps, int* chose
   // Candidates: index = row-transform shape + 2 * column scheme (0 blocks, 1/2
   // clusters of 4/8, 3 persistent pipelined groups) + 8 * stencil (0 tiles,
   // 1 warp streams).
-  for (int cand = 0; cand < 16 && rc == CFD_OK; ++cand) {
+  for (int cand = 0; cand < kBatchLaunchChoices && rc == CFD_OK; ++cand) {
     if (!batch_launch_choice(&b->shape, cand)) continue;
     b->dirty = true;
     rc = cfd_fvm_batch_run(b, stream, 1, 0);  // warm-up (and per-kernel smem setup)

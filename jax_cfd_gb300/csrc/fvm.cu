@@ -1137,6 +1137,85 @@ __global__ void __launch_bounds__(CG * (1 << LOG2N) / 16,
   cp_async_wait_all();
 }
 
+// The batched column pass with each (member, group) item staged by TMA: a
+// 3-D tensor map covers the spectra of all members (they sit at one fixed
+// stride in the batch's slab), so one thread loads an item's boxes at
+// coordinates (float offset, row, member).  Staging layout, transforms and
+// bits as fvm_batch_col_pinv_pipe_kernel; barriers and bounded waits as
+// fvm_col_pinv_tma_kernel.
+template <int LOG2N>
+__global__ void __launch_bounds__(4 * (1 << LOG2N) / 16, col_pipe_min_blocks(4 * (1 << LOG2N) / 16))
+    fvm_batch_col_pinv_tma_kernel(const FvmMember* __restrict__ mem, int count, int k,
+                                  const __grid_constant__ CUtensorMap tmap) {
+  constexpr int CG = 4;
+  using P = ColPipe<LOG2N>;
+  constexpr int N = P::N, BOX = N < 256 ? N : 256, NBOX = N / BOX;
+  constexpr uint32_t kGroupBytes = (uint32_t)N * CG * sizeof(float2);
+  extern __shared__ float2 sbuf[];  // no static shared memory: 128-byte aligned
+  const int L = mem[0].p.ny >> 1;
+  const int groups = L / CG + 1, items = count * groups;
+  const int w = threadIdx.x % CG, t = threadIdx.x / CG;
+  const int bstride = col_pipe_bstride<LOG2N, CG>();
+  float2* const buf[2] = {sbuf + w * bstride, sbuf + (CG + w) * bstride};
+  float2* const stage = sbuf + 2 * CG * bstride;
+  uint64_t* const bar =
+      reinterpret_cast<uint64_t*>(reinterpret_cast<char*>(sbuf) + col_pipe_smem<LOG2N, CG>());
+  constexpr int INV_FIRST = (P::PASSES - 1) & 1;
+  const float2* tw;
+  const float* lamx;
+  col_pipe_tables<LOG2N, CG>(sbuf, mem[0].p.twp_x, mem[0].p.lamx, &tw, &lamx);
+  if (threadIdx.x == 0) {
+    mbar_init(bar, 1);
+    mbar_fence_init();
+  }
+  __syncthreads();
+  pdl_wait();
+  pdl_trigger();
+  // Next item at or after `it` (stride gridDim.x) whose member takes step k;
+  // the same for every thread of the block.
+  auto next_active = [&](int it) {
+    while (it < items && k >= mem[it / groups].steps) it += gridDim.x;
+    return it;
+  };
+  auto issue = [&](int item) {
+    const int gg = item % groups, z = item / groups;
+    const int x = gg * CG >= L ? 0 : 2 * CG * gg;
+    mbar_arrive_expect_tx(bar, kGroupBytes);
+#pragma unroll
+    for (int b = 0; b < NBOX; ++b)
+      tma_load_3d(stage + b * BOX * CG, &tmap, x, b * BOX, z, bar);
+  };
+  int it = next_active(blockIdx.x);
+  if (it >= items) return;  // uniform per block
+  if (threadIdx.x == 0) issue(it);
+  uint32_t phase = 0;
+  float2 v[16];
+#pragma unroll 1
+  while (it < items) {
+    const FvmMember& m = mem[it / groups];
+    const int g = it % groups;
+    const bool landed = mbar_wait(bar, phase);
+    phase ^= 1u;
+    if (landed) col_pipe_take<LOG2N, CG>(stage, L, g, w, t, v);
+    // The staged item is read; a wait that gave up on any thread ends the
+    // whole block here (no copy is then issued, none other is in flight).
+    if (__syncthreads_or(!landed)) return;
+    const int nit = next_active(it + gridDim.x);
+    if (threadIdx.x == 0 && nit < items) {
+      fence_proxy_async_smem();
+      issue(nit);
+    }
+    col_pipe_fft<LOG2N, -1, 0>(v, buf, t, tw);
+    const int cp = g * CG >= L ? L : g * CG + w;  // pinv column index
+#pragma unroll
+    for (int mm = 0; mm < 16; ++mm)
+      v[mm] = c_scale(v[mm], pinv_diag_at(m.p, lamx[t + P::NTHR * mm], cp));
+    col_pipe_fft<LOG2N, 1, INV_FIRST>(v, buf, t, tw);
+    col_pipe_store<LOG2N, CG>(m.spec, L, g, w, t, v);
+    it = nit;
+  }
+}
+
 // Inverse packed real FFT of each row, in place: q^ rows -> q rows (floats).
 CFD_D void irfft_rows(const FvmParams& p, int blk, int rows, float2* spec) {
   extern __shared__ float2 sbuf[];
@@ -1999,6 +2078,38 @@ static cudaError_t batch_col_pipe_launch(const FvmParams& p, const FvmMember* me
   }
 }
 
+template <int LOG2N>
+static cudaError_t batch_col_tma_impl(const FvmParams& p, const FvmMember* mem, int count, int k,
+                                      cudaStream_t s) {
+  const size_t smem = col_pipe_smem<LOG2N, 4>() + 16;  // + the mbarrier
+  const int threads = 4 * (1 << LOG2N) / 16;
+  auto kern = fvm_batch_col_pinv_tma_kernel<LOG2N>;
+  cudaError_t e = set_smem(kern, smem);
+  if (e != cudaSuccess) return e;
+  static int per_sm = 0;
+  if (per_sm == 0) {
+    int nb = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, threads, smem);
+    if (e != cudaSuccess) return e;
+    per_sm = nb > 0 ? nb : 1;
+  }
+  const long long items = (long long)count * (p.ny / 2 / 4 + 1);
+  const long long slots = (long long)col_pipe_device_sms() * per_sm;
+  const CUtensorMap map = *static_cast<const CUtensorMap*>(p.col_tmap);
+  return launch_maybe_pdl(p.pdl, kern, dim3((int)(items < slots ? items : slots)), dim3(threads),
+                          smem, s, mem, count, k, map);
+}
+
+static cudaError_t batch_col_tma_launch(const FvmParams& p, const FvmMember* mem, int count,
+                                        int k, cudaStream_t s) {
+  switch (p.log2nx) {
+    case 8: return batch_col_tma_impl<8>(p, mem, count, k, s);
+    case 9: return batch_col_tma_impl<9>(p, mem, count, k, s);
+    case 10: return batch_col_tma_impl<10>(p, mem, count, k, s);
+    default: return batch_col_tma_impl<11>(p, mem, count, k, s);
+  }
+}
+
 cudaError_t launch_fvm_batch_step(const FvmParams& p, const FvmMember* mem, int count, int k,
                                   cudaStream_t s) {
   if (!fvm_batch_shape_ok(p) || count < 1 || count > 65535) return cudaErrorInvalidValue;
@@ -2031,7 +2142,9 @@ cudaError_t launch_fvm_batch_step(const FvmParams& p, const FvmMember* mem, int 
   e = p.fft_shape == 1 ? batch_rows_impl<64, 14>(p, 64, mem, count, k, false, s)
                        : batch_rows_impl<256, 3>(p, 256, mem, count, k, false, s);
   if (e != cudaSuccess) return e;
-  if (p.col_mode == 3 && col_pipe_ok(p, 0)) e = batch_col_pipe_launch(p, mem, count, k, s);
+  if (p.col_mode == 5 && p.col_tmap && col_tma_grid_ok(p))
+    e = batch_col_tma_launch(p, mem, count, k, s);
+  else if (p.col_mode == 3 && col_pipe_ok(p, 0)) e = batch_col_pipe_launch(p, mem, count, k, s);
   else if (p.col_mode == 2 && col_cluster_ok(p, 8)) e = batch_col_cluster_impl<8>(p, mem, count, k, s);
   else if ((p.col_mode == 1 || p.col_mode == 2) && col_cluster_ok(p, 4))
     e = batch_col_cluster_impl<4>(p, mem, count, k, s);

@@ -54,8 +54,8 @@ struct FvmParams {
   int col_diag;        // column-pass diagonal: 0 pinv(lambda), 1 x / (1 - x), x = dtnu lambda
   float dtnu;          // float32(dt * viscosity) for col_diag = 1
   int pdl;             // launch the step's kernels as programmatic dependents
-  const void* col_tmap;  // HOST pointer to the plan's CUtensorMap of its spectrum
-  const void* col_tmap_spec;  // the spectrum buffer col_tmap describes
+  const void* col_tmap;  // HOST pointer to the CUtensorMap of the plan's spectrum (a batch's: 3-D, all slots)
+  const void* col_tmap_spec;  // the spectrum buffer col_tmap describes (single plans)
                          // (col_mode 5), or null
 };
 
