@@ -348,16 +348,17 @@ static int fvm_params_from_config(const cfd_fvm_config* cfg, cfd::FvmParams* out
 // boxes of 8 floats x min(nx, 256) rows x 1 spectrum.
 static bool encode_spec_map(CUtensorMap* map, float2* spec, int nx, int ny, int count = 1,
                             size_t member_floats = 0) {
-  static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
-  if (!encode) {
+  // Looked up once (a function-local static: thread-safe initialisation).
+  static const PFN_cuTensorMapEncodeTiled_v12000 encode = []() {
     void* fn = nullptr;
     cudaDriverEntryPointQueryResult q;
     if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault,
                                          &q) != cudaSuccess ||
-        q != cudaDriverEntryPointSuccess || !fn)
-      return false;
-    encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
-  }
+        q != cudaDriverEntryPointSuccess)
+      fn = nullptr;
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  }();
+  if (!encode) return false;
   const cuuint64_t dims[3] = {(cuuint64_t)ny, (cuuint64_t)nx, (cuuint64_t)count};
   const cuuint64_t strides[2] = {(cuuint64_t)ny * sizeof(float),
                                  (cuuint64_t)member_floats * sizeof(float)};
