@@ -505,6 +505,7 @@ def run_differentiation(dev, args):
 def run_gb300(args):
   import torch  # pylint: disable=import-outside-toplevel
   import jax_cfd_gb300.base as cfd  # pylint: disable=import-outside-toplevel
+  from jax_cfd_gb300 import plans  # pylint: disable=import-outside-toplevel
   from jax_cfd_gb300.spectral import equations as seq  # pylint: disable=import-outside-toplevel
   from jax_cfd_gb300.spectral import time_stepping as sts  # pylint: disable=import-outside-toplevel
 
@@ -681,12 +682,7 @@ def run_gb300(args):
                              f'{chunk} time steps per bench step',
                  'grid': [n, n], 'time_steps_per_step': chunk, 'dt': dt,
                  'l2': 'flushed (256 MiB write) between bench steps',
-                 'launch_config': {'row_blocks': ['wide', 'narrow'][shape & 1],
-                                   'column_pass': ['blocks', 'cluster4', 'cluster8',
-                                                   'pipelined4', 'pipelined2',
-                                                   'pipelined4_tma'][(shape >> 1) % 6],
-                                   'stencil': ['tiles', 'warp_streams'][(shape // 12) & 1],
-                                   'row_feed': ['registers', 'bulk_copy'][shape // 24]},
+                 'launch_config': plans.FvmPlan.describe_launch(shape),
                  'parallelism': 'replicas' if world > 1 else 'single'},
       'roofline': {'kernel': dominant, 'bound': 'hbm', 'achieved': achieved, 'peak': peak,
                    'unit': 'GB/s', 'frac': achieved / peak, 'traffic': traffic,

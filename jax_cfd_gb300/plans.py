@@ -193,6 +193,24 @@ class FvmPlan:
     return int(chosen.value)
 
   LAUNCH_CHOICES = 48
+  ROW_BLOCKS = ('wide', 'narrow')
+  COLUMN_PASSES = ('blocks', 'cluster4', 'cluster8', 'pipelined4', 'pipelined2',
+                   'pipelined4_tma')
+  STENCILS = ('tiles', 'warp_streams')
+  ROW_FEEDS = ('registers', 'bulk_copy')
+
+  @classmethod
+  def describe_launch(cls, choice: int) -> dict:
+    """Names of the parts of launch configuration `choice` (row block shape
+    + 2 * column-pass scheme + 12 * stencil scheme + 24 * row feed, the
+    index cfd_fvm_plan_autotune reports)."""
+    choice = int(choice)
+    if not 0 <= choice < cls.LAUNCH_CHOICES:
+      raise ValueError(f'launch choice {choice} outside [0, {cls.LAUNCH_CHOICES})')
+    return {'row_blocks': cls.ROW_BLOCKS[choice & 1],
+            'column_pass': cls.COLUMN_PASSES[(choice >> 1) % 6],
+            'stencil': cls.STENCILS[(choice // 12) & 1],
+            'row_feed': cls.ROW_FEEDS[choice // 24]}
 
   def set_launch(self, choice: int):
     """Pins the launch configuration (see autotune); results do not change."""
