@@ -298,3 +298,79 @@ def test_float32_oracle_close_to_float64():
   a, b = s32(v32), s64(v64)
   for x, y in zip(a, b):
     assert np.linalg.norm(x - y) / np.linalg.norm(y) < 1e-6
+
+
+# --- equations_test.py:84-163 (semi_implicit_sinusoidal_velocity_fast_diag) -
+def test_fast_diag_sinusoidal_divergence_and_momentum():
+  """convect_linear + classic_rk4 + solve_fast_diag on 100^2 for 1000 steps:
+  max divergence below 2e-3, momentum conserved to 2e-3."""
+  g = fvm.Grid.make((100, 100), step=(1., 1.))
+  v0 = sinusoidal_velocity_field(g)
+  step = fvm.semi_implicit_navier_stokes(1., 1e-4, 1e-3, g, convect='linear',
+                                         tableau=fvm.CLASSIC_RK4)
+  out = fvm.repeated(step, 1000)(v0)
+  assert np.max(fvm.divergence(out, g.step)) < 2e-3
+  momentum = lambda v: np.array(v).sum() * 1. * np.prod(g.step)
+  np.testing.assert_allclose(momentum(out), momentum(v0), atol=2e-3)
+
+
+# --- time_stepping_test.py:25-83 (explicit tableaux on a harmonic oscillator) -
+@pytest.mark.parametrize('tableau,atol', [
+    (fvm.FORWARD_EULER, 1e-2), (fvm.MIDPOINT_RK2, 3e-5), (fvm.HEUN_RK2, 3e-5),
+    (fvm.CLASSIC_RK4, 4e-7)])
+def test_explicit_tableaux_harmonic_oscillator(tableau, atol):
+  """x' = y, y' = -x through navier_stokes_rk with an identity projection
+  (ExplicitNavierStokesODE), dt 1e-2, 5 frames of 20 steps, against
+  r (sin(t + theta), cos(t + theta))."""
+  x0 = (np.float64(1.), np.float64(1.))
+  step = fvm.navier_stokes_rk(tableau, lambda x: (x[1], -x[0]), lambda x: x, 1e-2)
+  _, frames = fvm.trajectory(fvm.repeated(step, 20), 5)(x0)
+  times = 1e-2 * 20 * (1 + np.arange(5))
+  theta, r = np.arctan(x0[0] / x0[1]), np.hypot(*x0)
+  np.testing.assert_allclose(frames[0], r * np.sin(times + theta), atol=atol, rtol=0)
+  np.testing.assert_allclose(frames[1], r * np.cos(times + theta), atol=atol, rtol=0)
+
+
+# --- diffusion_test.py:44-56 (explicit diffusion of a constant) --------------
+def test_explicit_diffusion_of_constant_is_zero():
+  g = fvm.Grid.make((101, 101), step=(1., 1.))
+  np.testing.assert_allclose(1. * fvm.laplacian(np.ones(g.shape, np.float32), g.step), 0.,
+                             atol=1e-6)
+
+
+# --- initial_conditions_test.py:38-60 (2-D case) -----------------------------
+def test_filtered_velocity_field_divergence_free_at_target_speed():
+  """1024^2 on [0, 2 pi]^2, maximum velocity 10, peak wavenumber 17: max
+  divergence within 5e-4 of 0, maximum speed within 1e-5 of 10 (the
+  oracle's own noise stands in for the reference's PRNG key)."""
+  g = fvm.Grid.make((1024, 1024), domain=((0, 2 * np.pi), (0, 2 * np.pi)))
+  v = oic.filtered_velocity_field(2323, g, 10., 17)
+  assert abs(float(np.max(fvm.divergence(v, g.step)))) <= 5e-4
+  speed = np.linalg.norm(np.array(v), axis=0).max()
+  np.testing.assert_allclose(speed, 10., atol=1e-5)
+
+
+# --- spectral/equations_test.py:213-263 (forced turbulence, viscosity order) -
+def _spectral_initial_vorticity_hat(g):
+  v0 = oic.filtered_velocity_field(42, g, 7, 4)
+  return np.fft.rfftn(fvm.curl_2d(v0, g.step))
+
+
+def test_spectral_forced_turbulence_runs_without_nan():
+  g = fvm.Grid.make((128, 128), domain=((0, 2 * np.pi), (0, 2 * np.pi)))
+  eq = ospec.NavierStokes2D(1e-3, g, drag=0.1, forcing_fn=fvm.kolmogorov_forcing)
+  _, traj = fvm.trajectory(ospec.crank_nicolson_rk4(eq, 1e-5), 100)(
+      _spectral_initial_vorticity_hat(g))
+  assert not np.isnan(traj).any()
+
+
+def test_spectral_higher_viscosity_decays_faster():
+  g = fvm.Grid.make((128, 128), domain=((0, 2 * np.pi), (0, 2 * np.pi)))
+  w0 = _spectral_initial_vorticity_hat(g)
+  norms = []
+  for nu in (1e-3, 1e-1, 1.):
+    dt = fvm.stable_time_step(7, .5, nu, g, implicit_diffusion=True)
+    eq = ospec.NavierStokes2D(nu, g, drag=0.1, forcing_fn=fvm.kolmogorov_forcing)
+    _, traj = fvm.trajectory(ospec.crank_nicolson_rk4(eq, dt), 100)(w0)
+    norms.append(np.linalg.norm(traj))
+  assert norms[2] < norms[1] < norms[0]
