@@ -374,3 +374,29 @@ def test_spectral_higher_viscosity_decays_faster():
     _, traj = fvm.trajectory(ospec.crank_nicolson_rk4(eq, dt), 100)(w0)
     norms.append(np.linalg.norm(traj))
   assert norms[2] < norms[1] < norms[0]
+
+
+# --- spectral/equations_test.py:305-391 (spectral vs finite volume, 512^2) ---
+@pytest.mark.parametrize('forced,n_steps,atol', [(True, 150, 0.07), (False, 500, 0.09)])
+def test_spectral_agrees_with_finite_volume(forced, n_steps, atol):
+  """Van Leer FVM (semi_implicit_navier_stokes, forward Euler) and CN-RK4
+  spectral runs from the same filtered initial velocity (maximum speed 2,
+  default peak wavenumber), nu = 1e-2, dt at CFL 0.1: final vorticities
+  agree to atol after the (1, 1) roll between the curl's offset and the
+  spectral grid.  Forced: simple_turbulence_forcing(1, 4, -0.1) against
+  ForcedNavierStokes2D."""
+  g = fvm.Grid.make((512, 512), domain=((0, 2 * np.pi), (0, 2 * np.pi)))
+  v0 = oic.filtered_velocity_field(0, g, 2.0)
+  dt = fvm.stable_time_step(2.0, .1, 1e-2, g)
+  if forced:
+    f = fvm.simple_turbulence_forcing(g, 1, 4, -0.1, 'kolmogorov')
+    eq = ospec.forced_navier_stokes_2d(1e-2, g)
+  else:
+    f = None
+    eq = ospec.NavierStokes2D(1e-2, g, drag=0., smooth=True)
+  v = fvm.repeated(fvm.semi_implicit_navier_stokes(1.0, 1e-2, dt, g, forcing=f), n_steps)(v0)
+  w_fvm = fvm.curl_2d(v, g.step)
+  w_hat = np.fft.rfftn(np.roll(fvm.curl_2d(v0, g.step), (1, 1), axis=(0, 1)))
+  w_hat = fvm.repeated(ospec.crank_nicolson_rk4(eq, dt), n_steps)(w_hat)
+  w_spec = np.roll(np.fft.irfftn(w_hat, s=g.shape, axes=(0, 1)), (-1, -1), axis=(0, 1))
+  np.testing.assert_allclose(w_fvm, w_spec, atol=atol, rtol=0)
