@@ -356,10 +356,11 @@ def _spectral_initial_vorticity_hat(g):
   return np.fft.rfftn(fvm.curl_2d(v0, g.step))
 
 
-def test_spectral_forced_turbulence_runs_without_nan():
+@pytest.mark.parametrize('stepper', [ospec.crank_nicolson_rk4, ospec.crank_nicolson_rk3])
+def test_spectral_forced_turbulence_runs_without_nan(stepper):
   g = fvm.Grid.make((128, 128), domain=((0, 2 * np.pi), (0, 2 * np.pi)))
   eq = ospec.NavierStokes2D(1e-3, g, drag=0.1, forcing_fn=fvm.kolmogorov_forcing)
-  _, traj = fvm.trajectory(ospec.crank_nicolson_rk4(eq, 1e-5), 100)(
+  _, traj = fvm.trajectory(stepper(eq, 1e-5), 100)(
       _spectral_initial_vorticity_hat(g))
   assert not np.isnan(traj).any()
 
