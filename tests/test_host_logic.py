@@ -190,3 +190,44 @@ def test_launch_choice_names_follow_the_abi_encoding():
     P.describe_launch(P.LAUNCH_CHOICES)
   header = (ROOT / 'include' / 'cfd_gb300.h').read_text()
   assert f'{P.LAUNCH_CHOICES} choices' in header
+
+
+def _zero_velocity(grid):
+  from jax_cfd_gb300.base import boundaries, grids
+  offsets = (np.eye(2) + np.ones((2, 2))) / 2.
+  bc = boundaries.periodic_boundary_conditions(2)
+  return tuple(grids.GridVariable(grids.GridArray(torch.zeros(grid.shape), tuple(o), grid), bc)
+               for o in offsets)
+
+
+@pytest.mark.parametrize('name,kwargs', [
+    ('taylor_green_forcing', dict(scale=1.0, k=2)),
+    ('kolmogorov_forcing', dict(scale=1.0, k=2)),
+    ('linear_forcing', dict(coefficient=2.0)),
+    ('no_forcing', {}),
+    ('simple_turbulence_forcing', dict(constant_magnitude=0.0, constant_wavenumber=2,
+                                       linear_coefficient=0.0, forcing_type='kolmogorov')),
+])
+def test_forcing_offsets_and_grid_match_velocity(name, kwargs):
+  """forcings_test.py:39-79 (2-D): each forcing's components carry the
+  offset and grid of the velocity component they act on."""
+  from jax_cfd_gb300.base import forcings, grids
+  g = grids.Grid((16, 16))
+  v = _zero_velocity(g)
+  force = getattr(forcings, name)(g, **kwargs)(v)
+  for f, u in zip(force, v):
+    assert tuple(float(o) for o in f.offset) == tuple(float(o) for o in u.offset)
+    assert f.grid == u.grid
+    assert tuple(f.data.shape) == tuple(u.data.shape)
+    assert torch.equal(0 * f.data, u.data)
+
+
+def test_sum_forcings_with_no_forcing_is_exact():
+  """forcings_test.py:81-91."""
+  from jax_cfd_gb300.base import forcings, grids
+  g = grids.Grid((16, 16))
+  v = _zero_velocity(g)
+  f1 = forcings.kolmogorov_forcing(g, scale=1.0, k=2)
+  total = forcings.sum_forcings(f1, forcings.no_forcing(g))(v)
+  for a, b in zip(total, f1(v)):
+    assert torch.equal(a.data, b.data)
