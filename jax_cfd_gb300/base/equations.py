@@ -12,8 +12,6 @@ from __future__ import annotations
 
 from typing import Callable, Optional
 
-import torch
-
 from jax_cfd_gb300 import _native as nat
 from jax_cfd_gb300 import plans
 from jax_cfd_gb300.base import advection

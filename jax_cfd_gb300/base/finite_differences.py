@@ -5,7 +5,7 @@ kernels; the single-array differences are torch ops on the device.
 """
 from __future__ import annotations
 
-from typing import Optional, Sequence, Tuple
+from typing import Sequence, Tuple
 
 import numpy as np
 import torch

@@ -5,8 +5,6 @@ timed region, which must agree on every rank."""
 import os
 import socket
 
-import pytest
-import torch
 import torch.distributed as dist
 import torch.multiprocessing as mp
 
