@@ -171,8 +171,9 @@ struct cfd_fvm_plan {
   float* rk = nullptr;  // Runge-Kutta stage terms k_j (u, v), allocated on first use
   double dt = 0;        // the configuration's dt (double, as the reference's Python float)
   long long bytes = 0;
-  // Tensor map of the packed spectrum for the TMA-staged column pass.
-  alignas(64) CUtensorMap spec_map;
+  // Tensor map of the packed spectrum for the TMA-staged column pass (the
+  // type's own alignment; plans come from C++17 aligned new).
+  CUtensorMap spec_map;
 };
 
 // A batch of same-shape FVM trajectories ("slots"): one device table of
@@ -200,7 +201,7 @@ struct cfd_fvm_batch {
   int graph_chunk = -1;
   long long bytes = 0;
   // 3-D tensor map of every slot's spectrum for the TMA-staged column pass.
-  alignas(64) CUtensorMap spec_map;
+  CUtensorMap spec_map;
 };
 
 // Several batches (one per grid shape) stepped together: a chunk forks one

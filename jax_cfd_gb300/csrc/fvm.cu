@@ -1333,7 +1333,7 @@ CFD_D void div_rfft_row_warp(const FvmParams& p, int i, const float* __restrict_
                              const float* __restrict__ vs, float2* __restrict__ spec,
                              float2* tile) {
   const int lane = threadIdx.x & 31;
-  const int L = p.ny >> 1, mx = p.nx - 1, my = p.ny - 1;
+  const int L = p.ny >> 1, mx = p.nx - 1;
   const size_t ny = (size_t)p.ny;
   const float2* ua = reinterpret_cast<const float2*>(us + i * ny);
   const float2* ub = reinterpret_cast<const float2*>(us + ((i - 1) & mx) * ny);
