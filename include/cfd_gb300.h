@@ -51,7 +51,8 @@ typedef enum cfd_status {
   CFD_ERR_INVALID_ARGUMENT = 1, /* bad shape / size / pointer: ValueError */
   CFD_ERR_UNSUPPORTED = 2,      /* option outside the hot path: NotImplementedError */
   CFD_ERR_CUDA = 3,             /* CUDA runtime error: RuntimeError */
-  CFD_ERR_OUT_OF_MEMORY = 4     /* device allocation failed: MemoryError */
+  CFD_ERR_OUT_OF_MEMORY = 4,    /* device allocation failed: MemoryError */
+  CFD_ERR_DEVICE_FAULT = 5      /* a kernel's bounded wait ran out: DeviceFaultError */
 } cfd_status;
 
 /* Advection schemes (the `convect` argument). */
@@ -85,8 +86,17 @@ typedef struct cfd_fvm_plan cfd_fvm_plan;
 const char* cfd_last_error(void);
 /* Device-side fault word: non-zero after a kernel's bounded wait on an
  * asynchronous copy ran out (1 = bulk-copy wait); the kernel then skipped its
- * work instead of spinning.  clear != 0 resets it.  Synchronous. */
+ * work instead of spinning.  Every compiled unit of the library keeps its own
+ * word; this reports the first non-zero one, and clear != 0 resets them all.
+ * Synchronous.  No counterpart in the reference (it has no device code). */
 int cfd_device_fault(unsigned int* code, int clear);
+/* Exercises the give-up path of the bounded waits (no counterpart in the
+ * reference): launches one warp whose mbarrier wait can never complete (no
+ * copy issued, no arrival) with a limit of `polls` polls, synchronises the
+ * stream, and returns CFD_ERR_DEVICE_FAULT with the fault word set to 1 when
+ * the wait gave up as designed.  Nothing is left running on the GPU.  Leaves
+ * the fault word set: read and clear it with cfd_device_fault. */
+int cfd_bounded_wait_selftest(void* stream, int polls);
 int cfd_version(void);
 
 int cfd_fvm_plan_create(const cfd_fvm_config* cfg, cfd_fvm_plan** plan);
@@ -162,6 +172,19 @@ int cfd_fvm_divergence(cfd_fvm_plan* plan, void* stream, const float* u,
 int cfd_fvm_curl_2d(cfd_fvm_plan* plan, void* stream, const float* u,
                     const float* v, float* out);
 
+/* funcutils.trajectory(repeated(step, inner), frames, post_process,
+ * start_with_input) (funcutils.py:95-126) for the forward-Euler step, in one
+ * call with the frames kept on the device: `frames` chunks of `inner` steps
+ * run in place in (u_out, v_out) (which may alias u/v), and frame k -- the
+ * state after chunk k, or before it with start_with_input -- is written to
+ * frames_out + k * frame_size: CFD_FRAME_VELOCITY stores u then v (2 nx ny
+ * floats; post_process = identity), CFD_FRAME_VORTICITY stores curl_2d of
+ * the state (nx ny floats at offset (1, 1); post_process = curl_2d). */
+enum { CFD_FRAME_VELOCITY = 0, CFD_FRAME_VORTICITY = 1 };
+int cfd_fvm_trajectory(cfd_fvm_plan* plan, void* stream, const float* u, const float* v,
+                       int inner, int frames, int frame_kind, int start_with_input,
+                       float* frames_out, float* u_out, float* v_out);
+
 /* Pressure projection that allocates nothing -- no counterpart in the
  * reference.  For callers that cannot call cudaMalloc (while capturing into a
  * graph memory pool they do not own, under allocators that forbid allocation
@@ -170,10 +193,12 @@ int cfd_fvm_curl_2d(cfd_fvm_plan* plan, void* stream, const float* u,
  * twiddles, Laplacian eigenvalues) is a fixed __device__ array that every GPU
  * loading the library keeps until exit.  Limit: nx * ny <= 262144 (512 x 512),
  * sides powers of two in [4, 4096]; larger grids return
- * CFD_ERR_INVALID_ARGUMENT.  The first call on a device looks up the array's
- * device address (cudaGetSymbolAddress), so make that first call before any
- * stream capture.  All calls share the array: calls that overlap on the GPU
- * race and must be ordered by the caller.  u_out/v_out may alias u/v. */
+ * CFD_ERR_INVALID_ARGUMENT.  Every call looks up the array's device address
+ * in the current context (cudaGetSymbolAddress; the first lookup on a device
+ * loads the module, so make the first call before any stream capture).  All
+ * calls share the array and it keeps the last call's contents (each call
+ * rewrites everything it reads): calls that overlap on the GPU race and must
+ * be ordered by the caller.  u_out/v_out may alias u/v. */
 int cfd_fvm_projection_noalloc(void* stream, int nx, int ny, double hx,
                                double hy, const float* u, const float* v,
                                float* u_out, float* v_out);
@@ -231,6 +256,23 @@ int cfd_fvm_batch_autotune(cfd_fvm_batch* batch, void* stream, int steps, int* c
  * Results do not depend on it. */
 int cfd_fvm_batch_set_launch(cfd_fvm_batch* batch, int choice);
 
+/* Per-slot health after a chunk (no counterpart in the reference, whose only
+ * failure checks are NaN checks on the state in its tests,
+ * spectral/equations_test.py:137,166,233).  Every run ends with a reduction
+ * over the state of each slot that ran: flags (CFD_HEALTH_NONFINITE: a NaN or
+ * an infinity is present) and max_abs (largest magnitude among the finite
+ * values: the largest velocity component for FVM slots, the largest
+ * |vorticity spectrum| component for spectral slots).  Slots that did not run
+ * keep their record.  The record is device memory owned by the batch, valid
+ * once the run has completed on its stream. */
+typedef struct cfd_health {
+  unsigned int flags;
+  float max_abs;
+} cfd_health;
+enum { CFD_HEALTH_NONFINITE = 1 };
+/* Device pointer to the batch's `count` records. */
+int cfd_fvm_batch_health(cfd_fvm_batch* batch, const cfd_health** records);
+
 /* A ragged ensemble: members of any grid shapes, grouped into one batch per
  * (shape, step, convection).  cfd_fvm_ensemble_step advances every member by
  * `steps`; the batches run on forked streams (overlapping on the device), and
@@ -243,6 +285,8 @@ int cfd_fvm_ensemble_size(const cfd_fvm_ensemble* ens);
 int cfd_fvm_ensemble_batches(const cfd_fvm_ensemble* ens);
 int cfd_fvm_ensemble_state(cfd_fvm_ensemble* ens, int index, float** u,
                            float** v);
+/* Device pointer to member `index`'s health record (see cfd_health). */
+int cfd_fvm_ensemble_health(cfd_fvm_ensemble* ens, int index, const cfd_health** record);
 int cfd_fvm_ensemble_autotune(cfd_fvm_ensemble* ens, void* stream, int steps);
 int cfd_fvm_ensemble_step(cfd_fvm_ensemble* ens, void* stream, int steps,
                           int use_graph);
@@ -339,6 +383,8 @@ int cfd_spec_batch_set_slot(cfd_spec_batch* batch, int slot, const cfd_spec_conf
                             const cfd_spec_plan* forcing);
 int cfd_spec_batch_set_steps(cfd_spec_batch* batch, int slot, int steps);
 int cfd_spec_batch_run(cfd_spec_batch* batch, void* stream, int chunk, int use_graph);
+/* Device pointer to the batch's `count` health records (see cfd_health). */
+int cfd_spec_batch_health(cfd_spec_batch* batch, const cfd_health** records);
 
 
 #ifdef __cplusplus

@@ -16,14 +16,27 @@ CFD_ERR_INVALID_ARGUMENT = 1
 CFD_ERR_UNSUPPORTED = 2
 CFD_ERR_CUDA = 3
 CFD_ERR_OUT_OF_MEMORY = 4
+CFD_ERR_DEVICE_FAULT = 5
 
 CONVECT_VAN_LEER = 0
 CONVECT_LINEAR = 1
+
+HEALTH_NONFINITE = 1
+
+FRAME_VELOCITY = 0
+FRAME_VORTICITY = 1
 
 FORCE_NONE = 0
 FORCE_U_OF_Y = 1
 FORCE_V_OF_X = 2
 FORCE_FULL = 3
+
+
+
+class DeviceFaultError(RuntimeError):
+  """A kernel's bounded wait ran out: it skipped its work and recorded a code
+  in the device fault word (read it with ``device_fault``)."""
+
 
 _f32p = ctypes.POINTER(ctypes.c_float)
 _f64p = ctypes.POINTER(ctypes.c_double)
@@ -74,9 +87,12 @@ _SIGNATURES = {
     'cfd_fvm_pressure_solve': (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp]),
     'cfd_fvm_divergence': (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp]),
     'cfd_fvm_curl_2d': (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp]),
+    'cfd_fvm_trajectory': (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_int, ctypes.c_int,
+                                           ctypes.c_int, ctypes.c_int, _vp, _vp, _vp]),
     'cfd_fvm_projection_noalloc': (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                                    ctypes.c_double, _vp, _vp, _vp, _vp]),
     'cfd_device_fault': (ctypes.c_int, [ctypes.POINTER(ctypes.c_uint), ctypes.c_int]),
+    'cfd_bounded_wait_selftest': (ctypes.c_int, [_vp, ctypes.c_int]),
     'cfd_fvm_plan_set_launch': (ctypes.c_int, [_vp, ctypes.c_int]),
     'cfd_fvm_plan_get_launch': (ctypes.c_int, [_vp]),
     'cfd_fvm_step_rk': (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_int, ctypes.c_int,
@@ -106,6 +122,9 @@ _SIGNATURES = {
     'cfd_fvm_ensemble_state': (ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(_vp),
                                                ctypes.POINTER(_vp)]),
     'cfd_fvm_ensemble_autotune': (ctypes.c_int, [_vp, _vp, ctypes.c_int]),
+    'cfd_fvm_batch_health': (ctypes.c_int, [_vp, ctypes.POINTER(_vp)]),
+    'cfd_fvm_ensemble_health': (ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(_vp)]),
+    'cfd_spec_batch_health': (ctypes.c_int, [_vp, ctypes.POINTER(_vp)]),
     'cfd_fvm_ensemble_step': (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_int]),
     'cfd_energy_spectrum_shells': (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_double,
                                                    ctypes.c_double, ctypes.c_double, ctypes.c_int,
@@ -184,7 +203,16 @@ def check(rc: int, what: str = '') -> None:
     raise NotImplementedError(msg)
   if rc == CFD_ERR_OUT_OF_MEMORY:
     raise MemoryError(msg)
+  if rc == CFD_ERR_DEVICE_FAULT:
+    raise DeviceFaultError(msg)
   raise RuntimeError(msg)
+
+
+def device_fault(clear: bool = False) -> int:
+  """The device fault word (0: no bounded wait has run out); synchronous."""
+  code = ctypes.c_uint(0)
+  check(load().cfd_device_fault(ctypes.byref(code), int(bool(clear))), 'cfd_device_fault')
+  return int(code.value)
 
 
 def call(name: str, *args) -> None:

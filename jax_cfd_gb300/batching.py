@@ -32,18 +32,39 @@ from jax_cfd_gb300 import plans
 
 
 class _DeviceArray:
-  """A float32 device array owned by a native object, exposed to torch through
+  """A device array owned by a native object, exposed to torch through
   ``__cuda_array_interface__`` (zero copy); holds a reference to its owner."""
 
-  def __init__(self, owner, address: int, shape):
+  def __init__(self, owner, address: int, shape, typestr: str = '<f4'):
     self._owner = owner
     self.__cuda_array_interface__ = {
-        'shape': tuple(int(s) for s in shape), 'typestr': '<f4',
+        'shape': tuple(int(s) for s in shape), 'typestr': typestr,
         'data': (int(address), False), 'version': 2, 'strides': None}
 
 
-def _view(owner, address: int, shape, device) -> torch.Tensor:
-  return torch.as_tensor(_DeviceArray(owner, address, shape), device=device)
+def _view(owner, address: int, shape, device, typestr: str = '<f4') -> torch.Tensor:
+  return torch.as_tensor(_DeviceArray(owner, address, shape, typestr), device=device)
+
+
+# Host layout of the native per-slot health records (cfd_health).
+HEALTH_DTYPE = np.dtype([('flags', '<u4'), ('max_abs', '<f4')])
+
+
+def decode_health(raw) -> np.ndarray:
+  """Health records from their int32 [count, 2] image (device or host)."""
+  a = raw.cpu().numpy() if isinstance(raw, torch.Tensor) else np.asarray(raw)
+  a = np.ascontiguousarray(a, dtype=np.int32).reshape(-1, 2)
+  rec = np.empty(a.shape[0], HEALTH_DTYPE)
+  rec['flags'] = a[:, 0].view(np.uint32)
+  rec['max_abs'] = a[:, 1].view(np.float32)
+  return rec
+
+
+def _health_view(owner, fn, handle, count: int, device, *index) -> torch.Tensor:
+  """int32 [count, 2] device view of health records returned by `fn`."""
+  ptr = ctypes.c_void_p()
+  nat.check(fn(handle, *index, ctypes.byref(ptr)), getattr(fn, '__name__', 'health'))
+  return _view(owner, ptr.value, (count, 2), device, '<i4')
 
 
 class FvmBatch:
@@ -142,6 +163,21 @@ class FvmBatch:
     nat.check(self._lib.cfd_fvm_batch_set_launch(self._h, int(choice)),
               'cfd_fvm_batch_set_launch')
 
+  def health_device(self) -> torch.Tensor:
+    """The per-slot health records as an int32 [count, 2] device view
+    (flags, bits of max_abs), written at the end of every run for the slots
+    that ran; decode with ``decode_health``."""
+    if getattr(self, '_health', None) is None:
+      self._health = _health_view(self, self._lib.cfd_fvm_batch_health, self._h, self.count,
+                                  self.device)
+    return self._health
+
+  def health(self) -> np.ndarray:
+    """Host copy of the health records (ordered after the current stream's
+    work): ``flags`` (HEALTH_NONFINITE when the state holds a NaN or an
+    infinity) and ``max_abs`` (largest finite |u| or |v|)."""
+    return decode_health(self.health_device())
+
 
 class SpecBatch:
   """Slots of one grid shape running NavierStokes2D + a low-storage RK/CN
@@ -237,6 +273,17 @@ class SpecBatch:
     nat.check(self._lib.cfd_spec_batch_run(self._h, plans.current_stream_ptr(self.device),
                                            int(chunk), 1 if graph else 0), 'cfd_spec_batch_run')
 
+  def health_device(self) -> torch.Tensor:
+    """As FvmBatch.health_device; max_abs is the largest finite component of
+    the vorticity spectrum."""
+    if getattr(self, '_health', None) is None:
+      self._health = _health_view(self, self._lib.cfd_spec_batch_health, self._h, self.count,
+                                  self.device)
+    return self._health
+
+  def health(self) -> np.ndarray:
+    return decode_health(self.health_device())
+
 
 class FvmEnsemble:
   """Members of any grid shapes (``cfd_fvm_ensemble``); ``members`` are dicts
@@ -299,6 +346,14 @@ class FvmEnsemble:
                                               int(steps), 1 if graph else 0),
               'cfd_fvm_ensemble_step')
 
+  def health(self) -> np.ndarray:
+    """Health records of every member after its last step (see
+    FvmBatch.health), in member order."""
+    if getattr(self, '_health', None) is None:
+      self._health = [_health_view(self, self._lib.cfd_fvm_ensemble_health, self._h, 1,
+                                   self.device, i) for i in range(len(self))]
+    return decode_health(torch.cat(self._health))
+
   def autotune(self, steps: int = 10):
     nat.check(self._lib.cfd_fvm_ensemble_autotune(self._h, plans.current_stream_ptr(self.device),
                                                   int(steps)), 'cfd_fvm_ensemble_autotune')
@@ -345,6 +400,14 @@ class Ensemble:
 
   def advance(self, steps: int, graph: bool = True):
     self.native.step(steps, graph=graph)
+
+  def health(self) -> np.ndarray:
+    """Per-member health records after the last advance (flags, max_abs)."""
+    return self.native.health()
+
+  def finite(self) -> np.ndarray:
+    """Whether each member's velocity is free of NaN and infinity."""
+    return (self.health()['flags'] & nat.HEALTH_NONFINITE) == 0
 
   def autotune(self, steps: int = 10):
     self.native.autotune(steps)

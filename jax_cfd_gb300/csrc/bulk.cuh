@@ -1,10 +1,11 @@
 // Bulk asynchronous copies (the TMA's untiled cp.async.bulk) into shared
 // memory with mbarrier completion, and bounded waits.
 //
-// Every wait on an mbarrier gives up after kBulkWaitLimit polls: the kernel
-// then records the failure in g_cfd_device_fault (read by
-// cfd_device_fault()), waits once more, with the same limit, for the copies it
-// issued, and leaves without using the data.  Nothing spins without bound.
+// Every wait on an mbarrier gives up after a bounded number of polls
+// (kBulkWaitLimit unless the caller passes a smaller limit): the kernel then
+// records the failure in its unit's fault word (read by cfd_device_fault()),
+// waits once more, with the same limit, for the copies it issued, and leaves
+// without using the data.  Nothing spins without bound.
 #pragma once
 
 #include <stdint.h>
@@ -13,12 +14,30 @@
 
 namespace cfd {
 
-// Non-zero after a bounded wait ran out (the code of the first failure).  One
-// word per translation unit that includes this header (the library reads the
-// one of the unit that launches bulk-copy kernels).
+// Non-zero after a bounded wait ran out (the code of the first failure).
+// Without relocatable device code every translation unit that includes this
+// header has its own word; each unit registers a reader of its word when the
+// library loads, and read_device_fault() (kernels.h) consults all of them.
 static __device__ unsigned int g_cfd_device_fault = 0;
 constexpr unsigned int kFaultBulkWait = 1;
 constexpr int kBulkWaitLimit = 1 << 22;
+
+// Reads (and optionally clears) one translation unit's fault word.
+using FaultWordReader = cudaError_t (*)(unsigned int* code, bool clear);
+// Adds a reader to the library's list (faults.cu); returns true.
+bool register_fault_word(FaultWordReader reader);
+
+namespace {
+cudaError_t unit_device_fault(unsigned int* code, bool clear) {
+  cudaError_t e = cudaMemcpyFromSymbol(code, g_cfd_device_fault, sizeof(unsigned int));
+  if (e == cudaSuccess && clear) {
+    const unsigned int zero = 0;
+    e = cudaMemcpyToSymbol(g_cfd_device_fault, &zero, sizeof(unsigned int));
+  }
+  return e;
+}
+const bool g_unit_fault_registered = register_fault_word(&unit_device_fault);
+}  // namespace
 
 CFD_D uint32_t smem_addr(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -86,14 +105,14 @@ CFD_D bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   return done != 0;
 }
 
-// Bounded wait for phase `parity`; false if the limit ran out (recorded).
-CFD_D bool mbar_wait(uint64_t* bar, uint32_t parity) {
-  for (int k = 0; k < kBulkWaitLimit; ++k)
+// Bounded wait for phase `parity`; false if `limit` polls ran out (recorded).
+CFD_D bool mbar_wait(uint64_t* bar, uint32_t parity, int limit = kBulkWaitLimit) {
+  for (int k = 0; k < limit; ++k)
     if (mbar_try_wait(bar, parity)) return true;
   atomicCAS(&g_cfd_device_fault, 0u, kFaultBulkWait);
   // Give the copies in flight one more bounded chance to land before the
   // block leaves (their destination is this block's shared memory).
-  for (int k = 0; k < kBulkWaitLimit; ++k)
+  for (int k = 0; k < limit; ++k)
     if (mbar_try_wait(bar, parity)) break;
   return false;
 }

@@ -16,6 +16,8 @@
 #include "fft.cuh"
 #include "wfft.cuh"
 
+static_assert(sizeof(cfd_health) == sizeof(cfd::Health), "cfd_health layout");
+
 namespace {
 
 thread_local std::string g_last_error;
@@ -174,6 +176,7 @@ struct cfd_fvm_plan {
   // Tensor map of the packed spectrum for the TMA-staged column pass (the
   // type's own alignment; plans come from C++17 aligned new).
   CUtensorMap spec_map;
+  CUtensorMap spec_map2;  // the same with 4-float boxes (2-column groups)
 };
 
 // A batch of same-shape FVM trajectories ("slots"): one device table of
@@ -202,6 +205,7 @@ struct cfd_fvm_batch {
   long long bytes = 0;
   // 3-D tensor map of every slot's spectrum for the TMA-staged column pass.
   CUtensorMap spec_map;
+  cfd::Health* health = nullptr;  // per slot, written at the end of every chunk
 };
 
 // Several batches (one per grid shape) stepped together: a chunk forks one
@@ -243,6 +247,7 @@ struct cfd_spec_batch {
   cudaGraphExec_t exec = nullptr;
   int graph_chunk = -1;
   long long bytes = 0;
+  cfd::Health* health = nullptr;  // per slot, written at the end of every chunk
 };
 
 struct cfd_spec_plan {
@@ -348,7 +353,7 @@ static int fvm_params_from_config(const cfd_fvm_config* cfg, cfd::FvmParams* out
 // floats per complex value), spectrum z at spec + z * member_floats floats;
 // boxes of 8 floats x min(nx, 256) rows x 1 spectrum.
 static bool encode_spec_map(CUtensorMap* map, float2* spec, int nx, int ny, int count = 1,
-                            size_t member_floats = 0) {
+                            size_t member_floats = 0, int box_floats = 8) {
   // Looked up once (a function-local static: thread-safe initialisation).
   static const PFN_cuTensorMapEncodeTiled_v12000 encode = []() {
     void* fn = nullptr;
@@ -363,7 +368,7 @@ static bool encode_spec_map(CUtensorMap* map, float2* spec, int nx, int ny, int 
   const cuuint64_t dims[3] = {(cuuint64_t)ny, (cuuint64_t)nx, (cuuint64_t)count};
   const cuuint64_t strides[2] = {(cuuint64_t)ny * sizeof(float),
                                  (cuuint64_t)member_floats * sizeof(float)};
-  const cuuint32_t box[3] = {8, (cuuint32_t)(nx < 256 ? nx : 256), 1};
+  const cuuint32_t box[3] = {(cuuint32_t)box_floats, (cuuint32_t)(nx < 256 ? nx : 256), 1};
   const cuuint32_t estride[3] = {1, 1, 1};
   if (count > 1 && (member_floats * sizeof(float)) % 16 != 0) return false;
   return encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, count > 1 ? 3 : 2, spec, dims, strides,
@@ -457,6 +462,7 @@ int cfd_fvm_plan_create(const cfd_fvm_config* cfg, cfd_fvm_plan** out) {
     p.col_tmap = &plan->spec_map;
     p.col_tmap_spec = plan->spec;
     if (p.col_mode == 3) p.col_mode = 5;
+    if (encode_spec_map(&plan->spec_map2, plan->spec, nx, ny, 1, 0, 4)) p.col_tmap2 = &plan->spec_map2;
   }
   *out = plan;
   return CFD_OK;
@@ -498,6 +504,46 @@ int cfd_fvm_step(cfd_fvm_plan* plan, void* stream, const float* u,
     t = av; av = bv; bv = t;
   }
   CFD_CHECK(cfd::launch_fvm_project_out(p, au, av, q, u_out, v_out, s), "project_out");
+  return CFD_OK;
+}
+
+// funcutils.trajectory(repeated(step, inner), frames, post_process)
+// (funcutils.py:95-126) in one call: each chunk of `inner` steps runs in place
+// in (u_out, v_out) and its frame is written into frames_out on the device.
+int cfd_fvm_trajectory(cfd_fvm_plan* plan, void* stream, const float* u, const float* v,
+                       int inner, int frames, int frame_kind, int start_with_input,
+                       float* frames_out, float* u_out, float* v_out) {
+  if (!plan || !u || !v || !u_out || !v_out || (frames > 0 && !frames_out))
+    return fail(CFD_ERR_INVALID_ARGUMENT, "cfd_fvm_trajectory: null pointer");
+  if (inner < 0 || frames < 0)
+    return fail(CFD_ERR_INVALID_ARGUMENT, "cfd_fvm_trajectory: negative step or frame count");
+  if (frame_kind != CFD_FRAME_VELOCITY && frame_kind != CFD_FRAME_VORTICITY)
+    return fail(CFD_ERR_UNSUPPORTED, "cfd_fvm_trajectory: unknown frame kind");
+  cudaStream_t s = as_stream(stream);
+  const cfd::FvmParams& p = plan->p;
+  const size_t n = (size_t)p.nx * p.ny;
+  const size_t per_frame = frame_kind == CFD_FRAME_VELOCITY ? 2 * n : n;
+  auto write_frame = [&](int k, const float* fu, const float* fv) -> int {
+    float* dst = frames_out + (size_t)k * per_frame;
+    if (frame_kind == CFD_FRAME_VELOCITY) {
+      CFD_CHECK(cudaMemcpyAsync(dst, fu, n * sizeof(float), cudaMemcpyDeviceToDevice, s), "frame");
+      CFD_CHECK(cudaMemcpyAsync(dst + n, fv, n * sizeof(float), cudaMemcpyDeviceToDevice, s),
+                "frame");
+    } else {
+      CFD_CHECK(cfd::launch_curl2d(p, fu, fv, dst, s), "frame curl_2d");
+    }
+    return CFD_OK;
+  };
+  const float *cu = u, *cv = v;
+  for (int k = 0; k < frames; ++k) {
+    int rc;
+    if (start_with_input && (rc = write_frame(k, cu, cv))) return rc;
+    if ((rc = cfd_fvm_step(plan, stream, cu, cv, u_out, v_out, inner))) return rc;
+    cu = u_out;
+    cv = v_out;
+    if (!start_with_input && (rc = write_frame(k, u_out, v_out))) return rc;
+  }
+  if (frames == 0) return cfd_fvm_step(plan, stream, u, v, u_out, v_out, 0);
   return CFD_OK;
 }
 
@@ -803,7 +849,8 @@ static void batch_drop_graph(cfd_fvm_batch* b) {
 int cfd_fvm_batch_destroy(cfd_fvm_batch* b) {
   if (!b) return CFD_OK;
   batch_drop_graph(b);
-  void* ptrs[] = {b->slab, b->force, b->lamx, b->lamy, b->twy, b->twpx, b->twpy, b->dev};
+  void* ptrs[] = {b->slab, b->force, b->lamx, b->lamy, b->twy, b->twpx, b->twpy, b->dev,
+                  b->health};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   delete b;
@@ -836,6 +883,8 @@ int cfd_fvm_batch_create(const cfd_fvm_config* shape, int count, cfd_fvm_batch**
   if (e == cudaSuccess)
     e = cudaMalloc((void**)&b->force, (size_t)count * (nx + ny) * sizeof(float));
   if (e == cudaSuccess) e = cudaMalloc((void**)&b->dev, (size_t)count * sizeof(cfd::FvmMember));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&b->health, (size_t)count * sizeof(cfd::Health));
+  if (e == cudaSuccess) e = cudaMemset(b->health, 0, (size_t)count * sizeof(cfd::Health));
   std::vector<float> lamx = laplacian_eigenvalues(nx, shape->hx, nx);
   std::vector<float> lamy = laplacian_eigenvalues(ny, shape->hy, ny / 2 + 1);
   std::vector<float2> twy = twiddles(ny);
@@ -958,6 +1007,7 @@ static int batch_enqueue(cfd_fvm_batch* b, cudaStream_t s, int chunk) {
   for (int k = 0; k < chunk; ++k)
     CFD_CHECK(cfd::launch_fvm_batch_step(b->shape, b->dev, b->count, k, s), "batch step");
   CFD_CHECK(cfd::launch_fvm_batch_project_out(b->shape, b->dev, b->count, s), "batch project_out");
+  CFD_CHECK(cfd::launch_fvm_batch_health(b->shape, b->dev, b->count, b->health, s), "batch health");
   return CFD_OK;
 }
 
@@ -1183,6 +1233,20 @@ int cfd_fvm_ensemble_state(cfd_fvm_ensemble* ens, int index, float** u, float** 
     return fail(CFD_ERR_INVALID_ARGUMENT, "cfd_fvm_ensemble_state: bad arguments");
   const auto w = ens->where[index];
   return cfd_fvm_batch_state(ens->batches[w.first], w.second, u, v);
+}
+
+int cfd_fvm_batch_health(cfd_fvm_batch* b, const cfd_health** out) {
+  if (!b || !out) return fail(CFD_ERR_INVALID_ARGUMENT, "cfd_fvm_batch_health: null pointer");
+  *out = reinterpret_cast<const cfd_health*>(b->health);
+  return CFD_OK;
+}
+
+int cfd_fvm_ensemble_health(cfd_fvm_ensemble* ens, int index, const cfd_health** out) {
+  if (!ens || !out || index < 0 || index >= (int)ens->where.size())
+    return fail(CFD_ERR_INVALID_ARGUMENT, "cfd_fvm_ensemble_health: bad arguments");
+  const auto w = ens->where[index];
+  *out = reinterpret_cast<const cfd_health*>(ens->batches[w.first]->health + w.second);
+  return CFD_OK;
 }
 
 int cfd_fvm_ensemble_autotune(cfd_fvm_ensemble* ens, void* stream, int steps) {
@@ -1722,7 +1786,7 @@ static void spec_batch_drop_graph(cfd_spec_batch* b) {
 int cfd_spec_batch_destroy(cfd_spec_batch* b) {
   if (!b) return CFD_OK;
   spec_batch_drop_graph(b);
-  void* ptrs[] = {b->slab, b->twy, b->twpx, b->twpy, b->kx, b->ky, b->dev};
+  void* ptrs[] = {b->slab, b->twy, b->twpx, b->twpy, b->kx, b->ky, b->dev, b->health};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   delete b;
@@ -1750,6 +1814,8 @@ int cfd_spec_batch_create(const cfd_spec_config* shape, int count, cfd_spec_batc
   cudaError_t e = cudaMalloc((void**)&b->slab, (size_t)count * 7 * ns * sizeof(float2));
   if (e == cudaSuccess) e = cudaMemset(b->slab, 0, (size_t)count * 7 * ns * sizeof(float2));
   if (e == cudaSuccess) e = cudaMalloc((void**)&b->dev, (size_t)count * sizeof(cfd::SpecMember));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&b->health, (size_t)count * sizeof(cfd::Health));
+  if (e == cudaSuccess) e = cudaMemset(b->health, 0, (size_t)count * sizeof(cfd::Health));
   const SpecTables t = spec_tables(p);
   if (e == cudaSuccess) e = upload(&b->twy, t.twy.data(), t.twy.size());
   if (e == cudaSuccess) e = upload(&b->twpx, t.twpx.data(), t.twpx.size());
@@ -1793,6 +1859,12 @@ int cfd_spec_batch_state(cfd_spec_batch* b, int slot, float** w) {
   if (!b || !w || slot < 0 || slot >= b->count)
     return fail(CFD_ERR_INVALID_ARGUMENT, "cfd_spec_batch_state: bad arguments");
   *w = reinterpret_cast<float*>(b->host[slot].w);
+  return CFD_OK;
+}
+
+int cfd_spec_batch_health(cfd_spec_batch* b, const cfd_health** out) {
+  if (!b || !out) return fail(CFD_ERR_INVALID_ARGUMENT, "cfd_spec_batch_health: null pointer");
+  *out = reinterpret_cast<const cfd_health*>(b->health);
   return CFD_OK;
 }
 
@@ -1855,6 +1927,7 @@ static int spec_batch_enqueue(cfd_spec_batch* b, cudaStream_t s, int chunk) {
       CFD_CHECK(cfd::launch_spec_batch_update(p, b->dev, b->count, k, st, s), "batch update");
       CFD_CHECK(cfd::launch_spec_batch_prep(p, b->dev, b->count, k, st, s), "batch prep");
     }
+  CFD_CHECK(cfd::launch_spec_batch_health(p, b->dev, b->count, b->health, s), "batch health");
   return CFD_OK;
 }
 

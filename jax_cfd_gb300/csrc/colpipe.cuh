@@ -95,7 +95,11 @@ CFD_D void col_pipe_tables(float2* sbuf, const float2* __restrict__ twp,
 // (it contains barriers).
 // LDG: twp is the global table (else a shared copy).  A thread with
 // active == false computes nothing but takes part in every barrier.
-template <int LOG2N, int SIGN, int FIRST, bool LDG = !col_pipe_smem_tables<LOG2N>()>
+// SINGLE: buf[0] == buf[1] (one exchange buffer per column); every write
+// then also waits for the block's previous reads of the buffer (one more
+// barrier per exchange, half the shared memory).
+template <int LOG2N, int SIGN, int FIRST, bool LDG = !col_pipe_smem_tables<LOG2N>(),
+          bool SINGLE = false>
 CFD_D void col_pipe_fft(float2 (&v)[16], float2* const (&buf)[2], int t,
                         const float2* __restrict__ twp, bool active = true) {
   using P = ColPipe<LOG2N>;
@@ -117,6 +121,7 @@ CFD_D void col_pipe_fft(float2 (&v)[16], float2* const (&buf)[2], int t,
     if (q > 0) tw_off += 15 << (4 * q);
     const bool last = q == P::N16 - 1 && P::REM == 0;
     if (!last) {
+      if (SINGLE) __syncthreads();
       if (active) {
         float2* out = buf[wsel];
         const int o = ((t - k) << 4) + k;

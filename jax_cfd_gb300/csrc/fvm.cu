@@ -258,6 +258,21 @@ CFD_D float2 add_diffusion_forcing(const FvmParams& p, float2 kk, float2 uv, flo
   return kk;
 }
 
+// add_diffusion_forcing<1> with the Kolmogorov table value fu_y[j] passed in
+// (loaded once per column by the streaming kernels): the same expressions.
+template <int FORCE>
+CFD_D float2 add_diffusion_forcing_fu(const FvmParams& p, float2 kk, float2 uv, float2 lx,
+                                      float2 ly, float fuy) {
+  static_assert(FORCE == 1, "simple_turbulence_forcing configuration only");
+  const float2 m2 = mul2(splat2(-2.f), uv);
+  float2 lap = fma2(lx, splat2(p.sx), mul2(m2, splat2(p.ssum)));
+  lap = fma2(ly, splat2(p.sy), lap);
+  kk = fma2(splat2(p.nu), lap, kk);
+  const float fu = p.lin * uv.x + fuy;
+  const float fv = p.lin * uv.y;
+  return make_float2(kk.x + fu, kk.y + fv);
+}
+
 // Whether FORCE = 1 applies.
 CFD_HD bool kolmogorov_config(const FvmParams& p) {
   return p.has_visc && p.has_forcing && p.has_lin && p.fu_y && !p.fv_x && !p.fu_full &&
@@ -568,6 +583,173 @@ CFD_D void explicit_stream_body(const FvmParams& p, int bx, const float* __restr
     CFD_STREAM_ROW(3, 0)
   }
 #undef CFD_STREAM_ROW
+}
+
+// ---- Paired-column warp streams ---------------------------------------------
+// As explicit_stream_body with two adjacent columns per lane: lane L holds
+// columns jl = j0 - 2 + 2L and jl + 1 (j0 = 60 s for strip s), so a warp
+// covers 64 columns of which lanes 1..30 produce 60.  Rows are fetched as
+// float2 pairs (jl is even, so the pairs are 8-byte aligned), results stored
+// as float2 pairs, and a lane's second column takes its left neighbour, its
+// x-face velocity and its left y-face flux from the lane's own first column:
+// half the shuffles and a third of the loads per cell of one column per lane.
+// Each column evaluates exactly the expressions of stream_row.
+constexpr int kSW2 = 60;
+
+struct StreamRaw2 {
+  float2 u, v, q;  // columns (jl, jl + 1)
+  float qr;        // q at column jl + 2
+};
+
+template <bool PROJECT>
+CFD_D StreamRaw2 stream2_fetch(const FvmParams& p, const float* __restrict__ ua,
+                               const float* __restrict__ va, const float* __restrict__ q,
+                               int row, int j, int jr) {
+  const unsigned base = (unsigned)(row & (p.nx - 1)) << p.log2ny;
+  StreamRaw2 r;
+  r.u = __ldg(reinterpret_cast<const float2*>(ua + base + j));
+  r.v = __ldg(reinterpret_cast<const float2*>(va + base + j));
+  r.q = PROJECT ? __ldg(reinterpret_cast<const float2*>(q + base + j)) : make_float2(0.f, 0.f);
+  r.qr = PROJECT ? __ldg(q + base + jr) : 0.f;
+  return r;
+}
+
+// Projected (u, v) of both columns; qn: q of the next row.
+template <bool PROJECT>
+CFD_D void stream2_project(const FvmParams& p, const StreamRaw2& r, float2 qn, float2& a,
+                           float2& b) {
+  if (!PROJECT) {
+    a = make_float2(r.u.x, r.v.x);
+    b = make_float2(r.u.y, r.v.y);
+    return;
+  }
+  a = make_float2(r.u.x - (qn.x - r.q.x) * p.inv_hx, r.v.x - (r.q.y - r.q.x) * p.inv_hy);
+  b = make_float2(r.u.y - (qn.y - r.q.y) * p.inv_hx, r.v.y - (r.qr - r.q.y) * p.inv_hy);
+}
+
+// Window of projected rows for both columns: w1 = row i - 1, w2 = row i,
+// w3 = row i + 1 (A: column jl, B: column jl + 1).
+struct Window2 {
+  float2 a1, a2, a3, b1, b2, b3;
+  float2 fxa, fxb;  // x-face fluxes after row i - 1
+};
+
+template <bool PROJECT, int CONVECT, int FORCE>
+CFD_D void stream2_row(const FvmParams& p, int i, int jA, bool out, float2 fuy, Window2& w,
+                       const float2 a4, const float2 b4, float* __restrict__ uo,
+                       float* __restrict__ vo) {
+  const float2 ihx = splat2(p.inv_hx), ihy = splat2(p.inv_hy);
+  // Row i of the neighbours: left lane's column B, right lane's columns A, B.
+  const float2 lb = shfl_up2(w.b2, 1), ra = shfl_down2(w.a2, 1), rb = shfl_down2(w.b2, 1);
+  // x-faces after row i.
+  const float2 fxa = stream_xface<CONVECT>(p, w.a1, w.a2, w.a3, a4, w.b2.x);
+  const float2 fxb = stream_xface<CONVECT>(p, w.b1, w.b2, w.b3, b4, ra.x);
+  // y-faces after columns jl and jl + 1 (stencils jl-1 .. jl+2, jl .. jl+3).
+  const float2 Va = mul2(splat2(0.5f), add2(splat2(w.a2.y), make_float2(w.a3.y, w.b2.y)));
+  const float2 Vb = mul2(splat2(0.5f), add2(splat2(w.b2.y), make_float2(w.b3.y, ra.y)));
+  float2 fya, fyb;
+  if (CONVECT == 0) {
+    fya = tvd_flux2(lb, w.a2, w.b2, ra, Va, p.cfl_y);
+    fyb = tvd_flux2(w.a2, w.b2, ra, rb, Vb, p.cfl_y);
+  } else {
+    const float2 ca = mul2(splat2(0.5f), add2(w.a2, w.b2));
+    const float2 cb = mul2(splat2(0.5f), add2(w.b2, ra));
+    fya = mul2(make_float2(ca.x, Va.y), make_float2(Va.x, Va.y));
+    fyb = mul2(make_float2(cb.x, Vb.y), make_float2(Vb.x, Vb.y));
+  }
+  const float2 fy_left = shfl_up2(fyb, 1);
+  if (out) {
+    const size_t at = ((size_t)i << p.log2ny) + jA;
+    float2 ka = fma2(sub2(fya, fy_left), ihy, mul2(sub2(fxa, w.fxa), ihx));
+    float2 kb = fma2(sub2(fyb, fya), ihy, mul2(sub2(fxb, w.fxb), ihx));
+    ka = make_float2(-ka.x, -ka.y);
+    kb = make_float2(-kb.x, -kb.y);
+    if (FORCE == 1) {
+      ka = add_diffusion_forcing_fu<1>(p, ka, w.a2, add2(w.a1, w.a3), add2(lb, w.b2), fuy.x);
+      kb = add_diffusion_forcing_fu<1>(p, kb, w.b2, add2(w.b1, w.b3), add2(w.a2, ra), fuy.y);
+    } else {
+      ka = add_diffusion_forcing<FORCE>(p, ka, w.a2, add2(w.a1, w.a3), add2(lb, w.b2), i, jA);
+      kb = add_diffusion_forcing<FORCE>(p, kb, w.b2, add2(w.b1, w.b3), add2(w.a2, ra), i,
+                                        jA + 1);
+    }
+    const float2 na = fma2(splat2(p.dt), ka, w.a2), nb = fma2(splat2(p.dt), kb, w.b2);
+    *reinterpret_cast<float2*>(uo + at) = make_float2(na.x, nb.x);
+    *reinterpret_cast<float2*>(vo + at) = make_float2(na.y, nb.y);
+  }
+  w.fxa = fxa;
+  w.fxb = fxb;
+  w.a1 = w.a2;
+  w.a2 = w.a3;
+  w.a3 = a4;
+  w.b1 = w.b2;
+  w.b2 = w.b3;
+  w.b3 = b4;
+}
+
+// bx: the block's index among the (ny / 60) x (nx / SH) / 4 blocks of a grid;
+// each warp walks SH rows of its strip with rows fetched PF ahead (a ring of
+// PF raw rows in registers).
+template <bool PROJECT, int CONVECT, int FORCE, int SH, int PF>
+CFD_D void explicit_stream2_body(const FvmParams& p, int bx, const float* __restrict__ ua,
+                                 const float* __restrict__ va, const float* __restrict__ q,
+                                 float* __restrict__ uo, float* __restrict__ vo) {
+  static_assert(SH % PF == 0, "rows per warp must be a multiple of the prefetch depth");
+  const int lane = threadIdx.x & 31;
+  const int warp = (int)((bx * blockDim.x + threadIdx.x) >> 5);
+  const int strips = (p.ny + kSW2 - 1) / kSW2;
+  const int s = warp % strips, t = warp / strips;
+  const int r0 = t * SH;
+  if (r0 >= p.nx) return;  // uniform per warp
+  const int my = p.ny - 1;
+  const int jl = s * kSW2 - 2 + 2 * lane;  // unwrapped first column of this lane
+  const int j = jl & my, jr = (jl + 2) & my;
+  const bool out = lane >= 1 && lane < 31 && jl < p.ny;
+  const float2 fuy = FORCE == 1 ? __ldg(reinterpret_cast<const float2*>(p.fu_y + j))
+                                : make_float2(0.f, 0.f);
+
+  // Window rows r0-2 .. r0+1 (projected), ring of raw rows r0+2 .. r0+PF+1.
+  const StreamRaw2 rm2 = stream2_fetch<PROJECT>(p, ua, va, q, r0 - 2, j, jr);
+  const StreamRaw2 rm1 = stream2_fetch<PROJECT>(p, ua, va, q, r0 - 1, j, jr);
+  const StreamRaw2 rz0 = stream2_fetch<PROJECT>(p, ua, va, q, r0, j, jr);
+  const StreamRaw2 rp1 = stream2_fetch<PROJECT>(p, ua, va, q, r0 + 1, j, jr);
+  StreamRaw2 ring[PF];
+#pragma unroll
+  for (int k = 0; k < PF; ++k) ring[k] = stream2_fetch<PROJECT>(p, ua, va, q, r0 + 2 + k, j, jr);
+  Window2 w;
+  float2 a0, b0;
+  stream2_project<PROJECT>(p, rm2, rm1.q, a0, b0);
+  stream2_project<PROJECT>(p, rm1, rz0.q, w.a1, w.b1);
+  stream2_project<PROJECT>(p, rz0, rp1.q, w.a2, w.b2);
+  stream2_project<PROJECT>(p, rp1, ring[0].q, w.a3, w.b3);
+  {
+    // x-faces after row r0 - 1.
+    const float2 ra1 = shfl_down2(w.a1, 1);
+    w.fxa = stream_xface<CONVECT>(p, a0, w.a1, w.a2, w.a3, w.b1.x);
+    w.fxb = stream_xface<CONVECT>(p, b0, w.b1, w.b2, w.b3, ra1.x);
+  }
+  // Row i projects row i + 2 (ring slot K, q of row i + 3 from slot K + 1, or
+  // from slot 0 already refilled) and refills slot K with row i + 2 + PF.
+#pragma unroll 1
+  for (int a = 0; a < SH; a += PF) {
+#pragma unroll
+    for (int K = 0; K < PF; ++K) {
+      const int i = r0 + a + K;
+      float2 a4, b4;
+      stream2_project<PROJECT>(p, ring[K], ring[(K + 1) % PF].q, a4, b4);
+      ring[K] = stream2_fetch<PROJECT>(p, ua, va, q, i + 2 + PF, j, jr);
+      stream2_row<PROJECT, CONVECT, FORCE>(p, i, j, out, fuy, w, a4, b4, uo, vo);
+    }
+  }
+}
+
+template <bool PROJECT, int CONVECT, int FORCE, int SH, int PF, int MINB>
+__global__ void __launch_bounds__(128, MINB)
+    fvm_explicit_stream2_kernel(FvmParams p, const float* __restrict__ ua,
+                                const float* __restrict__ va, const float* __restrict__ q,
+                                float* __restrict__ uo, float* __restrict__ vo) {
+  pdl_wait();
+  pdl_trigger();
+  explicit_stream2_body<PROJECT, CONVECT, FORCE, SH, PF>(p, blockIdx.x, ua, va, q, uo, vo);
 }
 
 template <bool PROJECT, int CONVECT, int FORCE>
@@ -1078,6 +1260,89 @@ __global__ void __launch_bounds__(4 * (1 << LOG2N) / 16, col_pipe_min_blocks(4 *
     for (int m = 0; m < 16; ++m)
       v[m] = c_scale(v[m], pinv_diag_at(p, lamx[t + P::NTHR * m], cp));
     col_pipe_fft<LOG2N, 1, INV_FIRST>(v, buf, t, tw);
+    col_pipe_store<LOG2N, CG>(spec, L, g, w, t, v);
+  }
+}
+
+// The TMA-staged persistent column pass with CG columns per group and one
+// exchange buffer per column (SINGLE): half the shared memory of
+// fvm_col_pinv_tma_kernel per column, so that two blocks share a
+// multiprocessor and one block's barriers and exchanges overlap the other's
+// arithmetic.  Boxes are 2 CG floats x 256 rows (tensor map `tmap` encoded
+// with that box); transforms, staging layout and bits as the 4-column pass.
+template <int LOG2N, int CG>
+CFD_HD size_t col_tma_single_smem() {
+  return ((size_t)CG * col_pipe_bstride<LOG2N, CG>() + (size_t)CG * (1 << LOG2N)) *
+             sizeof(float2) +
+         (col_pipe_smem_tables<LOG2N>()
+              ? (size_t)fft_pass_table_size(LOG2N) * sizeof(float2) +
+                    (size_t)(1 << LOG2N) * sizeof(float)
+              : 0);
+}
+
+template <int LOG2N, int CG>
+__global__ void __launch_bounds__(CG * (1 << LOG2N) / 16, CG <= 2 ? 2 : 1)
+    fvm_col_pinv_tma1_kernel(FvmParams p, float2* __restrict__ spec,
+                             const __grid_constant__ CUtensorMap tmap) {
+  using P = ColPipe<LOG2N>;
+  constexpr int N = P::N, BOX = N < 256 ? N : 256, NBOX = N / BOX;
+  constexpr uint32_t kGroupBytes = (uint32_t)N * CG * sizeof(float2);
+  extern __shared__ float2 sbuf[];  // no static shared memory: 128-byte aligned
+  const int L = p.ny >> 1, groups = L / CG + 1;
+  const int w = threadIdx.x % CG, t = threadIdx.x / CG;
+  const int bstride = col_pipe_bstride<LOG2N, CG>();
+  float2* const buf[2] = {sbuf + w * bstride, sbuf + w * bstride};
+  float2* const stage = sbuf + CG * bstride;
+  // The tables follow the staging slots (col_pipe_tables' layout with one
+  // buffer set): place them by hand.
+  float2* const tw_s = stage + CG * N;
+  float* const tab_s = reinterpret_cast<float*>(tw_s + fft_pass_table_size(LOG2N));
+  uint64_t* const bar =
+      reinterpret_cast<uint64_t*>(reinterpret_cast<char*>(sbuf) + col_tma_single_smem<LOG2N, CG>());
+  constexpr int INV_FIRST = (P::PASSES - 1) & 1;
+  int g = blockIdx.x;
+  if (g >= groups) return;  // uniform per block
+  const float2* tw = p.twp_x;
+  const float* lamx = p.lamx;
+  if (col_pipe_smem_tables<LOG2N>()) {
+    const int ntw = fft_pass_table_size(LOG2N);
+    for (int i = threadIdx.x; i < ntw; i += blockDim.x) tw_s[i] = __ldg(p.twp_x + i);
+    for (int i = threadIdx.x; i < N; i += blockDim.x) tab_s[i] = __ldg(p.lamx + i);
+    tw = tw_s;
+    lamx = tab_s;
+  }
+  if (threadIdx.x == 0) {
+    mbar_init(bar, 1);
+    mbar_fence_init();
+  }
+  __syncthreads();
+  pdl_wait();
+  pdl_trigger();
+  auto issue = [&](int gg) {
+    const int x = gg * CG >= L ? 0 : 2 * CG * gg;
+    mbar_arrive_expect_tx(bar, kGroupBytes);
+#pragma unroll
+    for (int b = 0; b < NBOX; ++b) tma_load_2d(stage + b * BOX * CG, &tmap, x, b * BOX, bar);
+  };
+  if (threadIdx.x == 0) issue(g);
+  uint32_t phase = 0;
+  float2 v[16];
+#pragma unroll 1
+  for (; g < groups; g += gridDim.x) {
+    const bool landed = mbar_wait(bar, phase);
+    phase ^= 1u;
+    if (landed) col_pipe_take<LOG2N, CG>(stage, L, g, w, t, v);
+    if (__syncthreads_or(!landed)) return;
+    if (threadIdx.x == 0 && g + gridDim.x < groups) {
+      fence_proxy_async_smem();
+      issue(g + gridDim.x);
+    }
+    col_pipe_fft<LOG2N, -1, 0, !col_pipe_smem_tables<LOG2N>(), true>(v, buf, t, tw);
+    const int cp = g * CG >= L ? L : g * CG + w;  // pinv column index
+#pragma unroll
+    for (int m = 0; m < 16; ++m)
+      v[m] = c_scale(v[m], pinv_diag_at(p, lamx[t + P::NTHR * m], cp));
+    col_pipe_fft<LOG2N, 1, INV_FIRST, !col_pipe_smem_tables<LOG2N>(), true>(v, buf, t, tw);
     col_pipe_store<LOG2N, CG>(spec, L, g, w, t, v);
   }
 }
@@ -1655,7 +1920,27 @@ template <bool PR, bool K0, int CV, int FO>
 static void launch_explicit_variant(const FvmParams& p, bool stream, bool tiled, dim3 grid,
                                     const float* ua, const float* va, const float* q,
                                     float* uo, float* vo, cudaStream_t s) {
-  if (stream) {
+  static const int stream2 = getenv("CFD_GB300_STREAM2") ? atoi(getenv("CFD_GB300_STREAM2")) : 0;
+  const long long strips2 = (p.ny + kSW2 - 1) / kSW2;
+#define CFD_S2(SH, PF, MB)                                                                  \
+  launch_maybe_pdl(p.pdl, fvm_explicit_stream2_kernel<PR, CV, FO, SH, PF, MB>,             \
+                   dim3((int)((strips2 * ((p.nx + SH - 1) / SH) + 3) / 4)), dim3(128), 0, s, \
+                   p, ua, va, q, uo, vo)
+  if (stream && stream2 == 1 && p.nx % 32 == 0) {
+    CFD_S2(32, 4, 1);
+  } else if (stream && stream2 == 2 && p.nx % 16 == 0) {
+    CFD_S2(16, 4, 1);
+  } else if (stream && stream2 == 3 && p.nx % 16 == 0) {
+    CFD_S2(16, 2, 1);
+  } else if (stream && stream2 == 4 && p.nx % 16 == 0) {
+    CFD_S2(16, 2, 8);
+  } else if (stream && stream2 == 5 && p.nx % 32 == 0) {
+    CFD_S2(32, 2, 1);
+  } else if (stream && stream2 == 6 && p.nx % 16 == 0) {
+    CFD_S2(16, 4, 8);
+  } else if (stream && stream2 == 7 && p.nx % 8 == 0) {
+    CFD_S2(8, 2, 8);
+  } else if (stream) {
     const long long warps = (long long)((p.ny + kSW - 1) / kSW) * ((p.nx + kSH - 1) / kSH);
     launch_maybe_pdl(p.pdl, fvm_explicit_stream_kernel<PR, CV, FO>, dim3((int)((warps + 3) / 4)),
                      dim3(128), 0, s, p, ua, va, q, uo, vo);
@@ -1665,6 +1950,7 @@ static void launch_explicit_variant(const FvmParams& p, bool stream, bool tiled,
   } else {
     fvm_explicit_kernel<PR, K0, CV><<<grid, kStencilThreads, 0, s>>>(p, ua, va, q, uo, vo);
   }
+#undef CFD_S2
 }
 
 cudaError_t launch_fvm_explicit(const FvmParams& p, bool project, bool out_k0,
@@ -1840,7 +2126,27 @@ static cudaError_t col_pinv_tma_impl(const FvmParams& p, float2* spec, cudaStrea
                           s, p, spec, map);
 }
 
+template <int LOG2N, int CG>
+static cudaError_t col_pinv_tma1_impl(const FvmParams& p, float2* spec, cudaStream_t s) {
+  const size_t smem = col_tma_single_smem<LOG2N, CG>() + 16;  // + the mbarrier
+  const int threads = CG * (1 << LOG2N) / 16;
+  auto kern = fvm_col_pinv_tma1_kernel<LOG2N, CG>;
+  cudaError_t e = set_smem(kern, smem);
+  if (e != cudaSuccess) return e;
+  int nb = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, threads, smem);
+  if (e != cudaSuccess) return e;
+  const int groups = p.ny / 2 / CG + 1;
+  const int slots = col_pipe_device_sms() * (nb > 0 ? nb : 1);
+  const CUtensorMap map = *static_cast<const CUtensorMap*>(p.col_tmap2);
+  return launch_maybe_pdl(p.pdl, kern, dim3(groups < slots ? groups : slots), dim3(threads), smem,
+                          s, p, spec, map);
+}
+
 static cudaError_t col_pinv_tma_launch(const FvmParams& p, float2* spec, cudaStream_t s) {
+  static const int tma1 = getenv("CFD_GB300_COLTMA1") ? atoi(getenv("CFD_GB300_COLTMA1")) : 0;
+  if (tma1 == 1 && p.col_tmap2 && p.log2nx == 11) return col_pinv_tma1_impl<11, 2>(p, spec, s);
+  if (tma1 == 2 && p.log2nx == 11) return col_pinv_tma1_impl<11, 4>(p, spec, s);
   switch (p.log2nx) {
     case 8: return col_pinv_tma_impl<8>(p, spec, s);
     case 9: return col_pinv_tma_impl<9>(p, spec, s);
@@ -1963,15 +2269,6 @@ cudaError_t launch_max_speed(int n, const float* u, const float* v,
 }
 
 bool stream_stencil_ok(const FvmParams& p) { return stream_ok(p); }
-
-cudaError_t read_device_fault(unsigned int* code, bool clear) {
-  cudaError_t e = cudaMemcpyFromSymbol(code, g_cfd_device_fault, sizeof(unsigned int));
-  if (e == cudaSuccess && clear) {
-    const unsigned int zero = 0;
-    e = cudaMemcpyToSymbol(g_cfd_device_fault, &zero, sizeof(unsigned int));
-  }
-  return e;
-}
 
 bool bulk_feed_ok(const FvmParams& p) {
   // Whole rows move by bulk copies: 16-byte multiples, and the staged rows of

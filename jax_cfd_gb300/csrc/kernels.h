@@ -55,6 +55,7 @@ struct FvmParams {
   float dtnu;          // float32(dt * viscosity) for col_diag = 1
   int pdl;             // launch the step's kernels as programmatic dependents
   const void* col_tmap;  // HOST pointer to the CUtensorMap of the plan's spectrum (a batch's: 3-D, all slots)
+  const void* col_tmap2;  // HOST pointer: the same spectrum with 4-float boxes (single plans)
   const void* col_tmap_spec;  // the spectrum buffer col_tmap describes (single plans)
                          // (col_mode 5), or null
 };
@@ -110,6 +111,18 @@ cudaError_t launch_fvm_batch_step(const FvmParams& shape, const FvmMember* membe
                                   int count, int k, cudaStream_t s);
 cudaError_t launch_fvm_batch_project_out(const FvmParams& shape, const FvmMember* members,
                                          int count, cudaStream_t s);
+// Health record of one batch slot after a chunk (layout of the C ABI's
+// cfd_health): flags (kHealthNonFinite: the state holds a NaN or an
+// infinity) and the largest magnitude among the state's finite values.
+struct Health {
+  unsigned int flags;
+  float max_abs;
+};
+constexpr unsigned int kHealthNonFinite = 1u;
+// Health of every member that ran in the chunk (steps > 0), written to
+// h[slot]; members that did not run keep their record.
+cudaError_t launch_fvm_batch_health(const FvmParams& shape, const FvmMember* members, int count,
+                                    Health* h, cudaStream_t s);
 // Vector-Jacobian product of one FVM step at state (u, v) for the projected
 // cotangent (wu, wv) = P g: (gu, gv) = w + dt (A^T w + nu lap w + lin w) and,
 // if nu_dot is not null, nu_dot = w . lap(v) per cell.
@@ -196,6 +209,9 @@ cudaError_t launch_spec_batch_row(const SpecParams& shape, const SpecMember* mem
                                   int k, cudaStream_t s);
 cudaError_t launch_spec_batch_update(const SpecParams& shape, const SpecMember* mem, int count,
                                      int k, int stage, cudaStream_t s);
+
+cudaError_t launch_spec_batch_health(const SpecParams& shape, const SpecMember* mem, int count,
+                                     Health* h, cudaStream_t s);
 
 cudaError_t launch_spec_col_prep(const SpecParams& p, const float2* w,
                                  float2* const t4[4], cudaStream_t s);

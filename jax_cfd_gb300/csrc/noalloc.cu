@@ -18,36 +18,48 @@
 // Calls whose work overlaps on the GPU (different streams, or different host
 // threads on one device) race on the array; callers must order them.
 #include <cmath>
-#include <mutex>
 #include <string>
 
 #include "../../include/cfd_gb300.h"
 #include "fft.cuh"
+#include "wfft.cuh"
 #include "kernels.h"
 
 namespace {
 
 constexpr int kNoallocMaxCells = 512 * 512;
 constexpr int kNoallocMaxSide = 4096;
-// Layout (in floats): spectrum [nx*ny] | tw_y [2*ny] | pass tables of the
-// column FFT [2*nx] and of the row FFT [2*(ny/2)] | lam_x [nx] |
-// lam_y [ny/2 + 1], each region rounded up to 64 floats.
+// Layout (in floats), each region rounded up to 64 floats: spectrum [nx*ny] |
+// tw_y [2*ny] | concatenated pass tables of the column FFT (length nx) and of
+// the row FFT (length ny/2), each followed by the one-warp 1024-point table
+// when its length is 1024 | lam_x [nx] | lam_y [ny/2 + 1].  A pass table of
+// length L holds fewer than L entries, so the bound below covers every shape
+// the size check admits (noalloc_layout checks it again per call).
 constexpr int kNoallocFloats =
-    kNoallocMaxCells + 2 * kNoallocMaxSide + 2 * kNoallocMaxSide + kNoallocMaxSide +
-    kNoallocMaxSide + (kNoallocMaxSide / 2 + 1) + 6 * 64;
+    kNoallocMaxCells + 2 * kNoallocMaxSide + 2 * (kNoallocMaxSide + 1024) +
+    2 * (kNoallocMaxSide / 2 + 1024) + kNoallocMaxSide + (kNoallocMaxSide / 2 + 1) + 6 * 64;
 
 __device__ __align__(256) float g_noalloc_scratch[kNoallocFloats];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_noalloc_mu;
-float* g_noalloc_ptr[kMaxDevices] = {};
-
 int round64(int n) { return (n + 63) & ~63; }
 
-// Angle numerator/denominator of entry `idx` of the concatenated pass tables
-// of a length-2^log2L FFT (layout in fft.cuh): the entry is
-// exp(-2 pi i num / den).
+// Entries of the concatenated pass tables of a length-2^log2L FFT (layout in
+// fft.cuh), followed, for length 1024, by the one-warp transform's table
+// (wfft.cuh: entry [k2 * 32 + n1] = exp(-2 pi i n1 k2 / 1024)).
+__host__ __device__ int table_entries(int log2L) {
+  return cfd::fft_pass_table_size(log2L) + cfd::wfft_table_size(log2L);
+}
+
+// Angle numerator/denominator of entry `idx` of table_entries(log2L): the
+// entry is exp(-2 pi i num / den).
 __device__ void pass_entry(int log2L, int idx, int* num, int* den) {
+  const int stockham = cfd::fft_pass_table_size(log2L);
+  if (idx >= stockham) {
+    const int w = idx - stockham;
+    *num = (w & 31) * (w >> 5);
+    *den = 1024;
+    return;
+  }
   int ns = 1;
   for (int q = 0; q < cfd::fft_num_passes(log2L); ++q) {
     const int R = cfd::fft_pass_radix(log2L, q);
@@ -73,7 +85,7 @@ __global__ void noalloc_tables_kernel(int nx, int ny, double hx, double hy,
                                       float2* tw_y, float2* twp_x, float2* twp_y,
                                       float* lam_x, float* lam_y) {
   const int log2nx = ilog2(nx), log2L = ilog2(ny) - 1;
-  const int sx = cfd::fft_pass_table_size(log2nx), sy = cfd::fft_pass_table_size(log2L);
+  const int sx = table_entries(log2nx), sy = table_entries(log2L);
   const int total = ny + sx + sy + nx + (ny / 2 + 1);
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total;
        t += gridDim.x * blockDim.x) {
@@ -106,24 +118,33 @@ int noalloc_fail(int code, const std::string& msg) {
   return code;
 }
 
-// Device address of the scratch array for the current device.  The first call
-// on each device looks it up with cudaGetSymbolAddress (host code may not use
-// the array's name as a device pointer).
+// Device address of the scratch array in the current device's context.  Host
+// code may not use the array's name as a device pointer, so every call looks
+// the address up with cudaGetSymbolAddress (cheap; an address cached across
+// calls would go stale when the context is destroyed and re-created, e.g.
+// after cudaDeviceReset, which reloads the module).
 int noalloc_scratch(float** out) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return noalloc_fail(CFD_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
-  if (dev < 0 || dev >= kMaxDevices) return noalloc_fail(CFD_ERR_UNSUPPORTED, "device ordinal out of range");
-  std::lock_guard<std::mutex> lock(g_noalloc_mu);
-  if (!g_noalloc_ptr[dev]) {
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || !p)
-      return noalloc_fail(CFD_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-    g_noalloc_ptr[dev] = static_cast<float*>(p);
-  }
-  *out = g_noalloc_ptr[dev];
+  void* p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess || !p)
+    return noalloc_fail(CFD_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+  *out = static_cast<float*>(p);
   return CFD_OK;
+}
+
+// Float offsets of the scratch regions for an nx x ny grid; false if they do
+// not fit the array.
+struct NoallocLayout {
+  int tw_y, twp_x, twp_y, lam_x, lam_y, end;
+};
+bool noalloc_layout(int nx, int ny, NoallocLayout* l) {
+  l->tw_y = round64(nx * ny);
+  l->twp_x = l->tw_y + round64(2 * ny);
+  l->twp_y = l->twp_x + round64(2 * table_entries(ilog2(nx)));
+  l->lam_x = l->twp_y + round64(2 * table_entries(ilog2(ny) - 1));
+  l->lam_y = l->lam_x + round64(nx);
+  l->end = l->lam_y + round64(ny / 2 + 1);
+  return l->end <= kNoallocFloats;
 }
 
 }  // namespace
@@ -147,12 +168,15 @@ extern "C" int cfd_fvm_projection_noalloc(void* stream, int nx, int ny, double h
   int rc = noalloc_scratch(&base);
   if (rc != CFD_OK) return rc;
 
+  NoallocLayout lay;
+  if (!noalloc_layout(nx, ny, &lay))
+    return noalloc_fail(CFD_ERR_INVALID_ARGUMENT, "cfd_fvm_projection_noalloc: scratch layout exceeds the array");
   float* spec = base;
-  float2* tw_y = reinterpret_cast<float2*>(spec + round64(nx * ny));
-  float2* twp_x = reinterpret_cast<float2*>(reinterpret_cast<float*>(tw_y) + round64(2 * ny));
-  float2* twp_y = reinterpret_cast<float2*>(reinterpret_cast<float*>(twp_x) + round64(2 * nx));
-  float* lam_x = reinterpret_cast<float*>(twp_y) + round64(ny);
-  float* lam_y = lam_x + round64(nx);
+  float2* tw_y = reinterpret_cast<float2*>(base + lay.tw_y);
+  float2* twp_x = reinterpret_cast<float2*>(base + lay.twp_x);
+  float2* twp_y = reinterpret_cast<float2*>(base + lay.twp_y);
+  float* lam_x = base + lay.lam_x;
+  float* lam_y = base + lay.lam_y;
 
   cfd::FvmParams p{};
   p.nx = nx;
@@ -172,7 +196,7 @@ extern "C" int cfd_fvm_projection_noalloc(void* stream, int nx, int ny, double h
   p.twp_y = twp_y;
 
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
-  const int total = ny + 2 * nx + ny + ny / 2 + 1;  // upper bound of the table entries
+  const int total = ny + table_entries(p.log2nx) + table_entries(p.log2ny - 1) + nx + ny / 2 + 1;
   noalloc_tables_kernel<<<(total + 255) / 256, 256, 0, s>>>(nx, ny, hx, hy, tw_y, twp_x,
                                                             twp_y, lam_x, lam_y);
   cudaError_t e = cudaGetLastError();

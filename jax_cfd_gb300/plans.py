@@ -134,6 +134,23 @@ class FvmPlan:
               'cfd_fvm_step')
     return u_out, v_out
 
+  def trajectory(self, u, v, inner: int, frames: int, frame_kind: int,
+                 start_with_input: bool = False):
+    """cfd_fvm_trajectory: (u_out, v_out, frames) with frames [frames, 2, nx,
+    ny] (velocity) or [frames, nx, ny] (vorticity) on the device."""
+    if inner < 0 or frames < 0:
+      raise ValueError('inner and frames must be non-negative')
+    u_out, v_out = torch.empty_like(u), torch.empty_like(v)
+    shape = ((frames, 2) if frame_kind == nat.FRAME_VELOCITY else (frames,)) + tuple(self.shape)
+    out = torch.empty(shape, dtype=torch.float32, device=u.device)
+    a = self._fields(u, v)
+    nat.check(self._lib.cfd_fvm_trajectory(self._h, current_stream_ptr(u.device), *a, int(inner),
+                                           int(frames), int(frame_kind),
+                                           int(bool(start_with_input)),
+                                           ptr(out) if frames else None, ptr(u_out),
+                                           ptr(v_out)), 'cfd_fvm_trajectory')
+    return u_out, v_out, out
+
   def step_implicit(self, u, v, steps: int, viscosity: float, u_out=None, v_out=None):
     """implicit_diffusion_navier_stokes (equations.py:154-195); the plan is
     made without explicit viscosity."""

@@ -22,6 +22,13 @@ within ``budget_bytes``; otherwise requests wait in their size's queue.
 Reported per request: arrival, admission and completion times (completion =
 result on the host); ``Server.stats`` gives p50/p99 latency and throughput.
 A request's result does not depend on which other requests share its pool.
+
+Health: every chunk ends with a per-slot reduction on the device (non-finite
+flag and largest finite magnitude of the state, ``cfd_health``), copied to the
+host with the chunk.  A request whose state holds a NaN or an infinity, or
+whose FVM velocity exceeds ``max_speed_factor`` times its initial maximum
+speed, is retired at that chunk boundary with ``status`` 'nonfinite' or
+'diverged', an ``error`` message and no result array, and its slot is freed.
 """
 from __future__ import annotations
 
@@ -34,6 +41,7 @@ from typing import Dict, List, Optional, Sequence, Tuple
 import numpy as np
 import torch
 
+HEALTH_NONFINITE = 1  # cfd_health flag: the state holds NaN or infinity
 TWO_PI = 2 * math.pi
 CFL = 0.5
 DRAG = 0.1
@@ -58,9 +66,14 @@ class Request:
   admitted: Optional[float] = None
   finished: Optional[float] = None
   result: Optional[Tuple[np.ndarray, ...]] = None
+  status: str = 'pending'  # 'ok', 'nonfinite' or 'diverged' once finished
+  error: Optional[str] = None
+  dt_override: Optional[float] = None  # replaces the stable dt when given
 
   @property
   def dt(self) -> float:
+    if self.dt_override is not None:
+      return float(self.dt_override)
     h = TWO_PI / self.n
     if self.kind == 'fvm':
       return min(CFL * h / self.vmax, h * h / (4 * self.viscosity))
@@ -126,6 +139,8 @@ class _Pool:
     else:
       self.batch = batching.SpecBatch((n, n), self.grid.step, capacity, device=dev)
     self.stream = torch.cuda.Stream(dev)
+    # Health records of the last chunk, copied to pinned memory with it.
+    self.health_host = torch.empty((capacity, 2), dtype=torch.int32, pin_memory=True)
     self.slots: List[Optional[Request]] = [None] * capacity
     self.remaining = [0] * capacity
     self.running = [0] * capacity
@@ -145,13 +160,15 @@ class Server:
   """The request loop (single host thread, one GPU)."""
 
   def __init__(self, device=None, budget_bytes: float = 150e9, chunk: int = 100,
-               graph: bool = True, capacity=default_capacity):
+               graph: bool = True, capacity=default_capacity,
+               max_speed_factor: float = 100.0):
     self.device = torch.device(device) if device is not None else torch.device(
         'cuda', torch.cuda.current_device())
     self.budget = float(budget_bytes)
     self.chunk = int(chunk)
     self.graph = graph
     self.capacity = capacity
+    self.max_speed_factor = float(max_speed_factor)
     self.pools: Dict[Tuple[str, int], List[_Pool]] = collections.defaultdict(list)
     self.queues: Dict[Tuple[str, int], collections.deque] = collections.defaultdict(
         collections.deque)
@@ -266,12 +283,33 @@ class Server:
     req.admitted = self.now()
 
   # -- the loop --------------------------------------------------------------
+  def _unhealthy(self, req: Request, record) -> Optional[Tuple[str, str]]:
+    """(status, message) when a slot's health record shows a failed state."""
+    if record['flags'] & HEALTH_NONFINITE:
+      return 'nonfinite', 'the state holds NaN or infinity'
+    limit = self.max_speed_factor * req.vmax
+    if req.kind == 'fvm' and record['max_abs'] > limit:
+      return 'diverged', (f'velocity {float(record["max_abs"]):.3g} exceeds '
+                          f'{self.max_speed_factor:g} x the initial maximum speed')
+    return None
+
   def _finish_chunk(self, pool: _Pool):
+    from jax_cfd_gb300 import batching  # pylint: disable=import-outside-toplevel
+    health = batching.decode_health(pool.health_host)
     for i, req in enumerate(pool.slots):
       if req is None:
         continue
+      ran = pool.running[i] > 0
       pool.remaining[i] -= pool.running[i]
       pool.running[i] = 0
+      failed = self._unhealthy(req, health[i]) if ran else None
+      if failed is not None:
+        # Retire now with an error status: no result, the slot is freed.
+        req.status, req.error = failed
+        req.finished = self.now()
+        self.done.append(req)
+        pool.slots[i] = None
+        continue
       if pool.remaining[i] <= 0:
         # Retire: copy the result to pinned host memory on the pool's stream.
         with torch.cuda.stream(pool.stream):
@@ -297,6 +335,7 @@ class Server:
     pool.stream.wait_event(ev)
     with torch.cuda.stream(pool.stream):
       pool.batch.run(self.chunk, graph=self.graph)
+      pool.health_host.copy_(pool.batch.health_device(), non_blocking=True)
       pool.event = torch.cuda.Event()
       pool.event.record(pool.stream)
     self.launches += 1
@@ -310,6 +349,7 @@ class Server:
       if ev.query():
         req.finished = self.now()
         req.result = tuple(h.numpy() for h in host)
+        req.status = 'ok'
         self.done.append(req)
         progressed = True
       else:
@@ -375,10 +415,14 @@ class Server:
   @staticmethod
   def stats(done: Sequence[Request], makespan: float) -> dict:
     lat = np.array([r.latency for r in done])
-    steps = sum(r.steps for r in done)
-    cells = sum(r.steps * r.n * r.n for r in done)
+    ok = [r for r in done if r.status == 'ok']
+    steps = sum(r.steps for r in ok)
+    cells = sum(r.steps * r.n * r.n for r in ok)
     return {
         'requests': len(done),
+        'completed_ok': len(ok),
+        'nonfinite': sum(r.status == 'nonfinite' for r in done),
+        'diverged': sum(r.status == 'diverged' for r in done),
         'p50_latency_s': float(np.percentile(lat, 50)) if len(lat) else None,
         'p99_latency_s': float(np.percentile(lat, 99)) if len(lat) else None,
         'mean_latency_s': float(lat.mean()) if len(lat) else None,
@@ -406,6 +450,7 @@ def run_plain(req: Request, device=None) -> Request:
         forcing=cfd.forcings.simple_turbulence_forcing(grid, 1, req.k, -0.1))
     out = cfd.funcutils.repeated(step, req.steps)(v0)
     req.result = tuple(o.data.cpu().numpy() for o in out)
+    req.status = 'ok'
   else:
     eq = seq.NavierStokes2D(req.viscosity, grid, drag=DRAG, smooth=True,
                             forcing_fn=lambda g: forcings.kolmogorov_forcing(
@@ -413,5 +458,6 @@ def run_plain(req: Request, device=None) -> Request:
     w0 = su.rfft2(cfd.finite_differences.curl_2d(v0).data, grid)
     out = cfd.funcutils.repeated(sts.crank_nicolson_rk4(eq, req.dt), req.steps)(w0)
     req.result = (out.cpu().numpy(),)
+    req.status = 'ok'
   return req
 

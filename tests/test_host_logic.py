@@ -47,9 +47,17 @@ def test_status_codes_map_to_reference_exceptions(lib):
   for code, exc in ((_native.CFD_ERR_INVALID_ARGUMENT, ValueError),
                     (_native.CFD_ERR_UNSUPPORTED, NotImplementedError),
                     (_native.CFD_ERR_OUT_OF_MEMORY, MemoryError),
-                    (_native.CFD_ERR_CUDA, RuntimeError)):
+                    (_native.CFD_ERR_CUDA, RuntimeError),
+                    (_native.CFD_ERR_DEVICE_FAULT, _native.DeviceFaultError)):
     with pytest.raises(exc):
       _native.check(code)
+
+
+def test_bounded_wait_selftest_validates_before_launching(lib):
+  from jax_cfd_gb300 import _native
+  for polls in (0, -3, (1 << 22) + 1):
+    assert lib.cfd_bounded_wait_selftest(None, polls) == _native.CFD_ERR_INVALID_ARGUMENT
+    assert 'polls' in _native.last_error()
 
 
 def test_plan_rejects_non_power_of_two_before_touching_the_gpu(lib):

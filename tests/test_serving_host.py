@@ -49,3 +49,24 @@ def test_pool_capacity_and_slot_bytes():
   assert serving.default_capacity('spectral', 2048) == 2
   assert serving.Server.slot_bytes('fvm', 64) == 7 * 64 * 64 * 4 + 8 * 64
   assert serving.Server.slot_bytes('spectral', 64) == 7 * 64 * 33 * 8
+
+
+def test_health_records_decode_and_failure_policy():
+  from jax_cfd_gb300 import batching, serving
+  raw = np.array([[0, np.float32(1.5).view(np.int32)], [1, 0],
+                  [0, np.float32(300.0).view(np.int32)]], dtype=np.int32)
+  rec = batching.decode_health(raw)
+  assert list(rec['flags']) == [0, 1, 0]
+  assert rec['max_abs'][0] == np.float32(1.5) and rec['max_abs'][2] == np.float32(300.0)
+  server = serving.Server.__new__(serving.Server)
+  server.max_speed_factor = 100.0
+  fvm = serving.Request(rid=0, kind='fvm', n=64, steps=1, viscosity=1e-3, k=4, vmax=2.0, seed=0)
+  spec = serving.Request(rid=1, kind='spectral', n=64, steps=1, viscosity=1e-3, k=4, vmax=2.0,
+                         seed=0)
+  assert server._unhealthy(fvm, rec[0]) is None
+  assert server._unhealthy(fvm, rec[1])[0] == 'nonfinite'
+  assert server._unhealthy(fvm, rec[2])[0] == 'diverged'
+  assert server._unhealthy(spec, rec[2]) is None  # spectral magnitudes are not speeds
+  assert server._unhealthy(spec, rec[1])[0] == 'nonfinite'
+  fvm.dt_override = 0.25
+  assert fvm.dt == 0.25

@@ -6,9 +6,12 @@ after start-up, plugin hosts that pass only pre-allocated buffers).  It keeps
 its scratch in a fixed device array of at most 512 x 512 cells.  This test
 calls it through the C ABI twice in a row, on different grids and data, and
 compares each result with ``cfd_fvm_projection`` (a plan with its own
-workspace) within the per-step tolerance the other parity tests use.  The file
-name sorts last so that a run stopping at the first failure has already run
-every other test.
+workspace) and with the oracle's projection, within the per-step tolerance
+the other parity tests use, and checks the projected field's divergence.  The
+shapes cover every row-transform path the array serves: the shared-memory
+Stockham rows, the one-warp 1024-point rows (ny = 2048) and very elongated
+grids.  The file name sorts last so that a run stopping at the first failure
+has already run every other test.
 """
 import ctypes
 
@@ -34,21 +37,36 @@ def _noalloc_projection(u, v, hx, hy):
   return uo, vo
 
 
-@pytest.mark.parametrize('calls', [((128, 256), 0.05, 11), ((512, 512), 0.1, 12)])
+def _divergence(u, v, h):
+  """Backward-difference divergence (finite_differences.py:136-143)."""
+  return (u - np.roll(u, 1, axis=0)) / h + (v - np.roll(v, 1, axis=1)) / h
+
+
+@pytest.mark.parametrize('calls', [((128, 256), 0.05, 11), ((512, 512), 0.1, 12),
+                                   ((128, 2048), 0.1, 13), ((2048, 128), 0.1, 14),
+                                   ((4096, 64), 0.1, 15)])
 def test_noalloc_projection_two_calls_match_plan(cuda_device, calls):
   from jax_cfd_gb300 import plans
+  from oracle import fvm as ofvm
   # Two calls in a row on one device: the second call reuses the array the
   # first one left behind (a different grid, so every table is rewritten).
   cases = [((64, 64), 0.2, 1), calls]
   for shape, h, seed in cases:
     rng = np.random.default_rng(seed)
-    u = torch.from_numpy((1 + 0.3 * rng.standard_normal(shape)).astype(np.float32)).to(cuda_device)
-    v = torch.from_numpy((1 + 0.3 * rng.standard_normal(shape)).astype(np.float32)).to(cuda_device)
+    u0 = (1 + 0.3 * rng.standard_normal(shape)).astype(np.float32)
+    v0 = (1 + 0.3 * rng.standard_normal(shape)).astype(np.float32)
+    u = torch.from_numpy(u0).to(cuda_device)
+    v = torch.from_numpy(v0).to(cuda_device)
     got = _noalloc_projection(u, v, h, h)
     want = plans.FvmPlan(shape, (h, h), device=cuda_device).projection(u, v)
     torch.cuda.synchronize(cuda_device)
-    for g, w in zip(got, want):
-      assert rel_l2(g.cpu().numpy(), w.cpu().numpy()) <= TOL
+    oracle = ofvm.projection((u0, v0), ofvm.Grid.make(shape, step=(h, h)))
+    got_np = [g.cpu().numpy() for g in got]
+    for g, w, o in zip(got_np, want, oracle):
+      assert rel_l2(g, w.cpu().numpy()) <= TOL
+      assert rel_l2(g, o) <= TOL
+    # pressure_test.py:91-111 holds the projected field's divergence to 1e-4.
+    assert np.abs(_divergence(got_np[0], got_np[1], h)).max() <= 1e-4
 
 
 def test_noalloc_projection_rejects_oversize_grid(cuda_device):
