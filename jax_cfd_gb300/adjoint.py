@@ -10,6 +10,10 @@ The forward pass keeps the state every ``checkpoint_every`` steps; the
 backward pass recomputes the states of one segment from its checkpoint before
 running that segment's adjoint steps, so memory is one segment plus the
 checkpoints.  Gradients flow to the initial velocity and to the viscosity.
+
+A batch of trajectories (a leading axis) runs concurrently: each trajectory
+has its own plan (workspace) and CUDA stream, forward and backward, and the
+caller's stream waits for all of them.
 """
 from __future__ import annotations
 
@@ -37,12 +41,14 @@ class RolloutSpec:
   force_v: Optional[tuple] = None
   checkpoint_every: int = 8
 
-  def plan(self, viscosity: float, device) -> plans.FvmPlan:
+  def plan(self, viscosity: float, device, index: int = 0) -> plans.FvmPlan:
+    """The step's plan; `index` selects one of several plans of the same
+    configuration (separate workspaces for trajectories run concurrently)."""
     import numpy as np  # pylint: disable=import-outside-toplevel
     arr = lambda t: None if t is None else np.asarray(t, dtype=np.float32)
     key = (device, self.shape, self.step, self.dt, self.density, self.convect,
            self.linear_coefficient, self.const_forcing, self.force_u, self.force_v,
-           float(viscosity))
+           float(viscosity), int(index))
     return plans.cached('adjoint', key, lambda: plans.FvmPlan(
         self.shape, self.step, density=self.density, viscosity=float(viscosity), dt=self.dt,
         convect=self.convect, linear_coefficient=self.linear_coefficient,
@@ -76,26 +82,124 @@ class _Rollout(torch.autograd.Function):
     nu_grad = torch.zeros((), dtype=torch.float64, device=u_last.device)
     for seg in reversed(range(len(ctx.checkpoints))):
       n = min(k, spec.steps - seg * k)
-      states = [ctx.checkpoints[seg]]
-      for _ in range(n - 1):
-        states.append(plan.step(*states[-1], 1))
-      for t in reversed(range(n)):
-        gu, gv, nu_dot = plan.adjoint_step(states[t][0], states[t][1], gu, gv)
-        nu_grad = nu_grad + nu_dot.double().sum()
+      gu, gv, part = _segment_adjoint(plan, ctx.checkpoints[seg], n, gu, gv)
+      nu_grad = nu_grad + part
     grad_nu = (nu_grad * (spec.dt / spec.density)).to(torch.float32).reshape(ctx.nu_shape)
     return gu, gv, grad_nu, None
+
+
+_STREAMS = {}
+
+
+def _side_streams(device, count: int):
+  """`count` CUDA streams of `device`, created once and reused."""
+  key = torch.device(device)
+  have = _STREAMS.setdefault(key, [])
+  while len(have) < count:
+    have.append(torch.cuda.Stream(key))
+  return have[:count]
+
+
+def _segment_adjoint(plan, checkpoint, n: int, gu, gv):
+  """Adjoint of `n` steps from `checkpoint`: recomputes the segment's states,
+  then runs its adjoint steps newest first; returns (gu, gv, sum of the
+  per-cell viscosity products in float64)."""
+  states = [checkpoint]
+  for _ in range(n - 1):
+    states.append(plan.step(*states[-1], 1))
+  acc = torch.zeros((), dtype=torch.float64, device=gu.device)
+  for t in reversed(range(n)):
+    gu, gv, nu_dot = plan.adjoint_step(states[t][0], states[t][1], gu, gv)
+    acc = acc + nu_dot.double().sum()
+  return gu, gv, acc
+
+
+class _BatchRollout(torch.autograd.Function):
+  """(u0, v0, viscosity) with a leading batch axis -> final states; each
+  trajectory on its own plan and stream."""
+
+  @staticmethod
+  def forward(ctx, u0, v0, viscosity, spec: RolloutSpec):  # pylint: disable=arguments-differ
+    dev = u0.device
+    count = u0.shape[0]
+    k = max(1, int(spec.checkpoint_every))
+    nu = float(viscosity)
+    plans_b = [spec.plan(nu, dev, index=b) for b in range(count)]
+    main = torch.cuda.current_stream(dev)
+    u0, v0 = u0.contiguous(), v0.contiguous()
+    uo, vo = torch.empty_like(u0), torch.empty_like(v0)
+    start = torch.cuda.Event()
+    start.record(main)
+    checkpoints = []
+    streams = _side_streams(dev, count)
+    for b, (plan, st) in enumerate(zip(plans_b, streams)):
+      st.wait_event(start)
+      with torch.cuda.stream(st):
+        cps = []
+        u, v = u0[b], v0[b]
+        for s0 in range(0, spec.steps, k):
+          cps.append((u, v))
+          n = min(k, spec.steps - s0)
+          if s0 + n >= spec.steps:
+            plan.step(u, v, n, uo[b], vo[b])
+          else:
+            u, v = plan.step(u, v, n)
+        if spec.steps == 0:
+          uo[b].copy_(u)
+          vo[b].copy_(v)
+        checkpoints.append(cps)
+      done = torch.cuda.Event()
+      done.record(st)
+      main.wait_event(done)
+    ctx.spec, ctx.plans, ctx.checkpoints, ctx.streams = spec, plans_b, checkpoints, streams
+    ctx.nu_shape = viscosity.shape
+    ctx.save_for_backward(u0, v0)
+    return uo, vo
+
+  @staticmethod
+  def backward(ctx, gu, gv):  # pylint: disable=arguments-differ
+    spec = ctx.spec
+    u0, _ = ctx.saved_tensors
+    dev = u0.device
+    gu = torch.zeros_like(u0) if gu is None else gu.contiguous().float()
+    gv = torch.zeros_like(u0) if gv is None else gv.contiguous().float()
+    k = max(1, int(spec.checkpoint_every))
+    main = torch.cuda.current_stream(dev)
+    gu_out, gv_out = torch.empty_like(gu), torch.empty_like(gv)
+    nu_parts = torch.zeros(len(ctx.plans), dtype=torch.float64, device=dev)
+    start = torch.cuda.Event()
+    start.record(main)
+    for b, (plan, st) in enumerate(zip(ctx.plans, ctx.streams)):
+      st.wait_event(start)
+      with torch.cuda.stream(st):
+        g_u, g_v = gu[b], gv[b]
+        acc = torch.zeros((), dtype=torch.float64, device=dev)
+        cps = ctx.checkpoints[b]
+        for seg in reversed(range(len(cps))):
+          n = min(k, spec.steps - seg * k)
+          g_u, g_v, part = _segment_adjoint(plan, cps[seg], n, g_u, g_v)
+          acc = acc + part
+        gu_out[b].copy_(g_u)
+        gv_out[b].copy_(g_v)
+        nu_parts[b].copy_(acc)
+      done = torch.cuda.Event()
+      done.record(st)
+      main.wait_event(done)
+    grad_nu = (nu_parts.sum() * (spec.dt / spec.density)).to(torch.float32).reshape(ctx.nu_shape)
+    ctx.checkpoints = None
+    return gu_out, gv_out, grad_nu, None
 
 
 def rollout(u0: torch.Tensor, v0: torch.Tensor, viscosity, spec: RolloutSpec):
   """Differentiable ``funcutils.repeated(step, spec.steps)`` of the FVM step
   on (u0, v0); ``viscosity`` is a float or a scalar tensor (gradients flow to
-  every tensor argument that requires them).  A leading batch axis runs each
-  trajectory in turn."""
+  every tensor argument that requires them).  With a leading batch axis the
+  trajectories run concurrently, one plan and one stream each (same results
+  as one at a time)."""
   nu = viscosity if isinstance(viscosity, torch.Tensor) else torch.tensor(
       float(viscosity), dtype=torch.float32, device=u0.device)
   if u0.dim() == 3:
-    outs = [_Rollout.apply(u0[b], v0[b], nu, spec) for b in range(u0.shape[0])]
-    return torch.stack([o[0] for o in outs]), torch.stack([o[1] for o in outs])
+    return _BatchRollout.apply(u0, v0, nu, spec)
   return _Rollout.apply(u0, v0, nu, spec)
 
 

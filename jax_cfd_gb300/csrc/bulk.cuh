@@ -2,10 +2,12 @@
 // memory with mbarrier completion, and bounded waits.
 //
 // Every wait on an mbarrier gives up after a bounded number of polls
-// (kBulkWaitLimit unless the caller passes a smaller limit): the kernel then
-// records the failure in its unit's fault word (read by cfd_device_fault()),
-// waits once more, with the same limit, for the copies it issued, and leaves
-// without using the data.  Nothing spins without bound.
+// (kBulkWaitLimit unless the caller passes a smaller limit) or kBulkWaitNs of
+// wall-clock time, whichever comes first: the kernel then records the failure
+// in its unit's fault word (read by cfd_device_fault()), waits once more,
+// with the same limits, for the copies it issued, and leaves without using
+// the data.  Nothing spins without bound, and a copy that can never complete
+// costs a launch tens of milliseconds, not seconds.
 #pragma once
 
 #include <stdint.h>
@@ -21,6 +23,7 @@ namespace cfd {
 static __device__ unsigned int g_cfd_device_fault = 0;
 constexpr unsigned int kFaultBulkWait = 1;
 constexpr int kBulkWaitLimit = 1 << 22;
+constexpr unsigned long long kBulkWaitNs = 20000000ull;  // 20 ms
 
 // Reads (and optionally clears) one translation unit's fault word.
 using FaultWordReader = cudaError_t (*)(unsigned int* code, bool clear);
@@ -105,15 +108,30 @@ CFD_D bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   return done != 0;
 }
 
-// Bounded wait for phase `parity`; false if `limit` polls ran out (recorded).
-CFD_D bool mbar_wait(uint64_t* bar, uint32_t parity, int limit = kBulkWaitLimit) {
-  for (int k = 0; k < limit; ++k)
+CFD_D unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Polls phase `parity` until it completes (true) or `limit` polls or
+// kBulkWaitNs have passed (false).
+CFD_D bool mbar_poll(uint64_t* bar, uint32_t parity, int limit) {
+  const unsigned long long t0 = global_ns();
+  for (int k = 0; k < limit; ++k) {
     if (mbar_try_wait(bar, parity)) return true;
+    if ((k & 255) == 255 && global_ns() - t0 > kBulkWaitNs) return false;
+  }
+  return false;
+}
+
+// Bounded wait for phase `parity`; false if it gave up (recorded).
+CFD_D bool mbar_wait(uint64_t* bar, uint32_t parity, int limit = kBulkWaitLimit) {
+  if (mbar_poll(bar, parity, limit)) return true;
   atomicCAS(&g_cfd_device_fault, 0u, kFaultBulkWait);
   // Give the copies in flight one more bounded chance to land before the
   // block leaves (their destination is this block's shared memory).
-  for (int k = 0; k < limit; ++k)
-    if (mbar_try_wait(bar, parity)) break;
+  mbar_poll(bar, parity, limit);
   return false;
 }
 

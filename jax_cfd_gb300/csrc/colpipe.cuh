@@ -1,5 +1,7 @@
 #pragma once
 
+#include <atomic>
+
 #include "common.cuh"
 #include "fft.cuh"
 
@@ -95,11 +97,7 @@ CFD_D void col_pipe_tables(float2* sbuf, const float2* __restrict__ twp,
 // (it contains barriers).
 // LDG: twp is the global table (else a shared copy).  A thread with
 // active == false computes nothing but takes part in every barrier.
-// SINGLE: buf[0] == buf[1] (one exchange buffer per column); every write
-// then also waits for the block's previous reads of the buffer (one more
-// barrier per exchange, half the shared memory).
-template <int LOG2N, int SIGN, int FIRST, bool LDG = !col_pipe_smem_tables<LOG2N>(),
-          bool SINGLE = false>
+template <int LOG2N, int SIGN, int FIRST, bool LDG = !col_pipe_smem_tables<LOG2N>()>
 CFD_D void col_pipe_fft(float2 (&v)[16], float2* const (&buf)[2], int t,
                         const float2* __restrict__ twp, bool active = true) {
   using P = ColPipe<LOG2N>;
@@ -121,7 +119,6 @@ CFD_D void col_pipe_fft(float2 (&v)[16], float2* const (&buf)[2], int t,
     if (q > 0) tw_off += 15 << (4 * q);
     const bool last = q == P::N16 - 1 && P::REM == 0;
     if (!last) {
-      if (SINGLE) __syncthreads();
       if (active) {
         float2* out = buf[wsel];
         const int o = ((t - k) << 4) + k;
@@ -171,6 +168,24 @@ static inline int col_pipe_device_sms() {
       cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n < 1)
     return 1;
   return n;
+}
+
+// Resident blocks per multiprocessor of `kern` at this block size and shared
+// memory (at least 1), queried once per call site and cached in `cache`; the
+// cache is atomic because any host thread may launch.
+template <typename K>
+inline cudaError_t cached_blocks_per_sm(K kern, int threads, size_t smem, std::atomic<int>& cache,
+                                        int* out) {
+  int v = cache.load(std::memory_order_relaxed);
+  if (v == 0) {
+    int nb = 0;
+    const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, threads, smem);
+    if (e != cudaSuccess) return e;
+    v = nb > 0 ? nb : 1;
+    cache.store(v, std::memory_order_relaxed);
+  }
+  *out = v;
+  return cudaSuccess;
 }
 
 // Register cap of 128 at every block size (512 threads per multiprocessor or

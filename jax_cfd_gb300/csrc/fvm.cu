@@ -442,15 +442,11 @@ __global__ void __launch_bounds__(kStencilThreads)
 
 // ---- Warp-streaming stencil ------------------------------------------------
 // The same step as explicit_tile with no shared memory and no block barrier:
-// a warp owns a strip of kSW = 28 output columns and walks down kSH = 32 rows.
-// Lane L holds column j0 - 2 + L; lanes 2..29 produce output, lanes 0, 1, 30,
-// 31 are the strip's halo.  Along x (rows) each lane keeps a five-row window
-// of projected (u, v) in registers and carries the previous x-face flux; along
-// y the neighbours' values and the left y-face flux come from warp shuffles.
-// Every expression is the one explicit_tile evaluates, in the same order, so
-// the two kernels produce identical bits.
-constexpr int kSW = 28;
-constexpr int kSH = 32;
+// a warp owns a strip of columns and walks down its rows with a window of
+// projected (u, v) rows in registers, carrying the previous x-face flux;
+// along y the neighbours' values and the left y-face flux come from warp
+// shuffles.  Every expression is the one explicit_tile evaluates, in the same
+// order, so the two kernels produce identical bits.
 constexpr unsigned kFull = 0xffffffffu;
 
 CFD_D float2 shfl_down2(float2 x, int d) {
@@ -471,142 +467,35 @@ CFD_D float2 stream_xface(const FvmParams& p, float2 cm, float2 c0, float2 c1, f
   return mul2(make_float2(U.x, cface.y), make_float2(U.x, U.y));
 }
 
-// Raw row data of one lane: u*, v*, q and q one column to the right.
-struct StreamRaw {
-  float u, v, q, qy;
-};
-
-template <bool PROJECT>
-CFD_D StreamRaw stream_fetch(const FvmParams& p, const float* __restrict__ ua,
-                             const float* __restrict__ va, const float* __restrict__ q,
-                             int row, int j, int j1) {
-  const size_t ny = (size_t)p.ny;
-  const size_t base = (size_t)(row & (p.nx - 1)) * ny;
-  StreamRaw r;
-  r.u = __ldg(ua + base + j);
-  r.v = __ldg(va + base + j);
-  r.q = PROJECT ? __ldg(q + base + j) : 0.f;
-  r.qy = PROJECT ? __ldg(q + base + j1) : 0.f;
-  return r;
-}
-
-// u = u* - (q[i+1] - q[i]) / hx ; v = v* - (q[j+1] - q[j]) / hy, as
-// explicit_tile evaluates it; q_next is q one row down.
-template <bool PROJECT>
-CFD_D float2 stream_project(const FvmParams& p, const StreamRaw& r, float q_next) {
-  if (!PROJECT) return make_float2(r.u, r.v);
-  return make_float2(r.u - (q_next - r.q) * p.inv_hx, r.v - (r.qy - r.q) * p.inv_hy);
-}
-
-template <bool PROJECT, int CONVECT, int FORCE>
-CFD_D void stream_row(const FvmParams& p, int i, int j, bool out, float2& w1, float2& w2,
-                      float2& w3, const float2 w4, float2& fx_prev, float* __restrict__ uo,
-                      float* __restrict__ vo) {
-  const size_t ny = (size_t)p.ny;
-  const float2 ihx = splat2(p.inv_hx), ihy = splat2(p.inv_hy);
-  // x-face after row i.
-  const float2 fx = stream_xface<CONVECT>(p, w1, w2, w3, w4, __shfl_down_sync(kFull, w2.x, 1));
-  // y-face after column j in row i: stencil columns j-1 .. j+2.
-  const float2 cm = shfl_up2(w2, 1), c1 = shfl_down2(w2, 1), c2 = shfl_down2(w2, 2);
-  const float2 V = mul2(splat2(0.5f), add2(splat2(w2.y), make_float2(w3.y, c1.y)));
-  float2 fy;
-  if (CONVECT == 0) {
-    fy = tvd_flux2(cm, w2, c1, c2, V, p.cfl_y);
-  } else {
-    const float2 cface = mul2(splat2(0.5f), add2(w2, c1));
-    fy = mul2(make_float2(cface.x, V.y), make_float2(V.x, V.y));
-  }
-  const float2 fy_left = shfl_up2(fy, 1);
-  if (out) {
-    const float2 uv = w2;
-    const float2 dx = mul2(sub2(fx, fx_prev), ihx);
-    float2 kk = fma2(sub2(fy, fy_left), ihy, dx);
-    kk = make_float2(-kk.x, -kk.y);
-    kk = add_diffusion_forcing<FORCE>(p, kk, uv, add2(w1, w3), add2(cm, c1), i, j);
-    const float2 nxt = fma2(splat2(p.dt), kk, uv);
-    uo[(size_t)i * ny + j] = nxt.x;
-    vo[(size_t)i * ny + j] = nxt.y;
-  }
-  fx_prev = fx;
-  w1 = w2;
-  w2 = w3;
-  w3 = w4;
-}
-
-// Rows are fetched four ahead of their use (a ring of raw rows in registers)
-// so that each warp keeps several row loads in flight.
-// bx: the block's index among the (ny / 28) x (nx / 32) / 4 blocks of a grid.
-template <bool PROJECT, int CONVECT, int FORCE>
-CFD_D void explicit_stream_body(const FvmParams& p, int bx, const float* __restrict__ ua,
-                                const float* __restrict__ va, const float* __restrict__ q,
-                                float* __restrict__ uo, float* __restrict__ vo) {
-  const int lane = threadIdx.x & 31;
-  const int warp = (int)((bx * blockDim.x + threadIdx.x) >> 5);
-  const int strips = (p.ny + kSW - 1) / kSW;
-  const int s = warp % strips, t = warp / strips;
-  const int r0 = t * kSH;
-  if (r0 >= p.nx) return;  // uniform per warp
-  const int my = p.ny - 1;
-  const int jl = s * kSW - 2 + lane;  // unwrapped column of this lane
-  const int j = jl & my, j1 = (jl + 1) & my;
-  const bool out = lane >= 2 && lane < 30 && jl < p.ny;
-
-  // Window rows r0-2 .. r0+1 (projected), then the ring of raw rows r0+2 .. r0+5.
-  StreamRaw ring0 = stream_fetch<PROJECT>(p, ua, va, q, r0 - 2, j, j1);
-  StreamRaw ring1 = stream_fetch<PROJECT>(p, ua, va, q, r0 - 1, j, j1);
-  StreamRaw ring2 = stream_fetch<PROJECT>(p, ua, va, q, r0, j, j1);
-  StreamRaw ring3 = stream_fetch<PROJECT>(p, ua, va, q, r0 + 1, j, j1);
-  StreamRaw nxt0 = stream_fetch<PROJECT>(p, ua, va, q, r0 + 2, j, j1);
-  const float2 w0 = stream_project<PROJECT>(p, ring0, ring1.q);
-  float2 w1 = stream_project<PROJECT>(p, ring1, ring2.q);
-  float2 w2 = stream_project<PROJECT>(p, ring2, ring3.q);
-  float2 w3 = stream_project<PROJECT>(p, ring3, nxt0.q);
-  ring0 = nxt0;
-  ring1 = stream_fetch<PROJECT>(p, ua, va, q, r0 + 3, j, j1);
-  ring2 = stream_fetch<PROJECT>(p, ua, va, q, r0 + 4, j, j1);
-  ring3 = stream_fetch<PROJECT>(p, ua, va, q, r0 + 5, j, j1);
-  float2 fx_prev = stream_xface<CONVECT>(p, w0, w1, w2, w3, __shfl_down_sync(kFull, w1.x, 1));
-  // Iteration for row i projects row i + 2 (ring slot i % 4, q from the next
-  // slot) and refills that slot with row i + 6.
-#define CFD_STREAM_ROW(K, KN)                                                          \
-  {                                                                                    \
-    const int i = r0 + a + K;                                                          \
-    const float2 w4 = stream_project<PROJECT>(p, ring##K, ring##KN.q);                 \
-    ring##K = stream_fetch<PROJECT>(p, ua, va, q, i + 6, j, j1);                       \
-    stream_row<PROJECT, CONVECT, FORCE>(p, i, j, out, w1, w2, w3, w4, fx_prev, uo, vo); \
-  }
-#pragma unroll 1
-  for (int a = 0; a < kSH; a += 4) {
-    CFD_STREAM_ROW(0, 1)
-    CFD_STREAM_ROW(1, 2)
-    CFD_STREAM_ROW(2, 3)
-    CFD_STREAM_ROW(3, 0)
-  }
-#undef CFD_STREAM_ROW
-}
-
 // ---- Paired-column warp streams ---------------------------------------------
-// As explicit_stream_body with two adjacent columns per lane: lane L holds
-// columns jl = j0 - 2 + 2L and jl + 1 (j0 = 60 s for strip s), so a warp
-// covers 64 columns of which lanes 1..30 produce 60.  Rows are fetched as
-// float2 pairs (jl is even, so the pairs are 8-byte aligned), results stored
-// as float2 pairs, and a lane's second column takes its left neighbour, its
-// x-face velocity and its left y-face flux from the lane's own first column:
-// half the shuffles and a third of the loads per cell of one column per lane.
-// Each column evaluates exactly the expressions of stream_row.
-constexpr int kSW2 = 60;
+// Two adjacent columns per lane: lane L holds columns jl = j0 - 2 + 2L and
+// jl + 1 (j0 = 60 s for strip s), so a warp covers 64 columns of which lanes
+// 1..30 produce 60 (lane 0's first y-face lacks its left stencil column,
+// lane 31's last its right one).  Rows are fetched as float2 pairs (jl is
+// even, so the pairs are 8-byte aligned), results stored as float2 pairs,
+// and a lane's second column takes its left neighbour, its x-face velocity
+// and its left y-face flux from the lane's own first column: half the
+// shuffles and a third of the loads per cell of one column per lane (which
+// measured 33.1 against 30.7 us at 2048^2).  Each column evaluates exactly
+// the expressions of explicit_tile.
+constexpr int kStreamCols = 60;
+// Rows per warp and prefetch depth (16 and 4 measured fastest at 2048^2:
+// 30.7 us against 31.0 for 32 rows, 31.3 for a prefetch of 2, 32.5 with the
+// registers capped at 64 for 32 warps per multiprocessor, and 33.1 for one
+// column per lane).
+constexpr int kStreamRows = 16, kStreamPrefetch = 4;
 
-struct StreamRaw2 {
+struct StreamRaw {
   float2 u, v, q;  // columns (jl, jl + 1)
   float qr;        // q at column jl + 2
 };
 
 template <bool PROJECT>
-CFD_D StreamRaw2 stream2_fetch(const FvmParams& p, const float* __restrict__ ua,
+CFD_D StreamRaw stream_fetch(const FvmParams& p, const float* __restrict__ ua,
                                const float* __restrict__ va, const float* __restrict__ q,
                                int row, int j, int jr) {
   const unsigned base = (unsigned)(row & (p.nx - 1)) << p.log2ny;
-  StreamRaw2 r;
+  StreamRaw r;
   r.u = __ldg(reinterpret_cast<const float2*>(ua + base + j));
   r.v = __ldg(reinterpret_cast<const float2*>(va + base + j));
   r.q = PROJECT ? __ldg(reinterpret_cast<const float2*>(q + base + j)) : make_float2(0.f, 0.f);
@@ -616,7 +505,7 @@ CFD_D StreamRaw2 stream2_fetch(const FvmParams& p, const float* __restrict__ ua,
 
 // Projected (u, v) of both columns; qn: q of the next row.
 template <bool PROJECT>
-CFD_D void stream2_project(const FvmParams& p, const StreamRaw2& r, float2 qn, float2& a,
+CFD_D void stream_project(const FvmParams& p, const StreamRaw& r, float2 qn, float2& a,
                            float2& b) {
   if (!PROJECT) {
     a = make_float2(r.u.x, r.v.x);
@@ -629,13 +518,14 @@ CFD_D void stream2_project(const FvmParams& p, const StreamRaw2& r, float2 qn, f
 
 // Window of projected rows for both columns: w1 = row i - 1, w2 = row i,
 // w3 = row i + 1 (A: column jl, B: column jl + 1).
-struct Window2 {
+struct StreamWindow {
   float2 a1, a2, a3, b1, b2, b3;
   float2 fxa, fxb;  // x-face fluxes after row i - 1
 };
 
+// Row i of the paired stream: u*, v* of both columns, stored when `out`.
 template <bool PROJECT, int CONVECT, int FORCE>
-CFD_D void stream2_row(const FvmParams& p, int i, int jA, bool out, float2 fuy, Window2& w,
+CFD_D void stream_row(const FvmParams& p, int i, int jA, bool out, float2 fuy, StreamWindow& w,
                        const float2 a4, const float2 b4, float* __restrict__ uo,
                        float* __restrict__ vo) {
   const float2 ihx = splat2(p.inv_hx), ihy = splat2(p.inv_hy);
@@ -690,37 +580,37 @@ CFD_D void stream2_row(const FvmParams& p, int i, int jA, bool out, float2 fuy, 
 // each warp walks SH rows of its strip with rows fetched PF ahead (a ring of
 // PF raw rows in registers).
 template <bool PROJECT, int CONVECT, int FORCE, int SH, int PF>
-CFD_D void explicit_stream2_body(const FvmParams& p, int bx, const float* __restrict__ ua,
+CFD_D void explicit_stream_body(const FvmParams& p, int bx, const float* __restrict__ ua,
                                  const float* __restrict__ va, const float* __restrict__ q,
                                  float* __restrict__ uo, float* __restrict__ vo) {
   static_assert(SH % PF == 0, "rows per warp must be a multiple of the prefetch depth");
   const int lane = threadIdx.x & 31;
   const int warp = (int)((bx * blockDim.x + threadIdx.x) >> 5);
-  const int strips = (p.ny + kSW2 - 1) / kSW2;
+  const int strips = (p.ny + kStreamCols - 1) / kStreamCols;
   const int s = warp % strips, t = warp / strips;
   const int r0 = t * SH;
   if (r0 >= p.nx) return;  // uniform per warp
   const int my = p.ny - 1;
-  const int jl = s * kSW2 - 2 + 2 * lane;  // unwrapped first column of this lane
+  const int jl = s * kStreamCols - 2 + 2 * lane;  // unwrapped first column of this lane
   const int j = jl & my, jr = (jl + 2) & my;
   const bool out = lane >= 1 && lane < 31 && jl < p.ny;
   const float2 fuy = FORCE == 1 ? __ldg(reinterpret_cast<const float2*>(p.fu_y + j))
                                 : make_float2(0.f, 0.f);
 
   // Window rows r0-2 .. r0+1 (projected), ring of raw rows r0+2 .. r0+PF+1.
-  const StreamRaw2 rm2 = stream2_fetch<PROJECT>(p, ua, va, q, r0 - 2, j, jr);
-  const StreamRaw2 rm1 = stream2_fetch<PROJECT>(p, ua, va, q, r0 - 1, j, jr);
-  const StreamRaw2 rz0 = stream2_fetch<PROJECT>(p, ua, va, q, r0, j, jr);
-  const StreamRaw2 rp1 = stream2_fetch<PROJECT>(p, ua, va, q, r0 + 1, j, jr);
-  StreamRaw2 ring[PF];
+  const StreamRaw rm2 = stream_fetch<PROJECT>(p, ua, va, q, r0 - 2, j, jr);
+  const StreamRaw rm1 = stream_fetch<PROJECT>(p, ua, va, q, r0 - 1, j, jr);
+  const StreamRaw rz0 = stream_fetch<PROJECT>(p, ua, va, q, r0, j, jr);
+  const StreamRaw rp1 = stream_fetch<PROJECT>(p, ua, va, q, r0 + 1, j, jr);
+  StreamRaw ring[PF];
 #pragma unroll
-  for (int k = 0; k < PF; ++k) ring[k] = stream2_fetch<PROJECT>(p, ua, va, q, r0 + 2 + k, j, jr);
-  Window2 w;
+  for (int k = 0; k < PF; ++k) ring[k] = stream_fetch<PROJECT>(p, ua, va, q, r0 + 2 + k, j, jr);
+  StreamWindow w;
   float2 a0, b0;
-  stream2_project<PROJECT>(p, rm2, rm1.q, a0, b0);
-  stream2_project<PROJECT>(p, rm1, rz0.q, w.a1, w.b1);
-  stream2_project<PROJECT>(p, rz0, rp1.q, w.a2, w.b2);
-  stream2_project<PROJECT>(p, rp1, ring[0].q, w.a3, w.b3);
+  stream_project<PROJECT>(p, rm2, rm1.q, a0, b0);
+  stream_project<PROJECT>(p, rm1, rz0.q, w.a1, w.b1);
+  stream_project<PROJECT>(p, rz0, rp1.q, w.a2, w.b2);
+  stream_project<PROJECT>(p, rp1, ring[0].q, w.a3, w.b3);
   {
     // x-faces after row r0 - 1.
     const float2 ra1 = shfl_down2(w.a1, 1);
@@ -735,34 +625,25 @@ CFD_D void explicit_stream2_body(const FvmParams& p, int bx, const float* __rest
     for (int K = 0; K < PF; ++K) {
       const int i = r0 + a + K;
       float2 a4, b4;
-      stream2_project<PROJECT>(p, ring[K], ring[(K + 1) % PF].q, a4, b4);
-      ring[K] = stream2_fetch<PROJECT>(p, ua, va, q, i + 2 + PF, j, jr);
-      stream2_row<PROJECT, CONVECT, FORCE>(p, i, j, out, fuy, w, a4, b4, uo, vo);
+      stream_project<PROJECT>(p, ring[K], ring[(K + 1) % PF].q, a4, b4);
+      ring[K] = stream_fetch<PROJECT>(p, ua, va, q, i + 2 + PF, j, jr);
+      stream_row<PROJECT, CONVECT, FORCE>(p, i, j, out, fuy, w, a4, b4, uo, vo);
     }
   }
-}
-
-template <bool PROJECT, int CONVECT, int FORCE, int SH, int PF, int MINB>
-__global__ void __launch_bounds__(128, MINB)
-    fvm_explicit_stream2_kernel(FvmParams p, const float* __restrict__ ua,
-                                const float* __restrict__ va, const float* __restrict__ q,
-                                float* __restrict__ uo, float* __restrict__ vo) {
-  pdl_wait();
-  pdl_trigger();
-  explicit_stream2_body<PROJECT, CONVECT, FORCE, SH, PF>(p, blockIdx.x, ua, va, q, uo, vo);
 }
 
 template <bool PROJECT, int CONVECT, int FORCE>
 __global__ void __launch_bounds__(128)
     fvm_explicit_stream_kernel(FvmParams p, const float* __restrict__ ua,
-                               const float* __restrict__ va, const float* __restrict__ q,
-                               float* __restrict__ uo, float* __restrict__ vo) {
+                                const float* __restrict__ va, const float* __restrict__ q,
+                                float* __restrict__ uo, float* __restrict__ vo) {
   pdl_wait();
   pdl_trigger();
-  explicit_stream_body<PROJECT, CONVECT, FORCE>(p, blockIdx.x, ua, va, q, uo, vo);
+  explicit_stream_body<PROJECT, CONVECT, FORCE, kStreamRows, kStreamPrefetch>(p, blockIdx.x, ua,
+                                                                               va, q, uo, vo);
 }
 
-bool stream_ok(const FvmParams& p) { return p.ny >= 64 && p.nx % kSH == 0; }
+bool stream_ok(const FvmParams& p) { return p.ny >= 64 && p.nx % 16 == 0; }
 
 // Backward-difference divergence of (u*, v*) (finite_differences.py:95-143)
 // followed by the packed real FFT of each row along y.  Shared memory holds
@@ -1264,89 +1145,6 @@ __global__ void __launch_bounds__(4 * (1 << LOG2N) / 16, col_pipe_min_blocks(4 *
   }
 }
 
-// The TMA-staged persistent column pass with CG columns per group and one
-// exchange buffer per column (SINGLE): half the shared memory of
-// fvm_col_pinv_tma_kernel per column, so that two blocks share a
-// multiprocessor and one block's barriers and exchanges overlap the other's
-// arithmetic.  Boxes are 2 CG floats x 256 rows (tensor map `tmap` encoded
-// with that box); transforms, staging layout and bits as the 4-column pass.
-template <int LOG2N, int CG>
-CFD_HD size_t col_tma_single_smem() {
-  return ((size_t)CG * col_pipe_bstride<LOG2N, CG>() + (size_t)CG * (1 << LOG2N)) *
-             sizeof(float2) +
-         (col_pipe_smem_tables<LOG2N>()
-              ? (size_t)fft_pass_table_size(LOG2N) * sizeof(float2) +
-                    (size_t)(1 << LOG2N) * sizeof(float)
-              : 0);
-}
-
-template <int LOG2N, int CG>
-__global__ void __launch_bounds__(CG * (1 << LOG2N) / 16, CG <= 2 ? 2 : 1)
-    fvm_col_pinv_tma1_kernel(FvmParams p, float2* __restrict__ spec,
-                             const __grid_constant__ CUtensorMap tmap) {
-  using P = ColPipe<LOG2N>;
-  constexpr int N = P::N, BOX = N < 256 ? N : 256, NBOX = N / BOX;
-  constexpr uint32_t kGroupBytes = (uint32_t)N * CG * sizeof(float2);
-  extern __shared__ float2 sbuf[];  // no static shared memory: 128-byte aligned
-  const int L = p.ny >> 1, groups = L / CG + 1;
-  const int w = threadIdx.x % CG, t = threadIdx.x / CG;
-  const int bstride = col_pipe_bstride<LOG2N, CG>();
-  float2* const buf[2] = {sbuf + w * bstride, sbuf + w * bstride};
-  float2* const stage = sbuf + CG * bstride;
-  // The tables follow the staging slots (col_pipe_tables' layout with one
-  // buffer set): place them by hand.
-  float2* const tw_s = stage + CG * N;
-  float* const tab_s = reinterpret_cast<float*>(tw_s + fft_pass_table_size(LOG2N));
-  uint64_t* const bar =
-      reinterpret_cast<uint64_t*>(reinterpret_cast<char*>(sbuf) + col_tma_single_smem<LOG2N, CG>());
-  constexpr int INV_FIRST = (P::PASSES - 1) & 1;
-  int g = blockIdx.x;
-  if (g >= groups) return;  // uniform per block
-  const float2* tw = p.twp_x;
-  const float* lamx = p.lamx;
-  if (col_pipe_smem_tables<LOG2N>()) {
-    const int ntw = fft_pass_table_size(LOG2N);
-    for (int i = threadIdx.x; i < ntw; i += blockDim.x) tw_s[i] = __ldg(p.twp_x + i);
-    for (int i = threadIdx.x; i < N; i += blockDim.x) tab_s[i] = __ldg(p.lamx + i);
-    tw = tw_s;
-    lamx = tab_s;
-  }
-  if (threadIdx.x == 0) {
-    mbar_init(bar, 1);
-    mbar_fence_init();
-  }
-  __syncthreads();
-  pdl_wait();
-  pdl_trigger();
-  auto issue = [&](int gg) {
-    const int x = gg * CG >= L ? 0 : 2 * CG * gg;
-    mbar_arrive_expect_tx(bar, kGroupBytes);
-#pragma unroll
-    for (int b = 0; b < NBOX; ++b) tma_load_2d(stage + b * BOX * CG, &tmap, x, b * BOX, bar);
-  };
-  if (threadIdx.x == 0) issue(g);
-  uint32_t phase = 0;
-  float2 v[16];
-#pragma unroll 1
-  for (; g < groups; g += gridDim.x) {
-    const bool landed = mbar_wait(bar, phase);
-    phase ^= 1u;
-    if (landed) col_pipe_take<LOG2N, CG>(stage, L, g, w, t, v);
-    if (__syncthreads_or(!landed)) return;
-    if (threadIdx.x == 0 && g + gridDim.x < groups) {
-      fence_proxy_async_smem();
-      issue(g + gridDim.x);
-    }
-    col_pipe_fft<LOG2N, -1, 0, !col_pipe_smem_tables<LOG2N>(), true>(v, buf, t, tw);
-    const int cp = g * CG >= L ? L : g * CG + w;  // pinv column index
-#pragma unroll
-    for (int m = 0; m < 16; ++m)
-      v[m] = c_scale(v[m], pinv_diag_at(p, lamx[t + P::NTHR * m], cp));
-    col_pipe_fft<LOG2N, 1, INV_FIRST, !col_pipe_smem_tables<LOG2N>(), true>(v, buf, t, tw);
-    col_pipe_store<LOG2N, CG>(spec, L, g, w, t, v);
-  }
-}
-
 // The persistent column pass over a same-shape batch: the work items are the
 // (member, group) pairs of the members that take this step, walked with the
 // grid as stride, so many members keep every block's staging pipeline full.
@@ -1594,6 +1392,25 @@ __global__ void __launch_bounds__(MAXT, MINB)
 CFD_HD bool warp_rows_ok(const FvmParams& p) { return p.log2ny - 1 == kWarpFftLog2; }
 constexpr int kWarpRows = 4;  // rows (warps) per block
 
+// The packed real FFT of row i from its samples (lane n1's x[n1 + 32 n2] in
+// v[n2], as pairs of reals), written to the row's spectrum.
+CFD_D void div_rfft_row_warp_tail(const FvmParams& p, int i, float2 (&v)[32],
+                                  float2* __restrict__ spec, float2* tile) {
+  const int lane = threadIdx.x & 31;
+  const int L = p.ny >> 1;
+  warp_fft1024<-1>(v, tile, p.twp_y + wfft_table_offset(kWarpFftLog2));
+  float2* out = spec + (size_t)i * L;
+#pragma unroll
+  for (int k1 = 0; k1 < 32; ++k1) {
+    const int k = lane + 32 * k1;
+    const float2 z = v[wfft_slot(k1)], zp = wfft_mirror(v, k1, lane);
+    float2 xk, xm;
+    rfft_post_pair(z, zp, __ldg(p.tw_y + k), &xk, &xm);
+    // element 0 packs the real DC and Nyquist values
+    out[k] = k == 0 ? make_float2(z.x + z.y, z.x - z.y) : xk;
+  }
+}
+
 CFD_D void div_rfft_row_warp(const FvmParams& p, int i, const float* __restrict__ us,
                              const float* __restrict__ vs, float2* __restrict__ spec,
                              float2* tile) {
@@ -1604,6 +1421,14 @@ CFD_D void div_rfft_row_warp(const FvmParams& p, int i, const float* __restrict_
   const float2* ub = reinterpret_cast<const float2*>(us + ((i - 1) & mx) * ny);
   const float2* vc = reinterpret_cast<const float2*>(vs + i * ny);
   float2 v[32], c[32];
+  if (p.row_field) {
+    // The field itself: a divergence the stencil already formed, or
+    // implicit diffusion's rfftn(u).
+#pragma unroll
+    for (int m = 0; m < 32; ++m) v[m] = __ldg(ua + lane + 32 * m);
+    div_rfft_row_warp_tail(p, i, v, spec, tile);
+    return;
+  }
 #pragma unroll
   for (int m = 0; m < 32; ++m) c[m] = __ldg(vc + lane + 32 * m);
   // v[j - 1] for j = 2n is the odd half of element n - 1, held by lane - 1 in
@@ -1622,17 +1447,7 @@ CFD_D void div_rfft_row_warp(const FvmParams& p, int i, const float* __restrict_
     v[m] = make_float2((a.x - b.x) * p.inv_hx + (c[m].x - cm) * p.inv_hy,
                        (a.y - b.y) * p.inv_hx + (c[m].y - c[m].x) * p.inv_hy);
   }
-  warp_fft1024<-1>(v, tile, p.twp_y + wfft_table_offset(kWarpFftLog2));
-  float2* out = spec + (size_t)i * L;
-#pragma unroll
-  for (int k1 = 0; k1 < 32; ++k1) {
-    const int k = lane + 32 * k1;
-    const float2 z = v[wfft_slot(k1)], zp = wfft_mirror(v, k1, lane);
-    float2 xk, xm;
-    rfft_post_pair(z, zp, __ldg(p.tw_y + k), &xk, &xm);
-    // element 0 packs the real DC and Nyquist values
-    out[k] = k == 0 ? make_float2(z.x + z.y, z.x - z.y) : xk;
-  }
+  div_rfft_row_warp_tail(p, i, v, spec, tile);
 }
 
 CFD_D void irfft_row_warp(const FvmParams& p, int i, float2* spec, float2* tile) {
@@ -1805,9 +1620,9 @@ __global__ void __launch_bounds__(128)
   if (k >= m.steps) return;
   const FvmParams p = m.p;
   const int src = batch_src(k), dst = batch_dst(k);
-  explicit_stream_body<PROJECT, CONVECT, 0>(p, blockIdx.x, m.f[src][0], m.f[src][1],
-                                            reinterpret_cast<const float*>(m.spec),
-                                            m.f[dst][0], m.f[dst][1]);
+  explicit_stream_body<PROJECT, CONVECT, 0, kStreamRows, kStreamPrefetch>(
+      p, blockIdx.x, m.f[src][0], m.f[src][1], reinterpret_cast<const float*>(m.spec),
+      m.f[dst][0], m.f[dst][1]);
 }
 
 template <int MAXT, int MINB>
@@ -1920,28 +1735,9 @@ template <bool PR, bool K0, int CV, int FO>
 static void launch_explicit_variant(const FvmParams& p, bool stream, bool tiled, dim3 grid,
                                     const float* ua, const float* va, const float* q,
                                     float* uo, float* vo, cudaStream_t s) {
-  static const int stream2 = getenv("CFD_GB300_STREAM2") ? atoi(getenv("CFD_GB300_STREAM2")) : 0;
-  const long long strips2 = (p.ny + kSW2 - 1) / kSW2;
-#define CFD_S2(SH, PF, MB)                                                                  \
-  launch_maybe_pdl(p.pdl, fvm_explicit_stream2_kernel<PR, CV, FO, SH, PF, MB>,             \
-                   dim3((int)((strips2 * ((p.nx + SH - 1) / SH) + 3) / 4)), dim3(128), 0, s, \
-                   p, ua, va, q, uo, vo)
-  if (stream && stream2 == 1 && p.nx % 32 == 0) {
-    CFD_S2(32, 4, 1);
-  } else if (stream && stream2 == 2 && p.nx % 16 == 0) {
-    CFD_S2(16, 4, 1);
-  } else if (stream && stream2 == 3 && p.nx % 16 == 0) {
-    CFD_S2(16, 2, 1);
-  } else if (stream && stream2 == 4 && p.nx % 16 == 0) {
-    CFD_S2(16, 2, 8);
-  } else if (stream && stream2 == 5 && p.nx % 32 == 0) {
-    CFD_S2(32, 2, 1);
-  } else if (stream && stream2 == 6 && p.nx % 16 == 0) {
-    CFD_S2(16, 4, 8);
-  } else if (stream && stream2 == 7 && p.nx % 8 == 0) {
-    CFD_S2(8, 2, 8);
-  } else if (stream) {
-    const long long warps = (long long)((p.ny + kSW - 1) / kSW) * ((p.nx + kSH - 1) / kSH);
+  if (stream) {
+    const long long warps =
+        (long long)((p.ny + kStreamCols - 1) / kStreamCols) * ((p.nx + kStreamRows - 1) / kStreamRows);
     launch_maybe_pdl(p.pdl, fvm_explicit_stream_kernel<PR, CV, FO>, dim3((int)((warps + 3) / 4)),
                      dim3(128), 0, s, p, ua, va, q, uo, vo);
   } else if (tiled) {
@@ -1950,7 +1746,6 @@ static void launch_explicit_variant(const FvmParams& p, bool stream, bool tiled,
   } else {
     fvm_explicit_kernel<PR, K0, CV><<<grid, kStencilThreads, 0, s>>>(p, ua, va, q, uo, vo);
   }
-#undef CFD_S2
 }
 
 cudaError_t launch_fvm_explicit(const FvmParams& p, bool project, bool out_k0,
@@ -1998,7 +1793,7 @@ static cudaError_t div_rfft_impl(const FvmParams& p, int target, const float* us
   }
   const int rows = fft_rows_per_block(log2L, p.nx, target);
   const bool aligned = (((uintptr_t)us | (uintptr_t)vs | (uintptr_t)spec) & 15) == 0;
-  if (p.row_feed == 1 && aligned) {
+  if (p.row_feed == 1 && aligned && !p.row_field) {
     const size_t smem = div_rfft_bulk_smem(p.ny, rows);
     cudaError_t e = set_smem(fvm_div_rfft_bulk_kernel<MAXT, MINB>, smem);
     if (e != cudaSuccess) return e;
@@ -2080,13 +1875,10 @@ static cudaError_t col_pinv_pipe_impl(const FvmParams& p, float2* spec, cudaStre
   auto kern = fvm_col_pinv_pipe_kernel<LOG2N, CG>;
   cudaError_t e = set_smem(kern, smem);
   if (e != cudaSuccess) return e;
-  static int per_sm = 0;  // same value for every device of one kind
-  if (per_sm == 0) {
-    int nb = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, threads, smem);
-    if (e != cudaSuccess) return e;
-    per_sm = nb > 0 ? nb : 1;
-  }
+  static std::atomic<int> per_sm_cache{0};  // per instantiation
+  int per_sm = 1;
+  e = cached_blocks_per_sm(kern, threads, smem, per_sm_cache, &per_sm);
+  if (e != cudaSuccess) return e;
   const int groups = p.ny / 2 / CG + 1;
   const int slots = col_pipe_device_sms() * per_sm;
   return launch_maybe_pdl(p.pdl, kern, dim3(groups < slots ? groups : slots), dim3(threads), smem,
@@ -2112,13 +1904,10 @@ static cudaError_t col_pinv_tma_impl(const FvmParams& p, float2* spec, cudaStrea
   auto kern = fvm_col_pinv_tma_kernel<LOG2N>;
   cudaError_t e = set_smem(kern, smem);
   if (e != cudaSuccess) return e;
-  static int per_sm = 0;  // same value for every device of one kind
-  if (per_sm == 0) {
-    int nb = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, threads, smem);
-    if (e != cudaSuccess) return e;
-    per_sm = nb > 0 ? nb : 1;
-  }
+  static std::atomic<int> per_sm_cache{0};  // per instantiation
+  int per_sm = 1;
+  e = cached_blocks_per_sm(kern, threads, smem, per_sm_cache, &per_sm);
+  if (e != cudaSuccess) return e;
   const int groups = p.ny / 2 / 4 + 1;
   const int slots = col_pipe_device_sms() * per_sm;
   const CUtensorMap map = *static_cast<const CUtensorMap*>(p.col_tmap);
@@ -2126,27 +1915,7 @@ static cudaError_t col_pinv_tma_impl(const FvmParams& p, float2* spec, cudaStrea
                           s, p, spec, map);
 }
 
-template <int LOG2N, int CG>
-static cudaError_t col_pinv_tma1_impl(const FvmParams& p, float2* spec, cudaStream_t s) {
-  const size_t smem = col_tma_single_smem<LOG2N, CG>() + 16;  // + the mbarrier
-  const int threads = CG * (1 << LOG2N) / 16;
-  auto kern = fvm_col_pinv_tma1_kernel<LOG2N, CG>;
-  cudaError_t e = set_smem(kern, smem);
-  if (e != cudaSuccess) return e;
-  int nb = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, threads, smem);
-  if (e != cudaSuccess) return e;
-  const int groups = p.ny / 2 / CG + 1;
-  const int slots = col_pipe_device_sms() * (nb > 0 ? nb : 1);
-  const CUtensorMap map = *static_cast<const CUtensorMap*>(p.col_tmap2);
-  return launch_maybe_pdl(p.pdl, kern, dim3(groups < slots ? groups : slots), dim3(threads), smem,
-                          s, p, spec, map);
-}
-
 static cudaError_t col_pinv_tma_launch(const FvmParams& p, float2* spec, cudaStream_t s) {
-  static const int tma1 = getenv("CFD_GB300_COLTMA1") ? atoi(getenv("CFD_GB300_COLTMA1")) : 0;
-  if (tma1 == 1 && p.col_tmap2 && p.log2nx == 11) return col_pinv_tma1_impl<11, 2>(p, spec, s);
-  if (tma1 == 2 && p.log2nx == 11) return col_pinv_tma1_impl<11, 4>(p, spec, s);
   switch (p.log2nx) {
     case 8: return col_pinv_tma_impl<8>(p, spec, s);
     case 9: return col_pinv_tma_impl<9>(p, spec, s);
@@ -2351,13 +2120,10 @@ static cudaError_t batch_col_pipe_impl(const FvmParams& p, const FvmMember* mem,
   auto kern = fvm_batch_col_pinv_pipe_kernel<LOG2N, CG>;
   cudaError_t e = set_smem(kern, smem);
   if (e != cudaSuccess) return e;
-  static int per_sm = 0;
-  if (per_sm == 0) {
-    int nb = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, threads, smem);
-    if (e != cudaSuccess) return e;
-    per_sm = nb > 0 ? nb : 1;
-  }
+  static std::atomic<int> per_sm_cache{0};  // per instantiation
+  int per_sm = 1;
+  e = cached_blocks_per_sm(kern, threads, smem, per_sm_cache, &per_sm);
+  if (e != cudaSuccess) return e;
   const long long items = (long long)count * (p.ny / 2 / CG + 1);
   const long long slots = (long long)col_pipe_device_sms() * per_sm;
   return launch_maybe_pdl(p.pdl, kern, dim3((int)(items < slots ? items : slots)), dim3(threads),
@@ -2383,13 +2149,10 @@ static cudaError_t batch_col_tma_impl(const FvmParams& p, const FvmMember* mem, 
   auto kern = fvm_batch_col_pinv_tma_kernel<LOG2N>;
   cudaError_t e = set_smem(kern, smem);
   if (e != cudaSuccess) return e;
-  static int per_sm = 0;
-  if (per_sm == 0) {
-    int nb = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, threads, smem);
-    if (e != cudaSuccess) return e;
-    per_sm = nb > 0 ? nb : 1;
-  }
+  static std::atomic<int> per_sm_cache{0};  // per instantiation
+  int per_sm = 1;
+  e = cached_blocks_per_sm(kern, threads, smem, per_sm_cache, &per_sm);
+  if (e != cudaSuccess) return e;
   const long long items = (long long)count * (p.ny / 2 / 4 + 1);
   const long long slots = (long long)col_pipe_device_sms() * per_sm;
   const CUtensorMap map = *static_cast<const CUtensorMap*>(p.col_tmap);
@@ -2411,7 +2174,8 @@ cudaError_t launch_fvm_batch_step(const FvmParams& p, const FvmMember* mem, int 
                                   cudaStream_t s) {
   if (!fvm_batch_shape_ok(p) || count < 1 || count > 65535) return cudaErrorInvalidValue;
   if (p.stencil == 1 && stream_ok(p)) {
-    const long long warps = (long long)((p.ny + kSW - 1) / kSW) * ((p.nx + kSH - 1) / kSH);
+    const long long warps =
+        (long long)((p.ny + kStreamCols - 1) / kStreamCols) * ((p.nx + kStreamRows - 1) / kStreamRows);
     const dim3 sg((unsigned)((warps + 3) / 4), count);
     if (p.convect == 0) {
       if (k > 0) launch_maybe_pdl(p.pdl, fvm_batch_explicit_stream_kernel<true, 0>, sg, dim3(128), 0, s, mem, k);

@@ -55,7 +55,6 @@ struct FvmParams {
   float dtnu;          // float32(dt * viscosity) for col_diag = 1
   int pdl;             // launch the step's kernels as programmatic dependents
   const void* col_tmap;  // HOST pointer to the CUtensorMap of the plan's spectrum (a batch's: 3-D, all slots)
-  const void* col_tmap2;  // HOST pointer: the same spectrum with 4-float boxes (single plans)
   const void* col_tmap_spec;  // the spectrum buffer col_tmap describes (single plans)
                          // (col_mode 5), or null
 };

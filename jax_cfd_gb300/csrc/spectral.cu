@@ -1077,13 +1077,10 @@ static cudaError_t spec_pipe_grid(K kern, int items, int* grid, size_t* smem, in
   *threads = CG * (1 << LOG2N) / 16;
   cudaError_t e = set_smem(kern, *smem);
   if (e != cudaSuccess) return e;
-  static int per_sm = 0;  // per instantiation; same for every device of one kind
-  if (per_sm == 0) {
-    int nb = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, *threads, *smem);
-    if (e != cudaSuccess) return e;
-    per_sm = nb > 0 ? nb : 1;
-  }
+  static std::atomic<int> per_sm_cache{0};  // per instantiation
+  int per_sm = 1;
+  e = cached_blocks_per_sm(kern, *threads, *smem, per_sm_cache, &per_sm);
+  if (e != cudaSuccess) return e;
   const int slots = col_pipe_device_sms() * per_sm;
   *grid = items < slots ? items : slots;
   return cudaSuccess;

@@ -161,7 +161,7 @@ class Server:
 
   def __init__(self, device=None, budget_bytes: float = 150e9, chunk: int = 100,
                graph: bool = True, capacity=default_capacity,
-               max_speed_factor: float = 100.0):
+               max_speed_factor: float = 100.0, check_health: bool = True):
     self.device = torch.device(device) if device is not None else torch.device(
         'cuda', torch.cuda.current_device())
     self.budget = float(budget_bytes)
@@ -169,6 +169,7 @@ class Server:
     self.graph = graph
     self.capacity = capacity
     self.max_speed_factor = float(max_speed_factor)
+    self.check_health = bool(check_health)
     self.pools: Dict[Tuple[str, int], List[_Pool]] = collections.defaultdict(list)
     self.queues: Dict[Tuple[str, int], collections.deque] = collections.defaultdict(
         collections.deque)
@@ -302,7 +303,7 @@ class Server:
       ran = pool.running[i] > 0
       pool.remaining[i] -= pool.running[i]
       pool.running[i] = 0
-      failed = self._unhealthy(req, health[i]) if ran else None
+      failed = self._unhealthy(req, health[i]) if ran and self.check_health else None
       if failed is not None:
         # Retire now with an error status: no result, the slot is freed.
         req.status, req.error = failed
@@ -335,7 +336,8 @@ class Server:
     pool.stream.wait_event(ev)
     with torch.cuda.stream(pool.stream):
       pool.batch.run(self.chunk, graph=self.graph)
-      pool.health_host.copy_(pool.batch.health_device(), non_blocking=True)
+      if self.check_health:
+        pool.health_host.copy_(pool.batch.health_device(), non_blocking=True)
       pool.event = torch.cuda.Event()
       pool.event.record(pool.stream)
     self.launches += 1

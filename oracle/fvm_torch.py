@@ -121,10 +121,22 @@ def advect(c, c_off, v, v_offs, dt, step, convect='van_leer'):
   return -divergence(flux, step)
 
 
+_DIAG = {}
+
+
+def _pinv_diagonal(grid: ofvm.Grid, device) -> torch.Tensor:
+  """float64 pseudoinverse diagonal of the periodic Laplacian on `device`."""
+  key = (grid.shape, grid.step, str(device))
+  if key not in _DIAG:
+    _DIAG[key] = torch.from_numpy(ofvm.pinv_diagonal(grid, np.float64)).to(device)
+  return _DIAG[key]
+
+
 def projection(v, grid: ofvm.Grid):
-  """pressure.py:115-198 with the rfft pseudoinverse (float64)."""
-  diag = torch.from_numpy(ofvm.pinv_diagonal(grid, np.float64))
+  """pressure.py:115-198 with the rfft pseudoinverse (float64); runs on the
+  device of `v` (CPU, or a GPU for large grids)."""
   rhs = divergence(v, grid.step)
+  diag = _pinv_diagonal(grid, rhs.device)
   q = torch.fft.irfftn(diag * torch.fft.rfftn(rhs), s=rhs.shape)
   return tuple(u - forward_difference(q, axis, grid.step) for axis, u in enumerate(v))
 

@@ -135,3 +135,72 @@ def test_rollout_gradient_matches_central_differences(cuda_device):
   assert worst <= 5e-3
   fd_nu = (loss64(x0, 1e-3 + 1e-6) - loss64(x0, 1e-3 - 1e-6)) / 2e-6
   assert abs(float(nug.grad) - fd_nu) <= 5e-3 * abs(fd_nu)
+
+
+def test_config3_gradient_at_512(cuda_device):
+  """The differentiation workload at its own scale, one trajectory: 512^2,
+  64 steps, a checkpoint every 8, loss = mean squared vorticity error against
+  a target produced by the float64 restatement from another seed (the
+  reference stand-in).  The GPU gradient (initial velocity and viscosity) is
+  compared with float64 autograd of the restatement (the jax.grad stand-in,
+  run on the GPU in float64) and with 32 central differences of the float64
+  forward along unit-norm random directions, eps 1e-3 (advection_test.py:298-314
+  differentiates the same kind of rollout with jax.grad through jax.remat).
+  A batch of two trajectories (run concurrently) gives the single
+  trajectories' bits."""
+  from jax_cfd_gb300 import adjoint
+  from oracle import fvm_torch as otorch
+  n, steps, every, nu0 = 512, 64, 8, 1e-3
+  og, v0, step, dt, const_u, _ = _case(n, seed=0)
+  _, vt, _, _, _, _ = _case(n, seed=100)
+  dev64 = lambda a: torch.from_numpy(np.asarray(a, dtype=np.float64)).to(cuda_device)
+  f64 = otorch.step_fn(1.0, nu0, dt, og, linear_coefficient=-0.1, const_u=dev64(const_u))
+  with torch.no_grad():
+    target = otorch.curl_2d(otorch.rollout(f64, tuple(dev64(a) for a in vt), steps), og.step)
+  # float64 autograd (viscosity differentiable)
+  nu = torch.tensor(nu0, dtype=torch.float64, device=cuda_device, requires_grad=True)
+  x = [dev64(a).requires_grad_() for a in v0]
+  fn = otorch.step_fn(1.0, nu, dt, og, linear_coefficient=-0.1, const_u=dev64(const_u))
+  out = otorch.rollout(fn, tuple(x), steps)
+  ((otorch.curl_2d(out, og.step) - target) ** 2).mean().backward()
+  # GPU hand-written adjoint
+  spec = adjoint.spec_for(step, steps, checkpoint_every=every)
+  u0 = torch.from_numpy(v0[0]).to(cuda_device).requires_grad_()
+  w0 = torch.from_numpy(v0[1]).to(cuda_device).requires_grad_()
+  nug = torch.tensor(nu0, device=cuda_device, requires_grad=True)
+  u, v = adjoint.rollout(u0, w0, nug, spec)
+  ((adjoint.vorticity(u, v, og.step) - target.float()) ** 2).mean().backward()
+  eu = rel_l2(u0.grad.cpu().numpy(), x[0].grad.cpu().numpy())
+  ev = rel_l2(w0.grad.cpu().numpy(), x[1].grad.cpu().numpy())
+  en = abs(float(nug.grad) - float(nu.grad)) / abs(float(nu.grad))
+  print(f'512^2 x 64 steps: gradient vs float64 autograd: u {eu:.2e}, v {ev:.2e}, nu {en:.2e}')
+  assert eu <= 1e-2 and ev <= 1e-2 and en <= 1e-2
+  # 32 central differences of the float64 forward.
+  gx = torch.cat([u0.grad.double().ravel(), w0.grad.double().ravel()])
+  rng = np.random.default_rng(21)
+  x0 = torch.cat([dev64(v0[0]).ravel(), dev64(v0[1]).ravel()])
+  cells = n * n
+
+  def loss64(xvec):
+    with torch.no_grad():
+      vv = (xvec[:cells].reshape(og.shape), xvec[cells:].reshape(og.shape))
+      return float(((otorch.curl_2d(otorch.rollout(f64, vv, steps), og.step) - target) ** 2).mean())
+  eps, worst = 1e-3, 0.0
+  for _ in range(32):
+    d = torch.from_numpy(rng.standard_normal(2 * cells)).to(cuda_device)
+    d /= torch.linalg.norm(d)
+    fd = (loss64(x0 + eps * d) - loss64(x0 - eps * d)) / (2 * eps)
+    worst = max(worst, abs(fd - float(gx @ d)) / (abs(fd) + 1e-30))
+  print(f'512^2 x 64 steps: worst relative error over 32 central differences {worst:.2e}')
+  assert worst <= 1e-2
+  # A batch of two runs concurrently and gives the single trajectories' bits.
+  _, v1, _, _, _, _ = _case(n, seed=1)
+  ub = torch.stack([torch.from_numpy(v0[0]), torch.from_numpy(v1[0])]).to(cuda_device).requires_grad_()
+  wb = torch.stack([torch.from_numpy(v0[1]), torch.from_numpy(v1[1])]).to(cuda_device).requires_grad_()
+  nub = torch.tensor(nu0, device=cuda_device, requires_grad=True)
+  a, b = adjoint.rollout(ub, wb, nub, spec)
+  assert torch.equal(a[0], u) and torch.equal(b[0], v)
+  ((adjoint.vorticity(a[0], b[0], og.step) - target.float()) ** 2).mean().backward()
+  assert torch.equal(ub.grad[0], u0.grad) and torch.equal(wb.grad[0], w0.grad)
+  assert torch.equal(nub.grad, nug.grad)
+  assert float(ub.grad[1].abs().max()) == 0.0
