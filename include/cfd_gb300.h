@@ -272,6 +272,13 @@ typedef struct cfd_health {
 enum { CFD_HEALTH_NONFINITE = 1 };
 /* Device pointer to the batch's `count` records. */
 int cfd_fvm_batch_health(cfd_fvm_batch* batch, const cfd_health** records);
+/* Also writes each run's records into `host_records` (`count` cfd_health in
+ * pinned host memory, cudaHostAlloc or cudaHostRegister; NULL stops it) from
+ * a kernel at the end of the chunk, so a host polling many batches reads
+ * them once the run's stream has passed that point, without a
+ * device-to-host copy (which would queue on the copy engine behind other
+ * transfers).  The memory must outlive the batch's runs. */
+int cfd_fvm_batch_set_health_mirror(cfd_fvm_batch* batch, void* host_records);
 
 /* A ragged ensemble: members of any grid shapes, grouped into one batch per
  * (shape, step, convection).  cfd_fvm_ensemble_step advances every member by
@@ -385,6 +392,8 @@ int cfd_spec_batch_set_steps(cfd_spec_batch* batch, int slot, int steps);
 int cfd_spec_batch_run(cfd_spec_batch* batch, void* stream, int chunk, int use_graph);
 /* Device pointer to the batch's `count` health records (see cfd_health). */
 int cfd_spec_batch_health(cfd_spec_batch* batch, const cfd_health** records);
+/* As cfd_fvm_batch_set_health_mirror. */
+int cfd_spec_batch_set_health_mirror(cfd_spec_batch* batch, void* host_records);
 
 
 #ifdef __cplusplus

@@ -125,6 +125,8 @@ _SIGNATURES = {
     'cfd_fvm_batch_health': (ctypes.c_int, [_vp, ctypes.POINTER(_vp)]),
     'cfd_fvm_ensemble_health': (ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(_vp)]),
     'cfd_spec_batch_health': (ctypes.c_int, [_vp, ctypes.POINTER(_vp)]),
+    'cfd_fvm_batch_set_health_mirror': (ctypes.c_int, [_vp, _vp]),
+    'cfd_spec_batch_set_health_mirror': (ctypes.c_int, [_vp, _vp]),
     'cfd_fvm_ensemble_step': (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_int]),
     'cfd_energy_spectrum_shells': (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_double,
                                                    ctypes.c_double, ctypes.c_double, ctypes.c_int,

@@ -60,6 +60,15 @@ def decode_health(raw) -> np.ndarray:
   return rec
 
 
+def _set_mirror(fn, handle, name: str, host: Optional[torch.Tensor], count: int):
+  """Points a batch's health mirror at `host` (pinned int32 [count, 2]) or
+  turns it off (None)."""
+  if host is not None:
+    if not host.is_pinned() or host.dtype != torch.int32 or tuple(host.shape) != (count, 2):
+      raise ValueError(f'{name}: the mirror must be a pinned int32 tensor of shape ({count}, 2)')
+  nat.check(fn(handle, None if host is None else ctypes.c_void_p(host.data_ptr())), name)
+
+
 def _health_view(owner, fn, handle, count: int, device, *index) -> torch.Tensor:
   """int32 [count, 2] device view of health records returned by `fn`."""
   ptr = ctypes.c_void_p()
@@ -178,6 +187,14 @@ class FvmBatch:
     infinity) and ``max_abs`` (largest finite |u| or |v|)."""
     return decode_health(self.health_device())
 
+  def set_health_mirror(self, host: Optional[torch.Tensor]):
+    """Every run also writes the records into `host` (a pinned int32
+    [count, 2] tensor, kept alive by the caller) from the device, readable
+    once the run's stream has passed it; None stops it."""
+    _set_mirror(self._lib.cfd_fvm_batch_set_health_mirror, self._h,
+                'cfd_fvm_batch_set_health_mirror', host, self.count)
+    self._mirror = host
+
 
 class SpecBatch:
   """Slots of one grid shape running NavierStokes2D + a low-storage RK/CN
@@ -283,6 +300,12 @@ class SpecBatch:
 
   def health(self) -> np.ndarray:
     return decode_health(self.health_device())
+
+  def set_health_mirror(self, host: Optional[torch.Tensor]):
+    """As FvmBatch.set_health_mirror."""
+    _set_mirror(self._lib.cfd_spec_batch_set_health_mirror, self._h,
+                'cfd_spec_batch_set_health_mirror', host, self.count)
+    self._mirror = host
 
 
 class FvmEnsemble:

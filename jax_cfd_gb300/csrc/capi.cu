@@ -205,6 +205,7 @@ struct cfd_fvm_batch {
   // 3-D tensor map of every slot's spectrum for the TMA-staged column pass.
   CUtensorMap spec_map;
   cfd::Health* health = nullptr;  // per slot, written at the end of every chunk
+  cfd::Health* mirror = nullptr;  // pinned host copy of `health`, or null
 };
 
 // Several batches (one per grid shape) stepped together: a chunk forks one
@@ -247,6 +248,7 @@ struct cfd_spec_batch {
   int graph_chunk = -1;
   long long bytes = 0;
   cfd::Health* health = nullptr;  // per slot, written at the end of every chunk
+  cfd::Health* mirror = nullptr;  // pinned host copy of `health`, or null
 };
 
 struct cfd_spec_plan {
@@ -1013,7 +1015,8 @@ static int batch_enqueue(cfd_fvm_batch* b, cudaStream_t s, int chunk) {
   for (int k = 0; k < chunk; ++k)
     CFD_CHECK(cfd::launch_fvm_batch_step(b->shape, b->dev, b->count, k, s), "batch step");
   CFD_CHECK(cfd::launch_fvm_batch_project_out(b->shape, b->dev, b->count, s), "batch project_out");
-  CFD_CHECK(cfd::launch_fvm_batch_health(b->shape, b->dev, b->count, b->health, s), "batch health");
+  CFD_CHECK(cfd::launch_fvm_batch_health(b->shape, b->dev, b->count, b->health, b->mirror, s),
+            "batch health");
   return CFD_OK;
 }
 
@@ -1244,6 +1247,34 @@ int cfd_fvm_ensemble_state(cfd_fvm_ensemble* ens, int index, float** u, float** 
 int cfd_fvm_batch_health(cfd_fvm_batch* b, const cfd_health** out) {
   if (!b || !out) return fail(CFD_ERR_INVALID_ARGUMENT, "cfd_fvm_batch_health: null pointer");
   *out = reinterpret_cast<const cfd_health*>(b->health);
+  return CFD_OK;
+}
+
+// A device-addressable host pointer for the health mirror: pinned memory
+// (cudaHostAlloc / cudaHostRegister) maps into the device's address space.
+static int health_mirror_ptr(void* host, int count, cfd::Health** out, const char* who) {
+  *out = nullptr;
+  if (!host) return CFD_OK;
+  cudaPointerAttributes a;
+  cudaError_t e = cudaPointerGetAttributes(&a, host);
+  if (e != cudaSuccess) return cuda_fail(e, who);
+  if (a.type != cudaMemoryTypeHost || !a.devicePointer)
+    return fail(CFD_ERR_INVALID_ARGUMENT,
+                std::string(who) + ": the mirror must be pinned host memory the device can address");
+  (void)count;
+  *out = static_cast<cfd::Health*>(a.devicePointer);
+  return CFD_OK;
+}
+
+int cfd_fvm_batch_set_health_mirror(cfd_fvm_batch* b, void* host_records) {
+  if (!b) return fail(CFD_ERR_INVALID_ARGUMENT, "cfd_fvm_batch_set_health_mirror: null batch");
+  cfd::Health* m = nullptr;
+  int rc = health_mirror_ptr(host_records, b->count, &m, "cfd_fvm_batch_set_health_mirror");
+  if (rc) return rc;
+  if (m != b->mirror) {
+    b->mirror = m;
+    batch_drop_graph(b);  // the pointer is part of the captured chunk
+  }
   return CFD_OK;
 }
 
@@ -1874,6 +1905,18 @@ int cfd_spec_batch_health(cfd_spec_batch* b, const cfd_health** out) {
   return CFD_OK;
 }
 
+int cfd_spec_batch_set_health_mirror(cfd_spec_batch* b, void* host_records) {
+  if (!b) return fail(CFD_ERR_INVALID_ARGUMENT, "cfd_spec_batch_set_health_mirror: null batch");
+  cfd::Health* m = nullptr;
+  int rc = health_mirror_ptr(host_records, b->count, &m, "cfd_spec_batch_set_health_mirror");
+  if (rc) return rc;
+  if (m != b->mirror) {
+    b->mirror = m;
+    spec_batch_drop_graph(b);  // the pointer is part of the captured chunk
+  }
+  return CFD_OK;
+}
+
 int cfd_spec_batch_set_slot(cfd_spec_batch* b, int slot, const cfd_spec_config* cfg,
                             const cfd_spec_plan* forcing) {
   if (!b || !cfg || slot < 0 || slot >= b->count)
@@ -1933,7 +1976,8 @@ static int spec_batch_enqueue(cfd_spec_batch* b, cudaStream_t s, int chunk) {
       CFD_CHECK(cfd::launch_spec_batch_update(p, b->dev, b->count, k, st, s), "batch update");
       CFD_CHECK(cfd::launch_spec_batch_prep(p, b->dev, b->count, k, st, s), "batch prep");
     }
-  CFD_CHECK(cfd::launch_spec_batch_health(p, b->dev, b->count, b->health, s), "batch health");
+  CFD_CHECK(cfd::launch_spec_batch_health(p, b->dev, b->count, b->health, b->mirror, s),
+            "batch health");
   return CFD_OK;
 }
 

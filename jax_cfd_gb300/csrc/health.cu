@@ -102,6 +102,17 @@ __global__ void __launch_bounds__(kHealthThreads)
   health_commit(bad, mx, h + blockIdx.y);
 }
 
+// Copies the records of the slots that ran to `mirror` (pinned host memory
+// the device can address): the host reads them after the chunk without a
+// device-to-host copy, which would queue on the copy engine behind other
+// streams' transfers.
+template <typename M>
+__global__ void health_publish_kernel(const M* __restrict__ mem, int count,
+                                      const Health* __restrict__ h, Health* mirror) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < count && mem[s].steps > 0) mirror[s] = h[s];
+}
+
 int health_blocks(size_t n4) {
   size_t b = (n4 + kHealthThreads - 1) / kHealthThreads;
   if (b > kHealthBlocksPerSlot) b = kHealthBlocksPerSlot;
@@ -111,18 +122,20 @@ int health_blocks(size_t n4) {
 }  // namespace
 
 cudaError_t launch_fvm_batch_health(const FvmParams& shape, const FvmMember* mem, int count,
-                                    Health* h, cudaStream_t s) {
+                                    Health* h, Health* mirror, cudaStream_t s) {
   health_reset_fvm_kernel<<<(count + 127) / 128, 128, 0, s>>>(mem, count, h);
   const size_t n4 = ((size_t)shape.nx * shape.ny) >> 2;
   health_fvm_kernel<<<dim3(health_blocks(n4), count), kHealthThreads, 0, s>>>(mem, h);
+  if (mirror) health_publish_kernel<<<(count + 127) / 128, 128, 0, s>>>(mem, count, h, mirror);
   return cudaGetLastError();
 }
 
 cudaError_t launch_spec_batch_health(const SpecParams& shape, const SpecMember* mem, int count,
-                                     Health* h, cudaStream_t s) {
+                                     Health* h, Health* mirror, cudaStream_t s) {
   health_reset_spec_kernel<<<(count + 127) / 128, 128, 0, s>>>(mem, count, h);
   const size_t n4 = ((size_t)shape.nx * (shape.ny / 2 + 1) * 2) >> 2;
   health_spec_kernel<<<dim3(health_blocks(n4), count), kHealthThreads, 0, s>>>(mem, h);
+  if (mirror) health_publish_kernel<<<(count + 127) / 128, 128, 0, s>>>(mem, count, h, mirror);
   return cudaGetLastError();
 }
 

@@ -119,9 +119,11 @@ struct Health {
 };
 constexpr unsigned int kHealthNonFinite = 1u;
 // Health of every member that ran in the chunk (steps > 0), written to
-// h[slot]; members that did not run keep their record.
+// h[slot]; members that did not run keep their record.  With mirror (pinned
+// host memory the device can address), the same records are stored there
+// too by a kernel.
 cudaError_t launch_fvm_batch_health(const FvmParams& shape, const FvmMember* members, int count,
-                                    Health* h, cudaStream_t s);
+                                    Health* h, Health* mirror, cudaStream_t s);
 // Vector-Jacobian product of one FVM step at state (u, v) for the projected
 // cotangent (wu, wv) = P g: (gu, gv) = w + dt (A^T w + nu lap w + lin w) and,
 // if nu_dot is not null, nu_dot = w . lap(v) per cell.
@@ -210,7 +212,7 @@ cudaError_t launch_spec_batch_update(const SpecParams& shape, const SpecMember* 
                                      int k, int stage, cudaStream_t s);
 
 cudaError_t launch_spec_batch_health(const SpecParams& shape, const SpecMember* mem, int count,
-                                     Health* h, cudaStream_t s);
+                                     Health* h, Health* mirror, cudaStream_t s);
 
 cudaError_t launch_spec_col_prep(const SpecParams& p, const float2* w,
                                  float2* const t4[4], cudaStream_t s);

@@ -24,8 +24,8 @@ result on the host); ``Server.stats`` gives p50/p99 latency and throughput.
 A request's result does not depend on which other requests share its pool.
 
 Health: every chunk ends with a per-slot reduction on the device (non-finite
-flag and largest finite magnitude of the state, ``cfd_health``), copied to the
-host with the chunk.  A request whose state holds a NaN or an infinity, or
+flag and largest finite magnitude of the state, ``cfd_health``), which the
+chunk's last kernel also writes into the pool's pinned host buffer.  A request whose state holds a NaN or an infinity, or
 whose FVM velocity exceeds ``max_speed_factor`` times its initial maximum
 speed, is retired at that chunk boundary with ``status`` 'nonfinite' or
 'diverged', an ``error`` message and no result array, and its slot is freed.
@@ -139,8 +139,10 @@ class _Pool:
     else:
       self.batch = batching.SpecBatch((n, n), self.grid.step, capacity, device=dev)
     self.stream = torch.cuda.Stream(dev)
-    # Health records of the last chunk, copied to pinned memory with it.
-    self.health_host = torch.empty((capacity, 2), dtype=torch.int32, pin_memory=True)
+    # Health records of the last chunk, written into pinned memory by the
+    # chunk's last kernel (no device-to-host copy behind other transfers).
+    self.health_host = torch.zeros((capacity, 2), dtype=torch.int32, pin_memory=True)
+    self.batch.set_health_mirror(self.health_host)
     self.slots: List[Optional[Request]] = [None] * capacity
     self.remaining = [0] * capacity
     self.running = [0] * capacity
@@ -336,8 +338,6 @@ class Server:
     pool.stream.wait_event(ev)
     with torch.cuda.stream(pool.stream):
       pool.batch.run(self.chunk, graph=self.graph)
-      if self.check_health:
-        pool.health_host.copy_(pool.batch.health_device(), non_blocking=True)
       pool.event = torch.cuda.Event()
       pool.event.record(pool.stream)
     self.launches += 1

@@ -54,9 +54,13 @@ def test_fvm_batch_flags_the_poisoned_slot_only(cuda_device, graph):
   clean = _fvm_batch(pairs, cuda_device)
   clean.run(6, graph=graph)
   poisoned = _fvm_batch(pairs, cuda_device, poison=1)
+  # The pinned-host mirror receives the same records from the device.
+  mirror = torch.full((3, 2), -1, dtype=torch.int32, pin_memory=True)
+  poisoned.set_health_mirror(mirror)
   poisoned.run(6, graph=graph)
   torch.cuda.synchronize(cuda_device)
   hc, hp = clean.health(), poisoned.health()
+  assert np.array_equal(mirror.numpy(), poisoned.health_device().cpu().numpy())
   assert (hc['flags'] == 0).all()
   assert hp['flags'][1] & nat.HEALTH_NONFINITE
   assert hp['flags'][0] == 0 and hp['flags'][2] == 0
