@@ -248,7 +248,9 @@ int cfd_fvm_batch_run(cfd_fvm_batch* batch, void* stream, int chunk, int use_gra
  * shape (0 wide, 1 narrow) + 2 * column scheme (0 blocks, 1/2 clusters of
  * 4/8, 3 persistent pipelined groups of 4 columns over all slots staged by
  * cp.async, 4 the same staged by TMA tensor loads) + 10 * stencil (0
- * shared-memory tiles, 1 warp streams): 20 choices.  Every configuration
+ * shared-memory tiles, 1 warp streams), or 20: each member's whole chunk
+ * resident in shared memory, one block per member and one launch per chunk
+ * (grids whose fields fit: 64x64, 64x128, 128x64): 21 choices.  Every configuration
  * gives the same bits.  Synchronises. */
 int cfd_fvm_batch_autotune(cfd_fvm_batch* batch, void* stream, int steps, int* chosen);
 /* Pins the batch's launch configuration (index as cfd_fvm_batch_autotune

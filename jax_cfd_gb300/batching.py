@@ -158,14 +158,15 @@ class FvmBatch:
 
   def autotune(self, steps: int = 10) -> int:
     """Times the launch configurations and keeps the fastest; returns its
-    index (row shape + 2 * column scheme + 10 * stencil)."""
+    index (row shape + 2 * column scheme + 10 * stencil, or 20: each member's
+    whole chunk resident in shared memory, for small grids)."""
     chosen = ctypes.c_int(-1)
     nat.check(self._lib.cfd_fvm_batch_autotune(self._h, plans.current_stream_ptr(self.device),
                                                int(steps), ctypes.byref(chosen)),
               'cfd_fvm_batch_autotune')
     return int(chosen.value)
 
-  LAUNCH_CHOICES = 20
+  LAUNCH_CHOICES = 21
 
   def set_launch(self, choice: int):
     """Pins the launch configuration (see autotune); results do not change."""

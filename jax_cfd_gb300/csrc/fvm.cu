@@ -1708,6 +1708,242 @@ __global__ void fvm_batch_project_out_kernel(const FvmMember* __restrict__ mem) 
                     reinterpret_cast<const float*>(m.spec), m.f[0][0], m.f[0][1]);
 }
 
+// ---- Shared-memory-resident chunk for small grids ----
+// One block per member runs the member's whole chunk with everything in
+// shared memory: the state (u*, v* after each stencil), its projected copy,
+// the packed row spectrum / pressure q, and the transform buffer.  Each phase
+// evaluates the expressions of the per-step kernels -- the tiles' face fluxes
+// and cell update (explicit_tile), div_rfft_rows, col_pinv_cols and
+// irfft_rows on the same Stockham engine, project_out_cells -- so a member's
+// bits equal those of the launch-per-step path; only the launches, the
+// global round trips and the grid-wide step boundaries go away.
+constexpr int kResidentThreads = 512;
+
+CFD_HD size_t resident_smem(int nx, int ny) {
+  const int L = ny / 2;
+  const size_t n = (size_t)nx * ny;
+  const size_t rows_w = (size_t)nx * padded_len(L);
+  const size_t cols_w = (size_t)(L + 1) * padded_len(nx);
+  return 5 * n * sizeof(float) + (rows_w > cols_w ? rows_w : cols_w) * sizeof(float2);
+}
+
+// x-face flux pair after row r at column j of the smem fields (u, v), as
+// explicit_tile computes it: rows r-1 .. r+2 and u at (r, j+1).
+template <int CONVECT>
+CFD_D float2 resident_xface(const FvmParams& p, const float* __restrict__ su,
+                            const float* __restrict__ sv, int r, int j) {
+  const int mx = p.nx - 1, my = p.ny - 1, lg = p.log2ny;
+  auto at = [&](int i, int jj) {
+    const int k = ((i & mx) << lg) + (jj & my);
+    return make_float2(su[k], sv[k]);
+  };
+  const float2 cm = at(r - 1, j), c0 = at(r, j), c1 = at(r + 1, j), c2 = at(r + 2, j);
+  const float uy1 = su[((r & mx) << lg) + ((j + 1) & my)];
+  const float2 U = mul2(splat2(0.5f), add2(splat2(c0.x), make_float2(c1.x, uy1)));
+  if (CONVECT == 0) return tvd_flux2(cm, c0, c1, c2, U, p.cfl_x);
+  const float2 cface = mul2(splat2(0.5f), add2(c0, c1));
+  return mul2(make_float2(U.x, cface.y), make_float2(U.x, U.y));
+}
+
+// y-face flux pair after column j at row i: columns j-1 .. j+2 and v at
+// (i+1, j).
+template <int CONVECT>
+CFD_D float2 resident_yface(const FvmParams& p, const float* __restrict__ su,
+                            const float* __restrict__ sv, int i, int j) {
+  const int mx = p.nx - 1, my = p.ny - 1, lg = p.log2ny;
+  const int row = (i & mx) << lg;
+  auto at = [&](int jj) {
+    const int k = row + (jj & my);
+    return make_float2(su[k], sv[k]);
+  };
+  const float2 cm = at(j - 1), c0 = at(j), c1 = at(j + 1), c2 = at(j + 2);
+  const float vx1 = sv[(((i + 1) & mx) << lg) + (j & my)];
+  const float2 V = mul2(splat2(0.5f), add2(splat2(c0.y), make_float2(vx1, c1.y)));
+  if (CONVECT == 0) return tvd_flux2(cm, c0, c1, c2, V, p.cfl_y);
+  const float2 cface = mul2(splat2(0.5f), add2(c0, c1));
+  return mul2(make_float2(cface.x, V.y), make_float2(V.x, V.y));
+}
+
+// fft_inplace as a call: the resident kernel makes four transforms, and four
+// inlined copies of the engine exhaust its registers (3 KB of stack and
+// spills); as calls each keeps the engine's own allocation.
+template <int SIGN>
+__device__ __noinline__ void resident_fft(float2* buf, int log2L, int batch, int bstride,
+                                          const float2* __restrict__ twp, int t) {
+  fft_inplace<SIGN>(buf, log2L, batch, bstride, twp, t);
+}
+
+template <int CONVECT>
+__global__ void __launch_bounds__(kResidentThreads, 1)
+    fvm_batch_resident_kernel(const FvmMember* __restrict__ mem) {
+  const FvmMember& m = mem[blockIdx.x];
+  const int steps = m.steps;
+  if (steps <= 0) return;  // uniform per block
+  const FvmParams p = m.p;
+  extern __shared__ float4 smem_resident[];
+  const int nx = p.nx, ny = p.ny, L = ny >> 1, lg = p.log2ny, log2L = lg - 1;
+  const int n = nx * ny, mx = nx - 1, my = ny - 1;
+  float* const Au = reinterpret_cast<float*>(smem_resident);  // projected input
+  float* const Av = Au + n;
+  float* const Bu = Av + n;  // u*, v* after the stencil
+  float* const Bv = Bu + n;
+  float* const Q = Bv + n;  // packed row spectrum, then q
+  float2* const Qc = reinterpret_cast<float2*>(Q);
+  float2* const W = reinterpret_cast<float2*>(Q + n);
+  const int tid = threadIdx.x, T = blockDim.x;
+  const int PL = padded_len(L), CS = padded_len(nx);
+  const float2 ihx = splat2(p.inv_hx), ihy = splat2(p.inv_hy);
+
+  for (int idx = tid; idx < n; idx += T) {
+    Au[idx] = m.f[0][0][idx];
+    Av[idx] = m.f[0][1][idx];
+  }
+  __syncthreads();
+#pragma unroll 1
+  for (int k = 0; k < steps; ++k) {
+    if (k > 0) {
+      // u = u* - (q[i+1] - q[i]) / hx, v = v* - (q[j+1] - q[j]) / hy
+      for (int idx = tid; idx < n; idx += T) {
+        const int i = idx >> lg, j = idx & my;
+        const float q0 = Q[idx];
+        const float qx = Q[(((i + 1) & mx) << lg) + j], qy = Q[(i << lg) + ((j + 1) & my)];
+        Au[idx] = Bu[idx] - (qx - q0) * p.inv_hx;
+        Av[idx] = Bv[idx] - (qy - q0) * p.inv_hy;
+      }
+      __syncthreads();
+    }
+    // Explicit terms and forward Euler (equations.py:102-110): (A) -> (B).
+    for (int idx = tid; idx < n; idx += T) {
+      const int i = idx >> lg, j = idx & my;
+      const float2 uv = make_float2(Au[idx], Av[idx]);
+      const float2 fx_hi = resident_xface<CONVECT>(p, Au, Av, i, j);
+      const float2 fx_lo = resident_xface<CONVECT>(p, Au, Av, i - 1, j);
+      const float2 fy_hi = resident_yface<CONVECT>(p, Au, Av, i, j);
+      const float2 fy_lo = resident_yface<CONVECT>(p, Au, Av, i, j - 1);
+      const float2 dx = mul2(sub2(fx_hi, fx_lo), ihx);
+      float2 kk = fma2(sub2(fy_hi, fy_lo), ihy, dx);
+      kk = make_float2(-kk.x, -kk.y);
+      const int up = (((i - 1) & mx) << lg) + j, dn = (((i + 1) & mx) << lg) + j;
+      const int lf = (i << lg) + ((j - 1) & my), rt = (i << lg) + ((j + 1) & my);
+      kk = add_diffusion_forcing<0>(p, kk, uv,
+                                    add2(make_float2(Au[up], Av[up]), make_float2(Au[dn], Av[dn])),
+                                    add2(make_float2(Au[lf], Av[lf]), make_float2(Au[rt], Av[rt])),
+                                    i, j);
+      const float2 nxt = fma2(splat2(p.dt), kk, uv);
+      Bu[idx] = nxt.x;
+      Bv[idx] = nxt.y;
+    }
+    __syncthreads();
+    // Backward-difference divergence and packed row rFFT (div_rfft_rows).
+    {
+      const int log2g = lg - 2;
+      for (int g = tid; g < (nx << log2g); g += T) {
+        const int i = g >> log2g, jj = (g & ((1 << log2g) - 1)) << 2;
+        const int a0 = (i << lg) + jj, b0 = (((i - 1) & mx) << lg) + jj;
+        const float cm = Bv[(i << lg) + ((jj - 1) & my)];
+        const float d0 = (Bu[a0] - Bu[b0]) * p.inv_hx + (Bv[a0] - cm) * p.inv_hy;
+        const float d1 = (Bu[a0 + 1] - Bu[b0 + 1]) * p.inv_hx + (Bv[a0 + 1] - Bv[a0]) * p.inv_hy;
+        const float d2 = (Bu[a0 + 2] - Bu[b0 + 2]) * p.inv_hx + (Bv[a0 + 2] - Bv[a0 + 1]) * p.inv_hy;
+        const float d3 = (Bu[a0 + 3] - Bu[b0 + 3]) * p.inv_hx + (Bv[a0 + 3] - Bv[a0 + 2]) * p.inv_hy;
+        float2* z = W + i * PL;
+        z[pidx(jj >> 1)] = make_float2(d0, d1);
+        z[pidx((jj >> 1) + 1)] = make_float2(d2, d3);
+      }
+      __syncthreads();
+      resident_fft<-1>(W, log2L, nx, PL, p.twp_y, tid);
+      const int half = L >> 1, log2h = log2L - 1;
+      for (int idx = tid; idx < (nx << log2h); idx += T) {
+        const int r = idx >> log2h, kq = idx & (half - 1);
+        float2* out = Qc + r * L;
+        const float2* z = W + r * PL;
+        if (kq == 0) {
+          const float2 z0 = z[0];
+          out[0] = make_float2(z0.x + z0.y, z0.x - z0.y);
+          float2 xk, xm;
+          const float2 zh = z[pidx(half)];
+          rfft_post_pair(zh, zh, __ldg(p.tw_y + half), &xk, &xm);
+          out[half] = xk;
+        } else {
+          float2 xk, xm;
+          rfft_post_pair(z[pidx(kq)], z[pidx(L - kq)], __ldg(p.tw_y + kq), &xk, &xm);
+          out[kq] = xk;
+          out[L - kq] = xm;
+        }
+      }
+      __syncthreads();
+    }
+    // Column pass (col_pinv_cols): the L complex columns, the DC column
+    // (column 0's real parts) and the Nyquist column (its imaginary parts) as
+    // L + 1 sequences.
+    {
+      for (int idx = tid; idx < (L + 1) * nx; idx += T) {
+        const int i = idx / (L + 1), w = idx - i * (L + 1);
+        float2 x;
+        if (w == L) x = make_float2(Q[i * L * 2 + 1], 0.f);
+        else if (w == 0) x = make_float2(Q[i * L * 2], 0.f);
+        else x = Qc[i * L + w];
+        W[w * CS + pidx(i)] = x;
+      }
+      __syncthreads();
+      resident_fft<-1>(W, p.log2nx, L + 1, CS, p.twp_x, tid);
+      for (int idx = tid; idx < (L + 1) * nx; idx += T) {
+        const int kx = idx / (L + 1), w = idx - kx * (L + 1);
+        float2* e = W + w * CS + pidx(kx);
+        *e = c_scale(*e, pinv_diag(p, kx, w));
+      }
+      __syncthreads();
+      resident_fft<1>(W, p.log2nx, L + 1, CS, p.twp_x, tid);
+      for (int idx = tid; idx < (L + 1) * nx; idx += T) {
+        const int i = idx / (L + 1), w = idx - i * (L + 1);
+        const float2 x = W[w * CS + pidx(i)];
+        if (w == L) Q[i * L * 2 + 1] = x.x;
+        else if (w == 0) Q[i * L * 2] = x.x;
+        else Qc[i * L + w] = x;
+      }
+      __syncthreads();
+    }
+    // Packed row irFFT -> q (irfft_rows).
+    {
+      const int half = L >> 1, log2h = log2L - 1;
+      for (int idx = tid; idx < (nx << log2h); idx += T) {
+        const int r = idx >> log2h, kq = idx & (half - 1);
+        const float2* in = Qc + r * L;
+        float2* z = W + r * PL;
+        if (kq == 0) {
+          const float2 x0 = in[0];
+          z[0] = make_float2(x0.x + x0.y, x0.x - x0.y);
+          const float2 xh = in[half];
+          float2 zk, zm;
+          irfft_pre_pair(xh, xh, __ldg(p.tw_y + half), &zk, &zm);
+          z[pidx(half)] = zk;
+        } else {
+          float2 zk, zm;
+          irfft_pre_pair(in[kq], in[L - kq], __ldg(p.tw_y + kq), &zk, &zm);
+          z[pidx(kq)] = zk;
+          z[pidx(L - kq)] = zm;
+        }
+      }
+      __syncthreads();
+      resident_fft<1>(W, log2L, nx, PL, p.twp_y, tid);
+      for (int idx = tid; idx < nx * L; idx += T) {
+        const int r = idx / L, nn = idx - r * L;
+        const float2 a = W[r * PL + pidx(nn)];
+        Q[r * ny + 2 * nn] = a.x;
+        Q[r * ny + 2 * nn + 1] = a.y;
+      }
+      __syncthreads();
+    }
+  }
+  // The chunk's final projection (project_out_cells) into the state.
+  for (int idx = tid; idx < n; idx += T) {
+    const int i = idx >> lg, j = idx & my;
+    const float q0 = Q[idx];
+    const float qx = Q[(((i + 1) & mx) << lg) + j], qy = Q[(i << lg) + ((j + 1) & my)];
+    m.f[0][0][idx] = Bu[idx] - (qx - q0) * p.inv_hx;
+    m.f[0][1][idx] = Bv[idx] - (qy - q0) * p.inv_hy;
+  }
+}
+
 int fft_rows_per_block(int log2L, int nrows, int target_threads = 256) {
   const int P = log2L >= 4 ? 16 : (1 << log2L);
   int rows = (target_threads * P) >> log2L;
@@ -2168,6 +2404,26 @@ static cudaError_t batch_col_tma_launch(const FvmParams& p, const FvmMember* mem
     case 10: return batch_col_tma_impl<10>(p, mem, count, k, s);
     default: return batch_col_tma_impl<11>(p, mem, count, k, s);
   }
+}
+
+bool fvm_batch_resident_ok(const FvmParams& p) {
+  return fvm_batch_shape_ok(p) && resident_smem(p.nx, p.ny) <= 227 * 1024;
+}
+
+cudaError_t launch_fvm_batch_resident(const FvmParams& p, const FvmMember* mem, int count,
+                                      cudaStream_t s) {
+  if (!fvm_batch_resident_ok(p) || count < 1) return cudaErrorInvalidValue;
+  const size_t smem = resident_smem(p.nx, p.ny);
+  if (p.convect == 0) {
+    cudaError_t e = set_smem(fvm_batch_resident_kernel<0>, smem);
+    if (e != cudaSuccess) return e;
+    fvm_batch_resident_kernel<0><<<count, kResidentThreads, smem, s>>>(mem);
+  } else {
+    cudaError_t e = set_smem(fvm_batch_resident_kernel<1>, smem);
+    if (e != cudaSuccess) return e;
+    fvm_batch_resident_kernel<1><<<count, kResidentThreads, smem, s>>>(mem);
+  }
+  return cudaGetLastError();
 }
 
 cudaError_t launch_fvm_batch_step(const FvmParams& p, const FvmMember* mem, int count, int k,

@@ -47,7 +47,8 @@ struct FvmParams {
   int col_mode;        // column pass: 0 per-block columns, 1/2 clusters of 4/8,
                        // 3/4 persistent register-pipelined groups of 4/2 columns,
                        // 5 as 3 with the groups staged by TMA tensor loads
-  int stencil;         // explicit step: 0 shared-memory tiles, 1 warp streams
+  int stencil;         // explicit step: 0 shared-memory tiles, 1 warp streams,
+                       // 2 (batches of small grids) whole chunks resident in shared memory
   int row_feed;        // row transforms: 0 loads through registers, 1 bulk copies
   // Implicit diffusion (diffusion.solve_fast_diag) on the same transforms:
   int row_field;       // forward row transform of the field us itself, not div
@@ -110,6 +111,13 @@ cudaError_t launch_fvm_batch_step(const FvmParams& shape, const FvmMember* membe
                                   int count, int k, cudaStream_t s);
 cudaError_t launch_fvm_batch_project_out(const FvmParams& shape, const FvmMember* members,
                                          int count, cudaStream_t s);
+// A whole chunk of every member (its steps, then the final projection into
+// the state) in one launch, one block per member with the member's fields in
+// shared memory; for grids whose fields fit (fvm_batch_resident_ok).  Same
+// bits as the per-step launches.
+bool fvm_batch_resident_ok(const FvmParams& shape);
+cudaError_t launch_fvm_batch_resident(const FvmParams& shape, const FvmMember* members,
+                                      int count, cudaStream_t s);
 // Health record of one batch slot after a chunk (layout of the C ABI's
 // cfd_health): flags (kHealthNonFinite: the state holds a NaN or an
 // infinity) and the largest magnitude among the state's finite values.

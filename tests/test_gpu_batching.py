@@ -108,6 +108,37 @@ def test_every_batch_launch_configuration_gives_the_same_bits(cuda_device, shape
         assert torch.equal(got, w), (choice, i)
 
 
+@pytest.mark.parametrize('shape', [(64, 64), (128, 64), (64, 128)])
+def test_resident_chunk_gives_the_per_step_bits(cuda_device, shape):
+  """Launch configuration 20 runs each member's whole chunk in one block with
+  the fields in shared memory; with ragged steps and an idle slot it must
+  give the per-step launches' bits (and so the single trajectories')."""
+  draws = [(shape, 31, 1e-3, 4, 2.0), (shape, 32, 1e-4, 2, 1.0), (shape, 33, 1e-3, 8, 3.0)]
+  pairs = [_member(*d) for d in draws]
+  b = _batch([m for m, _ in pairs], cuda_device)
+  results = {}
+  for choice in (0, 20):
+    b.set_launch(choice)
+    for graph in (False, True):
+      for i, (_, v0) in enumerate(pairs):
+        _load(b, i, v0, cuda_device)
+        b.set_steps(i, [12, 0, 7][i])
+      b.run(12, graph=graph)
+      torch.cuda.synchronize(cuda_device)
+      results[(choice, graph)] = [tuple(t.clone() for t in b.state(i)) for i in range(3)]
+  for key, states in results.items():
+    for i in range(3):
+      for got, want in zip(states[i], results[(0, False)][i]):
+        assert torch.equal(got, want), (key, i)
+  for i, (m, v0) in enumerate(pairs):
+    want = _single(m, v0, [12, 0, 7][i], cuda_device)
+    for got, w in zip(results[(20, True)][i], want):
+      assert torch.equal(got, w)
+  # Health records are written after the resident chunk too.
+  h = b.health()
+  assert h['flags'][0] == 0 and h['max_abs'][0] > 0
+
+
 def test_ragged_steps_and_idle_slots(cuda_device):
   draws = [((128, 64), 21, 1e-3, 4, 2.0), ((128, 64), 22, 3e-3, 2, 3.0),
            ((128, 64), 23, 1e-3, 8, 1.5)]
