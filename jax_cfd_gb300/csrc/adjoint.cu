@@ -17,9 +17,12 @@
 // derivative of apply_tvd_limiter(lax_wendroff, van_leer_limiter)
 // (interpolation.py:158-303) taken branch by branch the way jax.grad
 // differentiates jnp.where and safe_div (the unselected branch and the
-// replaced denominator get no gradient).  A thread owns one cell and gathers
-// the contributions of every face flux that reads the cell: as advected
-// quantity (4 faces per direction) and as face velocity (2 faces).
+// replaced denominator get no gradient).  A block owns a 16 x 32 tile of
+// cells: it first evaluates the vector-Jacobian product of every face of the
+// four flux families (u and v, x- and y-normal faces) that the tile's cells
+// read, once per face, into shared memory, then each cell gathers the
+// contributions of the faces that read it: as advected quantity (4 faces per
+// direction) and as face velocity (2 faces).
 #include "common.cuh"
 #include "kernels.h"
 
@@ -55,10 +58,13 @@ CFD_D FaceVjp face_vjp(float cm, float c0, float c1, float c2, float U, float cf
   const float d = c - b, n = b - a;
   // safe_div: where d == 0 the reference divides its own numerator by 1,
   // which is (b - a) for U > 0 and (a - b) otherwise.
-  const float r = d != 0.f ? n / d : (pos ? n : -n);
+  // (Approximate reciprocals: the derivative is compared with float64
+  // autograd within float32 tolerances, not bit for bit.)
+  const float r = d != 0.f ? __fdividef(n, d) : (pos ? n : -n);
   const bool lim = r > 0.f;
-  const float phi = lim ? 2.f * r / (1.f + r) : 0.f;
-  const float dphi = lim ? 2.f / ((1.f + r) * (1.f + r)) : 0.f;
+  const float inv = lim ? __fdividef(1.f, 1.f + r) : 0.f;
+  const float phi = 2.f * r * inv;
+  const float dphi = 2.f * inv * inv;
   const float cf = b + kap * d * phi;
   float da, db, dc;
   if (d != 0.f) {
@@ -102,73 +108,88 @@ CFD_D float lap_at(const FvmParams& p, const Field& f, int i, int j) {
          (f(i, j - 1) + f(i, j + 1)) * p.sy;
 }
 
+constexpr int kAdjTI = 16, kAdjTJ = 32;                  // cells per tile
+constexpr int kAdjFI = kAdjTI + 3, kAdjFJ = kAdjTJ + 3;  // faces: rows/cols from i0-2 / j0-2
+constexpr int kAdjFaces = kAdjFI * kAdjFJ;
+constexpr int kAdjThreads = 256;
+// Shared memory: 4 families x 5 values (g[0..3], gU) per face.
+constexpr size_t kAdjSmem = (size_t)4 * 5 * kAdjFaces * sizeof(float);
+
 template <int CONVECT>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(kAdjThreads)
     fvm_adjoint_kernel(FvmParams p, const float* __restrict__ u, const float* __restrict__ v,
                        const float* __restrict__ wu_, const float* __restrict__ wv_,
                        float* __restrict__ gu, float* __restrict__ gv,
                        float* __restrict__ nu_dot) {
+  extern __shared__ float adj_smem[];
   const int mx = p.nx - 1, my = p.ny - 1;
   const Field U{u, mx, my, p.log2ny}, V{v, mx, my, p.log2ny};
   const Field WU{wu_, mx, my, p.log2ny}, WV{wv_, mx, my, p.log2ny};
-  const size_t n = (size_t)p.nx * p.ny;
-  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < n;
-       idx += (size_t)gridDim.x * blockDim.x) {
-    const int i = (int)(idx >> p.log2ny), j = (int)(idx & my);
+  const int i0 = blockIdx.y * kAdjTI, j0 = blockIdx.x * kAdjTJ;
+  const int tid = threadIdx.x;
+  // Family f, value k of face slot s at adj_smem[(f * 5 + k) * kAdjFaces + s];
+  // slot s = (fi - i0 + 2) * kAdjFJ + (fj - j0 + 2).
+  auto rec = [&](int fam, int k, int fi, int fj) -> float& {
+    return adj_smem[(fam * 5 + k) * kAdjFaces + (fi - i0 + 2) * kAdjFJ + (fj - j0 + 2)];
+  };
+  for (int e = tid; e < 4 * kAdjFaces; e += kAdjThreads) {
+    const int fam = e / kAdjFaces, sl = e - fam * kAdjFaces;
+    const int fi = i0 - 2 + sl / kAdjFJ, fj = j0 - 2 + sl % kAdjFJ;
+    FaceVjp o;
+    if (fam == 0) {
+      // u's x-face after row fi: c = u along x, U = 0.5 u[fi] + 0.5 u[fi+1].
+      o = face_vjp<CONVECT>(U(fi - 1, fj), U(fi, fj), U(fi + 1, fj), U(fi + 2, fj),
+                            0.5f * U(fi, fj) + 0.5f * U(fi + 1, fj), p.cfl_x,
+                            (WU(fi + 1, fj) - WU(fi, fj)) * p.inv_hx);
+    } else if (fam == 1) {
+      // u's y-face after column fj: c = u along y, V = 0.5 v[fi] + 0.5 v[fi+1].
+      o = face_vjp<CONVECT>(U(fi, fj - 1), U(fi, fj), U(fi, fj + 1), U(fi, fj + 2),
+                            0.5f * V(fi, fj) + 0.5f * V(fi + 1, fj), p.cfl_y,
+                            (WU(fi, fj + 1) - WU(fi, fj)) * p.inv_hy);
+    } else if (fam == 2) {
+      // v's y-face after column fj: c = v along y, V = 0.5 v[fj] + 0.5 v[fj+1].
+      o = face_vjp<CONVECT>(V(fi, fj - 1), V(fi, fj), V(fi, fj + 1), V(fi, fj + 2),
+                            0.5f * V(fi, fj) + 0.5f * V(fi, fj + 1), p.cfl_y,
+                            (WV(fi, fj + 1) - WV(fi, fj)) * p.inv_hy);
+    } else {
+      // v's x-face after row fi: c = v along x, U = 0.5 u[fj] + 0.5 u[fj+1].
+      o = face_vjp<CONVECT>(V(fi - 1, fj), V(fi, fj), V(fi + 1, fj), V(fi + 2, fj),
+                            0.5f * U(fi, fj) + 0.5f * U(fi, fj + 1), p.cfl_x,
+                            (WV(fi + 1, fj) - WV(fi, fj)) * p.inv_hx);
+    }
+    float* base = adj_smem + fam * 5 * kAdjFaces + sl;
+    base[0] = o.g[0];
+    base[kAdjFaces] = o.g[1];
+    base[2 * kAdjFaces] = o.g[2];
+    base[3 * kAdjFaces] = o.g[3];
+    base[4 * kAdjFaces] = o.gU;
+  }
+  __syncthreads();
+  for (int c = tid; c < kAdjTI * kAdjTJ; c += kAdjThreads) {
+    const int i = i0 + c / kAdjTJ, j = j0 + c % kAdjTJ;
+    if (i > mx || j > my) continue;
     float au = 0.f, av = 0.f;
 #pragma unroll
     for (int q = -1; q <= 2; ++q) {
-      // u's x-faces f = i - q: c = u along x, U = 0.5 u[f] + 0.5 u[f+1].
-      {
-        const int f = i - q;
-        const FaceVjp o = face_vjp<CONVECT>(
-            U(f - 1, j), U(f, j), U(f + 1, j), U(f + 2, j), 0.5f * U(f, j) + 0.5f * U(f + 1, j),
-            p.cfl_x, (WU(f + 1, j) - WU(f, j)) * p.inv_hx);
-        au += o.g[q + 1];
-        if (q == 0 || q == 1) au += 0.5f * o.gU;
+      // u's x-faces f = i - q and v's x-faces f = i - q at column j.
+      au += rec(0, q + 1, i - q, j);
+      av += rec(3, q + 1, i - q, j);
+      // u's and v's y-faces g = j - q at row i.
+      au += rec(1, q + 1, i, j - q);
+      av += rec(2, q + 1, i, j - q);
+      if (q == 0 || q == 1) {
+        au += 0.5f * rec(0, 4, i - q, j);
+        av += 0.5f * rec(2, 4, i, j - q);
       }
-      // u's y-faces g = j - q: c = u along y, V = 0.5 v[i, g] + 0.5 v[i+1, g].
-      {
-        const int g = j - q;
-        const FaceVjp o = face_vjp<CONVECT>(
-            U(i, g - 1), U(i, g), U(i, g + 1), U(i, g + 2), 0.5f * V(i, g) + 0.5f * V(i + 1, g),
-            p.cfl_y, (WU(i, g + 1) - WU(i, g)) * p.inv_hy);
-        au += o.g[q + 1];
-        if (q == 0) av += 0.5f * o.gU;
-      }
-      // v's y-faces g = j - q: c = v along y, V = 0.5 v[g] + 0.5 v[g+1].
-      {
-        const int g = j - q;
-        const FaceVjp o = face_vjp<CONVECT>(
-            V(i, g - 1), V(i, g), V(i, g + 1), V(i, g + 2), 0.5f * V(i, g) + 0.5f * V(i, g + 1),
-            p.cfl_y, (WV(i, g + 1) - WV(i, g)) * p.inv_hy);
-        av += o.g[q + 1];
-        if (q == 0 || q == 1) av += 0.5f * o.gU;
-      }
-      // v's x-faces f = i - q: c = v along x, U = 0.5 u[f, j] + 0.5 u[f, j+1].
-      {
-        const int f = i - q;
-        const FaceVjp o = face_vjp<CONVECT>(
-            V(f - 1, j), V(f, j), V(f + 1, j), V(f + 2, j), 0.5f * U(f, j) + 0.5f * U(f, j + 1),
-            p.cfl_x, (WV(f + 1, j) - WV(f, j)) * p.inv_hx);
-        av += o.g[q + 1];
-        if (q == 0) au += 0.5f * o.gU;
+      if (q == 0) {
+        av += 0.5f * rec(1, 4, i, j);
+        au += 0.5f * rec(3, 4, i, j);
       }
     }
     // The two velocity-only faces: u's y-face (i-1, j) reads v[i, j] and v's
     // x-face (i, j-1) reads u[i, j].
-    {
-      const FaceVjp o = face_vjp<CONVECT>(
-          U(i - 1, j - 1), U(i - 1, j), U(i - 1, j + 1), U(i - 1, j + 2),
-          0.5f * V(i - 1, j) + 0.5f * V(i, j), p.cfl_y, (WU(i - 1, j + 1) - WU(i - 1, j)) * p.inv_hy);
-      av += 0.5f * o.gU;
-    }
-    {
-      const FaceVjp o = face_vjp<CONVECT>(
-          V(i - 1, j - 1), V(i, j - 1), V(i + 1, j - 1), V(i + 2, j - 1),
-          0.5f * U(i, j - 1) + 0.5f * U(i, j), p.cfl_x, (WV(i + 1, j - 1) - WV(i, j - 1)) * p.inv_hx);
-      au += 0.5f * o.gU;
-    }
+    av += 0.5f * rec(1, 4, i - 1, j);
+    au += 0.5f * rec(3, 4, i, j - 1);
     const float wu = WU(i, j), wv = WV(i, j);
     float ku = au, kv = av;
     if (p.has_visc) {
@@ -180,6 +201,7 @@ __global__ void __launch_bounds__(256)
       ku += lin * wu;
       kv += lin * wv;
     }
+    const size_t idx = ((size_t)i << p.log2ny) + j;
     gu[idx] = wu + p.dt * ku;
     gv[idx] = wv + p.dt * kv;
     if (nu_dot) nu_dot[idx] = wu * lap_at(p, U, i, j) + wv * lap_at(p, V, i, j);
@@ -191,13 +213,18 @@ __global__ void __launch_bounds__(256)
 cudaError_t launch_fvm_adjoint(const FvmParams& p, const float* u, const float* v,
                                const float* wu, const float* wv, float* gu, float* gv,
                                float* nu_dot, cudaStream_t s) {
-  const size_t n = (size_t)p.nx * p.ny;
-  size_t blocks = (n + 255) / 256;
-  if (blocks > 152 * 8) blocks = 152 * 8;
-  if (p.convect == 0)
-    fvm_adjoint_kernel<0><<<(int)blocks, 256, 0, s>>>(p, u, v, wu, wv, gu, gv, nu_dot);
-  else
-    fvm_adjoint_kernel<1><<<(int)blocks, 256, 0, s>>>(p, u, v, wu, wv, gu, gv, nu_dot);
+  const dim3 grid((p.ny + kAdjTJ - 1) / kAdjTJ, (p.nx + kAdjTI - 1) / kAdjTI);
+  if (p.convect == 0) {
+    cudaError_t e = cudaFuncSetAttribute(fvm_adjoint_kernel<0>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kAdjSmem);
+    if (e != cudaSuccess) return e;
+    fvm_adjoint_kernel<0><<<grid, kAdjThreads, kAdjSmem, s>>>(p, u, v, wu, wv, gu, gv, nu_dot);
+  } else {
+    cudaError_t e = cudaFuncSetAttribute(fvm_adjoint_kernel<1>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kAdjSmem);
+    if (e != cudaSuccess) return e;
+    fvm_adjoint_kernel<1><<<grid, kAdjThreads, kAdjSmem, s>>>(p, u, v, wu, wv, gu, gv, nu_dot);
+  }
   return cudaGetLastError();
 }
 
