@@ -144,7 +144,8 @@ int cfd_fvm_profile(cfd_fvm_plan* plan, void* stream, const float* u,
                     float* ms_out);
 /* Autotuner: times `steps` steps for each candidate launch configuration
  * (transform row-block shape x column-pass scheme x stencil scheme x row
- * feed; u, v read-only, results go to the scratch arrays), keeps the fastest
+ * feed x rows per stencil warp; u, v read-only, results go to the scratch
+ * arrays), keeps the fastest
  * in the plan and writes its index (see cfd_fvm_plan_set_launch) to *chosen
  * (may be NULL).  Synchronises the stream. */
 int cfd_fvm_plan_autotune(cfd_fvm_plan* plan, void* stream, const float* u,
@@ -155,8 +156,9 @@ int cfd_fvm_plan_autotune(cfd_fvm_plan* plan, void* stream, const float* u,
  * 1/2 clusters of 4/8, 3/4 persistent pipelined groups of 4/2 columns, 5
  * groups of 4 staged by TMA tensor loads) + 12 * stencil scheme (0
  * shared-memory tiles, 1 warp streams) + 24 * row feed (0 registers, 1 bulk
- * copies): 48 choices); results do not depend on it.  cfd_fvm_plan_get_launch
- * returns the current one. */
+ * copies) + 48 * rows per stencil warp (0: 16, 1: 8, 2: 32; 1 and 2 with warp
+ * streams only, each warp re-reading 4 halo rows): 144 choices); results do
+ * not depend on it.  cfd_fvm_plan_get_launch returns the current one. */
 int cfd_fvm_plan_set_launch(cfd_fvm_plan* plan, int choice);
 int cfd_fvm_plan_get_launch(const cfd_fvm_plan* plan);
 /* du/dt from advection + diffusion + forcing (no projection). */
@@ -332,8 +334,10 @@ long long cfd_spec_plan_bytes(const cfd_spec_plan* plan);
  * 4/2 columns with cp.async while transforming the current one in registers
  * (512 <= nx <= 4096), 4 as 2 with each stage's column update and the next
  * stage's column prep fused into one pass; plus 5 x the row scheme: 0 the
- * shared-memory row pass, 1 the register-pass row pass (512 <= ny <= 4096).
- * Results are bit-for-bit the same for every choice. */
+ * shared-memory row pass, 1 the register-pass row pass (512 <= ny <= 4096),
+ * 2 the same with registers sized for three blocks per multiprocessor
+ * (512 <= ny <= 2048): 15 choices.  Results are bit-for-bit the same for
+ * every choice. */
 int cfd_spec_plan_set_launch(cfd_spec_plan* plan, int choice);
 int cfd_spec_plan_get_launch(const cfd_spec_plan* plan);
 /* Velocity-independent forcing (fx, fy real [nx, ny] on the device, either may

@@ -104,14 +104,19 @@ cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
 // Launch configurations of the FVM step (see cfd_fvm_plan_autotune).
 // Index = row-transform shape + 2 * column scheme + 12 * stencil scheme
-// + 24 * row feed.
-constexpr int kLaunchChoices = 48;
+// + 24 * row feed + 48 * stream rows per warp (16, 8, 32; warp streams only).
+constexpr int kLaunchChoices = 144;
 bool launch_choice_ok(const cfd::FvmParams& p, int c) {
-  const int col = (c >> 1) % 6, stencil = (c / 12) & 1, feed = c / 24;
+  const int col = (c >> 1) % 6, stencil = (c / 12) & 1, feed = (c / 24) & 1, rows = c / 48;
   if ((col == 1 || col == 2) && !cfd::col_cluster_ok(p, col == 1 ? 4 : 8)) return false;
   if ((col == 3 || col == 4) && !cfd::col_pipe_ok(p, col == 4)) return false;
   if (col == 5 && !(p.col_tmap && cfd::col_tma_grid_ok(p))) return false;
-  if (stencil == 1 && !cfd::stream_stencil_ok(p)) return false;
+  if (rows != 0 && stencil != 1) return false;
+  if (stencil == 1) {
+    cfd::FvmParams q = p;
+    q.stream_rows = rows;
+    if (!cfd::stream_stencil_ok(q)) return false;
+  }
   if (feed == 1 && !cfd::bulk_feed_ok(p)) return false;
   return true;
 }
@@ -119,7 +124,8 @@ void set_launch_choice(cfd::FvmParams* p, int c) {
   p->fft_shape = c & 1;
   p->col_mode = (c >> 1) % 6;
   p->stencil = (c / 12) & 1;
-  p->row_feed = c / 24;
+  p->row_feed = (c / 24) & 1;
+  p->stream_rows = c / 48;
 }
 
 // Captures `enqueue` (run on a private capture stream) into an executable graph.
@@ -379,12 +385,35 @@ static bool encode_spec_map(CUtensorMap* map, float2* spec, int nx, int ny, int 
          CUDA_SUCCESS;
 }
 
+// Default launch of a single plan from 128^2 up, from a sweep of every
+// configuration of the step at 128^2 .. 2048^2 on GB300 (the default is the
+// fastest there or within 3 % of it; the autotuner can still revise it):
+// narrow row blocks, rows fed by bulk copies where they fit, the persistent
+// column pass from 256 rows (TMA-staged from 1024, where the map encodes),
+// warp streams with 8 rows per warp below 2^22 cells and 16 from there.  Per
+// step: 128^2 31.2 against 40.4 us for the earlier default (tiles, per-block
+// columns, register feed), 256^2 23.0 against 39.4, 512^2 25.0 against
+// 44.4, 1024^2 33.2 against 38.8; 2048^2 unchanged (65.0).
+static void plan_default_launch(cfd::FvmParams* p) {
+  if ((long long)p->nx * p->ny < (1LL << 14)) return;
+  p->fft_shape = 1;
+  p->row_feed = cfd::bulk_feed_ok(*p) ? 1 : 0;
+  if (p->nx >= 256 && cfd::col_pipe_ok(*p, 0)) p->col_mode = 3;
+  cfd::FvmParams q = *p;
+  q.stream_rows = (long long)p->nx * p->ny < (1LL << 22) ? 1 : 0;
+  if (cfd::stream_stencil_ok(q)) {
+    p->stencil = 1;
+    p->stream_rows = q.stream_rows;
+  }
+}
+
 int cfd_fvm_plan_create(const cfd_fvm_config* cfg, cfd_fvm_plan** out) {
   if (!cfg || !out) return fail(CFD_ERR_INVALID_ARGUMENT, "null config or output pointer");
   *out = nullptr;
   cfd::FvmParams params;
   int rc = fvm_params_from_config(cfg, &params);
   if (rc) return rc;
+  plan_default_launch(&params);
   cfd_fvm_plan* plan = new cfd_fvm_plan();
   cfd::FvmParams& p = plan->p;
   p = params;
@@ -458,11 +487,12 @@ int cfd_fvm_plan_create(const cfd_fvm_config* cfg, cfd_fvm_plan** out) {
   }
   plan->bytes = bytes;
   // The TMA-staged column pass is a launch choice where the map encodes,
-  // and replaces the cp.async-staged default (3% faster on 2048^2).
+  // and replaces the cp.async-staged default from 1024 rows (3% faster on
+  // 2048^2, even at 1024^2, 6% slower at 512^2).
   if (cfd::col_tma_grid_ok(p) && encode_spec_map(&plan->spec_map, plan->spec, nx, ny)) {
     p.col_tmap = &plan->spec_map;
     p.col_tmap_spec = plan->spec;
-    if (p.col_mode == 3) p.col_mode = 5;
+    if (p.col_mode == 3 && nx >= 1024) p.col_mode = 5;
   }
   *out = plan;
   return CFD_OK;
@@ -841,7 +871,7 @@ int cfd_fvm_plan_set_launch(cfd_fvm_plan* plan, int choice) {
 int cfd_fvm_plan_get_launch(const cfd_fvm_plan* plan) {
   if (!plan) return -1;
   return plan->p.fft_shape + 2 * plan->p.col_mode + 12 * plan->p.stencil +
-         24 * plan->p.row_feed;
+         24 * plan->p.row_feed + 48 * plan->p.stream_rows;
 }
 
 // ---- Same-shape batches -------------------------------------------------
@@ -1566,8 +1596,11 @@ int cfd_spec_plan_create(const cfd_spec_config* cfg, cfd_spec_plan** out) {
     p.col_mode = 4;
     if (!cfd::spec_pipe_ok(p)) p.col_mode = 0;
   }
-  // The register-pass row pass measured faster at 2048^2 (66.5 against 72.1 us).
+  // The register-pass row pass measured faster at 2048^2 (66.5 against 72.1 us),
+  // and with registers for three blocks per multiprocessor faster still at
+  // ny = 2048 (61.7 against 66.3 us) but slower at ny = 1024 (24.6 against 20.8).
   p.row_mode = cfd::spec_row_pipe_ok(p) ? 1 : 0;
+  if (p.row_mode == 1 && p.log2L == 10) p.row_mode = 2;
   plan->stages = stages;
   for (int k = 0; k < stages; ++k) plan->coef[k] = coef[k];
   const int nx = cfg->nx;
@@ -1611,15 +1644,15 @@ int cfd_spec_plan_create(const cfd_spec_config* cfg, cfd_spec_plan** out) {
 
 long long cfd_spec_plan_bytes(const cfd_spec_plan* plan) { return plan ? plan->bytes : 0; }
 
-// Spectral launch choice = column scheme (0..4) + 5 * row scheme (0..1).
+// Spectral launch choice = column scheme (0..4) + 5 * row scheme (0..2).
 int cfd_spec_plan_set_launch(cfd_spec_plan* plan, int choice) {
-  if (!plan || choice < 0 || choice >= 10)
+  if (!plan || choice < 0 || choice >= 15)
     return fail(CFD_ERR_INVALID_ARGUMENT, "cfd_spec_plan_set_launch: bad arguments");
   cfd::SpecParams q = plan->p;
   q.col_mode = choice % 5;
   q.row_mode = choice / 5;
   if ((q.col_mode == 1 && !cfd::spec_cluster_ok(q)) || (q.col_mode >= 2 && !cfd::spec_pipe_ok(q)) ||
-      (q.row_mode == 1 && !cfd::spec_row_pipe_ok(q)))
+      (q.row_mode >= 1 && !cfd::spec_row_pipe_ok(q)))
     return fail(CFD_ERR_UNSUPPORTED, "cfd_spec_plan_set_launch: choice not available on this grid");
   plan->p.col_mode = q.col_mode;
   plan->p.row_mode = q.row_mode;

@@ -482,8 +482,11 @@ constexpr int kStreamCols = 60;
 // Rows per warp and prefetch depth (16 and 4 measured fastest at 2048^2:
 // 30.7 us against 31.0 for 32 rows, 31.3 for a prefetch of 2, 32.5 with the
 // registers capped at 64 for 32 warps per multiprocessor, and 33.1 for one
-// column per lane).
+// column per lane).  A warp fetches SH + 4 rows for SH outputs, so the rows
+// per warp trade halo re-reads against warps in flight; single plans also
+// run 8 and 32 (FvmParams::stream_rows, an autotuner dimension).
 constexpr int kStreamRows = 16, kStreamPrefetch = 4;
+CFD_HD int stream_rows_of(int mode) { return mode == 1 ? 8 : mode == 2 ? 32 : kStreamRows; }
 
 struct StreamRaw {
   float2 u, v, q;  // columns (jl, jl + 1)
@@ -632,18 +635,21 @@ CFD_D void explicit_stream_body(const FvmParams& p, int bx, const float* __restr
   }
 }
 
-template <bool PROJECT, int CONVECT, int FORCE>
+template <bool PROJECT, int CONVECT, int FORCE, int SH>
 __global__ void __launch_bounds__(128)
     fvm_explicit_stream_kernel(FvmParams p, const float* __restrict__ ua,
                                 const float* __restrict__ va, const float* __restrict__ q,
                                 float* __restrict__ uo, float* __restrict__ vo) {
   pdl_wait();
   pdl_trigger();
-  explicit_stream_body<PROJECT, CONVECT, FORCE, kStreamRows, kStreamPrefetch>(p, blockIdx.x, ua,
-                                                                               va, q, uo, vo);
+  explicit_stream_body<PROJECT, CONVECT, FORCE, SH, kStreamPrefetch>(p, blockIdx.x, ua, va, q,
+                                                                     uo, vo);
 }
 
-bool stream_ok(const FvmParams& p) { return p.ny >= 64 && p.nx % 16 == 0; }
+// Every warp's SH rows lie inside the grid (nx a multiple of SH).
+bool stream_ok(const FvmParams& p) {
+  return p.ny >= 64 && p.nx % kStreamRows == 0 && p.nx % stream_rows_of(p.stream_rows) == 0;
+}
 
 // Backward-difference divergence of (u*, v*) (finite_differences.py:95-143)
 // followed by the packed real FFT of each row along y.  Shared memory holds
@@ -1454,14 +1460,20 @@ CFD_D void irfft_row_warp(const FvmParams& p, int i, float2* spec, float2* tile)
   const int lane = threadIdx.x & 31;
   const int L = p.ny >> 1;
   float2* row = spec + (size_t)i * L;
-  float2 v[32];
+  // Each element once (32 loads per lane, all in flight together); the
+  // mirror X[L - k] of k = lane + 32 m is lane (32 - lane)'s slot 31 - m, or
+  // lane 0's own slot 32 - m.
+  float2 x[32], v[32];
+#pragma unroll
+  for (int m = 0; m < 32; ++m) x[m] = row[lane + 32 * m];
 #pragma unroll
   for (int m = 0; m < 32; ++m) {
     const int k = lane + 32 * m;
-    const float2 x = row[k], xm = row[(L - k) & (L - 1)];
+    float2 xm = wfft_shfl_idx2(x[31 - m], (32 - lane) & 31);
+    if (lane == 0) xm = x[(32 - m) & 31];
     float2 zk, zm;
-    irfft_pre_pair(x, xm, __ldg(p.tw_y + k), &zk, &zm);
-    v[m] = k == 0 ? make_float2(x.x + x.y, x.x - x.y) : zk;
+    irfft_pre_pair(x[m], xm, __ldg(p.tw_y + k), &zk, &zm);
+    v[m] = k == 0 ? make_float2(x[m].x + x[m].y, x[m].x - x[m].y) : zk;
   }
   warp_fft1024<1>(v, tile, p.twp_y + wfft_table_offset(kWarpFftLog2));
   // q[2n], q[2n+1] = z[n] over the same row (every load above has completed:
@@ -1972,10 +1984,18 @@ static void launch_explicit_variant(const FvmParams& p, bool stream, bool tiled,
                                     const float* ua, const float* va, const float* q,
                                     float* uo, float* vo, cudaStream_t s) {
   if (stream) {
-    const long long warps =
-        (long long)((p.ny + kStreamCols - 1) / kStreamCols) * ((p.nx + kStreamRows - 1) / kStreamRows);
-    launch_maybe_pdl(p.pdl, fvm_explicit_stream_kernel<PR, CV, FO>, dim3((int)((warps + 3) / 4)),
-                     dim3(128), 0, s, p, ua, va, q, uo, vo);
+    const int sh = stream_rows_of(p.stream_rows);
+    const long long warps = (long long)((p.ny + kStreamCols - 1) / kStreamCols) * (p.nx / sh);
+    const dim3 grid_s((int)((warps + 3) / 4));
+    if (sh == 8)
+      launch_maybe_pdl(p.pdl, fvm_explicit_stream_kernel<PR, CV, FO, 8>, grid_s, dim3(128), 0, s,
+                       p, ua, va, q, uo, vo);
+    else if (sh == 32)
+      launch_maybe_pdl(p.pdl, fvm_explicit_stream_kernel<PR, CV, FO, 32>, grid_s, dim3(128), 0, s,
+                       p, ua, va, q, uo, vo);
+    else
+      launch_maybe_pdl(p.pdl, fvm_explicit_stream_kernel<PR, CV, FO, kStreamRows>, grid_s,
+                       dim3(128), 0, s, p, ua, va, q, uo, vo);
   } else if (tiled) {
     fvm_explicit_tiled_kernel<PR, K0, CV, FO><<<grid, kStencilThreads, 0, s>>>(p, ua, va, q, uo,
                                                                                vo);

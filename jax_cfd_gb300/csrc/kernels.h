@@ -50,6 +50,7 @@ struct FvmParams {
   int stencil;         // explicit step: 0 shared-memory tiles, 1 warp streams,
                        // 2 (batches of small grids) whole chunks resident in shared memory
   int row_feed;        // row transforms: 0 loads through registers, 1 bulk copies
+  int stream_rows;     // rows per warp of the warp-stream stencil: 0 16, 1 8, 2 32
   // Implicit diffusion (diffusion.solve_fast_diag) on the same transforms:
   int row_field;       // forward row transform of the field us itself, not div
   int col_diag;        // column-pass diagonal: 0 pinv(lambda), 1 x / (1 - x), x = dtnu lambda
@@ -177,14 +178,15 @@ struct SpecParams {
   const float* kx;      // fftfreq(nx, hx) in float32 (nx)
   const float* ky;      // rfftfreq(ny, hy) in float32 (L + 1)
   int pdl;              // launch the stage kernels as programmatic dependents
-  int row_mode;         // row pass: 0 shared-memory engine, 1 register passes
+  int row_mode;         // row pass: 0 shared-memory engine, 1 register passes,
+                        // 2 register passes with registers for 3 blocks per SM
 };
 
 // Whether the clustered spectral column passes (col_mode 1) apply to this grid.
 bool spec_cluster_ok(const SpecParams& p);
 // Whether the persistent spectral column passes (col_mode 2/3) apply to this grid.
 bool spec_pipe_ok(const SpecParams& p);
-// Whether the register-pass row pass (row_mode 1) applies to this grid.
+// Whether the register-pass row pass (row_mode 1 or 2) applies to this grid.
 bool spec_row_pipe_ok(const SpecParams& p);
 
 struct StageCoef {

@@ -711,8 +711,10 @@ CFD_D void spec_row_pipe_body(const SpecParams& p, int row, const float2* __rest
   }
 }
 
-template <int LOG2L>
-__global__ void __launch_bounds__(4 * (1 << LOG2L) / 16, 512 / (4 * (1 << LOG2L) / 16))
+// OCC: resident threads per multiprocessor the register budget is sized for
+// (512: 128 registers; 768: 80, three 256-thread blocks at ny = 2048).
+template <int LOG2L, int OCC>
+__global__ void __launch_bounds__(4 * (1 << LOG2L) / 16, OCC / (4 * (1 << LOG2L) / 16))
     spec_row_pipe_kernel(SpecParams p, const float2* __restrict__ t0,
                          const float2* __restrict__ t1, const float2* __restrict__ t2,
                          const float2* __restrict__ t3, float2* __restrict__ ahat) {
@@ -1213,27 +1215,37 @@ cudaError_t launch_spec_col_update(const SpecParams& p, const StageCoef& sc,
   return launch_spec_col_prep(p, w, t4, s);
 }
 
-template <int LOG2L>
+template <int LOG2L, int OCC>
 static cudaError_t spec_row_pipe_impl(const SpecParams& p, const float2* const t4[4],
                                       float2* ahat, cudaStream_t s) {
   const size_t smem = (size_t)8 * padded_len(1 << LOG2L) * sizeof(float2);
-  auto kern = spec_row_pipe_kernel<LOG2L>;
+  auto kern = spec_row_pipe_kernel<LOG2L, OCC>;
   cudaError_t e = set_smem(kern, smem);
   if (e != cudaSuccess) return e;
   return launch_maybe_pdl(p.pdl, kern, dim3(p.nx), dim3(4 * (1 << LOG2L) / 16), smem, s, p,
                           t4[0], t4[1], t4[2], t4[3], ahat);
 }
 
-bool spec_row_pipe_ok(const SpecParams& p) { return p.log2L >= 8 && p.log2L <= 11; }
+bool spec_row_pipe_ok(const SpecParams& p) {
+  // row_mode 2 sizes registers for 768 resident threads: blocks of <= 256.
+  return p.log2L >= 8 && p.log2L <= (p.row_mode == 2 ? 10 : 11);
+}
 
 cudaError_t launch_spec_row(const SpecParams& p, const float2* const t4[4],
                             float2* ahat, cudaStream_t s) {
-  if (p.row_mode == 1 && spec_row_pipe_ok(p)) {
+  if (p.row_mode == 2 && spec_row_pipe_ok(p)) {
     switch (p.log2L) {
-      case 8: return spec_row_pipe_impl<8>(p, t4, ahat, s);
-      case 9: return spec_row_pipe_impl<9>(p, t4, ahat, s);
-      case 10: return spec_row_pipe_impl<10>(p, t4, ahat, s);
-      default: return spec_row_pipe_impl<11>(p, t4, ahat, s);
+      case 8: return spec_row_pipe_impl<8, 768>(p, t4, ahat, s);
+      case 9: return spec_row_pipe_impl<9, 768>(p, t4, ahat, s);
+      default: return spec_row_pipe_impl<10, 768>(p, t4, ahat, s);
+    }
+  }
+  if (p.row_mode >= 1 && spec_row_pipe_ok(p)) {
+    switch (p.log2L) {
+      case 8: return spec_row_pipe_impl<8, 512>(p, t4, ahat, s);
+      case 9: return spec_row_pipe_impl<9, 512>(p, t4, ahat, s);
+      case 10: return spec_row_pipe_impl<10, 512>(p, t4, ahat, s);
+      default: return spec_row_pipe_impl<11, 512>(p, t4, ahat, s);
     }
   }
   const int rows = rows_per_block(p.log2L, 4, p.nx);

@@ -209,25 +209,27 @@ class FvmPlan:
               'cfd_fvm_plan_autotune')
     return int(chosen.value)
 
-  LAUNCH_CHOICES = 48
+  LAUNCH_CHOICES = 144
   ROW_BLOCKS = ('wide', 'narrow')
   COLUMN_PASSES = ('blocks', 'cluster4', 'cluster8', 'pipelined4', 'pipelined2',
                    'pipelined4_tma')
   STENCILS = ('tiles', 'warp_streams')
   ROW_FEEDS = ('registers', 'bulk_copy')
+  STREAM_ROWS = (16, 8, 32)
 
   @classmethod
   def describe_launch(cls, choice: int) -> dict:
     """Names of the parts of launch configuration `choice` (row block shape
-    + 2 * column-pass scheme + 12 * stencil scheme + 24 * row feed, the
-    index cfd_fvm_plan_autotune reports)."""
+    + 2 * column-pass scheme + 12 * stencil scheme + 24 * row feed + 48 *
+    rows per stencil warp, the index cfd_fvm_plan_autotune reports)."""
     choice = int(choice)
     if not 0 <= choice < cls.LAUNCH_CHOICES:
       raise ValueError(f'launch choice {choice} outside [0, {cls.LAUNCH_CHOICES})')
     return {'row_blocks': cls.ROW_BLOCKS[choice & 1],
             'column_pass': cls.COLUMN_PASSES[(choice >> 1) % 6],
             'stencil': cls.STENCILS[(choice // 12) & 1],
-            'row_feed': cls.ROW_FEEDS[choice // 24]}
+            'row_feed': cls.ROW_FEEDS[(choice // 24) & 1],
+            'stream_rows': cls.STREAM_ROWS[choice // 48]}
 
   def set_launch(self, choice: int):
     """Pins the launch configuration (see autotune); results do not change."""
@@ -374,15 +376,18 @@ class SpecPlan:
   def nbytes(self) -> int:
     return int(self._lib.cfd_spec_plan_bytes(self._h))
 
-  LAUNCH_CHOICES = 10
+  LAUNCH_CHOICES = 15
+  COLUMN_PASSES = ('blocks', 'cluster4', 'pipelined4', 'pipelined2', 'pipelined4_fused')
+  ROW_PASSES = ('shared_memory', 'register_passes', 'register_passes_3blocks')
 
   def set_launch(self, choice: int):
     """choice = column scheme + 5 * row scheme.  Column passes: 0 per-block
     columns, 1 clusters of four one-column blocks (256 <= nx <= 2048), 2/3
     persistent register-pipelined groups of 4/2 columns (512 <= nx <= 4096),
     4 as 2 with each stage's update and the next stage's prep fused.  Row
-    pass: 0 shared-memory engine, 1 register passes (512 <= ny <= 4096).
-    Results do not change."""
+    pass: 0 shared-memory engine, 1 register passes (512 <= ny <= 4096), 2
+    register passes with registers for three blocks per multiprocessor
+    (512 <= ny <= 2048).  Results do not change."""
     nat.check(self._lib.cfd_spec_plan_set_launch(self._h, int(choice)), 'cfd_spec_plan_set_launch')
 
   @property

@@ -126,7 +126,8 @@ def test_taylor_green_spectral_analytic(cuda_device):
 @pytest.mark.parametrize('forcing', ['smooth', 'kolmogorov'])
 def test_cluster_column_passes_are_bitwise(cuda_device, shape, forcing):
   """Every column scheme (per-block, clusters, persistent pipelined, fused
-  update + prep) and both row passes give exactly the per-block bits."""
+  update + prep) and every row pass (shared memory, register passes at two or
+  three blocks per multiprocessor) give exactly the per-block bits."""
   import jax_cfd_gb300.base as cfd
   from jax_cfd_gb300.spectral import equations as seq
   from jax_cfd_gb300.spectral import time_stepping as sts

@@ -180,20 +180,24 @@ def test_other_tableaux_build_rk_steps():
 
 def test_launch_choice_names_follow_the_abi_encoding():
   """FvmPlan.describe_launch decodes the index cfd_fvm_plan_autotune reports
-  (row shape + 2 * column scheme + 12 * stencil + 24 * row feed)."""
+  (row shape + 2 * column scheme + 12 * stencil + 24 * row feed + 48 * rows
+  per stencil warp)."""
   from jax_cfd_gb300 import plans
   P = plans.FvmPlan
   seen = set()
   for c in range(P.LAUNCH_CHOICES):
     d = P.describe_launch(c)
     key = (P.ROW_BLOCKS.index(d['row_blocks']), P.COLUMN_PASSES.index(d['column_pass']),
-           P.STENCILS.index(d['stencil']), P.ROW_FEEDS.index(d['row_feed']))
-    assert key[0] + 2 * key[1] + 12 * key[2] + 24 * key[3] == c
+           P.STENCILS.index(d['stencil']), P.ROW_FEEDS.index(d['row_feed']),
+           P.STREAM_ROWS.index(d['stream_rows']))
+    assert key[0] + 2 * key[1] + 12 * key[2] + 24 * key[3] + 48 * key[4] == c
     seen.add(key)
   assert len(seen) == P.LAUNCH_CHOICES
   assert P.describe_launch(19) == {'row_blocks': 'narrow', 'column_pass': 'pipelined4',
-                                   'stencil': 'warp_streams', 'row_feed': 'registers'}
+                                   'stencil': 'warp_streams', 'row_feed': 'registers',
+                                   'stream_rows': 16}
   assert P.describe_launch(23)['column_pass'] == 'pipelined4_tma'
+  assert P.describe_launch(23 + 96)['stream_rows'] == 32
   with pytest.raises(ValueError):
     P.describe_launch(P.LAUNCH_CHOICES)
   header = (ROOT / 'include' / 'cfd_gb300.h').read_text()
