@@ -1518,11 +1518,11 @@ static int spec_params_from_config(const cfd_spec_config* cfg, cfd::SpecParams* 
   const int nx = cfg->nx, ny = cfg->ny;
   p.nx = nx;
   p.ny = ny;
-  // Programmatic dependent launch of the stage kernels measured slower at
-  // 2048^2 (0.814 against 0.786 ms per CN-RK4 step): off unless
-  // CFD_GB300_PDL=1 asks for it.
+  // Programmatic dependent launch of the stage kernels: 0.713 against
+  // 0.735 ms per 2048^2 CN-RK4 step (CFD_GB300_PDL=0 turns it off; batches
+  // launch their kernels plainly whatever this says).
   const char* pdl = std::getenv("CFD_GB300_PDL");
-  p.pdl = (pdl && pdl[0] == '1') ? 1 : 0;
+  p.pdl = (pdl && pdl[0] == '0') ? 0 : 1;
   p.L = ny / 2;
   p.log2nx = ilog2(nx);
   p.log2ny = ilog2(ny);
