@@ -112,6 +112,12 @@ bool launch_choice_ok(const cfd::FvmParams& p, int c) {
   if ((col == 3 || col == 4) && !cfd::col_pipe_ok(p, col == 4)) return false;
   if (col == 5 && !(p.col_tmap && cfd::col_tma_grid_ok(p))) return false;
   if (rows != 0 && stencil != 1) return false;
+  {
+    cfd::FvmParams q = p;
+    q.fft_shape = c & 1;
+    q.col_mode = col;
+    if (!cfd::fft_shape_ok(q)) return false;
+  }
   if (stencil == 1) {
     cfd::FvmParams q = p;
     q.stream_rows = rows;
@@ -349,6 +355,7 @@ static int fvm_params_from_config(const cfd_fvm_config* cfg, cfd::FvmParams* out
   p.stencil = ((long long)nx * ny >= (1LL << 22) && cfd::stream_stencil_ok(p)) ? 1 : 0;
   // The persistent column pass measured fastest from 1024 rows up (GB300).
   p.col_mode = (nx >= 1024 && cfd::col_pipe_ok(p, 0)) ? 3 : 0;
+  if (!cfd::fft_shape_ok(p)) p.fft_shape = 0;
   // The step's kernels start as programmatic dependents of their predecessor
   // (CFD_GB300_PDL=0 in the environment turns this off, for comparison).
   const char* pdl = std::getenv("CFD_GB300_PDL");
@@ -399,6 +406,7 @@ static void plan_default_launch(cfd::FvmParams* p) {
   p->fft_shape = 1;
   p->row_feed = cfd::bulk_feed_ok(*p) ? 1 : 0;
   if (p->nx >= 256 && cfd::col_pipe_ok(*p, 0)) p->col_mode = 3;
+  if (!cfd::fft_shape_ok(*p)) p->fft_shape = 0;
   cfd::FvmParams q = *p;
   q.stream_rows = (long long)p->nx * p->ny < (1LL << 22) ? 1 : 0;
   if (cfd::stream_stencil_ok(q)) {
@@ -1111,6 +1119,7 @@ static bool batch_launch_choice(cfd::FvmParams* shape, int c) {
   if (q.col_mode == 3 && !cfd::col_pipe_ok(q, 0)) return false;
   if (q.col_mode == 5 && !(q.col_tmap && cfd::col_tma_grid_ok(q))) return false;
   if (q.stencil == 1 && !cfd::stream_stencil_ok(q)) return false;
+  if (!cfd::fft_shape_ok(q)) return false;
   *shape = q;
   return true;
 }

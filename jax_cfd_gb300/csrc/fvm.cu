@@ -484,7 +484,9 @@ constexpr int kStreamCols = 60;
 // registers capped at 64 for 32 warps per multiprocessor, and 33.1 for one
 // column per lane).  A warp fetches SH + 4 rows for SH outputs, so the rows
 // per warp trade halo re-reads against warps in flight; single plans also
-// run 8 and 32 (FvmParams::stream_rows, an autotuner dimension).
+// run 8 and 32 (FvmParams::stream_rows, an autotuner dimension).  24 rows
+// per warp (one wave of warps at 2048^2 instead of 1.47, the last warp of a
+// strip taking the remaining rows) measured slower: 33.4 against 31.4 us.
 constexpr int kStreamRows = 16, kStreamPrefetch = 4;
 CFD_HD int stream_rows_of(int mode) { return mode == 1 ? 8 : mode == 2 ? 32 : kStreamRows; }
 
@@ -2151,6 +2153,18 @@ bool col_pipe_ok(const FvmParams& p, int narrow) {
 
 bool col_tma_grid_ok(const FvmParams& p) {
   return p.log2nx >= 8 && p.log2nx <= 11 && (p.ny / 2) % 4 == 0;
+}
+
+// The narrow transform blocks hold one row's ny/32 workers in 64 threads and
+// one column's nx/16 workers in 128 threads: rows up to 2048 (at 2048 the
+// one-warp row kernels run whatever the shape) and, for the per-block column
+// pass, columns up to 2048.  The wide blocks (256 threads) hold either at
+// 4096.
+bool fft_shape_ok(const FvmParams& p) {
+  if (p.fft_shape != 1) return true;
+  const bool rows = warp_rows_ok(p) || p.ny <= 2048;
+  const bool cols = p.col_mode != 0 || p.nx <= 2048;
+  return rows && cols;
 }
 
 template <int LOG2N>

@@ -85,6 +85,9 @@ bool col_cluster_ok(const FvmParams& p, int cluster);
 // Whether the persistent column pass (col_mode 3, or 4 with narrow != 0)
 // applies to this grid.
 bool col_pipe_ok(const FvmParams& p, int narrow);
+// Whether the transform block shape (FvmParams::fft_shape) holds this grid's
+// rows and, for the per-block column pass, its columns.
+bool fft_shape_ok(const FvmParams& p);
 // Whether the TMA-staged column pass (col_mode 5) can run on this grid (a
 // tensor map of the spectrum is then needed in col_tmap).
 bool col_tma_grid_ok(const FvmParams& p);
