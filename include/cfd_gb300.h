@@ -216,6 +216,21 @@ int cfd_fvm_adjoint_step(cfd_fvm_plan* plan, void* stream, const float* u,
                          const float* v, const float* gu, const float* gv,
                          float* gu_out, float* gv_out, float* nu_dot);
 
+/* Adjoint of a segment of `steps` steps from the checkpoint (u0, v0), in one
+ * call: recomputes the segment's states 1 .. steps-1 by single steps into
+ * `states` (2 (steps - 1) nx ny floats, state k's u then v at
+ * states + 2 (k - 1) nx ny; NULL when steps == 1), then runs the adjoint
+ * steps newest first.  (gu, gv) hold the cotangent of the state after the
+ * segment on entry and that of the checkpoint on return.  With nu_acc (a
+ * device double) and nu_scratch (nx ny floats) both given, adds
+ * sum over steps and cells of nu_dot (cfd_fvm_adjoint_step) to *nu_acc,
+ * summed in double in a fixed order; both NULL skips it.  Each state and
+ * cotangent is the bits that cfd_fvm_step (one step) and
+ * cfd_fvm_adjoint_step give. */
+int cfd_fvm_adjoint_segment(cfd_fvm_plan* plan, void* stream, const float* u0,
+                            const float* v0, int steps, float* states, float* gu,
+                            float* gv, float* nu_scratch, double* nu_acc);
+
 /* ---- Batched FVM trajectories ----
  * Replaces the reference's one-trajectory-at-a-time use of
  * semi_implicit_navier_stokes + funcutils.repeated (equations.py:120-151,

@@ -98,6 +98,8 @@ _SIGNATURES = {
     'cfd_fvm_step_rk': (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_int, ctypes.c_int,
                                         _vp, _vp]),
     'cfd_fvm_adjoint_step': (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    'cfd_fvm_adjoint_segment': (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_int, _vp, _vp, _vp,
+                                               _vp, _vp]),
     'cfd_fvm_diffusion_solve': (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_double,
                                                 ctypes.c_double]),
     'cfd_fvm_step_implicit': (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_int,

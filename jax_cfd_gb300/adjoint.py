@@ -8,8 +8,10 @@ step (``cfd_fvm_adjoint_step``: projection of the cotangent, transposed Van
 Leer / linear advection, diffusion and forcing) once per step, newest first.
 The forward pass keeps the state every ``checkpoint_every`` steps; the
 backward pass recomputes the states of one segment from its checkpoint before
-running that segment's adjoint steps, so memory is one segment plus the
-checkpoints.  Gradients flow to the initial velocity and to the viscosity.
+running that segment's adjoint steps (``cfd_fvm_adjoint_segment``: one native
+call per segment, the viscosity products summed on the device), so memory is
+one segment plus the checkpoints.  Gradients flow to the initial velocity and
+to the viscosity.
 
 A batch of trajectories (a leading axis) runs concurrently: each trajectory
 has its own plan (workspace) and CUDA stream, forward and backward, and the
@@ -76,14 +78,13 @@ class _Rollout(torch.autograd.Function):
   def backward(ctx, gu, gv):  # pylint: disable=arguments-differ
     spec, plan = ctx.spec, ctx.plan
     u_last = ctx.checkpoints[0][0]
-    gu = torch.zeros_like(u_last) if gu is None else gu.contiguous().float()
-    gv = torch.zeros_like(u_last) if gv is None else gv.contiguous().float()
+    gu = _owned_cotangent(gu, u_last)
+    gv = _owned_cotangent(gv, u_last)
     k = max(1, int(spec.checkpoint_every))
     nu_grad = torch.zeros((), dtype=torch.float64, device=u_last.device)
     for seg in reversed(range(len(ctx.checkpoints))):
       n = min(k, spec.steps - seg * k)
-      gu, gv, part = _segment_adjoint(plan, ctx.checkpoints[seg], n, gu, gv)
-      nu_grad = nu_grad + part
+      _segment_adjoint(plan, ctx.checkpoints[seg], n, gu, gv, nu_grad)
     grad_nu = (nu_grad * (spec.dt / spec.density)).to(torch.float32).reshape(ctx.nu_shape)
     return gu, gv, grad_nu, None
 
@@ -100,18 +101,20 @@ def _side_streams(device, count: int):
   return have[:count]
 
 
-def _segment_adjoint(plan, checkpoint, n: int, gu, gv):
-  """Adjoint of `n` steps from `checkpoint`: recomputes the segment's states,
-  then runs its adjoint steps newest first; returns (gu, gv, sum of the
-  per-cell viscosity products in float64)."""
-  states = [checkpoint]
-  for _ in range(n - 1):
-    states.append(plan.step(*states[-1], 1))
-  acc = torch.zeros((), dtype=torch.float64, device=gu.device)
-  for t in reversed(range(n)):
-    gu, gv, nu_dot = plan.adjoint_step(states[t][0], states[t][1], gu, gv)
-    acc = acc + nu_dot.double().sum()
-  return gu, gv, acc
+def _owned_cotangent(g, like):
+  """A contiguous float32 copy of the incoming cotangent (zeros for None) that
+  the segment adjoints may update in place."""
+  if g is None:
+    return torch.zeros_like(like)
+  return g.detach().to(torch.float32).contiguous().clone()
+
+
+def _segment_adjoint(plan, checkpoint, n: int, gu, gv, nu_acc):
+  """Adjoint of `n` steps from `checkpoint` in one native call: recomputes the
+  segment's states, runs its adjoint steps newest first with (gu, gv) updated
+  in place, and adds the sum of the per-cell viscosity products (float64) to
+  the device scalar nu_acc."""
+  plan.adjoint_segment(checkpoint[0], checkpoint[1], n, gu, gv, nu_acc)
 
 
 class _BatchRollout(torch.autograd.Function):
@@ -161,27 +164,21 @@ class _BatchRollout(torch.autograd.Function):
     spec = ctx.spec
     u0, _ = ctx.saved_tensors
     dev = u0.device
-    gu = torch.zeros_like(u0) if gu is None else gu.contiguous().float()
-    gv = torch.zeros_like(u0) if gv is None else gv.contiguous().float()
+    # Owned copies, made on the caller's stream before the side streams start.
+    gu_out = _owned_cotangent(gu, u0)
+    gv_out = _owned_cotangent(gv, u0)
     k = max(1, int(spec.checkpoint_every))
     main = torch.cuda.current_stream(dev)
-    gu_out, gv_out = torch.empty_like(gu), torch.empty_like(gv)
     nu_parts = torch.zeros(len(ctx.plans), dtype=torch.float64, device=dev)
     start = torch.cuda.Event()
     start.record(main)
     for b, (plan, st) in enumerate(zip(ctx.plans, ctx.streams)):
       st.wait_event(start)
       with torch.cuda.stream(st):
-        g_u, g_v = gu[b], gv[b]
-        acc = torch.zeros((), dtype=torch.float64, device=dev)
         cps = ctx.checkpoints[b]
         for seg in reversed(range(len(cps))):
           n = min(k, spec.steps - seg * k)
-          g_u, g_v, part = _segment_adjoint(plan, cps[seg], n, g_u, g_v)
-          acc = acc + part
-        gu_out[b].copy_(g_u)
-        gv_out[b].copy_(g_v)
-        nu_parts[b].copy_(acc)
+          _segment_adjoint(plan, cps[seg], n, gu_out[b], gv_out[b], nu_parts[b])
       done = torch.cuda.Event()
       done.record(st)
       main.wait_event(done)

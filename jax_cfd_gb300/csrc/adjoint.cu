@@ -208,7 +208,42 @@ __global__ void __launch_bounds__(kAdjThreads)
   }
 }
 
+// Deterministic float -> double sum: kSumBlocks fixed blocks each reduce a
+// grid-stride share in a fixed tree, then one thread adds the block partials
+// in order to *acc.  The same inputs give the same bits whatever else runs.
+constexpr int kSumThreads = 256;
+__global__ void __launch_bounds__(kSumThreads)
+    sum_partials_kernel(const float* __restrict__ x, size_t n, double* __restrict__ partials) {
+  __shared__ double sh[kSumThreads];
+  double acc = 0.0;
+  for (size_t i = (size_t)blockIdx.x * kSumThreads + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * kSumThreads)
+    acc += (double)x[i];
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = kSumThreads / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partials[blockIdx.x] = sh[0];
+}
+
+__global__ void sum_finish_kernel(const double* __restrict__ partials, int count,
+                                  double* __restrict__ acc) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double t = 0.0;
+  for (int b = 0; b < count; ++b) t += partials[b];
+  *acc += t;
+}
+
 }  // namespace
+
+cudaError_t launch_sum_to_double(const float* x, size_t n, double* partials, double* acc,
+                                 cudaStream_t s) {
+  sum_partials_kernel<<<kSumBlocks, kSumThreads, 0, s>>>(x, n, partials);
+  sum_finish_kernel<<<1, 32, 0, s>>>(partials, kSumBlocks, acc);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_fvm_adjoint(const FvmParams& p, const float* u, const float* v,
                                const float* wu, const float* wv, float* gu, float* gv,

@@ -183,6 +183,7 @@ struct cfd_fvm_plan {
   float* fu = nullptr;
   float* fv = nullptr;
   float* rk = nullptr;  // Runge-Kutta stage terms k_j (u, v), allocated on first use
+  double* partials = nullptr;  // cfd::kSumBlocks doubles for the viscosity sums
   double dt = 0;        // the configuration's dt (double, as the reference's Python float)
   long long bytes = 0;
   // Tensor map of the packed spectrum for the TMA-staged column pass (the
@@ -296,7 +297,7 @@ int cfd_fvm_plan_destroy(cfd_fvm_plan* plan) {
   if (!plan) return CFD_OK;
   void* ptrs[] = {plan->au, plan->av, plan->bu, plan->bv, plan->spec, plan->lamx,
                   plan->lamy, plan->twy, plan->twpx, plan->twpy, plan->fu, plan->fv,
-                  plan->rk};
+                  plan->rk, plan->partials};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   delete plan;
@@ -1406,6 +1407,35 @@ int cfd_fvm_adjoint_step(cfd_fvm_plan* plan, void* stream, const float* u, const
             "project_out");
   CFD_CHECK(cfd::launch_fvm_adjoint(p, u, v, plan->au, plan->av, gu_out, gv_out, nu_dot, s),
             "adjoint");
+  return CFD_OK;
+}
+
+int cfd_fvm_adjoint_segment(cfd_fvm_plan* plan, void* stream, const float* u0,
+                            const float* v0, int steps, float* states, float* gu, float* gv,
+                            float* nu_scratch, double* nu_acc) {
+  if (!plan || !u0 || !v0 || !gu || !gv || steps < 1 || (steps > 1 && !states) ||
+      (!nu_scratch) != (!nu_acc))
+    return fail(CFD_ERR_INVALID_ARGUMENT, "cfd_fvm_adjoint_segment: bad arguments");
+  cudaStream_t s = as_stream(stream);
+  const size_t cells = (size_t)plan->p.nx * plan->p.ny;
+  if (nu_acc && !plan->partials)
+    CFD_CHECK(cudaMalloc((void**)&plan->partials, cfd::kSumBlocks * sizeof(double)),
+              "cfd_fvm_adjoint_segment: cudaMalloc");
+  // State k (k >= 1) of the segment at states + 2 (k - 1) cells (u, then v).
+  auto su = [&](int k) { return k == 0 ? u0 : states + 2 * (size_t)(k - 1) * cells; };
+  auto sv = [&](int k) { return k == 0 ? v0 : states + (2 * (size_t)(k - 1) + 1) * cells; };
+  for (int k = 1; k < steps; ++k) {
+    const int rc = cfd_fvm_step(plan, stream, su(k - 1), sv(k - 1), const_cast<float*>(su(k)),
+                                const_cast<float*>(sv(k)), 1);
+    if (rc) return rc;
+  }
+  for (int k = steps - 1; k >= 0; --k) {
+    const int rc = cfd_fvm_adjoint_step(plan, stream, su(k), sv(k), gu, gv, gu, gv, nu_scratch);
+    if (rc) return rc;
+    if (nu_acc)
+      CFD_CHECK(cfd::launch_sum_to_double(nu_scratch, cells, plan->partials, nu_acc, s),
+                "viscosity sum");
+  }
   return CFD_OK;
 }
 

@@ -139,6 +139,11 @@ cudaError_t launch_fvm_batch_health(const FvmParams& shape, const FvmMember* mem
 // Vector-Jacobian product of one FVM step at state (u, v) for the projected
 // cotangent (wu, wv) = P g: (gu, gv) = w + dt (A^T w + nu lap w + lin w) and,
 // if nu_dot is not null, nu_dot = w . lap(v) per cell.
+// *acc += sum of x[0..n) in double, deterministically (partials: kSumBlocks
+// doubles of scratch).
+constexpr int kSumBlocks = 152;
+cudaError_t launch_sum_to_double(const float* x, size_t n, double* partials, double* acc,
+                                 cudaStream_t s);
 cudaError_t launch_fvm_adjoint(const FvmParams& p, const float* u, const float* v,
                                const float* wu, const float* wv, float* gu, float* gv,
                                float* nu_dot, cudaStream_t s);

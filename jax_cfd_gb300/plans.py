@@ -263,6 +263,28 @@ class FvmPlan:
               'cfd_fvm_adjoint_step')
     return gu_out, gv_out, nu_dot
 
+  def adjoint_segment(self, u0, v0, steps: int, gu, gv, nu_acc=None):
+    """Adjoint of `steps` steps from the checkpoint (u0, v0) in one native
+    call: recomputes the segment's states, then runs its adjoint steps newest
+    first, updating the cotangent (gu, gv) in place (contiguous float32 on the
+    plan's device) from the state after the segment to the checkpoint.  With
+    nu_acc (a float64 device scalar) adds the segment's sum of the per-cell
+    viscosity products to it."""
+    steps = int(steps)
+    if steps < 1:
+      raise ValueError('steps must be >= 1')
+    a = self._fields(u0, v0, gu, gv)
+    if nu_acc is not None and not (nu_acc.dtype == torch.float64 and nu_acc.numel() == 1
+                                   and nu_acc.device == u0.device):
+      raise ValueError('nu_acc must be a float64 device scalar')
+    states = (torch.empty((steps - 1, 2) + tuple(u0.shape), dtype=torch.float32,
+                          device=u0.device) if steps > 1 else None)
+    scratch = torch.empty_like(u0) if nu_acc is not None else None
+    opt = lambda t: None if t is None else ptr(t)
+    nat.check(self._lib.cfd_fvm_adjoint_segment(
+        self._h, current_stream_ptr(u0.device), a[0], a[1], steps, opt(states), a[2], a[3],
+        opt(scratch), opt(nu_acc)), 'cfd_fvm_adjoint_segment')
+
   def explicit_terms(self, u, v):
     du, dv = torch.empty_like(u), torch.empty_like(v)
     a = self._fields(u, v, du, dv)

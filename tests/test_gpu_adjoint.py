@@ -66,6 +66,39 @@ def test_adjoint_step_matches_float64_autograd(cuda_device, convect):
   assert abs(nu_grad - float(nu.grad)) <= 1e-4 * abs(float(nu.grad))
 
 
+@pytest.mark.parametrize('n', [64, 256])
+def test_adjoint_segment_matches_the_step_loop(cuda_device, n):
+  """cfd_fvm_adjoint_segment (one native call per checkpoint segment) gives
+  the bits of recomputing the segment with single steps and running
+  cfd_fvm_adjoint_step newest first; its viscosity sum (double, fixed order)
+  agrees with the float64 sum of the per-step products."""
+  og, v0, step, dt, const_u, _ = _case(n, seed=8)
+  plan = step.plan(cuda_device)
+  dev = lambda a: torch.from_numpy(np.ascontiguousarray(a, dtype=np.float32)).to(cuda_device)
+  rng = np.random.default_rng(4)
+  g0 = [dev(rng.standard_normal(og.shape)) for _ in range(2)]
+  u0, w0 = dev(v0[0]), dev(v0[1])
+  steps = 5
+  states = [(u0, w0)]
+  for _ in range(steps - 1):
+    states.append(plan.step(*states[-1], 1))
+  gu, gv = g0[0].clone(), g0[1].clone()
+  want_nu = 0.0
+  for t in reversed(range(steps)):
+    gu, gv, nu_dot = plan.adjoint_step(states[t][0], states[t][1], gu, gv)
+    want_nu += float(nu_dot.double().sum())
+  su, sv = g0[0].clone(), g0[1].clone()
+  acc = torch.zeros((), dtype=torch.float64, device=cuda_device)
+  plan.adjoint_segment(u0, w0, steps, su, sv, acc)
+  assert torch.equal(su, gu) and torch.equal(sv, gv)
+  assert abs(float(acc) - want_nu) <= 1e-12 * abs(want_nu)
+  # One step: no recomputed states.
+  su1, sv1 = g0[0].clone(), g0[1].clone()
+  plan.adjoint_segment(u0, w0, 1, su1, sv1)
+  gu1, gv1, _ = plan.adjoint_step(u0, w0, g0[0], g0[1])
+  assert torch.equal(su1, gu1) and torch.equal(sv1, gv1)
+
+
 def _vorticity64(v, og):
   from oracle import fvm_torch as otorch
   return otorch.curl_2d(v, og.step)

@@ -60,6 +60,21 @@ def test_bounded_wait_selftest_validates_before_launching(lib):
     assert 'polls' in _native.last_error()
 
 
+def test_adjoint_segment_validates_before_launching(lib):
+  from jax_cfd_gb300 import _native
+  fake = 0x1000  # never dereferenced: validation fails first
+  # no plan; zero steps; missing state buffer for steps > 1; one of the two
+  # viscosity pointers without the other
+  cases = [(None, fake, fake, 2, fake, fake, fake, None, None),
+           (fake, fake, fake, 0, fake, fake, fake, None, None),
+           (fake, fake, fake, 3, None, fake, fake, None, None),
+           (fake, fake, fake, 1, None, fake, fake, fake, None)]
+  for plan, u, v, steps, states, gu, gv, scratch, acc in cases:
+    rc = lib.cfd_fvm_adjoint_segment(plan, None, u, v, steps, states, gu, gv, scratch, acc)
+    assert rc == _native.CFD_ERR_INVALID_ARGUMENT
+    assert 'cfd_fvm_adjoint_segment' in _native.last_error()
+
+
 def test_plan_rejects_non_power_of_two_before_touching_the_gpu(lib):
   import ctypes
   from jax_cfd_gb300 import _native
