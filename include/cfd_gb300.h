@@ -267,8 +267,10 @@ int cfd_fvm_batch_run(cfd_fvm_batch* batch, void* stream, int chunk, int use_gra
  * cp.async, 4 the same staged by TMA tensor loads) + 10 * stencil (0
  * shared-memory tiles, 1 warp streams), or 20: each member's whole chunk
  * resident in shared memory, one block per member and one launch per chunk
- * (grids whose fields fit: 64x64, 64x128, 128x64): 21 choices.  Every configuration
- * gives the same bits.  Synchronises. */
+ * (grids whose fields fit: 64x64, 64x128, 128x64), or 21 + (0 .. 19): the
+ * same with the row transforms fed by bulk copies (rows of up to 1024
+ * points): 41 choices.  Every configuration gives the same bits.
+ * Synchronises. */
 int cfd_fvm_batch_autotune(cfd_fvm_batch* batch, void* stream, int steps, int* chosen);
 /* Pins the batch's launch configuration (index as cfd_fvm_batch_autotune
  * reports); CFD_ERR_UNSUPPORTED for a configuration the grid cannot take.

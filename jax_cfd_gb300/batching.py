@@ -159,14 +159,17 @@ class FvmBatch:
   def autotune(self, steps: int = 10) -> int:
     """Times the launch configurations and keeps the fastest; returns its
     index (row shape + 2 * column scheme + 10 * stencil, or 20: each member's
-    whole chunk resident in shared memory, for small grids)."""
+    whole chunk resident in shared memory, for small grids, or 21 + the first
+    form with the rows fed by bulk copies)."""
     chosen = ctypes.c_int(-1)
     nat.check(self._lib.cfd_fvm_batch_autotune(self._h, plans.current_stream_ptr(self.device),
                                                int(steps), ctypes.byref(chosen)),
               'cfd_fvm_batch_autotune')
     return int(chosen.value)
 
-  LAUNCH_CHOICES = 21
+  # row shape + 2 * column scheme + 10 * stencil (0..19), 20 resident chunks,
+  # 21 + (0..19) the same with bulk-copy row feed (cfd_fvm_batch_autotune).
+  LAUNCH_CHOICES = 41
 
   def set_launch(self, choice: int):
     """Pins the launch configuration (see autotune); results do not change."""

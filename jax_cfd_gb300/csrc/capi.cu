@@ -1050,6 +1050,7 @@ static int batch_upload(cfd_fvm_batch* b, cudaStream_t s, int chunk) {
     b->host[i].steps = std::min(b->want[i], chunk);
     b->host[i].p.fft_shape = b->shape.fft_shape;
     b->host[i].p.col_mode = b->shape.col_mode;
+    b->host[i].p.row_feed = b->shape.row_feed;
   }
   CFD_CHECK(cudaMemcpyAsync(b->dev, b->host.data(), b->host.size() * sizeof(cfd::FvmMember),
                             cudaMemcpyHostToDevice, s),
@@ -1100,10 +1101,16 @@ int cfd_fvm_batch_run(cfd_fvm_batch* b, void* stream, int chunk, int use_graph) 
 // pipelined groups of 4 staged by cp.async, 4 the same staged by TMA, run as
 // col_mode 5) + 10 * stencil (0 tiles, 1 warp streams, 2 whole chunks
 // resident in shared memory: one configuration, index 20, small grids only).
-constexpr int kBatchLaunchChoices = 21;
+constexpr int kBatchLaunchChoices = 41;
 static bool batch_launch_choice(cfd::FvmParams* shape, int c) {
   if (c < 0 || c >= kBatchLaunchChoices) return false;
   cfd::FvmParams q = *shape;
+  // 21 .. 40: choices 0 .. 19 with the rows fed by bulk copies.
+  q.row_feed = c > 20 ? 1 : 0;
+  if (c > 20) {
+    c -= 21;
+    if (!cfd::bulk_feed_ok(q)) return false;
+  }
   const int col = (c >> 1) % 5;
   q.fft_shape = c & 1;
   q.col_mode = col == 4 ? 5 : col;

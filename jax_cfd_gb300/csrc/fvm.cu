@@ -1651,6 +1651,31 @@ __global__ void __launch_bounds__(MAXT, MINB)
   div_rfft_rows(p, blockIdx.x, rows, m.f[dst][0], m.f[dst][1], m.spec);
 }
 
+// The bulk-copy row feed over a batch (the single kernels' bodies; slot on
+// grid axis y).  The slots' fields sit at 16-byte multiples in the batch slab.
+template <int MAXT, int MINB>
+__global__ void __launch_bounds__(MAXT, MINB)
+    fvm_batch_div_rfft_bulk_kernel(const FvmMember* __restrict__ mem, int k, int rows) {
+  pdl_wait();
+  pdl_trigger();
+  const FvmMember& m = mem[blockIdx.y];
+  if (k >= m.steps) return;
+  const FvmParams p = m.p;
+  const int dst = batch_dst(k);
+  div_rfft_rows_bulk(p, blockIdx.x, rows, m.f[dst][0], m.f[dst][1], m.spec);
+}
+
+template <int MAXT, int MINB>
+__global__ void __launch_bounds__(MAXT, MINB)
+    fvm_batch_irfft_bulk_kernel(const FvmMember* __restrict__ mem, int k, int rows) {
+  pdl_wait();
+  pdl_trigger();
+  const FvmMember& m = mem[blockIdx.y];
+  if (k >= m.steps) return;
+  const FvmParams p = m.p;
+  irfft_rows_bulk(p, blockIdx.x, rows, m.spec);
+}
+
 template <int MAXT, int MINB>
 __global__ void __launch_bounds__(MAXT, MINB)
     fvm_batch_col_pinv_kernel(const FvmMember* __restrict__ mem, int k, int W, int log2W,
@@ -2342,6 +2367,20 @@ static cudaError_t batch_rows_impl(const FvmParams& p, int target, const FvmMemb
   const dim3 grid(p.nx / rows, count);
   const int threads = block_threads(fft_workers(log2L, rows));
   cudaError_t e;
+  if (p.row_feed == 1 && bulk_feed_ok(p)) {
+    if (inverse) {
+      const size_t bs = irfft_bulk_smem(p.ny, rows);
+      if ((e = set_smem(fvm_batch_irfft_bulk_kernel<MAXT, MINB>, bs)) != cudaSuccess) return e;
+      launch_maybe_pdl(p.pdl, fvm_batch_irfft_bulk_kernel<MAXT, MINB>, grid, dim3(threads), bs, s,
+                       mem, k, rows);
+    } else {
+      const size_t bs = div_rfft_bulk_smem(p.ny, rows);
+      if ((e = set_smem(fvm_batch_div_rfft_bulk_kernel<MAXT, MINB>, bs)) != cudaSuccess) return e;
+      launch_maybe_pdl(p.pdl, fvm_batch_div_rfft_bulk_kernel<MAXT, MINB>, grid, dim3(threads), bs,
+                       s, mem, k, rows);
+    }
+    return cudaGetLastError();
+  }
   if (inverse) {
     if ((e = set_smem(fvm_batch_irfft_kernel<MAXT, MINB>, smem)) != cudaSuccess) return e;
     launch_maybe_pdl(p.pdl, fvm_batch_irfft_kernel<MAXT, MINB>, grid, dim3(threads), smem, s, mem, k,

@@ -83,8 +83,9 @@ def test_batch_slots_equal_single_trajectories(cuda_device, graph, shape):
 def test_every_batch_launch_configuration_gives_the_same_bits(cuda_device, shape):
   """Tiles vs warp-streaming stencil, wide vs narrow row blocks, per-block,
   cluster and persistent pipelined column passes (staged by cp.async or by
-  TMA tensor loads) over a batch with an idle slot: identical results, equal
-  to the single trajectories."""
+  TMA tensor loads), rows fed through registers or by bulk copies, over a
+  batch with an idle slot: identical results, equal to the single
+  trajectories."""
   draws = [(shape, 21, 1e-3, 4, 2.0), (shape, 22, 1e-4, 2, 1.0), (shape, 23, 1e-3, 8, 3.0)]
   pairs = [_member(*d) for d in draws]
   b = _batch([m for m, _ in pairs], cuda_device)
@@ -100,7 +101,8 @@ def test_every_batch_launch_configuration_gives_the_same_bits(cuda_device, shape
     b.run(5, graph=choice % 2 == 0)
     torch.cuda.synchronize(cuda_device)
     results[choice] = [tuple(t.clone() for t in b.state(i)) for i in range(len(pairs))]
-  assert all(c in results for c in (0, 6, 8, 16, 18))  # blocks, pipelined, TMA x 2 stencils
+  # blocks, pipelined, TMA x 2 stencils; the same with bulk-copy row feed
+  assert all(c in results for c in (0, 6, 8, 16, 18, 21, 29, 39))
   for i, (m, v0) in enumerate(pairs):
     want = _single(m, v0, [5, 0, 3][i], cuda_device)
     for choice, states in results.items():
