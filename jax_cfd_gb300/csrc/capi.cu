@@ -925,6 +925,16 @@ int cfd_fvm_batch_create(const cfd_fvm_config* shape, int count, cfd_fvm_batch**
     p.stencil = 2;
     p.fft_shape = 0;
     p.col_mode = 0;
+  } else if ((long long)p.nx * p.ny >= (1LL << 14)) {
+    // The fastest configuration of every square size measured from 128^2 to
+    // 1024^2 (batches of 15-24 slots, 20-step chunks): narrow row blocks fed by
+    // bulk copies, the persistent column pass from 256 rows (TMA-staged where
+    // its map encodes), warp streams from 512^2.
+    p.fft_shape = 1;
+    p.row_feed = cfd::bulk_feed_ok(p) ? 1 : 0;
+    if (p.nx >= 256 && cfd::col_pipe_ok(p, 0)) p.col_mode = 3;
+    p.stencil = ((long long)p.nx * p.ny >= (1LL << 18) && cfd::stream_stencil_ok(p)) ? 1 : 0;
+    if (!cfd::fft_shape_ok(p)) p.fft_shape = 0;
   }
   cfd_fvm_batch* b = new cfd_fvm_batch();
   b->shape = p;
