@@ -62,6 +62,14 @@ CFD_D float2 prep_factor(const SpecParams& p, int f, int kx, int c, float2 u) {
 }
 
 // ky-side factors: vx = i ay A, vy = -i B, gx = i C, gy = i ay D.
+// kyf: the ky wavenumber of column k (from the table, wherever it is read).
+CFD_D float2 row_factor_k(const SpecParams& p, int f, float kyf, float2 x) {
+  if (f == 1) return make_float2(x.y, -x.x);
+  if (f == 2) return make_float2(-x.y, x.x);
+  const float ay = p.two_pi * kyf;
+  return make_float2(-(ay * x.y), ay * x.x);
+}
+
 CFD_D float2 row_factor(const SpecParams& p, int f, int k, float2 x) {
   if (f == 1) return make_float2(x.y, -x.x);
   if (f == 2) return make_float2(-x.y, x.x);
@@ -635,18 +643,49 @@ CFD_D void spec_row_pipe_body(const SpecParams& p, int row, const float2* __rest
   // buffer, all of a thread's loads issued before any store, and the
   // pre-untangling reads it there: read from global memory inside the branchy
   // loop below, the loads of each element and its mirror were taken one
-  // round trip at a time (about 60 % of the block's time; 61.9 -> 57.1 us per
-  // 2048^2 row pass).  The transform writes the second buffer only after its
-  // first exchange's barrier, which follows every read of the copy.
+  // round trip at a time (about 60 % of the block's time).  The transform
+  // writes the second buffer only after its first exchange's barrier, which
+  // follows every read of the copy.
   float2* const in = buf[1];
+  // The ky table (L + 1 floats) and the untangling twiddles (L values) go to
+  // the first buffers of fields 0 and 1 for the same reason; a barrier after
+  // the pre-untangling keeps the transform's first exchange (which writes
+  // those buffers) behind every read of them.  2048^2 row pass: 61.9 us
+  // reading global memory in the loop, 57.1 with the rows staged, 48.2 with
+  // the tables staged as well.
+  float* const kys = reinterpret_cast<float*>(sbuf);
+  float2* const tws = sbuf + bstride;
   {
     float2 x[16];
 #pragma unroll
     for (int r = 0; r < 16; ++r) x[r] = gin[t + NTHR * r];
     const float2 xl = t == 0 ? gin[L] : make_float2(0.f, 0.f);
+    constexpr int T = 4 * NTHR;
+    float kv[(L + T) / T];
+    float2 tv[(L + T - 1) / T];
+#pragma unroll
+    for (int r = 0; r < (L + T) / T; ++r) {
+      const int e = (int)threadIdx.x + T * r;
+      kv[r] = e <= L ? __ldg(p.ky + e) : 0.f;
+    }
+#pragma unroll
+    for (int r = 0; r < (L + T - 1) / T; ++r) {
+      const int e = (int)threadIdx.x + T * r;
+      tv[r] = e < L ? __ldg(p.tw_y + e) : make_float2(0.f, 0.f);
+    }
 #pragma unroll
     for (int r = 0; r < 16; ++r) in[t + NTHR * r] = x[r];
     if (t == 0) in[L] = xl;
+#pragma unroll
+    for (int r = 0; r < (L + T) / T; ++r) {
+      const int e = (int)threadIdx.x + T * r;
+      if (e <= L) kys[e] = kv[r];
+    }
+#pragma unroll
+    for (int r = 0; r < (L + T - 1) / T; ++r) {
+      const int e = (int)threadIdx.x + T * r;
+      if (e < L) tws[e] = tv[r];
+    }
   }
   __syncthreads();
   float2 v[16];
@@ -655,26 +694,27 @@ CFD_D void spec_row_pipe_body(const SpecParams& p, int row, const float2* __rest
     const int k = t + NTHR * r;
     float2 zk, zm;
     if (k == 0) {
-      const float2 x0 = row_factor(p, f, 0, in[0]);
-      const float2 xl = row_factor(p, f, L, in[L]);
+      const float2 x0 = row_factor_k(p, f, kys[0], in[0]);
+      const float2 xl = row_factor_k(p, f, kys[L], in[L]);
       v[r] = make_float2(x0.x + xl.x, x0.x - xl.x);
     } else if (k == half) {
-      const float2 xh = row_factor(p, f, half, in[half]);
-      irfft_pre_pair(xh, xh, __ldg(p.tw_y + half), &zk, &zm);
+      const float2 xh = row_factor_k(p, f, kys[half], in[half]);
+      irfft_pre_pair(xh, xh, tws[half], &zk, &zm);
       v[r] = zk;
     } else if (k < half) {
-      const float2 xk = row_factor(p, f, k, in[k]);
-      const float2 xm = row_factor(p, f, L - k, in[L - k]);
-      irfft_pre_pair(xk, xm, __ldg(p.tw_y + k), &zk, &zm);
+      const float2 xk = row_factor_k(p, f, kys[k], in[k]);
+      const float2 xm = row_factor_k(p, f, kys[L - k], in[L - k]);
+      irfft_pre_pair(xk, xm, tws[k], &zk, &zm);
       v[r] = zk;
     } else {
       const int kp = L - k;
-      const float2 xk = row_factor(p, f, kp, in[kp]);
-      const float2 xm = row_factor(p, f, k, in[k]);
-      irfft_pre_pair(xk, xm, __ldg(p.tw_y + kp), &zk, &zm);
+      const float2 xk = row_factor_k(p, f, kys[kp], in[kp]);
+      const float2 xm = row_factor_k(p, f, kys[k], in[k]);
+      irfft_pre_pair(xk, xm, tws[kp], &zk, &zm);
       v[r] = zm;
     }
   }
+  __syncthreads();
   col_pipe_fft<LOG2L, 1, 0, true>(v, buf, t, p.twp_y);
   // Samples n = t + NTHR m of every field into its first buffer (free: its
   // last reader was the transform's second pass).
