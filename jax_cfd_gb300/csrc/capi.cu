@@ -273,6 +273,8 @@ struct cfd_spec_plan {
   float2* h = nullptr;
   float2* fc = nullptr;     // forcing curl table (full or row 0)
   float2* work = nullptr;   // scratch spectrum for rfft2 / irfft2 / filter
+  float2* wt = nullptr;     // state and h in the column-group tiled layout during a
+  float2* ht = nullptr;     // chunk of the fused column stage (cfd::spec_state_tiled_ok)
   float2* twy = nullptr;
   float2* twpx = nullptr;
   float2* twpy = nullptr;
@@ -1552,7 +1554,7 @@ int cfd_spec_plan_destroy(cfd_spec_plan* plan) {
   if (!plan) return CFD_OK;
   void* ptrs[] = {plan->t4[0], plan->t4[1], plan->t4[2], plan->t4[3], plan->ahat,
                   plan->h, plan->fc, plan->work, plan->twy, plan->twpx, plan->twpy,
-                  plan->kx, plan->ky};
+                  plan->kx, plan->ky, plan->wt, plan->ht};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   delete plan;
@@ -1611,6 +1613,7 @@ static int spec_params_from_config(const cfd_spec_config* cfg, cfd::SpecParams* 
     c.write_h = (k + 1 < cfg->num_stages) ? 1 : 0;
     c.prep_next = 1;
     c.explicit_only = 0;
+    c.tiled = 0;
   }
   return CFD_OK;
 }
@@ -1676,6 +1679,16 @@ int cfd_spec_plan_create(const cfd_spec_config* cfg, cfd_spec_plan** out) {
   CFD_ALLOC(plan->ahat, ns);
   CFD_ALLOC(plan->h, ns);
   CFD_ALLOC(plan->work, ns);
+  {
+    // The tiled state for the fused column stage, on grids where that launch
+    // choice exists (whatever the current one).
+    cfd::SpecParams q = p;
+    q.col_mode = 4;
+    if (cfd::spec_state_tiled_ok(q)) {
+      CFD_ALLOC(plan->wt, cfd::spec_tiled_elems(q));
+      CFD_ALLOC(plan->ht, cfd::spec_tiled_elems(q));
+    }
+  }
 #undef CFD_ALLOC
   const SpecTables t = spec_tables(p);
   if ((e = upload(&plan->twy, t.twy.data(), t.twy.size())) != cudaSuccess ||
@@ -1821,16 +1834,24 @@ int cfd_spec_step(cfd_spec_plan* plan, void* stream, const float* w_in,
     CFD_CHECK(cudaMemcpyAsync(w_out, w_in, ns * sizeof(float2), cudaMemcpyDeviceToDevice, s),
               "copy");
   if (steps == 0) return CFD_OK;
+  // The fused column stage keeps the state and h tiled by column groups for
+  // the chunk (same values, contiguous per group); converted once each way.
+  const bool tiled = plan->wt && cfd::spec_state_tiled_ok(p);
+  float2* ws = tiled ? plan->wt : w;
+  float2* hs = tiled ? plan->ht : plan->h;
   CFD_CHECK(cfd::launch_spec_col_prep(p, w, plan->t4, s), "col_prep");
+  if (tiled) CFD_CHECK(cfd::spec_tile_state(p, w, ws, true, s), "tile state");
   for (int st = 0; st < steps; ++st) {
     for (int k = 0; k < plan->stages; ++k) {
       CFD_CHECK(cfd::launch_spec_row(p, plan->t4, plan->ahat, s), "row");
       cfd::StageCoef c = plan->coef[k];
       c.prep_next = (st + 1 == steps && k + 1 == plan->stages) ? 0 : 1;
-      CFD_CHECK(cfd::launch_spec_col_update(p, c, plan->ahat, w, plan->h, plan->t4, s),
+      c.tiled = tiled ? 1 : 0;
+      CFD_CHECK(cfd::launch_spec_col_update(p, c, plan->ahat, ws, hs, plan->t4, s),
                 "col_update");
     }
   }
+  if (tiled) CFD_CHECK(cfd::spec_tile_state(p, ws, w, false, s), "untile state");
   return CFD_OK;
 }
 
@@ -1861,9 +1882,14 @@ int cfd_spec_profile(cfd_spec_plan* plan, void* stream, const float* w_in,
       ++li;
     }
   };
+  // The same tiled state as cfd_spec_step (conversions outside the timed launches).
+  const bool tiled = fused && plan->wt && cfd::spec_state_tiled_ok(p);
+  float2* ws = tiled ? plan->wt : w;
+  float2* hs = tiled ? plan->ht : plan->h;
   rec(2, true);
   if (e == cudaSuccess) e = cfd::launch_spec_col_prep(p, w, plan->t4, s);
   rec(2, false);
+  if (e == cudaSuccess && tiled) e = cfd::spec_tile_state(p, w, ws, true, s);
   for (int st = 0; st < steps && e == cudaSuccess; ++st) {
     for (int k = 0; k < plan->stages && e == cudaSuccess; ++k) {
       rec(0, true);
@@ -1874,14 +1900,16 @@ int cfd_spec_profile(cfd_spec_plan* plan, void* stream, const float* w_in,
       if (prep && fused) {
         // Update and the next stage's prep in one launch.
         c.prep_next = 1;
+        c.tiled = tiled ? 1 : 0;
         rec(3, true);
-        if (e == cudaSuccess) e = cfd::launch_spec_col_update(p, c, plan->ahat, w, plan->h, plan->t4, s);
+        if (e == cudaSuccess) e = cfd::launch_spec_col_update(p, c, plan->ahat, ws, hs, plan->t4, s);
         rec(3, false);
         continue;
       }
       c.prep_next = 0;
+      c.tiled = tiled ? 1 : 0;
       rec(1, true);
-      if (e == cudaSuccess) e = cfd::launch_spec_col_update(p, c, plan->ahat, w, plan->h, plan->t4, s);
+      if (e == cudaSuccess) e = cfd::launch_spec_col_update(p, c, plan->ahat, ws, hs, plan->t4, s);
       rec(1, false);
       if (prep) {
         rec(2, true);
@@ -1890,6 +1918,7 @@ int cfd_spec_profile(cfd_spec_plan* plan, void* stream, const float* w_in,
       }
     }
   }
+  if (e == cudaSuccess && tiled) e = cfd::spec_tile_state(p, ws, w, false, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   double sum[4] = {0, 0, 0, 0};
   int cnt[4] = {0, 0, 0, 0};

@@ -194,6 +194,13 @@ struct SpecParams {
 bool spec_cluster_ok(const SpecParams& p);
 // Whether the persistent spectral column passes (col_mode 2/3) apply to this grid.
 bool spec_pipe_ok(const SpecParams& p);
+// Whether the persistent column passes of this grid can keep the state and h
+// in the column-group tiled layout (groups of 4 columns, each group's
+// nx x 4 values contiguous) during a chunk; spec_tile_state converts.
+bool spec_state_tiled_ok(const SpecParams& p);
+size_t spec_tiled_elems(const SpecParams& p);
+cudaError_t spec_tile_state(const SpecParams& p, const float2* src, float2* dst, bool to_tiled,
+                            cudaStream_t s);
 // Whether the register-pass row pass (row_mode 1 or 2) applies to this grid.
 bool spec_row_pipe_ok(const SpecParams& p);
 
@@ -205,6 +212,7 @@ struct StageCoef {
   int write_h;    // a later stage of this step reads h
   int prep_next;  // build the next stage's column-transformed fields
   int explicit_only;  // store F(u) into the state buffer instead of updating
+  int tiled;      // state and h in the column-group tiled layout (spec_state_tiled_ok)
 };
 
 // One slot of a same-shape batch of spectral trajectories.

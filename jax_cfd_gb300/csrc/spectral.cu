@@ -427,7 +427,16 @@ CFD_D void spec_pipe_prefetch(const float2* __restrict__ src, int ncols, int c, 
     cp_async8(stage + r * T + tid, src + (size_t)(t + NTHR * r) * ncols + c);
 }
 
-template <int LOG2N, int CG>
+// Element (kx, c) of the state or h: row-major [nx, L + 1], or tiled by
+// column groups of CG ([group][kx][c % CG], each group's values contiguous) so
+// that a warp of the persistent column passes (8 workers x CG columns) reads
+// and writes 256 contiguous bytes instead of 8 separate 32-byte row segments.
+template <int CG, bool TILED>
+CFD_D size_t state_at(int nx, int ncols, int kx, int c) {
+  return TILED ? ((size_t)(c / CG) * nx + kx) * CG + (c % CG) : (size_t)kx * ncols + c;
+}
+
+template <int LOG2N, int CG, bool TILED = false>
 __global__ void __launch_bounds__(CG * (1 << LOG2N) / 16,
                                   col_pipe_min_blocks(CG * (1 << LOG2N) / 16))
     spec_col_update_pipe_kernel(SpecParams p, StageCoef sc, const float2* __restrict__ ahat,
@@ -466,7 +475,7 @@ __global__ void __launch_bounds__(CG * (1 << LOG2N) / 16,
       // used (each element is read and written by this thread only).
 #pragma unroll
       for (int m = 0; m < 16; ++m) {
-        const size_t gi = (size_t)(t + P::NTHR * m) * ncols + c;
+        const size_t gi = state_at<CG, TILED>(p.nx, ncols, t + P::NTHR * m, c);
         us[m] = wst[gi];
         hs[m] = sc.has_h_in ? hst[gi] : make_float2(0.f, 0.f);
       }
@@ -476,7 +485,7 @@ __global__ void __launch_bounds__(CG * (1 << LOG2N) / 16,
 #pragma unroll
       for (int m = 0; m < 16; ++m) {
         const int kx = t + P::NTHR * m;
-        const size_t gi = (size_t)kx * ncols + c;
+        const size_t gi = state_at<CG, TILED>(p.nx, ncols, kx, c);
         if (sc.explicit_only) {
           stage_update_at(p, sc, kx, c, v[m], wst, hst);
         } else {
@@ -497,7 +506,7 @@ __global__ void __launch_bounds__(CG * (1 << LOG2N) / 16,
 // transformed without re-reading the state.  Every value is the one the
 // separate update and prep passes compute, so the bits are the same.  One
 // item makes ten exchanges (five transforms), so items start on buffer 0.
-template <int LOG2N, int CG>
+template <int LOG2N, int CG, bool TILED = false>
 __global__ void __launch_bounds__(CG * (1 << LOG2N) / 16,
                                   col_pipe_min_blocks(CG * (1 << LOG2N) / 16))
     spec_col_stage_pipe_kernel(SpecParams p, StageCoef sc, const float2* __restrict__ ahat,
@@ -536,7 +545,7 @@ __global__ void __launch_bounds__(CG * (1 << LOG2N) / 16,
     // (each element is read and written by this thread only).
 #pragma unroll
     for (int m = 0; m < 16; ++m) {
-      const size_t gi = (size_t)(t + P::NTHR * m) * ncols + c;
+      const size_t gi = state_at<CG, TILED>(p.nx, ncols, t + P::NTHR * m, c);
       u[m] = live ? wst[gi] : make_float2(0.f, 0.f);
       hs[m] = (live && sc.has_h_in) ? hst[gi] : make_float2(0.f, 0.f);
     }
@@ -545,7 +554,7 @@ __global__ void __launch_bounds__(CG * (1 << LOG2N) / 16,
 #pragma unroll
       for (int m = 0; m < 16; ++m) {
         const int kx = t + P::NTHR * m;
-        const size_t gi = (size_t)kx * ncols + c;
+        const size_t gi = state_at<CG, TILED>(p.nx, ncols, kx, c);
         float2 h;
         u[m] = stage_update_core_k(p, sc, kx, kxt[kx], c, v[m], u[m], hs[m], &h);
         wst[gi] = u[m];
@@ -1164,7 +1173,8 @@ static cudaError_t spec_stage_pipe_impl(const SpecParams& p, const StageCoef& sc
                                         cudaStream_t s) {
   int grid, threads;
   size_t smem;
-  auto kern = spec_col_stage_pipe_kernel<LOG2N, CG>;
+  auto kern = sc.tiled ? spec_col_stage_pipe_kernel<LOG2N, CG, true>
+                       : spec_col_stage_pipe_kernel<LOG2N, CG, false>;
   cudaError_t e = spec_pipe_grid<LOG2N, CG>(kern, (p.L + 1 + CG - 1) / CG, &grid, &smem,
                                             &threads);
   if (e != cudaSuccess) return e;
@@ -1178,7 +1188,8 @@ static cudaError_t spec_update_pipe_impl(const SpecParams& p, const StageCoef& s
                                          cudaStream_t s) {
   int grid, threads;
   size_t smem;
-  auto kern = spec_col_update_pipe_kernel<LOG2N, CG>;
+  auto kern = sc.tiled ? spec_col_update_pipe_kernel<LOG2N, CG, true>
+                       : spec_col_update_pipe_kernel<LOG2N, CG, false>;
   cudaError_t e = spec_pipe_grid<LOG2N, CG>(kern, (p.L + 1 + CG - 1) / CG, &grid, &smem,
                                             &threads);
   if (e != cudaSuccess) return e;
@@ -1282,6 +1293,44 @@ static cudaError_t spec_row_pipe_impl(const SpecParams& p, const float2* const t
   if (e != cudaSuccess) return e;
   return launch_maybe_pdl(p.pdl, kern, dim3(p.nx), dim3(4 * (1 << LOG2L) / 16), smem, s, p,
                           t4[0], t4[1], t4[2], t4[3], ahat);
+}
+
+// The tiled layout serves the groups of 4 columns of the fused column stage
+// (rows up to 2048; 4096 rows take groups of 2).
+bool spec_state_tiled_ok(const SpecParams& p) {
+  return p.col_mode == 4 && spec_pipe_ok(p) && p.log2nx <= 11;
+}
+
+size_t spec_tiled_elems(const SpecParams& p) {
+  return (size_t)((p.L + 1 + 3) / 4) * p.nx * 4;
+}
+
+// Row-major [nx, L + 1] <-> tiled by groups of 4 columns (state_at); the
+// tiled side is walked in order, so its accesses are contiguous.  Padding
+// columns of the last group read as zeros and are not written back.
+__global__ void spec_tile_state_kernel(int nx, int ncols, const float2* __restrict__ src,
+                                       float2* __restrict__ dst, int to_tiled) {
+  const size_t total = (size_t)((ncols + 3) / 4) * nx * 4;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const int w = (int)(i & 3);
+    const size_t r = i >> 2;
+    const int kx = (int)(r % (size_t)nx), c = (int)(r / (size_t)nx) * 4 + w;
+    const size_t j = (size_t)kx * ncols + c;
+    if (to_tiled)
+      dst[i] = c < ncols ? src[j] : make_float2(0.f, 0.f);
+    else if (c < ncols)
+      dst[j] = src[i];
+  }
+}
+
+cudaError_t spec_tile_state(const SpecParams& p, const float2* src, float2* dst, bool to_tiled,
+                            cudaStream_t s) {
+  const size_t total = spec_tiled_elems(p);
+  size_t blocks = (total + 255) / 256;
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  spec_tile_state_kernel<<<(int)blocks, 256, 0, s>>>(p.nx, p.L + 1, src, dst, to_tiled ? 1 : 0);
+  return cudaGetLastError();
 }
 
 bool spec_row_pipe_ok(const SpecParams& p) {
