@@ -1582,6 +1582,7 @@ static int spec_params_from_config(const cfd_spec_config* cfg, cfd::SpecParams* 
   const char* pdl = std::getenv("CFD_GB300_PDL");
   p.pdl = (pdl && pdl[0] == '0') ? 0 : 1;
   p.L = ny / 2;
+  p.pitch = p.L + 4;
   p.log2nx = ilog2(nx);
   p.log2ny = ilog2(ny);
   p.log2L = p.log2ny - 1;
@@ -1675,8 +1676,11 @@ int cfd_spec_plan_create(const cfd_spec_config* cfg, cfd_spec_plan** out) {
     }                                                                      \
     bytes += (long long)((count) * sizeof(*(ptr)));                        \
   } while (0)
-  for (int f = 0; f < 4; ++f) CFD_ALLOC(plan->t4[f], ns);
-  CFD_ALLOC(plan->ahat, ns);
+  // The four column-transformed fields and the advection spectrum: rows of
+  // p.pitch values (32-byte multiples), of which the first L + 1 are columns.
+  const size_t nsp = (size_t)nx * p.pitch;
+  for (int f = 0; f < 4; ++f) CFD_ALLOC(plan->t4[f], nsp);
+  CFD_ALLOC(plan->ahat, nsp);
   CFD_ALLOC(plan->h, ns);
   CFD_ALLOC(plan->work, ns);
   {
@@ -1987,9 +1991,13 @@ int cfd_spec_batch_create(const cfd_spec_config* shape, int count, cfd_spec_batc
   b->stages = stages;
   b->count = count;
   const size_t ns = (size_t)p.nx * (p.L + 1);
+  // Each slot's seven buffers (state, h, four fields, advection spectrum) at
+  // a stride of nx * pitch values: the fields and the spectrum use rows of
+  // p.pitch values, the state and h their first ns values.
+  const size_t nsp = (size_t)p.nx * p.pitch;
   b->ns = ns;
-  cudaError_t e = cudaMalloc((void**)&b->slab, (size_t)count * 7 * ns * sizeof(float2));
-  if (e == cudaSuccess) e = cudaMemset(b->slab, 0, (size_t)count * 7 * ns * sizeof(float2));
+  cudaError_t e = cudaMalloc((void**)&b->slab, (size_t)count * 7 * nsp * sizeof(float2));
+  if (e == cudaSuccess) e = cudaMemset(b->slab, 0, (size_t)count * 7 * nsp * sizeof(float2));
   if (e == cudaSuccess) e = cudaMalloc((void**)&b->dev, (size_t)count * sizeof(cfd::SpecMember));
   if (e == cudaSuccess) e = cudaMalloc((void**)&b->health, (size_t)count * sizeof(cfd::Health));
   if (e == cudaSuccess) e = cudaMemset(b->health, 0, (size_t)count * sizeof(cfd::Health));
@@ -2003,7 +2011,7 @@ int cfd_spec_batch_create(const cfd_spec_config* shape, int count, cfd_spec_batc
     cfd_spec_batch_destroy(b);
     return cuda_fail(e, "cfd_spec_batch_create");
   }
-  b->bytes = (long long)count * 7 * (long long)ns * 8 + (long long)count * sizeof(cfd::SpecMember);
+  b->bytes = (long long)count * 7 * (long long)nsp * 8 + (long long)count * sizeof(cfd::SpecMember);
   b->host.assign(count, cfd::SpecMember());
   b->want.assign(count, 0);
   for (int i = 0; i < count; ++i) {
@@ -2017,11 +2025,11 @@ int cfd_spec_batch_create(const cfd_spec_config* shape, int count, cfd_spec_batc
     m.p.ky = b->ky;
     for (int k = 0; k < stages; ++k) m.coef[k] = coef[k];
     m.stages = stages;
-    float2* base = b->slab + (size_t)i * 7 * ns;
+    float2* base = b->slab + (size_t)i * 7 * nsp;
     m.w = base;
-    m.h = base + ns;
-    for (int f = 0; f < 4; ++f) m.t[f] = base + (2 + f) * ns;
-    m.ahat = base + 6 * ns;
+    m.h = base + nsp;
+    for (int f = 0; f < 4; ++f) m.t[f] = base + (2 + f) * nsp;
+    m.ahat = base + 6 * nsp;
     m.steps = 0;
   }
   *out = b;

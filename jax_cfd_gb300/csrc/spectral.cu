@@ -103,7 +103,7 @@ CFD_D void col_prep_cols(const SpecParams& p, int blk, int f, int W, int log2W, 
 #pragma unroll 4
   for (int e = tid; e < W * N; e += blockDim.x) {
     const int ww = e & (W - 1), i = e >> log2W, c = c0 + ww;
-    if (c < ncols) dst[(size_t)i * ncols + c] = sbuf[ww * bstride + pidx(i)];
+    if (c < ncols) dst[(size_t)i * p.pitch + c] = sbuf[ww * bstride + pidx(i)];
   }
 }
 
@@ -180,7 +180,7 @@ CFD_D void col_update_cols(const SpecParams& p, const StageCoef& sc, int blk, in
   for (int e = tid; e < W * N; e += blockDim.x) {
     const int w = e & (W - 1), i = e >> log2W, c = c0 + w;
     sbuf[w * bstride + pidx(i)] =
-        c < ncols ? ahat[(size_t)i * ncols + c] : make_float2(0.f, 0.f);
+        c < ncols ? ahat[(size_t)i * p.pitch + c] : make_float2(0.f, 0.f);
   }
   __syncthreads();
   fft_inplace<-1>(sbuf, p.log2nx, W, bstride, p.twp_x, tid);
@@ -213,7 +213,7 @@ CFD_D void row_advect_rows(const SpecParams& p, int blk, int rows,
   for (int idx = threadIdx.x; idx < ((rows * 4) << log2h); idx += blockDim.x) {
     const int rf = idx >> log2h, k = idx & (half - 1);
     const int r = rf >> 2, f = rf & 3;
-    const float2* in = tf[f] + (size_t)(i0 + r) * ncols;
+    const float2* in = tf[f] + (size_t)(i0 + r) * p.pitch;
     float2* z = sbuf + rf * PL;
     if (k == 0) {
       const float2 x0 = row_factor(p, f, 0, in[0]);
@@ -248,7 +248,7 @@ CFD_D void row_advect_rows(const SpecParams& p, int blk, int rows,
   for (int idx = threadIdx.x; idx < (rows << log2h); idx += blockDim.x) {
     const int r = idx >> log2h, k = idx & (half - 1);
     const float2* z = sbuf + (r * 4) * PL;
-    float2* out = ahat + (size_t)(i0 + r) * ncols;
+    float2* out = ahat + (size_t)(i0 + r) * p.pitch;
     if (k == 0) {
       const float2 z0 = z[0];
       out[0] = make_float2(z0.x + z0.y, 0.f);
@@ -365,7 +365,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(128, 7)
 #pragma unroll
     for (int q = 0; q < CL; ++q) {
       const int col = c0 + q;
-      if (col < ncols) dst[(size_t)row * ncols + col] = cluster.map_shared_rank(sbuf, q)[pidx(row)];
+      if (col < ncols) dst[(size_t)row * p.pitch + col] = cluster.map_shared_rank(sbuf, q)[pidx(row)];
     }
   }
   // No block may leave while a peer still reads its shared memory.
@@ -389,7 +389,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(128, 7)
     for (int q = 0; q < CL; ++q) {
       const int col = c0 + q;
       cluster.map_shared_rank(sbuf, q)[pidx(row)] =
-          col < ncols ? ahat[(size_t)row * ncols + col] : make_float2(0.f, 0.f);
+          col < ncols ? ahat[(size_t)row * p.pitch + col] : make_float2(0.f, 0.f);
     }
   }
   cluster.sync();
@@ -416,15 +416,16 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(128, 7)
 // the expressions col_update_cols / col_prep_cols evaluate, after the same
 // butterflies, so all column schemes give the same bits.  One transform makes
 // two exchanges at 512 to 4096 rows, so every item starts on buffer 0.
+// src: rows of `pitch` values, of which the first ncols are columns.
 template <int LOG2N, int CG>
-CFD_D void spec_pipe_prefetch(const float2* __restrict__ src, int ncols, int c, int t,
+CFD_D void spec_pipe_prefetch(const float2* __restrict__ src, int pitch, int ncols, int c, int t,
                               float2* __restrict__ stage) {
   constexpr int NTHR = ColPipe<LOG2N>::NTHR, T = CG * NTHR;
   if (c >= ncols) return;
   const int tid = t * CG + (c % CG);
 #pragma unroll
   for (int r = 0; r < 16; ++r)
-    cp_async8(stage + r * T + tid, src + (size_t)(t + NTHR * r) * ncols + c);
+    cp_async8(stage + r * T + tid, src + (size_t)(t + NTHR * r) * pitch + c);
 }
 
 // Element (kx, c) of the state or h: row-major [nx, L + 1], or tiled by
@@ -458,7 +459,7 @@ __global__ void __launch_bounds__(CG * (1 << LOG2N) / 16,
   col_pipe_tables<LOG2N, CG>(sbuf, p.twp_x, p.kx, &tw, &kxt);
   pdl_wait();
   pdl_trigger();
-  spec_pipe_prefetch<LOG2N, CG>(ahat, ncols, g * CG + w, t, stage);
+  spec_pipe_prefetch<LOG2N, CG>(ahat, p.pitch, ncols, g * CG + w, t, stage);
   cp_async_commit();
   float2 v[16], us[16], hs[16];
 #pragma unroll 1
@@ -468,7 +469,7 @@ __global__ void __launch_bounds__(CG * (1 << LOG2N) / 16,
 #pragma unroll
     for (int r = 0; r < 16; ++r) v[r] = c < ncols ? stage[r * T + tid] : make_float2(0.f, 0.f);
     const int gn = g + gridDim.x;
-    if (gn < groups) spec_pipe_prefetch<LOG2N, CG>(ahat, ncols, gn * CG + w, t, stage);
+    if (gn < groups) spec_pipe_prefetch<LOG2N, CG>(ahat, p.pitch, ncols, gn * CG + w, t, stage);
     cp_async_commit();
     if (c < ncols && !sc.explicit_only) {
       // All of this column's state and h values are requested before any is
@@ -528,7 +529,7 @@ __global__ void __launch_bounds__(CG * (1 << LOG2N) / 16,
   col_pipe_tables<LOG2N, CG>(sbuf, p.twp_x, p.kx, &tw, &kxt);
   pdl_wait();
   pdl_trigger();
-  spec_pipe_prefetch<LOG2N, CG>(ahat, ncols, g * CG + w, t, stage);
+  spec_pipe_prefetch<LOG2N, CG>(ahat, p.pitch, ncols, g * CG + w, t, stage);
   cp_async_commit();
   float2 v[16], u[16], hs[16];
 #pragma unroll 1
@@ -539,7 +540,7 @@ __global__ void __launch_bounds__(CG * (1 << LOG2N) / 16,
 #pragma unroll
     for (int r = 0; r < 16; ++r) v[r] = live ? stage[r * T + tid] : make_float2(0.f, 0.f);
     const int gn = g + gridDim.x;
-    if (gn < groups) spec_pipe_prefetch<LOG2N, CG>(ahat, ncols, gn * CG + w, t, stage);
+    if (gn < groups) spec_pipe_prefetch<LOG2N, CG>(ahat, p.pitch, ncols, gn * CG + w, t, stage);
     cp_async_commit();
     // The column's state and h values are requested before the transform
     // (each element is read and written by this thread only).
@@ -572,7 +573,7 @@ __global__ void __launch_bounds__(CG * (1 << LOG2N) / 16,
       if (live) {
         float2* dst = f == 0 ? t4.t[0] : f == 1 ? t4.t[1] : f == 2 ? t4.t[2] : t4.t[3];
 #pragma unroll
-        for (int m = 0; m < 16; ++m) dst[(size_t)(t + P::NTHR * m) * ncols + c] = v[m];
+        for (int m = 0; m < 16; ++m) dst[(size_t)(t + P::NTHR * m) * p.pitch + c] = v[m];
       }
     }
   }
@@ -598,7 +599,7 @@ __global__ void __launch_bounds__(CG * (1 << LOG2N) / 16,
   col_pipe_tables<LOG2N, CG>(sbuf, p.twp_x, p.kx, &tw, &kxt);
   pdl_wait();
   pdl_trigger();
-  spec_pipe_prefetch<LOG2N, CG>(wst, ncols, (it >> 2) * CG + w, t, stage);
+  spec_pipe_prefetch<LOG2N, CG>(wst, ncols, ncols, (it >> 2) * CG + w, t, stage);
   cp_async_commit();
   float2 v[16];
 #pragma unroll 1
@@ -612,13 +613,13 @@ __global__ void __launch_bounds__(CG * (1 << LOG2N) / 16,
                        : make_float2(0.f, 0.f);
     }
     const int in = it + gridDim.x;
-    if (in < items) spec_pipe_prefetch<LOG2N, CG>(wst, ncols, (in >> 2) * CG + w, t, stage);
+    if (in < items) spec_pipe_prefetch<LOG2N, CG>(wst, ncols, ncols, (in >> 2) * CG + w, t, stage);
     cp_async_commit();
     col_pipe_fft<LOG2N, 1, 0>(v, buf, t, tw);
     if (c < ncols) {
       float2* dst = f == 0 ? t4.t[0] : f == 1 ? t4.t[1] : f == 2 ? t4.t[2] : t4.t[3];
 #pragma unroll
-      for (int m = 0; m < 16; ++m) dst[(size_t)(t + P::NTHR * m) * ncols + c] = v[m];
+      for (int m = 0; m < 16; ++m) dst[(size_t)(t + P::NTHR * m) * p.pitch + c] = v[m];
     }
   }
   cp_async_wait_all();
@@ -647,7 +648,7 @@ CFD_D void spec_row_pipe_body(const SpecParams& p, int row, const float2* __rest
   const int ncols = L + 1;
   const int bstride = padded_len(L);
   float2* const buf[2] = {sbuf + f * bstride, sbuf + (4 + f) * bstride};
-  const float2* gin = (f == 0 ? t0 : f == 1 ? t1 : f == 2 ? t2 : t3) + (size_t)row * ncols;
+  const float2* gin = (f == 0 ? t0 : f == 1 ? t1 : f == 2 ? t2 : t3) + (size_t)row * p.pitch;
   // The field's row (ncols <= bstride values) is first copied into its second
   // buffer, all of a thread's loads issued before any store, and the
   // pre-untangling reads it there: read from global memory inside the branchy
@@ -756,7 +757,7 @@ CFD_D void spec_row_pipe_body(const SpecParams& p, int row, const float2* __rest
   }
   __syncthreads();
   if (!lead) return;
-  float2* out = ahat + (size_t)row * ncols;
+  float2* out = ahat + (size_t)row * p.pitch;
 #pragma unroll
   for (int m = 0; m < 16; ++m) {
     const int k = t + NTHR * m;
@@ -829,7 +830,7 @@ __global__ void __launch_bounds__(CG * (1 << LOG2N) / 16,
   };
   int it = next_active(blockIdx.x);
   if (it >= items) return;  // uniform per block
-  spec_pipe_prefetch<LOG2N, CG>(mem[it / groups].ahat, ncols, (it % groups) * CG + w, t, stg);
+  spec_pipe_prefetch<LOG2N, CG>(mem[it / groups].ahat, mem[0].p.pitch, ncols, (it % groups) * CG + w, t, stg);
   cp_async_commit();
   float2 v[16], u[16], hs[16];
 #pragma unroll 1
@@ -845,7 +846,7 @@ __global__ void __launch_bounds__(CG * (1 << LOG2N) / 16,
     for (int r = 0; r < 16; ++r) v[r] = live ? stg[r * T + tid] : make_float2(0.f, 0.f);
     const int nit = next_active(it + gridDim.x);
     if (nit < items)
-      spec_pipe_prefetch<LOG2N, CG>(mem[nit / groups].ahat, ncols, (nit % groups) * CG + w, t, stg);
+      spec_pipe_prefetch<LOG2N, CG>(mem[nit / groups].ahat, mem[0].p.pitch, ncols, (nit % groups) * CG + w, t, stg);
     cp_async_commit();
 #pragma unroll
     for (int mm = 0; mm < 16; ++mm) {
@@ -877,7 +878,7 @@ __global__ void __launch_bounds__(CG * (1 << LOG2N) / 16,
         if (live) {
           float2* dst = m.t[f];
 #pragma unroll
-          for (int mm = 0; mm < 16; ++mm) dst[(size_t)(t + P::NTHR * mm) * ncols + c] = v[mm];
+          for (int mm = 0; mm < 16; ++mm) dst[(size_t)(t + P::NTHR * mm) * mem[0].p.pitch + c] = v[mm];
         }
       }
     }
@@ -907,7 +908,7 @@ __global__ void __launch_bounds__(CG * (1 << LOG2N) / 16,
   };
   int it = next_active(blockIdx.x);
   if (it >= items) return;  // uniform per block
-  spec_pipe_prefetch<LOG2N, CG>(mem[it / per].w, ncols, ((it % per) >> 2) * CG + w, t, stg);
+  spec_pipe_prefetch<LOG2N, CG>(mem[it / per].w, ncols, ncols, ((it % per) >> 2) * CG + w, t, stg);
   cp_async_commit();
   float2 v[16];
 #pragma unroll 1
@@ -923,13 +924,13 @@ __global__ void __launch_bounds__(CG * (1 << LOG2N) / 16,
     }
     const int nit = next_active(it + gridDim.x);
     if (nit < items)
-      spec_pipe_prefetch<LOG2N, CG>(mem[nit / per].w, ncols, ((nit % per) >> 2) * CG + w, t, stg);
+      spec_pipe_prefetch<LOG2N, CG>(mem[nit / per].w, ncols, ncols, ((nit % per) >> 2) * CG + w, t, stg);
     cp_async_commit();
     col_pipe_fft<LOG2N, 1, 0>(v, buf, t, tw);
     if (c < ncols) {
       float2* dst = m.t[f];
 #pragma unroll
-      for (int mm = 0; mm < 16; ++mm) dst[(size_t)(t + P::NTHR * mm) * ncols + c] = v[mm];
+      for (int mm = 0; mm < 16; ++mm) dst[(size_t)(t + P::NTHR * mm) * mem[0].p.pitch + c] = v[mm];
     }
     it = nit;
   }
