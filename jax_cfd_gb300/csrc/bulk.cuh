@@ -92,6 +92,26 @@ CFD_D void tma_load_3d(void* dst_smem, const void* tmap, int x, int y, int z, ui
       : "memory");
 }
 
+// Tiled 2-D TMA store of one box from shared memory (16-byte aligned) to the
+// tensor map's global memory at element coordinates (x, y): x times the
+// element size a multiple of 16 B, both coordinates non-negative.  Joins the
+// calling thread's current bulk group.
+CFD_D void tma_store_2d(const void* tmap, int x, int y, const void* src_smem) {
+  asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%1, %2}], [%3];" ::
+                   "l"(tmap), "r"(x), "r"(y), "r"(smem_addr(src_smem))
+               : "memory");
+}
+
+// Closes the calling thread's current bulk group.
+CFD_D void bulk_commit_group() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+
+// Waits until every committed bulk group of the calling thread has read its
+// shared-memory source (the buffer may then be rewritten).
+CFD_D void bulk_wait_read_all() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+
+// Waits until every committed bulk group of the calling thread has completed.
+CFD_D void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+
 // Orders this thread's earlier generic-proxy accesses to shared memory before
 // its later async-proxy (TMA) accesses.
 CFD_D void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }

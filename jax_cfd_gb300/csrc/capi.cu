@@ -264,6 +264,9 @@ struct cfd_spec_batch {
   cfd::Health* mirror = nullptr;  // pinned host copy of `health`, or null
 };
 
+static_assert(sizeof(CUtensorMap) == 128 && alignof(CUtensorMap) <= 128,
+              "SpecStageMaps holds CUtensorMaps as 128-byte blocks");
+
 struct cfd_spec_plan {
   cfd::SpecParams p;
   int stages = 0;
@@ -275,6 +278,7 @@ struct cfd_spec_plan {
   float2* work = nullptr;   // scratch spectrum for rfft2 / irfft2 / filter
   float2* wt = nullptr;     // state and h in the column-group tiled layout during a
   float2* ht = nullptr;     // chunk of the fused column stage (cfd::spec_state_tiled_ok)
+  cfd::SpecStageMaps maps;  // TMA maps of ahat and t4 (p.stage_maps when they encode)
   float2* twy = nullptr;
   float2* twpx = nullptr;
   float2* twpy = nullptr;
@@ -369,9 +373,9 @@ static int fvm_params_from_config(const cfd_fvm_config* cfg, cfd::FvmParams* out
 // Tensor map of `count` packed row spectra, each nx rows of ny float32 (2
 // floats per complex value), spectrum z at spec + z * member_floats floats;
 // boxes of 8 floats x min(nx, 256) rows x 1 spectrum.
-static bool encode_spec_map(CUtensorMap* map, float2* spec, int nx, int ny, int count = 1,
-                            size_t member_floats = 0) {
-  // Looked up once (a function-local static: thread-safe initialisation).
+// The driver's cuTensorMapEncodeTiled, looked up once (a function-local
+// static: thread-safe initialisation); null where the lookup fails.
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
   static const PFN_cuTensorMapEncodeTiled_v12000 encode = []() {
     void* fn = nullptr;
     cudaDriverEntryPointQueryResult q;
@@ -381,6 +385,28 @@ static bool encode_spec_map(CUtensorMap* map, float2* spec, int nx, int ny, int 
       fn = nullptr;
     return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
   }();
+  return encode;
+}
+
+// 2-D map of float32 rows [rows][width] (width * 4 bytes a multiple of 16)
+// with boxes of 8 floats x min(rows, 256) rows.
+static bool encode_rows_map(void* map, const void* base, int width, int rows) {
+  const PFN_cuTensorMapEncodeTiled_v12000 encode = tensor_map_encoder();
+  if (!encode || ((size_t)width * sizeof(float)) % 16 != 0) return false;
+  const cuuint64_t dims[2] = {(cuuint64_t)width, (cuuint64_t)rows};
+  const cuuint64_t strides[1] = {(cuuint64_t)width * sizeof(float)};
+  const cuuint32_t box[2] = {8, (cuuint32_t)(rows < 256 ? rows : 256)};
+  const cuuint32_t estride[2] = {1, 1};
+  return encode(static_cast<CUtensorMap*>(map), CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2,
+                const_cast<void*>(base), dims, strides, box, estride,
+                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) ==
+         CUDA_SUCCESS;
+}
+
+static bool encode_spec_map(CUtensorMap* map, float2* spec, int nx, int ny, int count = 1,
+                            size_t member_floats = 0) {
+  const PFN_cuTensorMapEncodeTiled_v12000 encode = tensor_map_encoder();
   if (!encode) return false;
   const cuuint64_t dims[3] = {(cuuint64_t)ny, (cuuint64_t)nx, (cuuint64_t)count};
   const cuuint64_t strides[2] = {(cuuint64_t)ny * sizeof(float),
@@ -1694,6 +1720,14 @@ int cfd_spec_plan_create(const cfd_spec_config* cfg, cfd_spec_plan** out) {
     }
   }
 #undef CFD_ALLOC
+  {
+    // TMA maps for the fused column stage (its groups of 4 columns, rows up
+    // to 2048); without them the stage stages by cp.async (same results).
+    bool ok = nx >= 256 && nx <= 2048;
+    ok = ok && encode_rows_map(plan->maps.ahat, plan->ahat, 2 * p.pitch, nx);
+    for (int f = 0; f < 4 && ok; ++f) ok = encode_rows_map(plan->maps.t[f], plan->t4[f], 2 * p.pitch, nx);
+    p.stage_maps = ok ? &plan->maps : nullptr;
+  }
   const SpecTables t = spec_tables(p);
   if ((e = upload(&plan->twy, t.twy.data(), t.twy.size())) != cudaSuccess ||
       (e = upload(&plan->twpx, t.twpx.data(), t.twpx.size())) != cudaSuccess ||

@@ -191,6 +191,17 @@ struct SpecParams {
   int pitch;            // row pitch (complex values) of the internal half spectra
                         // (the four column-transformed fields and the advection
                         // spectrum): L + 4, rows of a 32-byte multiple
+  const void* stage_maps;  // HOST pointer to the plan's SpecStageMaps, or null
+};
+
+// Tensor maps (CUtensorMap: 128 bytes, 128-byte aligned) of a single
+// spectral plan's advection spectrum and four column-transformed fields, as
+// float32 [nx][2 pitch] with boxes of 8 floats x min(nx, 256) rows: the fused
+// column stage stages its column groups by TMA loads and writes its fields by
+// TMA stores where they encode.
+struct alignas(128) SpecStageMaps {
+  unsigned char ahat[128];
+  unsigned char t[4][128];
 };
 
 // Whether the clustered spectral column passes (col_mode 1) apply to this grid.
@@ -204,6 +215,9 @@ bool spec_state_tiled_ok(const SpecParams& p);
 size_t spec_tiled_elems(const SpecParams& p);
 cudaError_t spec_tile_state(const SpecParams& p, const float2* src, float2* dst, bool to_tiled,
                             cudaStream_t s);
+// Whether the fused column stage runs its TMA-staged form (the plan's maps
+// encoded; groups of 4 columns of up to 2048 rows).
+bool spec_stage_tma_ok(const SpecParams& p);
 // Whether the register-pass row pass (row_mode 1 or 2) applies to this grid.
 bool spec_row_pipe_ok(const SpecParams& p);
 

@@ -18,7 +18,10 @@
 // factors are applied on the row side.  All transforms are unnormalised; the
 // irfftn 1/(nx*ny) is a power of two applied once to the product.
 #include <cooperative_groups.h>
+#include <cstring>
+#include <cuda.h>
 
+#include "bulk.cuh"
 #include "colpipe.cuh"
 #include "fft.cuh"
 #include "kernels.h"
@@ -578,6 +581,122 @@ __global__ void __launch_bounds__(CG * (1 << LOG2N) / 16,
     }
   }
   cp_async_wait_all();
+}
+
+// The fused stage with TMA: each group's advection-spectrum columns arrive
+// by TMA tensor loads (boxes of 4 columns x BOX rows, one thread issuing onto
+// an mbarrier, the next group's while this one is transformed), and each of
+// the four fields leaves by TMA tensor stores from the transform's second
+// exchange buffers, which the field's values are copied into in the boxes'
+// row-major layout once the inverse transform has read them; the thread that
+// issued the stores waits for them to have read shared memory before its
+// next transform's first barrier, so no thread rewrites those buffers
+// earlier.  Same values as spec_col_stage_pipe_kernel; groups of 4 columns.
+struct SpecT4Maps {
+  CUtensorMap t[4];
+};
+
+template <int LOG2N, bool TILED>
+__global__ void __launch_bounds__(4 * (1 << LOG2N) / 16,
+                                  col_pipe_min_blocks(4 * (1 << LOG2N) / 16))
+    spec_col_stage_tma_kernel(SpecParams p, StageCoef sc, const __grid_constant__ CUtensorMap amap,
+                              const __grid_constant__ SpecT4Maps tmaps, float2* __restrict__ wst,
+                              float2* __restrict__ hst) {
+  constexpr int CG = 4;
+  using P = ColPipe<LOG2N>;
+  constexpr int N = P::N, BOX = N < 256 ? N : 256, NBOX = N / BOX;
+  constexpr uint32_t kGroupBytes = (uint32_t)N * CG * sizeof(float2);
+  extern __shared__ float2 sbuf[];  // no static shared memory: 128-byte aligned
+  const int ncols = p.L + 1, groups = (ncols + CG - 1) / CG;
+  const int w = threadIdx.x % CG, t = threadIdx.x / CG, tid = threadIdx.x;
+  const int bstride = col_pipe_bstride<LOG2N, CG>();
+  float2* const buf[2] = {sbuf + w * bstride, sbuf + (CG + w) * bstride};
+  float2* const stage = sbuf + 2 * CG * bstride;
+  // The four columns' second exchange buffers, contiguous: the store boxes.
+  float2* const out = sbuf + CG * bstride;
+  uint64_t* const bar =
+      reinterpret_cast<uint64_t*>(reinterpret_cast<char*>(sbuf) + col_pipe_smem<LOG2N, CG>());
+  int g = blockIdx.x;
+  if (g >= groups) return;  // uniform per block
+  const float2* tw;
+  const float* kxt;
+  col_pipe_tables<LOG2N, CG>(sbuf, p.twp_x, p.kx, &tw, &kxt);
+  if (tid == 0) {
+    mbar_init(bar, 1);
+    mbar_fence_init();
+  }
+  __syncthreads();
+  pdl_wait();
+  pdl_trigger();
+  auto issue = [&](int gg) {
+    mbar_arrive_expect_tx(bar, kGroupBytes);
+#pragma unroll
+    for (int b = 0; b < NBOX; ++b) tma_load_2d(stage + b * BOX * CG, &amap, 8 * gg, b * BOX, bar);
+  };
+  if (tid == 0) issue(g);
+  uint32_t phase = 0;
+  float2 v[16], u[16], hs[16];
+#pragma unroll 1
+  for (; g < groups; g += gridDim.x) {
+    const int c = g * CG + w;
+    const bool live = c < ncols;
+    const bool landed = mbar_wait(bar, phase);
+    phase ^= 1u;
+#pragma unroll
+    for (int r = 0; r < 16; ++r) v[r] = live ? stage[(t + P::NTHR * r) * CG + w] : make_float2(0.f, 0.f);
+    // The staged group is read; a wait that gave up on any thread ends the
+    // block (after its own stores have left shared memory).
+    if (__syncthreads_or(!landed)) {
+      if (tid == 0) bulk_wait_all();
+      return;
+    }
+    if (tid == 0 && g + gridDim.x < groups) {
+      fence_proxy_async_smem();
+      issue(g + gridDim.x);
+    }
+#pragma unroll
+    for (int m = 0; m < 16; ++m) {
+      const size_t gi = state_at<CG, TILED>(p.nx, ncols, t + P::NTHR * m, c);
+      u[m] = live ? wst[gi] : make_float2(0.f, 0.f);
+      hs[m] = (live && sc.has_h_in) ? hst[gi] : make_float2(0.f, 0.f);
+    }
+    if (tid == 0) bulk_wait_read_all();
+    col_pipe_fft<LOG2N, -1, 0>(v, buf, t, tw);
+    if (live) {
+#pragma unroll
+      for (int m = 0; m < 16; ++m) {
+        const int kx = t + P::NTHR * m;
+        const size_t gi = state_at<CG, TILED>(p.nx, ncols, kx, c);
+        float2 h;
+        u[m] = stage_update_core_k(p, sc, kx, kxt[kx], c, v[m], u[m], hs[m], &h);
+        wst[gi] = u[m];
+        if (sc.write_h) hst[gi] = h;
+      }
+    }
+#pragma unroll 1
+    for (int f = 0; f < 4; ++f) {
+#pragma unroll
+      for (int r = 0; r < 16; ++r) {
+        const int kx = t + P::NTHR * r;
+        v[r] = live ? prep_factor_k(p, f, kx, kxt[kx], c, u[r]) : make_float2(0.f, 0.f);
+      }
+      if (tid == 0) bulk_wait_read_all();
+      col_pipe_fft<LOG2N, 1, 0>(v, buf, t, tw);
+      // Every thread is past the transform's reads of the second buffers.
+      __syncthreads();
+#pragma unroll
+      for (int m = 0; m < 16; ++m) out[(t + P::NTHR * m) * CG + w] = v[m];
+      fence_proxy_async_smem();
+      __syncthreads();
+      if (tid == 0) {
+#pragma unroll
+        for (int b = 0; b < NBOX; ++b)
+          tma_store_2d(&tmaps.t[f], 8 * g, b * BOX, out + b * BOX * CG);
+        bulk_commit_group();
+      }
+    }
+  }
+  if (tid == 0) bulk_wait_all();
 }
 
 template <int LOG2N, int CG>
@@ -1183,6 +1302,35 @@ static cudaError_t spec_stage_pipe_impl(const SpecParams& p, const StageCoef& sc
                           tt);
 }
 
+template <int LOG2N>
+static cudaError_t spec_stage_tma_impl(const SpecParams& p, const StageCoef& sc, float2* w,
+                                       float2* h, cudaStream_t s) {
+  const SpecStageMaps* maps = static_cast<const SpecStageMaps*>(p.stage_maps);
+  CUtensorMap amap;
+  SpecT4Maps tm;
+  std::memcpy(&amap, maps->ahat, sizeof(amap));
+  for (int f = 0; f < 4; ++f) std::memcpy(&tm.t[f], maps->t[f], sizeof(CUtensorMap));
+  auto kern = sc.tiled ? spec_col_stage_tma_kernel<LOG2N, true>
+                       : spec_col_stage_tma_kernel<LOG2N, false>;
+  const size_t smem = col_pipe_smem<LOG2N, 4>() + 16;  // + the mbarrier
+  const int threads = 4 * (1 << LOG2N) / 16;
+  cudaError_t e = set_smem(kern, smem);
+  if (e != cudaSuccess) return e;
+  static std::atomic<int> per_sm_cache{0};
+  int per_sm = 1;
+  e = cached_blocks_per_sm(kern, threads, smem, per_sm_cache, &per_sm);
+  if (e != cudaSuccess) return e;
+  const int items = (p.L + 1 + 3) / 4, slots = col_pipe_device_sms() * per_sm;
+  return launch_maybe_pdl(p.pdl, kern, dim3(items < slots ? items : slots), dim3(threads), smem,
+                          s, p, sc, amap, tm, w, h);
+}
+
+// The TMA-staged fused stage: groups of 4 columns of up to 2048 rows, where
+// the plan's maps encoded.
+bool spec_stage_tma_ok(const SpecParams& p) {
+  return p.stage_maps && p.col_mode == 4 && spec_pipe_ok(p) && p.log2nx <= 11;
+}
+
 template <int LOG2N, int CG>
 static cudaError_t spec_update_pipe_impl(const SpecParams& p, const StageCoef& sc,
                                          const float2* ahat, float2* w, float2* h,
@@ -1241,6 +1389,13 @@ cudaError_t launch_spec_col_update(const SpecParams& p, const StageCoef& sc,
   cudaError_t e;
   if (spec_pipe_ok(p) && p.col_mode == 4 && sc.prep_next && !sc.explicit_only) {
     // Update and the next stage's prep in one pass.
+    if (spec_stage_tma_ok(p)) {
+      switch (p.log2nx) {
+        case 9: return spec_stage_tma_impl<9>(p, sc, w, h, s);
+        case 10: return spec_stage_tma_impl<10>(p, sc, w, h, s);
+        default: return spec_stage_tma_impl<11>(p, sc, w, h, s);
+      }
+    }
     T4 tt{{t4[0], t4[1], t4[2], t4[3]}};
     switch (p.log2nx) {
       case 9: return spec_stage_pipe_impl<9, 4>(p, sc, ahat, w, h, tt, s);
