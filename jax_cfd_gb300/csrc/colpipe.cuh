@@ -89,6 +89,18 @@ CFD_D void col_pipe_tables(float2* sbuf, const float2* __restrict__ twp,
   __syncthreads();
 }
 
+// The barrier of a transform's exchanges: the whole block (BARN == 0), or the
+// BARN threads (whole warps) that own one column, on named barrier bar_id.
+template <int BARN>
+CFD_D void col_pipe_sync(int bar_id) {
+  if constexpr (BARN == 0) {
+    __syncthreads();
+  } else {
+    static_assert(BARN % 32 == 0, "a named barrier counts whole warps");
+    asm volatile("bar.sync %0, %1;\n" ::"r"(bar_id), "n"(BARN) : "memory");
+  }
+}
+
 // One transform of sign SIGN of the calling worker's column; twp is the pass
 // table as col_pipe_tables returned it.  v: the pass-0
 // inputs x[t + NTHR r] on entry, X[t + NTHR m] in v[m] on return.  buf[0],
@@ -97,9 +109,12 @@ CFD_D void col_pipe_tables(float2* sbuf, const float2* __restrict__ twp,
 // (it contains barriers).
 // LDG: twp is the global table (else a shared copy).  A thread with
 // active == false computes nothing but takes part in every barrier.
-template <int LOG2N, int SIGN, int FIRST, bool LDG = !col_pipe_smem_tables<LOG2N>()>
+// BARN != 0: the exchanges synchronise only the BARN threads of this column
+// (named barrier bar_id), for columns whose buffers no other thread touches.
+template <int LOG2N, int SIGN, int FIRST, bool LDG = !col_pipe_smem_tables<LOG2N>(),
+          int BARN = 0>
 CFD_D void col_pipe_fft(float2 (&v)[16], float2* const (&buf)[2], int t,
-                        const float2* __restrict__ twp, bool active = true) {
+                        const float2* __restrict__ twp, bool active = true, int bar_id = 0) {
   using P = ColPipe<LOG2N>;
   int wsel = FIRST;
   int tw_off = 0;
@@ -126,7 +141,7 @@ CFD_D void col_pipe_fft(float2 (&v)[16], float2* const (&buf)[2], int t,
         for (int r = 0; r < 16; ++r) out[pidx(o + r * Ns)] = v[r];
       }
       wsel ^= 1;
-      __syncthreads();
+      col_pipe_sync<BARN>(bar_id);
     }
   }
   if constexpr (P::REM > 0) {

@@ -844,13 +844,41 @@ CFD_D void spec_row_pipe_body(const SpecParams& p, int row, const float2* __rest
     }
   }
   __syncthreads();
-  col_pipe_fft<LOG2L, 1, 0, true>(v, buf, t, p.twp_y);
+  // From 32 workers per field on, each field's transform synchronises only its
+  // own warps (named barrier 1 + f): its buffers are its own until the samples
+  // meet below.
+  constexpr int BARN = NTHR >= 32 ? NTHR : 0;
+  col_pipe_fft<LOG2L, 1, 0, true, BARN>(v, buf, t, p.twp_y, true, 1 + f);
   // Samples n = t + NTHR m of every field into its first buffer (free: its
   // last reader was the transform's second pass).
 #pragma unroll
   for (int m = 0; m < 16; ++m) buf[0][pidx(t + NTHR * m)] = v[m];
   __syncthreads();
   const bool lead = f == 0;
+  // The untangling twiddles of the post-untangling, staged in field 1's
+  // second buffer (free after its transform) by the warps of fields 1-3 while
+  // the field-0 warps form the product and run the forward transform; those
+  // warps then signal named barrier 5 and leave.  The post-untangling's
+  // global twiddle loads, taken in its branches, were one round trip each.
+  float2* const tw2 = sbuf + 5 * bstride;
+  if constexpr (BARN != 0) {
+    if (!lead) {
+      constexpr int T3 = 3 * NTHR, R3 = (L + T3 - 1) / T3;
+      float2 tv[R3];
+#pragma unroll
+      for (int r = 0; r < R3; ++r) {
+        const int e = (int)threadIdx.x - NTHR + T3 * r;
+        tv[r] = e < L ? __ldg(p.tw_y + e) : make_float2(0.f, 0.f);
+      }
+#pragma unroll
+      for (int r = 0; r < R3; ++r) {
+        const int e = (int)threadIdx.x - NTHR + T3 * r;
+        if (e < L) tw2[e] = tv[r];
+      }
+      asm volatile("bar.arrive 5, %0;\n" ::"n"(4 * NTHR) : "memory");
+      return;
+    }
+  }
   if (lead) {
     // advection = -(gx * vx + gy * vy), each field scaled by 1/(nx*ny).
     const float s2 = p.scale * p.scale;
@@ -867,15 +895,20 @@ CFD_D void spec_row_pipe_body(const SpecParams& p, int row, const float2* __rest
   // Forward transform of the advection (field-0 threads); it starts on the
   // second buffers, which nobody reads any more, while the first buffers of
   // fields 1-3 may still be read above.
-  col_pipe_fft<LOG2L, -1, 1, true>(v, buf, t, p.twp_y, lead);
+  col_pipe_fft<LOG2L, -1, 1, true, BARN>(v, buf, t, p.twp_y, lead, 1);
   // Z[k] into field 0's second buffer (its last reader was the forward
   // transform's first read), then each output from the pair (k, L - k).
   if (lead) {
 #pragma unroll
     for (int m = 0; m < 16; ++m) buf[1][pidx(t + NTHR * m)] = v[m];
   }
-  __syncthreads();
+  if constexpr (BARN != 0) {
+    asm volatile("bar.sync 5, %0;\n" ::"n"(4 * NTHR) : "memory");
+  } else {
+    __syncthreads();
+  }
   if (!lead) return;
+  auto twv = [&](int e) { return BARN != 0 ? tw2[e] : __ldg(p.tw_y + e); };
   float2* out = ahat + (size_t)row * p.pitch;
 #pragma unroll
   for (int m = 0; m < 16; ++m) {
@@ -886,13 +919,13 @@ CFD_D void spec_row_pipe_body(const SpecParams& p, int row, const float2* __rest
       out[0] = make_float2(z.x + z.y, 0.f);
       out[L] = make_float2(z.x - z.y, 0.f);
     } else if (k == half) {
-      rfft_post_pair(z, z, __ldg(p.tw_y + half), &xk, &xm);
+      rfft_post_pair(z, z, twv(half), &xk, &xm);
       out[half] = xk;
     } else if (k < half) {
-      rfft_post_pair(z, buf[1][pidx(L - k)], __ldg(p.tw_y + k), &xk, &xm);
+      rfft_post_pair(z, buf[1][pidx(L - k)], twv(k), &xk, &xm);
       out[k] = xk;
     } else {
-      rfft_post_pair(buf[1][pidx(L - k)], z, __ldg(p.tw_y + L - k), &xk, &xm);
+      rfft_post_pair(buf[1][pidx(L - k)], z, twv(L - k), &xk, &xm);
       out[k] = xm;
     }
   }
