@@ -426,10 +426,11 @@ static bool encode_spec_map(CUtensorMap* map, float2* spec, int nx, int ny, int 
 // fastest there or within 3 % of it; the autotuner can still revise it):
 // narrow row blocks, rows fed by bulk copies where they fit, the persistent
 // column pass from 256 rows (TMA-staged from 1024, where the map encodes),
-// warp streams with 8 rows per warp below 2^22 cells and 16 from there.  Per
+// warp streams with 8 rows per warp up to 2^22 cells and 16 above.  Per
 // step: 128^2 31.2 against 40.4 us for the earlier default (tiles, per-block
 // columns, register feed), 256^2 23.0 against 39.4, 512^2 25.0 against
-// 44.4, 1024^2 33.2 against 38.8; 2048^2 unchanged (65.0).
+// 44.4, 1024^2 33.2 against 38.8; 2048^2 63.7 (8 rows per warp) against
+// 64.6 (16).
 static void plan_default_launch(cfd::FvmParams* p) {
   if ((long long)p->nx * p->ny < (1LL << 14)) return;
   p->fft_shape = 1;
@@ -437,7 +438,7 @@ static void plan_default_launch(cfd::FvmParams* p) {
   if (p->nx >= 256 && cfd::col_pipe_ok(*p, 0)) p->col_mode = 3;
   if (!cfd::fft_shape_ok(*p)) p->fft_shape = 0;
   cfd::FvmParams q = *p;
-  q.stream_rows = (long long)p->nx * p->ny < (1LL << 22) ? 1 : 0;
+  q.stream_rows = (long long)p->nx * p->ny <= (1LL << 22) ? 1 : 0;
   if (cfd::stream_stencil_ok(q)) {
     p->stencil = 1;
     p->stream_rows = q.stream_rows;

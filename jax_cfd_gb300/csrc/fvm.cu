@@ -479,15 +479,25 @@ CFD_D float2 stream_xface(const FvmParams& p, float2 cm, float2 c0, float2 c1, f
 // measured 33.1 against 30.7 us at 2048^2).  Each column evaluates exactly
 // the expressions of explicit_tile.
 constexpr int kStreamCols = 60;
-// Rows per warp and prefetch depth (16 and 4 measured fastest at 2048^2:
-// 30.7 us against 31.0 for 32 rows, 31.3 for a prefetch of 2, 32.5 with the
-// registers capped at 64 for 32 warps per multiprocessor, and 33.1 for one
-// column per lane).  A warp fetches SH + 4 rows for SH outputs, so the rows
-// per warp trade halo re-reads against warps in flight; single plans also
-// run 8 and 32 (FvmParams::stream_rows, an autotuner dimension).  24 rows
-// per warp (one wave of warps at 2048^2 instead of 1.47, the last warp of a
-// strip taking the remaining rows) measured slower: 33.4 against 31.4 us.
-constexpr int kStreamRows = 16, kStreamPrefetch = 4;
+// Rows per warp and prefetch depth.  A warp fetches SH + 4 rows for SH
+// outputs, so the rows per warp trade halo re-reads against warps in flight;
+// plans run 16, 8 and 32 (FvmParams::stream_rows, an autotuner dimension).
+// The kernel is issue-bound, and registers set the warps in flight: with a
+// prefetch of 2 rows the projecting Kolmogorov-forcing kernel (PROJECT,
+// FORCE = 1: every step of a chunk but the first) fits 80 registers without
+// spills, six 128-thread blocks (24 warps) per multiprocessor (the other
+// variants would spill there and keep the compiler's choice).  2048^2 step (stencil): 63.7 us
+// (29.4) at 8 rows per warp, 64.6 (30.9) at 16, against 65.0 (31.1) for the
+// earlier 4-row prefetch at 94 registers (20 warps); the 4-row prefetch held
+// to 80 registers spills (65.5), 72 registers (28 warps) spill too (65.4).
+// Also measured slower: 24 rows per warp (one wave of warps at 2048^2, the
+// last warp of a strip taking the remaining rows), 33.4 against 31.4 us; 64
+// registers (32 warps), 32.5 against 30.7; one column per lane, 33.1.
+constexpr int kStreamRows = 16, kStreamPrefetch = 2;
+constexpr int kStreamBlocksPerSM = 6;
+// The batched stream (run-time forcing flags, no register cap) keeps the
+// 4-row prefetch it was measured with.
+constexpr int kBatchStreamPrefetch = 4;
 CFD_HD int stream_rows_of(int mode) { return mode == 1 ? 8 : mode == 2 ? 32 : kStreamRows; }
 
 struct StreamRaw {
@@ -638,7 +648,7 @@ CFD_D void explicit_stream_body(const FvmParams& p, int bx, const float* __restr
 }
 
 template <bool PROJECT, int CONVECT, int FORCE, int SH>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(128, PROJECT && FORCE == 1 ? kStreamBlocksPerSM : 1)
     fvm_explicit_stream_kernel(FvmParams p, const float* __restrict__ ua,
                                 const float* __restrict__ va, const float* __restrict__ q,
                                 float* __restrict__ uo, float* __restrict__ vo) {
@@ -1634,7 +1644,7 @@ __global__ void __launch_bounds__(128)
   if (k >= m.steps) return;
   const FvmParams p = m.p;
   const int src = batch_src(k), dst = batch_dst(k);
-  explicit_stream_body<PROJECT, CONVECT, 0, kStreamRows, kStreamPrefetch>(
+  explicit_stream_body<PROJECT, CONVECT, 0, kStreamRows, kBatchStreamPrefetch>(
       p, blockIdx.x, m.f[src][0], m.f[src][1], reinterpret_cast<const float*>(m.spec),
       m.f[dst][0], m.f[dst][1]);
 }
