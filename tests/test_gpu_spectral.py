@@ -54,7 +54,8 @@ def test_explicit_terms_match_oracle(cuda_device, shape, forced):
   assert rel_l2(got, oeq.explicit_terms(w0)) <= STEP_TOL
 
 
-@pytest.mark.parametrize('shape', [(16, 16), (64, 64), (256, 256), (64, 128), (256, 2048)])
+@pytest.mark.parametrize('shape', [(16, 16), (64, 64), (256, 256), (64, 128), (128, 512),
+                                   (64, 1024), (256, 2048)])
 def test_cn_rk4_step_matches_oracle(cuda_device, shape):
   import jax_cfd_gb300.base as cfd
   from jax_cfd_gb300.spectral import equations as seq
@@ -122,7 +123,7 @@ def test_taylor_green_spectral_analytic(cuda_device):
   assert np.abs(got - want).max() <= 1e-3
 
 
-@pytest.mark.parametrize('shape', [(256, 256), (512, 256), (2048, 2048)])
+@pytest.mark.parametrize('shape', [(256, 256), (512, 256), (256, 1024), (2048, 2048)])
 @pytest.mark.parametrize('forcing', ['smooth', 'kolmogorov'])
 def test_cluster_column_passes_are_bitwise(cuda_device, shape, forcing):
   """Every column scheme (per-block, clusters, persistent pipelined, fused
