@@ -274,7 +274,7 @@ def test_runge_kutta_tableaux_match_oracle(cuda_device, name, shape):
 
 
 # --- implicit_diffusion_navier_stokes / diffusion.solve_fast_diag ----------
-@pytest.mark.parametrize('shape', [(64, 64), (128, 64), (2048, 256)])
+@pytest.mark.parametrize('shape', [(64, 64), (128, 64), (2048, 256), (64, 2048)])
 def test_diffusion_solve_matches_oracle(cuda_device, shape):
   """diffusion.py:166-212 on the native transforms: the diffused fields and
   the small diffusive increment both match the oracle."""
