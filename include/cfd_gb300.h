@@ -352,8 +352,8 @@ long long cfd_spec_plan_bytes(const cfd_spec_plan* plan);
  * (512 <= nx <= 4096), 4 as 2 with each stage's column update and the next
  * stage's column prep fused into one pass; plus 5 x the row scheme: 0 the
  * shared-memory row pass, 1 the register-pass row pass (512 <= ny <= 4096),
- * 2 the same with registers sized for three blocks per multiprocessor
- * (512 <= ny <= 2048): 15 choices.  Results are bit-for-bit the same for
+ * 2 the same with registers sized for three blocks per multiprocessor (four
+ * at ny = 2048; 512 <= ny <= 2048): 15 choices.  Results are bit-for-bit the same for
  * every choice. */
 int cfd_spec_plan_set_launch(cfd_spec_plan* plan, int choice);
 int cfd_spec_plan_get_launch(const cfd_spec_plan* plan);

@@ -1684,8 +1684,10 @@ int cfd_spec_plan_create(const cfd_spec_config* cfg, cfd_spec_plan** out) {
     if (!cfd::spec_pipe_ok(p)) p.col_mode = 0;
   }
   // The register-pass row pass measured faster at 2048^2 (66.5 against 72.1 us),
-  // and with registers for three blocks per multiprocessor faster still at
-  // ny = 2048 (61.7 against 66.3 us) but slower at ny = 1024 (24.6 against 20.8).
+  // and with registers for more blocks per multiprocessor faster still at
+  // ny = 2048 (three blocks: 61.7 against 66.3 us; four, with one exchange
+  // buffer per field: 42.1 against 43.6 us at three and 48.2 for the earlier
+  // two-buffer layout) but not at ny = 1024 (24.6 against 20.8 us).
   p.row_mode = cfd::spec_row_pipe_ok(p) ? 1 : 0;
   if (p.row_mode == 1 && p.log2L == 10) p.row_mode = 2;
   plan->stages = stages;

@@ -111,8 +111,11 @@ CFD_D void col_pipe_sync(int bar_id) {
 // active == false computes nothing but takes part in every barrier.
 // BARN != 0: the exchanges synchronise only the BARN threads of this column
 // (named barrier bar_id), for columns whose buffers no other thread touches.
+// SINGLE: buf[0] and buf[1] are one buffer, so each exchange after the first
+// also waits for every read of the previous one before it writes (half the
+// shared memory, one more barrier per exchange).
 template <int LOG2N, int SIGN, int FIRST, bool LDG = !col_pipe_smem_tables<LOG2N>(),
-          int BARN = 0>
+          int BARN = 0, bool SINGLE = false>
 CFD_D void col_pipe_fft(float2 (&v)[16], float2* const (&buf)[2], int t,
                         const float2* __restrict__ twp, bool active = true, int bar_id = 0) {
   using P = ColPipe<LOG2N>;
@@ -134,6 +137,9 @@ CFD_D void col_pipe_fft(float2 (&v)[16], float2* const (&buf)[2], int t,
     if (q > 0) tw_off += 15 << (4 * q);
     const bool last = q == P::N16 - 1 && P::REM == 0;
     if (!last) {
+      if constexpr (SINGLE) {
+        if (q > 0) col_pipe_sync<BARN>(bar_id);
+      }
       if (active) {
         float2* out = buf[wsel];
         const int o = ((t - k) << 4) + k;

@@ -188,6 +188,7 @@ struct SpecParams {
   int pdl;              // launch the stage kernels as programmatic dependents
   int row_mode;         // row pass: 0 shared-memory engine, 1 register passes,
                         // 2 register passes with registers for 3 blocks per SM
+                        //   (4 at ny = 2048)
   int pitch;            // row pitch (complex values) of the internal half spectra
                         // (the four column-transformed fields and the advection
                         // spectrum): L + 4, rows of a 32-byte multiple

@@ -754,36 +754,47 @@ __global__ void __launch_bounds__(CG * (1 << LOG2N) / 16,
 // advection product, which the field-0 threads form at exactly the forward
 // transform's first-pass positions; the post-untangling partners again come
 // from shared memory.  Same butterflies, twiddles and element formulas as
-// row_advect_rows, so the same bits, with one barrier per exchange and no
-// shared-memory round trip around the transforms' global loads and stores.
+// row_advect_rows, so the same bits, with no shared-memory round trip around
+// the transforms' global loads and stores.
+//
+// Shared memory: one exchange buffer per field (each exchange waits for the
+// previous one's reads before it writes) and a table region that nothing
+// overwrites, holding the ky table and the untangling twiddles for the pre-
+// and post-untangling.  At ny = 2048 that is 47 KB per block, so that four
+// blocks (64 registers) fit on a multiprocessor; with two buffers per field
+// and the tables in them it was 68 KB and three blocks.
+template <int LOG2L>
+CFD_HD size_t spec_row_pipe_smem() {
+  constexpr int L = 1 << LOG2L;
+  return ((size_t)4 * padded_len(L) + (L + 2) / 2 + L) * sizeof(float2);
+}
+
 template <int LOG2L>
 CFD_D void spec_row_pipe_body(const SpecParams& p, int row, const float2* __restrict__ t0,
                               const float2* __restrict__ t1, const float2* __restrict__ t2,
                               const float2* __restrict__ t3, float2* __restrict__ ahat) {
   using P = ColPipe<LOG2L>;
   constexpr int NTHR = P::NTHR, L = P::N, half = L / 2;
+  // From 32 workers per field on, a field's transforms synchronise only its
+  // own warps (named barrier 1 + f): its buffer is its own until the samples
+  // meet for the product.
+  constexpr int BARN = NTHR >= 32 ? NTHR : 0;
   extern __shared__ float2 sbuf[];
   const int f = threadIdx.x / NTHR, t = threadIdx.x % NTHR;
-  const int ncols = L + 1;
   const int bstride = padded_len(L);
-  float2* const buf[2] = {sbuf + f * bstride, sbuf + (4 + f) * bstride};
+  float2* const fb = sbuf + f * bstride;
+  float2* const buf[2] = {fb, fb};
+  float* const kys = reinterpret_cast<float*>(sbuf + 4 * bstride);  // L + 1 values
+  float2* const tws = sbuf + 4 * bstride + (L + 2) / 2;             // L values
   const float2* gin = (f == 0 ? t0 : f == 1 ? t1 : f == 2 ? t2 : t3) + (size_t)row * p.pitch;
-  // The field's row (ncols <= bstride values) is first copied into its second
-  // buffer, all of a thread's loads issued before any store, and the
-  // pre-untangling reads it there: read from global memory inside the branchy
-  // loop below, the loads of each element and its mirror were taken one
-  // round trip at a time (about 60 % of the block's time).  The transform
-  // writes the second buffer only after its first exchange's barrier, which
-  // follows every read of the copy.
-  float2* const in = buf[1];
-  // The ky table (L + 1 floats) and the untangling twiddles (L values) go to
-  // the first buffers of fields 0 and 1 for the same reason; a barrier after
-  // the pre-untangling keeps the transform's first exchange (which writes
-  // those buffers) behind every read of them.  2048^2 row pass: 61.9 us
-  // reading global memory in the loop, 57.1 with the rows staged, 48.2 with
-  // the tables staged as well.
-  float* const kys = reinterpret_cast<float*>(sbuf);
-  float2* const tws = sbuf + bstride;
+  // The field's row (L + 1 values), the ky table and the twiddles are first
+  // copied into shared memory, all of a thread's loads issued before any
+  // store, and the pre-untangling reads them there: read from global memory
+  // inside the branchy loop below, the loads of each element, its mirror, ky
+  // and the twiddle were taken one round trip at a time.  2048^2 row pass:
+  // 61.9 us reading global memory in the loop, 57.1 with the rows staged,
+  // 48.2 with the tables staged as well.
+  float2* const in = fb;
   {
     float2 x[16];
 #pragma unroll
@@ -843,41 +854,18 @@ CFD_D void spec_row_pipe_body(const SpecParams& p, int row, const float2* __rest
       v[r] = zm;
     }
   }
-  __syncthreads();
-  // From 32 workers per field on, each field's transform synchronises only its
-  // own warps (named barrier 1 + f): its buffers are its own until the samples
-  // meet below.
-  constexpr int BARN = NTHR >= 32 ? NTHR : 0;
-  col_pipe_fft<LOG2L, 1, 0, true, BARN>(v, buf, t, p.twp_y, true, 1 + f);
-  // Samples n = t + NTHR m of every field into its first buffer (free: its
-  // last reader was the transform's second pass).
+  // The transform's first exchange rewrites the copy of the row.
+  col_pipe_sync<BARN>(1 + f);
+  col_pipe_fft<LOG2L, 1, 0, true, BARN, true>(v, buf, t, p.twp_y, true, 1 + f);
+  // Samples n = t + NTHR m of every field into its buffer, once the
+  // transform's last reads of it are done.
+  col_pipe_sync<BARN>(1 + f);
 #pragma unroll
-  for (int m = 0; m < 16; ++m) buf[0][pidx(t + NTHR * m)] = v[m];
+  for (int m = 0; m < 16; ++m) fb[pidx(t + NTHR * m)] = v[m];
   __syncthreads();
   const bool lead = f == 0;
-  // The untangling twiddles of the post-untangling, staged in field 1's
-  // second buffer (free after its transform) by the warps of fields 1-3 while
-  // the field-0 warps form the product and run the forward transform; those
-  // warps then signal named barrier 5 and leave.  The post-untangling's
-  // global twiddle loads, taken in its branches, were one round trip each.
-  float2* const tw2 = sbuf + 5 * bstride;
   if constexpr (BARN != 0) {
-    if (!lead) {
-      constexpr int T3 = 3 * NTHR, R3 = (L + T3 - 1) / T3;
-      float2 tv[R3];
-#pragma unroll
-      for (int r = 0; r < R3; ++r) {
-        const int e = (int)threadIdx.x - NTHR + T3 * r;
-        tv[r] = e < L ? __ldg(p.tw_y + e) : make_float2(0.f, 0.f);
-      }
-#pragma unroll
-      for (int r = 0; r < R3; ++r) {
-        const int e = (int)threadIdx.x - NTHR + T3 * r;
-        if (e < L) tw2[e] = tv[r];
-      }
-      asm volatile("bar.arrive 5, %0;\n" ::"n"(4 * NTHR) : "memory");
-      return;
-    }
+    if (!lead) return;  // fields 1-3 are done; the field-0 warps go on alone
   }
   if (lead) {
     // advection = -(gx * vx + gy * vy), each field scaled by 1/(nx*ny).
@@ -892,23 +880,18 @@ CFD_D void spec_row_pipe_body(const SpecParams& p, int row, const float2* __rest
       v[m] = make_float2(-(gx.x * vx.x + gy.x * vy.x) * s2, -(gx.y * vx.y + gy.y * vy.y) * s2);
     }
   }
-  // Forward transform of the advection (field-0 threads); it starts on the
-  // second buffers, which nobody reads any more, while the first buffers of
-  // fields 1-3 may still be read above.
-  col_pipe_fft<LOG2L, -1, 1, true, BARN>(v, buf, t, p.twp_y, lead, 1);
-  // Z[k] into field 0's second buffer (its last reader was the forward
-  // transform's first read), then each output from the pair (k, L - k).
+  // Forward transform of the advection (field-0 threads) in field 0's buffer,
+  // whose samples nobody reads.
+  col_pipe_fft<LOG2L, -1, 1, true, BARN, true>(v, buf, t, p.twp_y, lead, 1);
+  // Z[k] into field 0's buffer once the transform's last reads of it are
+  // done, then each output from the pair (k, L - k).
+  col_pipe_sync<BARN>(1);
   if (lead) {
 #pragma unroll
-    for (int m = 0; m < 16; ++m) buf[1][pidx(t + NTHR * m)] = v[m];
+    for (int m = 0; m < 16; ++m) fb[pidx(t + NTHR * m)] = v[m];
   }
-  if constexpr (BARN != 0) {
-    asm volatile("bar.sync 5, %0;\n" ::"n"(4 * NTHR) : "memory");
-  } else {
-    __syncthreads();
-  }
+  col_pipe_sync<BARN>(1);
   if (!lead) return;
-  auto twv = [&](int e) { return BARN != 0 ? tw2[e] : __ldg(p.tw_y + e); };
   float2* out = ahat + (size_t)row * p.pitch;
 #pragma unroll
   for (int m = 0; m < 16; ++m) {
@@ -919,20 +902,21 @@ CFD_D void spec_row_pipe_body(const SpecParams& p, int row, const float2* __rest
       out[0] = make_float2(z.x + z.y, 0.f);
       out[L] = make_float2(z.x - z.y, 0.f);
     } else if (k == half) {
-      rfft_post_pair(z, z, twv(half), &xk, &xm);
+      rfft_post_pair(z, z, tws[half], &xk, &xm);
       out[half] = xk;
     } else if (k < half) {
-      rfft_post_pair(z, buf[1][pidx(L - k)], twv(k), &xk, &xm);
+      rfft_post_pair(z, fb[pidx(L - k)], tws[k], &xk, &xm);
       out[k] = xk;
     } else {
-      rfft_post_pair(buf[1][pidx(L - k)], z, twv(L - k), &xk, &xm);
+      rfft_post_pair(fb[pidx(L - k)], z, tws[L - k], &xk, &xm);
       out[k] = xm;
     }
   }
 }
 
 // OCC: resident threads per multiprocessor the register budget is sized for
-// (512: 128 registers; 768: 80, three 256-thread blocks at ny = 2048).
+// (512: 128 registers; 768: 80, three blocks; 1024: 64, four 256-thread blocks
+// at ny = 2048, which the row pass's 47 KB of shared memory also allows).
 template <int LOG2L, int OCC>
 __global__ void __launch_bounds__(4 * (1 << LOG2L) / 16, OCC / (4 * (1 << LOG2L) / 16))
     spec_row_pipe_kernel(SpecParams p, const float2* __restrict__ t0,
@@ -1476,7 +1460,7 @@ cudaError_t launch_spec_col_update(const SpecParams& p, const StageCoef& sc,
 template <int LOG2L, int OCC>
 static cudaError_t spec_row_pipe_impl(const SpecParams& p, const float2* const t4[4],
                                       float2* ahat, cudaStream_t s) {
-  const size_t smem = (size_t)8 * padded_len(1 << LOG2L) * sizeof(float2);
+  const size_t smem = spec_row_pipe_smem<LOG2L>();
   auto kern = spec_row_pipe_kernel<LOG2L, OCC>;
   cudaError_t e = set_smem(kern, smem);
   if (e != cudaSuccess) return e;
@@ -1523,7 +1507,8 @@ cudaError_t spec_tile_state(const SpecParams& p, const float2* src, float2* dst,
 }
 
 bool spec_row_pipe_ok(const SpecParams& p) {
-  // row_mode 2 sizes registers for 768 resident threads: blocks of <= 256.
+  // row_mode 2 sizes registers for 768 resident threads (1024 at ny = 2048):
+  // blocks of <= 256.
   return p.log2L >= 8 && p.log2L <= (p.row_mode == 2 ? 10 : 11);
 }
 
@@ -1533,7 +1518,7 @@ cudaError_t launch_spec_row(const SpecParams& p, const float2* const t4[4],
     switch (p.log2L) {
       case 8: return spec_row_pipe_impl<8, 768>(p, t4, ahat, s);
       case 9: return spec_row_pipe_impl<9, 768>(p, t4, ahat, s);
-      default: return spec_row_pipe_impl<10, 768>(p, t4, ahat, s);
+      default: return spec_row_pipe_impl<10, 1024>(p, t4, ahat, s);
     }
   }
   if (p.row_mode >= 1 && spec_row_pipe_ok(p)) {
@@ -1657,7 +1642,7 @@ cudaError_t launch_spec_batch_prep(const SpecParams& p, const SpecMember* mem, i
 template <int LOG2L>
 static cudaError_t spec_batch_row_pipe_impl(const SpecParams& p, const SpecMember* mem, int count,
                                             int k, cudaStream_t s) {
-  const size_t smem = (size_t)8 * padded_len(1 << LOG2L) * sizeof(float2);
+  const size_t smem = spec_row_pipe_smem<LOG2L>();
   auto kern = spec_batch_row_pipe_kernel<LOG2L>;
   cudaError_t e = set_smem(kern, smem);
   if (e != cudaSuccess) return e;

@@ -400,7 +400,7 @@ class SpecPlan:
 
   LAUNCH_CHOICES = 15
   COLUMN_PASSES = ('blocks', 'cluster4', 'pipelined4', 'pipelined2', 'pipelined4_fused')
-  ROW_PASSES = ('shared_memory', 'register_passes', 'register_passes_3blocks')
+  ROW_PASSES = ('shared_memory', 'register_passes', 'register_passes_high_occupancy')
 
   def set_launch(self, choice: int):
     """choice = column scheme + 5 * row scheme.  Column passes: 0 per-block
@@ -408,8 +408,8 @@ class SpecPlan:
     persistent register-pipelined groups of 4/2 columns (512 <= nx <= 4096),
     4 as 2 with each stage's update and the next stage's prep fused.  Row
     pass: 0 shared-memory engine, 1 register passes (512 <= ny <= 4096), 2
-    register passes with registers for three blocks per multiprocessor
-    (512 <= ny <= 2048).  Results do not change."""
+    register passes with registers for three blocks per multiprocessor (four
+    at ny = 2048; 512 <= ny <= 2048).  Results do not change."""
     nat.check(self._lib.cfd_spec_plan_set_launch(self._h, int(choice)), 'cfd_spec_plan_set_launch')
 
   @property
