@@ -19,6 +19,7 @@
 // irfftn 1/(nx*ny) is a power of two applied once to the product.
 #include <cooperative_groups.h>
 #include <cstring>
+#include <type_traits>
 #include <cuda.h>
 
 #include "bulk.cuh"
@@ -62,6 +63,31 @@ CFD_D float2 prep_factor_k(const SpecParams& p, int f, int kx, float kxf, int c,
 
 CFD_D float2 prep_factor(const SpecParams& p, int f, int kx, int c, float2 u) {
   return prep_factor_k(p, f, kx, kx_of(p, kx), c, u);
+}
+
+// Field f's 16 prep values of a column-pipe worker (rows t + NTHR r) from the
+// state u[r], with f resolved at compile time: inside the stage kernels'
+// field loop a run-time f left every element with the code of all four
+// fields (the gy field is the state itself, gx one product, vx/vy a
+// reciprocal); 2048^2 fused stage: 1.5 us of each field's 3.6 us per group
+// before.  Same expressions, same bits.
+template <int NTHR>
+CFD_D void prep_fields(const SpecParams& p, int f, const float* kxt, int c, bool live, int t,
+                       const float2 (&u)[16], float2 (&v)[16]) {
+  auto fill = [&](auto fc) {
+    constexpr int F = decltype(fc)::value;
+#pragma unroll
+    for (int r = 0; r < 16; ++r) {
+      const int kx = t + NTHR * r;
+      v[r] = live ? prep_factor_k(p, F, kx, kxt[kx], c, u[r]) : make_float2(0.f, 0.f);
+    }
+  };
+  switch (f) {
+    case 0: fill(std::integral_constant<int, 0>{}); break;
+    case 1: fill(std::integral_constant<int, 1>{}); break;
+    case 2: fill(std::integral_constant<int, 2>{}); break;
+    default: fill(std::integral_constant<int, 3>{}); break;
+  }
 }
 
 // ky-side factors: vx = i ay A, vy = -i B, gx = i C, gy = i ay D.
@@ -567,11 +593,7 @@ __global__ void __launch_bounds__(CG * (1 << LOG2N) / 16,
     }
 #pragma unroll 1
     for (int f = 0; f < 4; ++f) {
-#pragma unroll
-      for (int r = 0; r < 16; ++r) {
-        const int kx = t + P::NTHR * r;
-        v[r] = live ? prep_factor_k(p, f, kx, kxt[kx], c, u[r]) : make_float2(0.f, 0.f);
-      }
+      prep_fields<P::NTHR>(p, f, kxt, c, live, t, u, v);
       col_pipe_fft<LOG2N, 1, 0>(v, buf, t, tw);
       if (live) {
         float2* dst = f == 0 ? t4.t[0] : f == 1 ? t4.t[1] : f == 2 ? t4.t[2] : t4.t[3];
@@ -675,11 +697,7 @@ __global__ void __launch_bounds__(4 * (1 << LOG2N) / 16,
     }
 #pragma unroll 1
     for (int f = 0; f < 4; ++f) {
-#pragma unroll
-      for (int r = 0; r < 16; ++r) {
-        const int kx = t + P::NTHR * r;
-        v[r] = live ? prep_factor_k(p, f, kx, kxt[kx], c, u[r]) : make_float2(0.f, 0.f);
-      }
+      prep_fields<P::NTHR>(p, f, kxt, c, live, t, u, v);
       if (tid == 0) bulk_wait_read_all();
       col_pipe_fft<LOG2N, 1, 0>(v, buf, t, tw);
       // Every thread is past the transform's reads of the second buffers.
@@ -1005,11 +1023,7 @@ __global__ void __launch_bounds__(CG * (1 << LOG2N) / 16,
     if (prep) {
 #pragma unroll 1
       for (int f = 0; f < 4; ++f) {
-#pragma unroll
-        for (int r = 0; r < 16; ++r) {
-          const int kx = t + P::NTHR * r;
-          v[r] = live ? prep_factor_k(p, f, kx, kxt[kx], c, u[r]) : make_float2(0.f, 0.f);
-        }
+        prep_fields<P::NTHR>(p, f, kxt, c, live, t, u, v);
         col_pipe_fft<LOG2N, 1, 0>(v, buf, t, tw);
         if (live) {
           float2* dst = m.t[f];
