@@ -658,6 +658,17 @@ __global__ void __launch_bounds__(4 * (1 << LOG2N) / 16,
   if (tid == 0) issue(g);
   uint32_t phase = 0;
   float2 v[16], u[16], hs[16];
+  // The state of a group is loaded while the previous group's last field is
+  // transformed (u is free once that field's prep has read it), so the loads
+  // are in flight during that transform; the first group's here.
+  auto load_state = [&](int gg) {
+    const int cc = gg * CG + w;
+    const bool ll = gg < groups && cc < ncols;
+#pragma unroll
+    for (int m = 0; m < 16; ++m)
+      u[m] = ll ? wst[state_at<CG, TILED>(p.nx, ncols, t + P::NTHR * m, cc)] : make_float2(0.f, 0.f);
+  };
+  load_state(g);
 #pragma unroll 1
   for (; g < groups; g += gridDim.x) {
     const int c = g * CG + w;
@@ -679,7 +690,6 @@ __global__ void __launch_bounds__(4 * (1 << LOG2N) / 16,
 #pragma unroll
     for (int m = 0; m < 16; ++m) {
       const size_t gi = state_at<CG, TILED>(p.nx, ncols, t + P::NTHR * m, c);
-      u[m] = live ? wst[gi] : make_float2(0.f, 0.f);
       hs[m] = (live && sc.has_h_in) ? hst[gi] : make_float2(0.f, 0.f);
     }
     if (tid == 0) bulk_wait_read_all();
@@ -698,6 +708,7 @@ __global__ void __launch_bounds__(4 * (1 << LOG2N) / 16,
 #pragma unroll 1
     for (int f = 0; f < 4; ++f) {
       prep_fields<P::NTHR>(p, f, kxt, c, live, t, u, v);
+      if (f == 3) load_state(g + gridDim.x);
       if (tid == 0) bulk_wait_read_all();
       col_pipe_fft<LOG2N, 1, 0>(v, buf, t, tw);
       // Every thread is past the transform's reads of the second buffers.
