@@ -729,7 +729,8 @@ def run_gb300(args):
         'row_pass': splan.ROW_PASSES[s_launch // 5],
         'launches_per_time_step': s_per_step,
         'roofline': {'kernel': s_dom, 'bound': 'hbm', 'achieved': s_ach, 'peak': peak,
-                     'unit': 'GB/s', 'frac': s_ach / peak},
+                     'unit': 'GB/s', 'frac': s_ach / peak,
+                     'traffic': _traffic_table().get(f'spec_{s_dom}_{n}')},
         'finite': bool(torch.isfinite(torch.view_as_real(w)).all()),
     }
 
