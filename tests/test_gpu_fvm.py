@@ -1,6 +1,6 @@
 """GPU parity of the staggered-grid (FVM) path against the NumPy oracle.
 
-Tolerances: the spec bar is per-step relative L2 <= 1e-5 on velocity
+Tolerances: the parity bar is per-step relative L2 <= 1e-5 on velocity
 (float32).  Operator-level checks (explicit terms, pressure solve) use the same
 bound; divergence after projection must be at float32 round-off.
 """

@@ -11,7 +11,7 @@
   ``rfftn(curl_2d(v0))``.
 
 Each step is compared with the float32 oracle (per-step relative L2 <= 1e-5,
-the spec bar) and, as the stand-in for a ``jax_enable_x64`` run of the
+the parity bar) and, as the stand-in for a ``jax_enable_x64`` run of the
 reference, both the GPU result and the float32 oracle are compared with the
 float64 oracle; the two errors are printed and the GPU's is held to the same
 1e-5 bar (measured: both about 5e-8 for FVM).  The FVM step's projected field
