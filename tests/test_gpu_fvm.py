@@ -129,7 +129,7 @@ def test_fused_chunk_equals_single_steps(cuda_device):
     assert torch.equal(x.data, y.data)
 
 
-def test_config0_trajectory_tracks_oracle(cuda_device):
+def test_kolmogorov_64x64_500_steps_track_oracle(cuda_device):
   """64^2 Kolmogorov flow, 500 steps (the reference's CPU-runnable case):
   every 50 steps the GPU state stays within 1e-5 per step of the oracle
   restarted from the GPU state, and the final state stays close."""
