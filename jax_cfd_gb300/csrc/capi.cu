@@ -373,7 +373,7 @@ static int fvm_params_from_config(const cfd_fvm_config* cfg, cfd::FvmParams* out
 // Tensor map of `count` packed row spectra, each nx rows of ny float32 (2
 // floats per complex value), spectrum z at spec + z * member_floats floats;
 // boxes of 8 floats x min(nx, 256) rows x 1 spectrum.
-// The driver's cuTensorMapEncodeTiled, looked up once (a function-local
+// The CUDA driver's cuTensorMapEncodeTiled, looked up once (a function-local
 // static: thread-safe initialisation); null where the lookup fails.
 static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
   static const PFN_cuTensorMapEncodeTiled_v12000 encode = []() {

@@ -1,7 +1,7 @@
 """NumPy restatement of the reference's flow diagnostics.
 
-TEST INFRASTRUCTURE: the checker for the on-device diagnostics and the
-long-horizon statistics, never the product.  Follows
+TEST INFRASTRUCTURE: the oracle the tests compare the on-device diagnostics and the
+long-horizon statistics with, never the product.  Follows
 jax_cfd/data/xarray_utils.py (the reference computes these through xarray;
 the arithmetic is the same on plain arrays):
 

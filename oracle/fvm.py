@@ -1,6 +1,7 @@
 """NumPy restatement of the reference's staggered-grid (FVM) hot path.
 
-TEST INFRASTRUCTURE: the checker for the CUDA path, never the product.
+TEST INFRASTRUCTURE: the oracle the parity tests compare the CUDA path with, never
+the product.
 
 Every function cites the reference line range (paths relative to the jax-cfd
 project root) whose arithmetic it follows.  A "variable" here is a pair

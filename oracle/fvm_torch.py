@@ -1,6 +1,6 @@
 """torch (float64, autograd) restatement of the FVM step for gradient checks.
 
-TEST INFRASTRUCTURE: the checker for the hand-written CUDA adjoint, never the
+TEST INFRASTRUCTURE: the oracle the tests compare the hand-written CUDA adjoint with, never the
 product.  JAX is not installable here, so ``jax.grad`` of the reference is
 replaced by torch autograd through this restatement, which follows the same
 reference lines as ``oracle/fvm.py`` op for op and mirrors jnp's

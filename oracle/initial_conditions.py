@@ -1,6 +1,7 @@
 """NumPy restatement of the reference's initial-condition pipeline.
 
-TEST INFRASTRUCTURE: the checker for the CUDA path, never the product.
+TEST INFRASTRUCTURE: the oracle the parity tests compare the CUDA path with, never
+the product.
 
 Follows ``jax_cfd/base/initial_conditions.py:60-121`` and
 ``jax_cfd/base/filter_utils.py:25-42``.  The reference draws its noise with

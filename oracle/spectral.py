@@ -1,6 +1,7 @@
 """NumPy restatement of the reference's pseudospectral vorticity step.
 
-TEST INFRASTRUCTURE: the checker for the CUDA path, never the product.
+TEST INFRASTRUCTURE: the oracle the parity tests compare the CUDA path with, never
+the product.
 
 Follows ``jax_cfd/spectral/equations.py:129-220``, ``spectral/utils.py:128-134,
 154-203`` and ``spectral/time_stepping.py:117-197``.  The state is the
