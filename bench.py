@@ -82,6 +82,20 @@ def _peaks():
     return 6800.0, 'fallback'
 
 
+def spectral_launches_per_time_step(chunk: int) -> dict:
+  """Launches of each spectral kernel per time step in a chunk of `chunk`
+  steps: five row passes and five column stages per step, of which the last
+  of the chunk is the plain update; the prep runs once per chunk."""
+  return {'row': 5.0, 'col_stage': 5.0 - 1.0 / chunk, 'col_update': 1.0 / chunk,
+          'col_prep': 1.0 / chunk}
+
+
+def spectral_dominant_kernel(kernel_ms: dict, chunk: int) -> str:
+  """The spectral kernel with the most device time per time step."""
+  per_step = spectral_launches_per_time_step(chunk)
+  return max(per_step, key=lambda k: kernel_ms[k] * per_step[k])
+
+
 def _traffic_table():
   path = os.path.join(ROOT, 'profiles', 'dram_traffic.json')
   try:
@@ -708,13 +722,8 @@ def run_gb300(args):
       s_ms += s0.elapsed_time(s1)
     s_value = cells * args.spectral_chunk * 3 / (s_ms / 1000.0)
     sk = sstep.plan(dev).profile(w0, 2)
-    # The dominant kernel is the one with the most device time per time step:
-    # five row passes and five column stages per step, of which the last of a
-    # chunk is the plain update; the prep runs once per chunk.
-    c = args.spectral_chunk
-    s_per_step = {'row': 5.0, 'col_stage': 5.0 - 1.0 / c, 'col_update': 1.0 / c,
-                  'col_prep': 1.0 / c}
-    s_dom = max(s_per_step, key=lambda k: sk[k] * s_per_step[k])
+    s_per_step = spectral_launches_per_time_step(args.spectral_chunk)
+    s_dom = spectral_dominant_kernel(sk, args.spectral_chunk)
     s_ach = SPEC_BYTES_PER_CELL[s_dom] * cells / (sk[s_dom] / 1000.0) / 1e9
     spectral = {
         'workload': f'NavierStokes2D {n}x{n} crank_nicolson_rk4 dt=1e-3, Kolmogorov k=4, drag 0.1',
